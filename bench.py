@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 SPH fluid step on the 1,048,576-particle dam break.
+
+One "step" is one substep of the plain SPH solver (grid build, density and
+pressure, forces + integration + walls) over all particles of the tank at
+dt = 1/600 s. Inputs are seeded synthetic (jittered emit lattice).
+
+Our arm (default) prints one JSON line with
+  value    sim-s x particles / s with the state resident in HBM, device time
+           from CUDA events on the solver's stream, L2 flushed before every
+           timed substep (a 256 MB write);
+  e2e      the same metric through the C ABI with host buffers: every step
+           uploads the state from pinned host memory, runs the substep and
+           downloads the new state;
+  roofline the dominant kernel's algorithmic bytes per launch over its
+           event-timed duration, against the measured HBM copy bandwidth;
+  cpu_baseline  the CPU oracle (a restatement of the reference's CPU solver)
+           timed on this host's cores on a bounded sample.
+`--impl reference` times the reference's CPU solver path (the oracle port,
+all host threads) on the same workload and metric.
+
+With torchrun (N > 1) every rank advances its own replica of the tank (the
+single-tank step does not shard); value sums particles over ranks and takes
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "sim-s×particles/s @1M: plain vs learned 5×dt (≤1% density err); % HBM peak"
+UNIT = "sim-s*particles/s"
+FALLBACK_HBM_GBS = 6800.0
+FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--e2e-steps", type=int, default=None, help="steps of the end-to-end leg (default: --steps)")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload_config(case, world: int) -> dict:
+    p = case.params
+    return {
+        "workload": case.name,
+        "particles": case.count,
+        "dt": case.dt,
+        "lattice": [int(p.lattice[0]), int(p.lattice[1]), int(p.lattice[2])],
+        "box": [[float(p.container_min[a]) for a in range(3)], [float(p.container_max[a]) for a in range(3)]],
+        "buckets": int(p.lattice[3]),
+        "smoothing_radius": float(p.smoothing_radius),
+        "spacing": float(p.emitter_half_extents[3]),
+        "jitter": "uniform +-1e-4 m, splitmix64 seed 0",
+        "l2": "flushed before every timed substep (256 MB write); working set ~120 MB",
+        "parallelism": "single tank" if world == 1 else f"{world} replicas (no data exchange)",
+    }
+
+
+def measured_hbm_peak():
+    path = ROOT / "MEASURED_PEAKS.json"
+    try:
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        self.file.flush()
+
+    def summary(self) -> dict:
+        self.file.seek(0)
+        rows = list(csv.reader(io.StringIO(self.file.read())))
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in rows:
+            if len(row) < 9:
+                continue
+            try:
+                sm.append(float(row[1]))
+                mx.append(float(row[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, row[5:9]):
+                if flag.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(case, seconds: float) -> dict:
+    """The CPU oracle on a bounded sample: whole-tank substeps until `seconds` pass."""
+    from oracle.bind import Oracle
+
+    oracle = Oracle()
+    threads = oracle.hardware_threads
+    pos, vel = case.initial_state()
+    start = time.perf_counter()
+    steps = 0
+    while True:
+        pos, vel = oracle.substep(case.params, pos, vel, case.dt, threads=threads)
+        steps += 1
+        if time.perf_counter() - start >= seconds:
+            break
+    wall = time.perf_counter() - start
+    return {
+        "value": case.count * case.dt * steps / wall,
+        "unit": UNIT,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{steps} substeps of the full {case.count}-particle tank from its initial state ({wall:.1f} s)",
+        "ms_per_step": 1e3 * wall / steps,
+    }
+
+
+def run_reference(args) -> None:
+    """The reference's CPU solver path (oracle port, all host threads)."""
+    from computer_graphics_lab_00_gb300 import workloads as W
+
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.bind import Oracle
+
+    case = W.dam_break_1m()
+    oracle = Oracle()
+    threads = oracle.hardware_threads
+    pos, vel = case.initial_state()
+    for _ in range(max(args.warmup, 0)):
+        t0 = time.perf_counter()
+        pos, vel = oracle.substep(case.params, pos, vel, case.dt, threads=threads)
+        last = time.perf_counter() - t0
+    # Keep the whole run within a few minutes: cap the timed substeps.
+    steps = args.steps
+    budget = 150.0
+    per = last if args.warmup > 0 else 1.0
+    timed = max(1, min(steps, int(budget / max(per, 1e-3))))
+    start = time.perf_counter()
+    for _ in range(timed):
+        pos, vel = oracle.substep(case.params, pos, vel, case.dt, threads=threads)
+    wall = time.perf_counter() - start
+    value = case.count * case.dt * timed / wall
+    sample = (f"{timed} whole-tank substeps of the {case.count}-particle tank"
+              + ("" if timed == steps else f" (of {steps} requested; capped to ~{budget:.0f} s)"))
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": timed, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wall / timed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "config": workload_config(case, 1), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gb300(args) -> None:
+    import torch
+
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    case = W.dam_break_1m()
+    n = case.count
+    dt = case.dt
+    pos0, vel0 = case.initial_state()
+    solver = FluidSolverGpu(case.params, n, device=local)
+    solver.upload(pos0, vel0)
+    pairs = solver.stats()  # candidate and in-range pair counts of the initial state
+    stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # Warm-up (builds the CUDA graph).
+    solver.run(dt, max(args.warmup, 3))
+    solver.synchronize()
+
+    # Timed leg: device-resident state, one substep per timed interval.
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.__enter__()
+    barrier()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            starts[k].record(stream)
+        solver.run(dt, 1)
+        ends[k].record(stream)
+    barrier()
+    wall = time.perf_counter() - wall0
+    if sampler:
+        sampler.__exit__(None, None, None)
+    device_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    launches = solver.launches_per_substep() * args.steps
+
+    # Per-phase device times (same kernels, launched one by one between events).
+    phases = {name: 0.0 for name in FluidSolverGpu.PROFILE_PHASES}
+    prof_steps = min(args.steps, 50)
+    for _ in range(prof_steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        for name, ms in solver.profile(dt, 1).items():
+            phases[name] += ms
+    phases = {k: v / prof_steps for k, v in phases.items()}
+
+    # End-to-end leg: host state in pinned memory, copies inside the timed region.
+    e2e_steps = args.e2e_steps or min(args.steps, 100)
+    host_pos = torch.from_numpy(pos0.copy()).pin_memory()
+    host_vel = torch.from_numpy(vel0.copy()).pin_memory()
+    solver.upload_from(host_pos.data_ptr(), host_vel.data_ptr(), n)
+    solver.substep(dt)
+    solver.download_to(host_pos.data_ptr(), host_vel.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        solver.upload_from(host_pos.data_ptr(), host_vel.data_ptr(), n)
+        solver.substep(dt)
+        solver.download_to(host_pos.data_ptr(), host_vel.data_ptr())
+    barrier()
+    e2e_wall = time.perf_counter() - t0
+
+    # Max over ranks.
+    times = torch.tensor([device_ms, e2e_wall], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    device_ms, e2e_wall = float(times[0]), float(times[1])
+    if rank != 0:
+        solver.close()
+        return
+
+    total_particles = n * world
+    value = total_particles * dt * args.steps / (device_ms / 1e3)
+    e2e_value = total_particles * dt * e2e_steps / e2e_wall
+
+    # Roofline of the dominant kernel: algorithmic bytes per launch.
+    cells = int(case.params.lattice[3])
+    alg_bytes = {
+        "keys": 20 * n + 8 * cells,
+        "sort": 16 * n + 20 * n * 2,
+        "bounds_gather": 72 * n,
+        "density": 24 * n,     # read own position 16 B, write rho + pressure 8 B
+        "integrate": 64 * n,   # read own pos + vel 32 B, write pos + vel 32 B
+    }
+    dominant = max(phases, key=phases.get)
+    peak, peak_kind = measured_hbm_peak()
+    achieved = alg_bytes[dominant] / (phases[dominant] / 1e3) / 1e9
+    traffic = None
+    traffic_file = ROOT / "profiles" / "traffic_per_launch.json"
+    if traffic_file.exists():
+        try:
+            traffic = json.loads(traffic_file.read_text()).get(dominant)
+        except Exception:
+            traffic = None
+    step_alg = 120 * n + 12 * cells
+    step_ms = device_ms / args.steps
+    flops = 20 * pairs.candidates + 55 * pairs.pairs_in_range
+    nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+
+    clocks = sampler.summary() if sampler else None
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": step_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": workload_config(case, world),
+        "particle_steps_per_s": total_particles * args.steps / (device_ms / 1e3),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                "steps": e2e_steps, "ms_per_step": 1e3 * e2e_wall / e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "traffic": traffic,
+                     "alg_bytes_per_launch": alg_bytes[dominant]},
+        "step_roofline": {"alg_bytes": step_alg, "achieved_gbs": step_alg / (step_ms / 1e3) / 1e9,
+                          "frac_of_peak": step_alg / (step_ms / 1e3) / 1e9 / peak},
+        "fp32": {"alg_flops_per_step": flops, "achieved_tflops": flops / (step_ms / 1e3) / 1e12,
+                 "nominal_peak_tflops": nominal_fp32, "candidates": pairs.candidates,
+                 "pairs_in_range": pairs.pairs_in_range},
+        "phase_ms": phases,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "wall_s_timed": wall,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(case, args.cpu_seconds)
+    solver.close()
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,632 @@
+// sph_engine.cu — device state, the substep pipeline and its CUDA graph.
+#include "sph_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace sph {
+
+namespace {
+// std::numbers::pi_v<float> (fluid_sph.cpp:20).
+constexpr float kPi = 3.14159265358979323846F;
+
+uint32_t bit_width(uint32_t v) {
+    uint32_t bits = 0;
+    while (v != 0) {
+        ++bits;
+        v >>= 1;
+    }
+    return bits;
+}
+}  // namespace
+
+// fluid_sph.cpp:128-136.
+uint32_t fluid_substeps(const sph_params& params, float delta_seconds) {
+    float h = params.smoothing_radius;
+    float gx = params.gravity[0];
+    float gy = params.gravity[1];
+    float gz = params.gravity[2];
+    float gravity = std::max(std::sqrt(gx * gx + gy * gy + gz * gz), 0.1F);
+    float stable = std::min(0.4F * h / std::sqrt(std::max(params.stiffness, 1.0F)), 0.25F * std::sqrt(h / gravity));
+    float frame_step = std::min(std::max(delta_seconds, 0.0F), SPH_MAX_FRAME_STEP);
+    auto steps = static_cast<uint32_t>(std::ceil(frame_step / std::max(stable, 1e-5F)));
+    return std::clamp(steps, 1U, 8U);
+}
+
+// The per-particle constants of fluid_sph.cpp:24-46 and :194-285, each from
+// the reference's own float expression (std::pow(float, float) is powf).
+TankConst make_tank_const(const sph_params& p, float dt) {
+    TankConst t{};
+    float h = p.smoothing_radius;
+    t.h = h;
+    t.h2 = h * h;
+    t.c_poly6 = 315.0F / (64.0F * kPi * std::pow(h, 9.0F));
+    t.c_spiky = -45.0F / (kPi * std::pow(h, 6.0F));
+    t.c_visc = 45.0F / (kPi * std::pow(h, 6.0F));
+    t.mass = p.gravity[3];
+    t.neg_mass = -t.mass;
+    t.visc_mass = p.viscosity * t.mass;
+    t.rest_density = p.rest_density;
+    t.stiffness = p.stiffness;
+    t.dt = dt;
+    t.max_speed = dt > 0.0F ? 0.4F * h / dt : 0.0F;
+    for (int a = 0; a < 3; ++a) {
+        t.gravity[a] = p.gravity[a];
+        t.low[a] = p.container_min[a] + p.container_min[3];
+        t.high[a] = p.container_max[a] - p.container_min[3];
+        t.lattice[a] = p.lattice[a];
+    }
+    t.restitution = p.container_max[3];
+    t.rest_w = p.rest_density;
+    t.spacing = p.emitter_half_extents[3];
+    t.cell_mask = p.lattice[3] - 1U;
+    t.active = 1;
+    std::memcpy(t.emitter_world, p.emitter_world, sizeof(t.emitter_world));
+    return t;
+}
+
+int validate_params(const sph_params& p) {
+    uint32_t cells = p.lattice[3];
+    if (cells == 0 || (cells & (cells - 1)) != 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (!(p.smoothing_radius > 0.0F) || !std::isfinite(p.smoothing_radius)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (p.collider_count != 0 || p.field_count != 0) {
+        // Shape colliders and force fields are not on the device path.
+        return SPH_ERR_UNSUPPORTED;
+    }
+    return SPH_OK;
+}
+
+Engine::~Engine() { release(); }
+
+int Engine::fail(cudaError_t error, const char* what) {
+    last_error_ = std::string(what) + ": " + cudaGetErrorString(error);
+    cudaGetLastError();
+    return error == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;
+}
+
+#define SPH_CUDA(call)                                \
+    do {                                              \
+        cudaError_t sph_error_ = (call);              \
+        if (sph_error_ != cudaSuccess) {              \
+            return fail(sph_error_, #call);           \
+        }                                             \
+    } while (0)
+
+template <typename T> int Engine::alloc(T** ptr, size_t count) {
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    SPH_CUDA(cudaMalloc(reinterpret_cast<void**>(ptr), bytes));
+    device_bytes_ += bytes;
+    return SPH_OK;
+}
+
+void Engine::release() {
+    if (device_bytes_ == 0 && stream_ == nullptr) {
+        return;
+    }
+    cudaSetDevice(device_);
+    if (graph_ != nullptr) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    for (cudaEvent_t& e : events_) {
+        if (e != nullptr) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    }
+    void* buffers[] = {d_tanks_,       pos_,          vel_,         prev_,        tank_of_,   stank_,
+                       grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
+                       bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
+                       bucket_stats_};
+    for (void* b : buffers) {
+        if (b != nullptr) {
+            cudaFree(b);
+        }
+    }
+    if (stream_ != nullptr) {
+        cudaStreamDestroy(stream_);
+        stream_ = nullptr;
+    }
+    device_bytes_ = 0;
+}
+
+int Engine::init(int device, const std::vector<sph_params>& params, const std::vector<uint32_t>& capacities) {
+    if (params.empty() || params.size() != capacities.size() || params.size() > 65535) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    for (const sph_params& p : params) {
+        int status = validate_params(p);
+        if (status != SPH_OK) {
+            return status;
+        }
+    }
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) {
+        cudaGetLastError();
+        last_error_ = "no CUDA device";
+        return SPH_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= devices) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    device_ = device;
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+
+    params_ = params;
+    capacity_ = capacities;
+    tanks_.resize(params.size());
+    uint64_t particles = 0;
+    uint64_t buckets = 0;
+    for (size_t t = 0; t < params.size(); ++t) {
+        tanks_[t] = make_tank_const(params[t], 0.0F);
+        tanks_[t].particle_base = static_cast<uint32_t>(particles);
+        tanks_[t].bucket_base = static_cast<uint32_t>(buckets);
+        tanks_[t].particle_count = params.size() == 1 ? 0 : capacities[t];
+        particles += capacities[t];
+        buckets += params[t].lattice[3];
+    }
+    if (particles == 0 || particles > 0x7FFFFFFFu || buckets > 0x7FFFFFFFu) {
+        return SPH_ERR_CAPACITY;
+    }
+    total_capacity_ = static_cast<uint32_t>(particles);
+    total_buckets_ = static_cast<uint32_t>(buckets);
+    total_count_ = params.size() == 1 ? 0 : total_capacity_;
+    plan_ = plan_radix(bit_width(total_buckets_ - 1U), radix_bits_);
+
+    uint32_t n = total_capacity_;
+    int status = SPH_OK;
+    if ((status = alloc(&d_tanks_, tanks_.size())) != SPH_OK || (status = alloc(&pos_, n)) != SPH_OK ||
+        (status = alloc(&vel_, n)) != SPH_OK || (status = alloc(&prev_, n)) != SPH_OK ||
+        (status = alloc(&grid_.keys, n)) != SPH_OK || (status = alloc(&grid_.keys_a, n)) != SPH_OK ||
+        (status = alloc(&grid_.vals_a, n)) != SPH_OK || (status = alloc(&grid_.keys_b, n)) != SPH_OK ||
+        (status = alloc(&grid_.vals_b, n)) != SPH_OK ||
+        (status = alloc(&grid_.hist, static_cast<size_t>(radix_tiles(n)) * kRadixMaxBins)) != SPH_OK ||
+        (status = alloc(&bucket_, total_buckets_)) != SPH_OK || (status = alloc(&spos_, n)) != SPH_OK ||
+        (status = alloc(&spos2_, n)) != SPH_OK || (status = alloc(&svel_, n)) != SPH_OK ||
+        (status = alloc(&counters_, 1)) != SPH_OK ||
+        (status = alloc(&stats_acc_, tanks_.size() * kStatsPerTank)) != SPH_OK ||
+        (status = alloc(&bucket_stats_, 2)) != SPH_OK) {
+        return status;
+    }
+    if (tanks_.size() > 1) {
+        if ((status = alloc(&tank_of_, n)) != SPH_OK || (status = alloc(&stank_, n)) != SPH_OK) {
+            return status;
+        }
+        std::vector<uint16_t> owner(n);
+        for (size_t t = 0; t < tanks_.size(); ++t) {
+            std::fill(owner.begin() + tanks_[t].particle_base,
+                      owner.begin() + tanks_[t].particle_base + capacities[t], static_cast<uint16_t>(t));
+        }
+        SPH_CUDA(cudaMemcpy(tank_of_, owner.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+    SPH_CUDA(cudaMemsetAsync(pos_, 0, sizeof(float4) * n, stream_));
+    SPH_CUDA(cudaMemsetAsync(vel_, 0, sizeof(float4) * n, stream_));
+    SPH_CUDA(cudaMemsetAsync(prev_, 0, sizeof(float4) * n, stream_));
+    consts_dirty_ = true;
+    return SPH_OK;
+}
+
+int Engine::set_params(uint32_t tank, const sph_params& params) {
+    if (tank >= tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    int status = validate_params(params);
+    if (status != SPH_OK) {
+        return status;
+    }
+    if (params.lattice[3] != params_[tank].lattice[3]) {
+        // The bucket table is laid out at create; a new bucket count needs a new context.
+        return SPH_ERR_CAPACITY;
+    }
+    TankConst fresh = make_tank_const(params, tanks_[tank].dt);
+    fresh.particle_base = tanks_[tank].particle_base;
+    fresh.bucket_base = tanks_[tank].bucket_base;
+    fresh.particle_count = tanks_[tank].particle_count;
+    fresh.active = tanks_[tank].active;
+    tanks_[tank] = fresh;
+    params_[tank] = params;
+    consts_dirty_ = true;
+    return SPH_OK;
+}
+
+int Engine::refresh_constants(float dt) {
+    if (!consts_dirty_ && dt == const_dt_) {
+        return SPH_OK;
+    }
+    for (TankConst& t : tanks_) {
+        t.dt = dt;
+        t.max_speed = dt > 0.0F ? 0.4F * t.h / dt : 0.0F;
+    }
+    SPH_CUDA(cudaMemcpyAsync(d_tanks_, tanks_.data(), tanks_.size() * sizeof(TankConst), cudaMemcpyHostToDevice,
+                             stream_));
+    const_dt_ = dt;
+    consts_dirty_ = false;
+    return SPH_OK;
+}
+
+int Engine::upload(uint32_t tank, const float* pos, const float* vel, uint32_t count) {
+    if (tank >= tanks_.size() || (count > 0 && pos == nullptr)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (count > capacity_[tank] || (tanks_.size() > 1 && count != capacity_[tank])) {
+        return SPH_ERR_CAPACITY;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    uint32_t base = tanks_[tank].particle_base;
+    size_t bytes = sizeof(float4) * count;
+    if (count > 0) {
+        SPH_CUDA(cudaMemcpyAsync(pos_ + base, pos, bytes, cudaMemcpyHostToDevice, stream_));
+        if (vel != nullptr) {
+            SPH_CUDA(cudaMemcpyAsync(vel_ + base, vel, bytes, cudaMemcpyHostToDevice, stream_));
+        } else {
+            SPH_CUDA(cudaMemsetAsync(vel_ + base, 0, bytes, stream_));
+        }
+        SPH_CUDA(cudaMemcpyAsync(prev_ + base, pos_ + base, bytes, cudaMemcpyDeviceToDevice, stream_));
+        // Non-finite xyz in either array is rejected (checked on the device,
+        // where the data already is).
+        SPH_CUDA(cudaMemsetAsync(bucket_stats_, 0, sizeof(uint32_t), stream_));
+        SPH_CUDA(launch_count_nonfinite(pos_ + base, vel_ + base, count, bucket_stats_, stream_));
+        SPH_CUDA(cudaMemcpyAsync(&nonfinite_host_, bucket_stats_, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    } else {
+        nonfinite_host_ = 0;
+    }
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    if (nonfinite_host_ != 0) {
+        return SPH_ERR_NONFINITE;
+    }
+    if (tanks_.size() == 1) {
+        tanks_[0].particle_count = count;
+        total_count_ = count;
+        consts_dirty_ = true;
+    }
+    grid_valid_ = false;
+    return SPH_OK;
+}
+
+int Engine::download(uint32_t tank, float* pos, float* vel) {
+    if (tank >= tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    uint32_t base = tanks_[tank].particle_base;
+    size_t bytes = sizeof(float4) * tanks_[tank].particle_count;
+    if (bytes == 0) {
+        return SPH_OK;
+    }
+    if (pos != nullptr) {
+        SPH_CUDA(cudaMemcpy(pos, pos_ + base, bytes, cudaMemcpyDeviceToHost));
+    }
+    if (vel != nullptr) {
+        SPH_CUDA(cudaMemcpy(vel, vel_ + base, bytes, cudaMemcpyDeviceToHost));
+    }
+    return SPH_OK;
+}
+
+int Engine::download_previous(uint32_t tank, float* pos) {
+    if (tank >= tanks_.size() || pos == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    size_t bytes = sizeof(float4) * tanks_[tank].particle_count;
+    if (bytes > 0) {
+        SPH_CUDA(cudaMemcpy(pos, prev_ + tanks_[tank].particle_base, bytes, cudaMemcpyDeviceToHost));
+    }
+    return SPH_OK;
+}
+
+int Engine::keep_rendered() {
+    SPH_CUDA(cudaSetDevice(device_));
+    if (total_count_ > 0) {
+        SPH_CUDA(cudaMemcpyAsync(prev_, pos_, sizeof(float4) * total_count_, cudaMemcpyDeviceToDevice, stream_));
+    }
+    return SPH_OK;
+}
+
+int Engine::emit(uint32_t tank, uint32_t count) {
+    if (tank >= tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (count > capacity_[tank] || (tanks_.size() > 1 && count != capacity_[tank])) {
+        return SPH_ERR_CAPACITY;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    if (tanks_.size() == 1) {
+        tanks_[0].particle_count = count;
+        total_count_ = count;
+        consts_dirty_ = true;
+    }
+    int status = refresh_constants(const_dt_ < 0.0F ? 0.0F : const_dt_);
+    if (status != SPH_OK) {
+        return status;
+    }
+    SPH_CUDA(launch_emit(d_tanks_ + tank, tanks_[tank].particle_base, count, pos_, vel_, prev_, stream_));
+    grid_valid_ = false;
+    return SPH_OK;
+}
+
+int Engine::enqueue_grid(uint32_t* launches) {
+    uint32_t n = total_count_;
+    SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
+    SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
+    SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, launches));
+    SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_, svel_,
+                                  stank_, stream_));
+    if (launches != nullptr) {
+        *launches += 2;
+    }
+    return SPH_OK;
+}
+
+int Engine::enqueue_substep(uint32_t* launches) {
+    int status = enqueue_grid(launches);
+    if (status != SPH_OK) {
+        return status;
+    }
+    uint32_t n = total_count_;
+    SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_));
+    SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_));
+    if (launches != nullptr) {
+        *launches += 2;
+    }
+    return SPH_OK;
+}
+
+int Engine::ensure_graph() {
+    if (graph_ != nullptr && graph_count_ == total_count_) {
+        return SPH_OK;
+    }
+    if (graph_ != nullptr) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    SPH_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    uint32_t launches = 0;
+    int status = enqueue_substep(&launches);
+    cudaError_t end = cudaStreamEndCapture(stream_, &graph);
+    if (status != SPH_OK) {
+        if (graph != nullptr) {
+            cudaGraphDestroy(graph);
+        }
+        return status;
+    }
+    if (end != cudaSuccess) {
+        return fail(end, "cudaStreamEndCapture");
+    }
+    cudaError_t inst = cudaGraphInstantiate(&graph_, graph, 0);
+    cudaGraphDestroy(graph);
+    if (inst != cudaSuccess) {
+        graph_ = nullptr;
+        return fail(inst, "cudaGraphInstantiate");
+    }
+    graph_count_ = total_count_;
+    launches_per_substep_ = launches;
+    return SPH_OK;
+}
+
+int Engine::run(float dt, uint32_t substeps) {
+    if (!(dt > 0.0F) || !std::isfinite(dt)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (total_count_ == 0 || substeps == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = refresh_constants(dt);
+    if (status != SPH_OK) {
+        return status;
+    }
+    status = ensure_graph();
+    if (status != SPH_OK) {
+        return status;
+    }
+    for (uint32_t s = 0; s < substeps; ++s) {
+        SPH_CUDA(cudaGraphLaunch(graph_, stream_));
+    }
+    grid_valid_ = true;
+    return SPH_OK;
+}
+
+int Engine::build_grid() {
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = refresh_constants(const_dt_ < 0.0F ? 0.0F : const_dt_);
+    if (status != SPH_OK) {
+        return status;
+    }
+    status = enqueue_grid(nullptr);
+    if (status == SPH_OK) {
+        grid_valid_ = true;
+    }
+    return status;
+}
+
+int Engine::grid_download(uint32_t tank, uint32_t* cell_of, uint32_t* cell_counts, uint32_t* cell_particles) {
+    if (tank >= tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (!grid_valid_) {
+        int status = build_grid();
+        if (status != SPH_OK) {
+            return status;
+        }
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    // The sort buffers an earlier substep left hold its result.
+    if (grid_.sorted_keys == nullptr) {
+        RadixPlan p = plan_;
+        grid_.sorted_keys = p.passes % 2 == 1 ? grid_.keys_a : grid_.keys_b;
+        grid_.sorted_ids = p.passes % 2 == 1 ? grid_.vals_a : grid_.vals_b;
+    }
+    const TankConst& t = tanks_[tank];
+    uint32_t n = t.particle_count;
+    uint32_t cells = params_[tank].lattice[3];
+    if (cell_of != nullptr && n > 0) {
+        SPH_CUDA(cudaMemcpy(cell_of, grid_.keys + t.particle_base, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < n; ++i) {
+            cell_of[i] -= t.bucket_base;
+        }
+    }
+    std::vector<uint2> table(cells);
+    SPH_CUDA(cudaMemcpy(table.data(), bucket_ + t.bucket_base, cells * sizeof(uint2), cudaMemcpyDeviceToHost));
+    if (cell_counts != nullptr) {
+        for (uint32_t b = 0; b < cells; ++b) {
+            cell_counts[b] = table[b].y - table[b].x;
+        }
+    }
+    if (cell_particles != nullptr && total_count_ > 0) {
+        std::vector<uint32_t> ids(total_count_);
+        SPH_CUDA(cudaMemcpy(ids.data(), grid_.sorted_ids, total_count_ * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint32_t b = 0; b < cells; ++b) {
+            uint32_t count = std::min(table[b].y - table[b].x, kCellCapacity);
+            for (uint32_t k = 0; k < count; ++k) {
+                cell_particles[static_cast<size_t>(b) * kCellCapacity + k] = ids[table[b].x + k] - t.particle_base;
+            }
+        }
+    }
+    return SPH_OK;
+}
+
+int Engine::stats(uint32_t tank, sph_stats* out, bool with_pairs) {
+    if (tank >= tanks_.size() || out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::memset(out, 0, sizeof(*out));
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = refresh_constants(const_dt_ < 0.0F ? 0.0F : const_dt_);
+    if (status != SPH_OK) {
+        return status;
+    }
+    uint32_t n = total_count_;
+    SPH_CUDA(cudaMemsetAsync(stats_acc_, 0, sizeof(double) * kStatsPerTank * tanks_.size(), stream_));
+    SPH_CUDA(launch_stats(pos_, vel_, tank_of_, d_tanks_, n, stats_acc_, stream_));
+    StepCounters counters{};
+    uint32_t bucket_info[2] = {0, 0};
+    if (with_pairs && n > 0) {
+        status = enqueue_grid(nullptr);
+        if (status != SPH_OK) {
+            return status;
+        }
+        grid_valid_ = true;
+        SPH_CUDA(cudaMemsetAsync(counters_, 0, sizeof(StepCounters), stream_));
+        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, counters_, stream_));
+        SPH_CUDA(cudaMemsetAsync(bucket_stats_, 0, 2 * sizeof(uint32_t), stream_));
+        SPH_CUDA(launch_bucket_stats(bucket_ + tanks_[tank].bucket_base, params_[tank].lattice[3], bucket_stats_,
+                                     stream_));
+        SPH_CUDA(cudaMemcpyAsync(&counters, counters_, sizeof(StepCounters), cudaMemcpyDeviceToHost, stream_));
+        SPH_CUDA(cudaMemcpyAsync(bucket_info, bucket_stats_, sizeof(bucket_info), cudaMemcpyDeviceToHost, stream_));
+    }
+    std::vector<double> acc(kStatsPerTank * tanks_.size());
+    SPH_CUDA(cudaMemcpyAsync(acc.data(), stats_acc_, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    const double* a = acc.data() + static_cast<size_t>(tank) * kStatsPerTank;
+    double count = a[8];
+    out->particles = tanks_[tank].particle_count;
+    out->buckets = params_[tank].lattice[3];
+    out->max_bucket_count = bucket_info[0];
+    out->overflow_buckets = bucket_info[1];
+    out->candidates = tanks_.size() == 1 ? counters.candidates : 0;
+    out->pairs_in_range = tanks_.size() == 1 ? counters.in_range : 0;
+    if (count > 0) {
+        out->mean_density = a[0] / count;
+        out->mean_compression = a[1] / count;
+        out->centre_of_mass[0] = a[3] / count;
+        out->centre_of_mass[1] = a[4] / count;
+        out->centre_of_mass[2] = a[5] / count;
+    }
+    uint64_t bits = 0;
+    std::memcpy(&bits, &a[2], sizeof(bits));
+    std::memcpy(&out->max_density, &bits, sizeof(bits));
+    out->kinetic_energy = a[6];
+    out->nonfinite = static_cast<uint32_t>(a[7]);
+    return SPH_OK;
+}
+
+int Engine::synchronize() {
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+int Engine::set_active(const std::vector<uint8_t>& active) {
+    if (active.size() != tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    for (size_t t = 0; t < tanks_.size(); ++t) {
+        tanks_[t].active = active[t] != 0 ? 1U : 0U;
+    }
+    consts_dirty_ = true;
+    return SPH_OK;
+}
+
+int Engine::set_radix_bits(uint32_t bits) {
+    if (bits < 1 || bits > kRadixMaxBits) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    radix_bits_ = bits;
+    plan_ = plan_radix(bit_width(total_buckets_ - 1U), radix_bits_);
+    if (graph_ != nullptr) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    grid_.sorted_keys = nullptr;
+    grid_.sorted_ids = nullptr;
+    grid_valid_ = false;
+    return SPH_OK;
+}
+
+int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
+    if (phase_ms == nullptr || !(dt > 0.0F)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    for (uint32_t k = 0; k < kProfilePhases; ++k) {
+        phase_ms[k] = 0.0;
+    }
+    if (total_count_ == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = refresh_constants(dt);
+    if (status != SPH_OK) {
+        return status;
+    }
+    if (events_[0] == nullptr) {
+        for (cudaEvent_t& e : events_) {
+            SPH_CUDA(cudaEventCreate(&e));
+        }
+    }
+    uint32_t n = total_count_;
+    for (uint32_t s = 0; s < substeps; ++s) {
+        SPH_CUDA(cudaEventRecord(events_[0], stream_));
+        SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
+        SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
+        SPH_CUDA(cudaEventRecord(events_[1], stream_));
+        SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, nullptr));
+        SPH_CUDA(cudaEventRecord(events_[2], stream_));
+        SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_,
+                                      svel_, stank_, stream_));
+        SPH_CUDA(cudaEventRecord(events_[3], stream_));
+        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_));
+        SPH_CUDA(cudaEventRecord(events_[4], stream_));
+        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_));
+        SPH_CUDA(cudaEventRecord(events_[5], stream_));
+        SPH_CUDA(cudaEventSynchronize(events_[5]));
+        for (uint32_t k = 0; k < kProfilePhases; ++k) {
+            float ms = 0.0F;
+            SPH_CUDA(cudaEventElapsedTime(&ms, events_[k], events_[k + 1]));
+            phase_ms[k] += ms;
+        }
+    }
+    grid_valid_ = true;
+    return SPH_OK;
+}
+
+}  // namespace sph

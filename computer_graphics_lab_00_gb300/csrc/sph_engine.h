@@ -1,0 +1,115 @@
+// sph_engine.h — host-side owner of the device state of one or more tanks.
+//
+// A tank is one independent fluid (the reference's FluidSolver,
+// src/physics/fluid_sph.h:101-127). The engine keeps all tanks' particles in
+// one id-ordered array (tank t owns [particle_base, particle_base + count)),
+// and all tanks' bucket tables in one global table (tank t owns
+// [bucket_base, bucket_base + cells)). One substep advances every active
+// tank with the same kernel launches; a single tank is the case T = 1.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sph_c.h"
+#include "sph_kernels.h"
+
+namespace sph {
+
+// Host restatements of the reference's parameter rules.
+uint32_t fluid_substeps(const sph_params& params, float delta_seconds);  // fluid_sph.cpp:128-136
+TankConst make_tank_const(const sph_params& params, float dt);           // constants of one tank
+int validate_params(const sph_params& params);
+
+class Engine {
+public:
+    ~Engine();
+
+    // Allocates for `tanks` tanks with the given capacities (particles) and
+    // bucket counts. Returns a status code.
+    int init(int device, const std::vector<sph_params>& params, const std::vector<uint32_t>& capacities);
+
+    int set_params(uint32_t tank, const sph_params& params);
+    int upload(uint32_t tank, const float* pos, const float* vel, uint32_t count);
+    int download(uint32_t tank, float* pos, float* vel);
+    int download_previous(uint32_t tank, float* pos);
+    int keep_rendered();
+    int emit(uint32_t tank, uint32_t count);
+
+    // Enqueues `substeps` substeps of length dt for every active tank.
+    int run(float dt, uint32_t substeps);
+    // Grid build only (for inspection).
+    int build_grid();
+    int grid_download(uint32_t tank, uint32_t* cell_of, uint32_t* cell_counts, uint32_t* cell_particles);
+    int stats(uint32_t tank, sph_stats* out, bool with_pairs);
+    int synchronize();
+    int set_active(const std::vector<uint8_t>& active);
+    int set_radix_bits(uint32_t bits);
+    // Runs substeps without the graph, timing each phase with CUDA events on
+    // the context stream: keys, sort, bounds+gather, density, integrate.
+    static constexpr uint32_t kProfilePhases = 5;
+    int profile(float dt, uint32_t substeps, double* phase_ms);
+
+    uint32_t tank_count() const { return static_cast<uint32_t>(tanks_.size()); }
+    uint32_t count(uint32_t tank) const { return tanks_[tank].particle_count; }
+    uint32_t total_count() const { return total_count_; }
+    const sph_params& params(uint32_t tank) const { return params_[tank]; }
+    uint32_t launches_per_substep() const { return launches_per_substep_; }
+    uint64_t device_bytes() const { return device_bytes_; }
+    cudaStream_t stream() const { return stream_; }
+    float4* positions() const { return pos_; }
+    float4* velocities() const { return vel_; }
+    const char* last_error() const { return last_error_.c_str(); }
+    // Records a CUDA failure and maps it to a status code.
+    int fail(cudaError_t error, const char* what);
+
+private:
+    int enqueue_grid(uint32_t* launches);
+    int enqueue_substep(uint32_t* launches);
+    int refresh_constants(float dt);
+    int ensure_graph();
+    void release();
+    template <typename T> int alloc(T** ptr, size_t count);
+
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    std::vector<sph_params> params_;
+    std::vector<TankConst> tanks_;
+    std::vector<uint32_t> capacity_;
+    uint32_t total_capacity_ = 0;
+    uint32_t total_count_ = 0;
+    uint32_t total_buckets_ = 0;
+    uint32_t radix_bits_ = 7;
+    RadixPlan plan_{};
+    float const_dt_ = -1.0f;
+    bool consts_dirty_ = true;
+
+    TankConst* d_tanks_ = nullptr;
+    float4* pos_ = nullptr;
+    float4* vel_ = nullptr;
+    float4* prev_ = nullptr;
+    uint16_t* tank_of_ = nullptr;  // null when there is one tank
+    uint16_t* stank_ = nullptr;
+    GridScratch grid_{};
+    uint2* bucket_ = nullptr;
+    float4* spos_ = nullptr;
+    float4* spos2_ = nullptr;
+    float4* svel_ = nullptr;
+    StepCounters* counters_ = nullptr;
+    double* stats_acc_ = nullptr;
+    uint32_t* bucket_stats_ = nullptr;
+    uint64_t device_bytes_ = 0;
+
+    cudaGraphExec_t graph_ = nullptr;
+    uint32_t graph_count_ = 0xFFFFFFFFu;
+    uint32_t launches_per_substep_ = 0;
+    bool grid_valid_ = false;
+    uint32_t nonfinite_host_ = 0;
+    cudaEvent_t events_[kProfilePhases + 1] = {};
+    std::string last_error_;
+};
+
+}  // namespace sph

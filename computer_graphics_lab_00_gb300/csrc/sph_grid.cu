@@ -1,0 +1,292 @@
+// sph_grid.cu — spatial-hash grid build on the GPU.
+//
+// The reference inserts particles serially in ascending id into fixed
+// 32-slot buckets (src/physics/fluid_sph.cpp:160-188) so that every bucket
+// lists its particles in id order, and its Vulkan twin does the same insert
+// with one atomic per particle (shaders/fluid_grid.comp:9-21), which loses
+// that order. Here the grid is a stable counting sort instead: keys are
+// bucket indices, an LSD radix sort over (key, id) keeps ids ascending inside
+// every bucket, and a bounds pass turns the sorted keys into a
+// (start, end) table. The first min(count, 32) ids of a bucket are exactly
+// the reference's cellParticles slots and end - start is its un-truncated
+// cellCounts entry.
+//
+// Digit histograms use warp-aggregated shared-memory atomics
+// (__match_any_sync groups lanes with the same digit; one lane adds the
+// group's population). Ranks inside a tile come from the same match masks,
+// so the sort is stable without any per-element atomics in global memory.
+#include "sph_kernels.h"
+
+namespace sph {
+
+namespace {
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t mask;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(mask));
+    return mask;
+}
+
+__global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ pos, const uint16_t* __restrict__ tank_of,
+                                                   const TankConst* __restrict__ tanks, uint32_t n,
+                                                   uint32_t* __restrict__ keys) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (tank_of != nullptr ? tank_of[i] : 0);
+    float h = __ldg(&t->h);
+    float4 p = pos[i];
+    uint32_t cx = static_cast<uint32_t>(cell_coord(p.x, h));
+    uint32_t cy = static_cast<uint32_t>(cell_coord(p.y, h));
+    uint32_t cz = static_cast<uint32_t>(cell_coord(p.z, h));
+    keys[i] = __ldg(&t->bucket_base) + spatial_hash(cx, cy, cz, __ldg(&t->cell_mask));
+}
+
+// Per-tile digit histogram, written digit-major: hist[d * tiles + tile].
+__global__ void __launch_bounds__(kRadixThreads) radix_upsweep(const uint32_t* __restrict__ keys, uint32_t n,
+                                                               uint32_t shift, uint32_t mask, uint32_t tiles,
+                                                               uint32_t* __restrict__ hist) {
+    __shared__ uint32_t counts[kRadixMaxBins];
+    for (uint32_t d = threadIdx.x; d <= mask; d += blockDim.x) {
+        counts[d] = 0;
+    }
+    __syncthreads();
+    uint32_t warp = threadIdx.x >> 5;
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t base = blockIdx.x * kRadixTile + warp * (kRadixItems * 32);
+#pragma unroll 4
+    for (uint32_t r = 0; r < kRadixItems; ++r) {
+        uint32_t idx = base + r * 32 + lane;
+        bool valid = idx < n;
+        uint32_t digit = valid ? (keys[idx] >> shift) & mask : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) {
+            atomicAdd(&counts[digit], static_cast<uint32_t>(__popc(peers)));
+        }
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d <= mask; d += blockDim.x) {
+        hist[d * tiles + blockIdx.x] = counts[d];
+    }
+}
+
+// Exclusive scan of m counters in one block (m is bins x tiles, at most a
+// few hundred thousand).
+__global__ void __launch_bounds__(1024) scan_exclusive_block(uint32_t* __restrict__ data, uint32_t m) {
+    __shared__ uint32_t warp_sums[32];
+    uint32_t per = (m + blockDim.x - 1) / blockDim.x;
+    uint32_t begin = threadIdx.x * per;
+    uint32_t end = min(begin + per, m);
+    uint32_t sum = 0;
+    for (uint32_t i = begin; i < end; ++i) {
+        sum += data[i];
+    }
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t warp = threadIdx.x >> 5;
+    uint32_t inclusive = sum;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
+        if (lane >= o) {
+            inclusive += v;
+        }
+    }
+    if (lane == 31) {
+        warp_sums[warp] = inclusive;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
+        uint32_t inc = v;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) {
+                inc += u;
+            }
+        }
+        warp_sums[lane] = inc - v;
+    }
+    __syncthreads();
+    uint32_t run = warp_sums[warp] + inclusive - sum;
+    for (uint32_t i = begin; i < end; ++i) {
+        uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+}
+
+// Stable scatter of one radix pass. Warp w of a tile owns 512 consecutive
+// keys and walks them in 16 rounds of 32, so (round, lane) is input order;
+// the per-warp digit counters give each key its rank among equal digits
+// before it, and a prefix over warps makes the rank tile-wide.
+__global__ void __launch_bounds__(kRadixThreads) radix_downsweep(const uint32_t* __restrict__ keys_in,
+                                                                 const uint32_t* __restrict__ vals_in,
+                                                                 uint32_t* __restrict__ keys_out,
+                                                                 uint32_t* __restrict__ vals_out, uint32_t n,
+                                                                 uint32_t shift, uint32_t mask, uint32_t tiles,
+                                                                 const uint32_t* __restrict__ hist) {
+    constexpr uint32_t kWarps = kRadixThreads / 32;
+    __shared__ uint32_t warp_counts[kWarps][kRadixMaxBins];
+    __shared__ uint32_t tile_offset[kRadixMaxBins];
+    for (uint32_t k = threadIdx.x; k < kWarps * kRadixMaxBins; k += blockDim.x) {
+        (&warp_counts[0][0])[k] = 0;
+    }
+    __syncthreads();
+    uint32_t warp = threadIdx.x >> 5;
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t below = lanemask_lt();
+    uint32_t base = blockIdx.x * kRadixTile + warp * (kRadixItems * 32);
+    uint32_t key[kRadixItems];
+    uint32_t val[kRadixItems];
+    uint32_t rank[kRadixItems];
+#pragma unroll
+    for (uint32_t r = 0; r < kRadixItems; ++r) {
+        uint32_t idx = base + r * 32 + lane;
+        bool valid = idx < n;
+        key[r] = valid ? keys_in[idx] : 0;
+        val[r] = valid ? (vals_in != nullptr ? vals_in[idx] : idx) : 0;
+        uint32_t digit = valid ? (key[r] >> shift) & mask : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        uint32_t before = valid ? warp_counts[warp][digit] : 0;
+        rank[r] = valid ? before + static_cast<uint32_t>(__popc(peers & below)) : 0xFFFFFFFFu;
+        __syncwarp();
+        if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) {
+            warp_counts[warp][digit] = before + static_cast<uint32_t>(__popc(peers));
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d <= mask; d += blockDim.x) {
+        uint32_t running = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < kWarps; ++w) {
+            uint32_t c = warp_counts[w][d];
+            warp_counts[w][d] = running;
+            running += c;
+        }
+        tile_offset[d] = hist[d * tiles + blockIdx.x];
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t r = 0; r < kRadixItems; ++r) {
+        if (rank[r] != 0xFFFFFFFFu) {
+            uint32_t digit = (key[r] >> shift) & mask;
+            uint32_t dst = tile_offset[digit] + warp_counts[warp][digit] + rank[r];
+            keys_out[dst] = key[r];
+            vals_out[dst] = val[r];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __restrict__ sorted_keys,
+                                                            const uint32_t* __restrict__ sorted_ids, uint32_t n,
+                                                            uint32_t* __restrict__ bucket_words,
+                                                            const float4* __restrict__ pos,
+                                                            const float4* __restrict__ vel,
+                                                            const uint16_t* __restrict__ tank_of,
+                                                            float4* __restrict__ spos, float4* __restrict__ svel,
+                                                            uint16_t* __restrict__ stank) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) {
+        return;
+    }
+    uint32_t key = sorted_keys[p];
+    if (p == 0 || sorted_keys[p - 1] != key) {
+        bucket_words[2 * static_cast<size_t>(key)] = p;
+    }
+    if (p + 1 == n || sorted_keys[p + 1] != key) {
+        bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
+    }
+    uint32_t i = sorted_ids[p];
+    spos[p] = pos[i];
+    svel[p] = vel[i];
+    if (tank_of != nullptr) {
+        stank[p] = tank_of[i];
+    }
+}
+
+}  // namespace
+
+RadixPlan plan_radix(uint32_t key_bits, uint32_t digit_bits) {
+    RadixPlan plan;
+    digit_bits = digit_bits < 1 ? 1 : (digit_bits > kRadixMaxBits ? kRadixMaxBits : digit_bits);
+    if (key_bits == 0) {
+        key_bits = 1;
+    }
+    uint32_t passes = (key_bits + digit_bits - 1) / digit_bits;
+    if (passes > 8) {
+        passes = 8;
+    }
+    // Spread the bits evenly so no pass carries a nearly empty digit.
+    uint32_t shift = 0;
+    for (uint32_t p = 0; p < passes; ++p) {
+        uint32_t remaining = key_bits - shift;
+        uint32_t width = (remaining + (passes - p) - 1) / (passes - p);
+        plan.shift[p] = shift;
+        plan.bits[p] = width;
+        shift += width;
+    }
+    plan.passes = passes;
+    return plan;
+}
+
+cudaError_t launch_keys(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n, uint32_t* keys,
+                        cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    keys_kernel<<<(n + 255) / 256, 256, 0, stream>>>(pos, tank_of, tanks, n, keys);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_radix_sort(GridScratch& s, uint32_t n, const RadixPlan& plan, cudaStream_t stream,
+                              uint32_t* launches) {
+    if (n == 0) {
+        s.sorted_keys = s.keys_a;
+        s.sorted_ids = s.vals_a;
+        return cudaSuccess;
+    }
+    uint32_t tiles = radix_tiles(n);
+    const uint32_t* kin = s.keys;
+    const uint32_t* vin = nullptr;
+    uint32_t* kout = s.keys_a;
+    uint32_t* vout = s.vals_a;
+    for (uint32_t p = 0; p < plan.passes; ++p) {
+        uint32_t mask = (1u << plan.bits[p]) - 1u;
+        radix_upsweep<<<tiles, kRadixThreads, 0, stream>>>(kin, n, plan.shift[p], mask, tiles, s.hist);
+        scan_exclusive_block<<<1, 1024, 0, stream>>>(s.hist, (mask + 1) * tiles);
+        radix_downsweep<<<tiles, kRadixThreads, 0, stream>>>(kin, vin, kout, vout, n, plan.shift[p], mask, tiles,
+                                                             s.hist);
+        if (launches != nullptr) {
+            *launches += 3;
+        }
+        kin = kout;
+        vin = vout;
+        if (kout == s.keys_a) {
+            kout = s.keys_b;
+            vout = s.vals_b;
+        } else {
+            kout = s.keys_a;
+            vout = s.vals_a;
+        }
+    }
+    s.sorted_keys = kin;
+    s.sorted_ids = vin;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
+                                 const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
+                                 float4* svel, uint16_t* stank, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    bounds_gather_kernel<<<(n + 255) / 256, 256, 0, stream>>>(sorted_keys, sorted_ids, n,
+                                                              reinterpret_cast<uint32_t*>(bucket), pos, vel, tank_of,
+                                                              spos, svel, stank);
+    return cudaGetLastError();
+}
+
+}  // namespace sph

@@ -1,0 +1,91 @@
+// sph_kernels.h — launchers of the SPH step's CUDA kernels (sm_103a).
+//
+// Pipeline of one substep (src/physics/fluid_sph.cpp:190-309), all on one
+// stream, state in HBM:
+//   keys        pos (id order)           -> key[i] = bucket of particle i
+//   radix sort  (key, id) stable LSD     -> ids in (bucket, id) order
+//   bounds      sorted keys              -> bucket table (start, end)
+//   gather      pos, vel by sorted id    -> cell-ordered copies
+//   density     27-bucket poly6 sum      -> rho, pressure (cell order)
+//   integrate   27-bucket forces + walls -> pos, vel (id order, in place)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+constexpr uint32_t kRadixThreads = 256;
+constexpr uint32_t kRadixItems = 16;
+constexpr uint32_t kRadixTile = kRadixThreads * kRadixItems;  // 4096 keys per tile
+constexpr uint32_t kRadixMaxBits = 8;
+constexpr uint32_t kRadixMaxBins = 1u << kRadixMaxBits;
+
+inline uint32_t radix_tiles(uint32_t n) { return (n + kRadixTile - 1) / kRadixTile; }
+
+// One pass plan of the LSD radix sort over keys of `key_bits` bits.
+struct RadixPlan {
+    uint32_t passes = 0;
+    uint32_t shift[8] = {};
+    uint32_t bits[8] = {};
+};
+RadixPlan plan_radix(uint32_t key_bits, uint32_t digit_bits);
+
+// Scratch of the grid build. Sizes: n for the key/id arrays, tiles *
+// kRadixMaxBins for the histogram.
+struct GridScratch {
+    uint32_t* keys = nullptr;    // id order: bucket of particle i
+    uint32_t* keys_a = nullptr;  // radix ping-pong
+    uint32_t* vals_a = nullptr;
+    uint32_t* keys_b = nullptr;
+    uint32_t* vals_b = nullptr;
+    uint32_t* hist = nullptr;
+    // Results of the last sort (point into a or b).
+    const uint32_t* sorted_keys = nullptr;
+    const uint32_t* sorted_ids = nullptr;
+};
+
+cudaError_t launch_keys(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n, uint32_t* keys,
+                        cudaStream_t stream);
+
+// Stable LSD radix sort of (keys, implicit ids 0..n-1). Sets
+// scratch.sorted_keys / sorted_ids. `launches` counts kernels enqueued.
+cudaError_t launch_radix_sort(GridScratch& scratch, uint32_t n, const RadixPlan& plan, cudaStream_t stream,
+                              uint32_t* launches);
+
+// Bucket table (start, end) from sorted keys (table pre-zeroed) and the
+// cell-ordered copies of position, velocity and tank id.
+cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
+                                 const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
+                                 float4* svel, uint16_t* stank, cudaStream_t stream);
+
+// Density and pressure (fluid_sph.cpp:200-222). Writes spos2 = (xyz, rho)
+// and svel[p].w = pressure. `counters` may be null (no pair counting).
+cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, const uint2* bucket, const TankConst* tanks,
+                           const uint16_t* stank, uint32_t n, StepCounters* counters, cudaStream_t stream);
+
+// Forces, semi-implicit Euler, speed clamp and walls (fluid_sph.cpp:225-305).
+// Writes the id-order state.
+cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
+                             const TankConst* tanks, const uint16_t* stank, uint32_t n, float4* pos, float4* vel,
+                             cudaStream_t stream);
+
+// FluidSolver::emit lattice (fluid_sph.cpp:138-154) for particles
+// [first, first + count) of one tank.
+cudaError_t launch_emit(const TankConst* tank, uint32_t first, uint32_t count, float4* pos, float4* vel, float4* prev,
+                        cudaStream_t stream);
+
+// FP64 per-tank statistics of the id-order state. acc holds 10 doubles per
+// tank: sum rho, sum compression, max rho (as bits), com xyz, kinetic,
+// nonfinite count, count.
+constexpr uint32_t kStatsPerTank = 10;
+cudaError_t launch_stats(const float4* pos, const float4* vel, const uint16_t* tank_of, const TankConst* tanks,
+                         uint32_t n, double* acc, cudaStream_t stream);
+// Counts particles whose position or velocity xyz is not finite (adds to *out).
+cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_t n, uint32_t* out, cudaStream_t stream);
+// Largest bucket count and number of buckets above capacity.
+cudaError_t launch_bucket_stats(const uint2* bucket, uint32_t buckets, uint32_t* out2, cudaStream_t stream);
+
+}  // namespace sph

@@ -1,0 +1,224 @@
+"""Seeded synthetic workloads for the SPH step.
+
+No public dataset exists for this path, so every case is generated here:
+
+* the reference's emit lattice (src/physics/fluid_sph.cpp:138-154) placed as
+  a block whose lower corner sits one spacing inside the container, then
+* a per-axis uniform jitter of +-1e-4 m drawn from splitmix64
+  (the mixer of src/gfx/neural_math.cpp:18-24) keyed by (seed, 3*i + axis),
+  using its top 24 bits as a uniform in [0, 1).
+
+All float arithmetic is numpy float32, one rounding per operation, in the
+order the reference writes it, so the same case is bit-identical on x86-64
+and aarch64 hosts.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .abi import SphParams
+
+GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+MIX1 = np.uint64(0xBF58476D1CE4E5B9)
+MIX2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(values: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser over a uint64 array (wrapping arithmetic)."""
+    v = np.asarray(values, dtype=np.uint64).copy()
+    with np.errstate(over="ignore"):
+        v += GOLDEN
+        v = (v ^ (v >> np.uint64(30))) * MIX1
+        v = (v ^ (v >> np.uint64(27))) * MIX2
+    return v ^ (v >> np.uint64(31))
+
+
+def uniform01(seed: int, index: np.ndarray) -> np.ndarray:
+    """[0, 1) float32 from the top 24 bits of splitmix64(seed * golden + index)."""
+    with np.errstate(over="ignore"):
+        key = np.uint64(seed) * GOLDEN + np.asarray(index, dtype=np.uint64)
+    bits = splitmix64(key) >> np.uint64(40)
+    return bits.astype(np.float32) * np.float32(1.0 / 16777216.0)
+
+
+def bit_ceil(x: int) -> int:
+    return 1 if x <= 1 else 1 << (int(x) - 1).bit_length()
+
+
+def cell_count_for(particles: int) -> int:
+    """gfx::cellCountFor (src/gfx/fluid.cpp:50-52)."""
+    return min(max(bit_ceil(max(particles, 1) * 2), 1024), 65536)
+
+
+def cell_count_uncapped(particles: int) -> int:
+    """cellCountFor without the 65536 ceiling (tanks beyond the reference's cap)."""
+    return max(bit_ceil(max(particles, 1) * 2), 1024)
+
+
+def translation(t) -> list[float]:
+    """Column-major mat4 of a translation (glm::translate(mat4{1}, t))."""
+    m = [0.0] * 16
+    m[0] = m[5] = m[10] = m[15] = 1.0
+    m[12], m[13], m[14] = float(t[0]), float(t[1]), float(t[2])
+    return m
+
+
+def make_params(
+    *,
+    container_min,
+    container_max,
+    lattice,
+    cell_count: int,
+    spacing: float = 0.02,
+    smoothing_radius: float = 0.04,
+    rest_density: float = 1000.0,
+    stiffness: float = 50.0,
+    viscosity: float = 0.5,
+    gravity=(0.0, -9.81, 0.0),
+    emitter_world=None,
+    restitution: float = 0.3,
+) -> SphParams:
+    """A parameter block following deriveFluidParams (fluid_sph.cpp:65-100)."""
+    f32 = np.float32
+    s = f32(spacing)
+    p = SphParams()
+    if emitter_world is None:
+        # Block whose lower corner is one spacing inside container_min.
+        centre = [
+            f32(container_min[a]) + s + f32(lattice[a] - 1) * s * f32(0.5) for a in range(3)
+        ]
+        emitter_world = translation(centre)
+    for k in range(16):
+        p.emitter_world[k] = float(f32(emitter_world[k]))
+    for a in range(3):
+        p.emitter_half_extents[a] = float(f32(lattice[a]) * s * f32(0.5))
+        p.container_min[a] = float(container_min[a])
+        p.container_max[a] = float(container_max[a])
+        p.gravity[a] = float(gravity[a])
+        p.lattice[a] = int(lattice[a])
+    p.emitter_half_extents[3] = float(s)
+    p.container_min[3] = float(s * f32(0.5))
+    p.container_max[3] = float(f32(restitution))
+    rho0 = f32(rest_density)
+    p.gravity[3] = float(rho0 * s * s * s)
+    p.smoothing_radius = float(max(f32(smoothing_radius), s))
+    p.rest_density = float(rho0)
+    p.stiffness = float(stiffness)
+    p.viscosity = float(viscosity)
+    p.lattice[3] = int(cell_count)
+    return p
+
+
+def emit_positions(params: SphParams, count: int) -> np.ndarray:
+    """FluidSolver::emit lattice positions (N, 4) float32, w = rest density."""
+    f32 = np.float32
+    cx, cy, cz = (max(int(params.lattice[a]), 1) for a in range(3))
+    s = f32(params.emitter_half_extents[3])
+    i = np.arange(count, dtype=np.uint64)
+    index = [i % np.uint64(cx), (i // np.uint64(cx)) % np.uint64(cy), i // np.uint64(cx * cy)]
+    counts = (cx, cy, cz)
+    local = []
+    for a in range(3):
+        extent = f32(counts[a] - 1) * s * f32(0.5)
+        local.append(index[a].astype(np.float32) * s - extent)
+    m = np.array(params.emitter_world[:], dtype=np.float32).reshape(4, 4)  # m[col][row]
+    out = np.empty((count, 4), dtype=np.float32)
+    one = f32(1.0)
+    for r in range(3):
+        add0 = m[0, r] * local[0] + m[1, r] * local[1]
+        add1 = m[2, r] * local[2] + m[3, r] * one
+        out[:, r] = add0 + add1
+    out[:, 3] = f32(params.rest_density)
+    return out
+
+
+def jitter(count: int, seed: int, amplitude: float = 1e-4) -> np.ndarray:
+    """(N, 3) float32 uniform in [-amplitude, +amplitude) from splitmix64(seed, 3i+axis)."""
+    idx = np.arange(3 * count, dtype=np.uint64)
+    u = uniform01(seed, idx).reshape(count, 3)
+    return (u - np.float32(0.5)) * np.float32(2.0 * amplitude)
+
+
+def jittered_block(params: SphParams, count: int, seed: int = 0, amplitude: float = 1e-4):
+    """Positions (N,4) and zero velocities (N,4) of a jittered emit lattice."""
+    pos = emit_positions(params, count)
+    pos[:, :3] += jitter(count, seed, amplitude)
+    vel = np.zeros((count, 4), dtype=np.float32)
+    return pos, vel
+
+
+@dataclass
+class Case:
+    """One single-tank workload: constants, particle count, step size and length."""
+
+    name: str
+    params: SphParams
+    count: int
+    dt: float
+    steps: int
+    seed: int = 0
+    notes: str = ""
+    extra: dict = field(default_factory=dict)
+
+    def initial_state(self):
+        return jittered_block(self.params, self.count, self.seed)
+
+
+def dam_break_16k(seed: int = 0) -> Case:
+    """Dam break, 16,384 particles in a 1 m box at s = 0.02, h = 0.04, dt = 1/600.
+
+    The stated 0.32 x 0.64 x 0.32 m block holds 8,192 particles; the count is
+    authoritative, so the reference's overflow rule (extra layers stack along
+    z, fluid_sph.h:59) gives a 16 x 32 x 32 lattice.
+    """
+    n = 16384
+    params = make_params(
+        container_min=(0.0, 0.0, 0.0),
+        container_max=(1.0, 1.0, 1.0),
+        lattice=(16, 32, 32),
+        cell_count=cell_count_for(n),
+    )
+    return Case("dam_break_16k", params, n, 1.0 / 600.0, 600, seed,
+                "lattice 16x32x32 at 0.02 m, box [0,1]^3, C=32768")
+
+
+def dam_break_1m(seed: int = 0) -> Case:
+    """Dam break, 1,048,576 particles in a 4 x 2 x 2 m box at s = 0.02, h = 0.04.
+
+    The stated 1.28 x 1.28 x 0.64 m block holds 131,072 particles; keeping the
+    spacing and the count gives a 192 x 64 x 86 lattice (last z layer
+    partial). The bucket count is bit_ceil(2N) = 2^21 without the
+    reference's 65,536 ceiling, which would overflow the 32-slot buckets.
+    """
+    n = 1 << 20
+    params = make_params(
+        container_min=(0.0, 0.0, 0.0),
+        container_max=(4.0, 2.0, 2.0),
+        lattice=(192, 64, 86),
+        cell_count=cell_count_uncapped(n),
+    )
+    return Case("dam_break_1m", params, n, 1.0 / 600.0, 1000, seed,
+                "lattice 192x64x86 at 0.02 m, box 4x2x2 m, C=2^21")
+
+
+def reference_test_scene(count: int = 1024, cell_count: int = 1024) -> SphParams:
+    """The scene of the reference's fluid test (tests/fluid_test.cpp:19-32):
+    scene::Fluid defaults, emitter at (0, 1, 0)."""
+    f32 = np.float32
+    r = f32(0.025)
+    spacing = r * f32(2.0)
+    half = f32(0.5)
+    along = max(1, int(math.floor(float(half * f32(2.0) / spacing))))
+    nz = max(1, (count + along * along - 1) // (along * along))
+    return make_params(
+        container_min=(-1.0, 0.0, -1.0),
+        container_max=(1.0, 2.0, 1.0),
+        lattice=(along, along, nz),
+        cell_count=cell_count,
+        spacing=float(spacing),
+        smoothing_radius=0.1,
+        emitter_world=translation((0.0, 1.0, 0.0)),
+    )

@@ -1,0 +1,221 @@
+/*
+ * sph_c.h — C ABI of the GB300 SPH fluid step.
+ *
+ * This is the drop-in boundary for the reference's CPU fluid solver
+ * (`physics::FluidSolver`, src/physics/fluid_sph.h:101-127) and for the
+ * parameter block its Vulkan twin uploads (`gfx::GpuFluidParams`,
+ * src/gfx/fluid.h:81-102). Everything here is plain C: pointers, sizes and
+ * status codes. No CUDA or torch type crosses it.
+ *
+ * Conventions
+ *   - Every call returns an `int` status: SPH_OK (0) or a negative
+ *     `sph_status`. No call aborts the process.
+ *   - Host pointers are owned by the caller. Device buffers are owned by the
+ *     context. Particle arrays are the reference's AoS float4 layout:
+ *     positions (x, y, z, density) and velocities (vx, vy, vz, pressure),
+ *     `4*n` floats each, particles in id order.
+ *   - A context owns one CUDA stream. A context is not thread-safe; distinct
+ *     contexts are independent.
+ *   - Calls that launch work enqueue it on the context stream. Calls that
+ *     return host data synchronise that stream first.
+ */
+#ifndef SPH_C_H
+#define SPH_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+/* Bucket capacity of the hash grid (src/physics/fluid_sph.h:23). */
+#define SPH_CELL_CAPACITY 32u
+/* Array sizes of the parameter block (fluid_sph.h:22, force_field.h:17). */
+#define SPH_MAX_COLLIDERS 8u
+#define SPH_MAX_FORCE_FIELDS 8u
+/* Longest frame a step catches up on (fluid_sph.h:76). */
+#define SPH_MAX_FRAME_STEP (1.0f / 30.0f)
+
+typedef enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_INVALID_ARGUMENT = -1,
+    SPH_ERR_CAPACITY = -2,
+    SPH_ERR_CUDA = -3,
+    SPH_ERR_OUT_OF_MEMORY = -4,
+    SPH_ERR_UNSUPPORTED = -5,
+    SPH_ERR_TIMEOUT = -6,
+    SPH_ERR_NO_DEVICE = -7,
+    SPH_ERR_NONFINITE = -8
+} sph_status;
+
+/* One shape collider; layout of gfx::GpuFluidCollider (fluid.h:50-58). */
+typedef struct sph_collider {
+    float data0[4];          /* xyz half extents, w radius */
+    float inverse_world[16]; /* column-major */
+    float world[16];         /* column-major */
+    uint32_t type;           /* scene::ColliderShape: 0 sphere, 1 box, 2 plane, 3 cylinder, 4 capsule */
+    uint32_t pad[3];
+} sph_collider;
+
+/* One force field; layout of gfx::GpuForceField (fluid.h:61-68). */
+typedef struct sph_force_field {
+    float position_radius[4]; /* xyz centre, w radius (0 = unbounded) */
+    float axis_strength[4];   /* xyz direction or axis, w strength */
+    float falloff;
+    uint32_t type; /* 0 wind, 1 vortex, 2 point */
+    uint32_t pad[2];
+} sph_force_field;
+
+/*
+ * Simulation constants; scalar layout of gfx::GpuFluidParams
+ * (fluid.h:81-102), which carries physics::FluidParams (fluid_sph.h:42-67).
+ */
+typedef struct sph_params {
+    float emitter_world[16];       /* column-major mat4 */
+    float emitter_half_extents[4]; /* xyz half extents, w lattice spacing */
+    float container_min[4];        /* xyz, w particle radius */
+    float container_max[4];        /* xyz, w wall restitution */
+    float gravity[4];              /* xyz, w particle mass */
+    float smoothing_radius;
+    float rest_density;
+    float stiffness;
+    float viscosity;
+    uint32_t lattice[4]; /* xyz emit lattice counts, w bucket count (power of two) */
+    uint32_t collider_count;
+    uint32_t pad0, pad1, pad2;
+    sph_collider colliders[SPH_MAX_COLLIDERS];
+    uint32_t field_count;
+    uint32_t field_pad0, field_pad1, field_pad2;
+    sph_force_field fields[SPH_MAX_FORCE_FIELDS];
+} sph_params;
+
+/* The physics fields of scene::Fluid (src/scene/scene.h:186-218). */
+typedef struct sph_fluid_settings {
+    float emitter_half_extents[3];
+    float particle_radius;
+    float smoothing_radius;
+    float rest_density;
+    float stiffness;
+    float viscosity;
+    float container_min[3];
+    float container_max[3];
+    float gravity[3];
+} sph_fluid_settings;
+
+/* Per-substep statistics; FP64 reductions on the device. */
+typedef struct sph_stats {
+    uint32_t particles;
+    uint32_t buckets;
+    uint32_t max_bucket_count;  /* largest un-truncated bucket count */
+    uint32_t overflow_buckets;  /* buckets holding more than SPH_CELL_CAPACITY */
+    uint64_t candidates;        /* neighbour candidates visited by density */
+    uint64_t pairs_in_range;    /* candidates with squared distance < h^2 */
+    double mean_density;
+    double mean_compression;    /* mean over particles of max(0, rho - rho0) / rho0 */
+    double max_density;
+    double centre_of_mass[3];
+    double kinetic_energy;
+    uint32_t nonfinite;         /* particles with a non-finite position or velocity */
+    uint32_t pad;
+} sph_stats;
+
+typedef struct sph_ctx sph_ctx;
+
+/* ---- version and diagnostics ---------------------------------------- */
+
+/* ABI version of the loaded library (SPH_ABI_VERSION). */
+int sph_abi_version(void);
+/* Static, human-readable text for a status code. */
+const char* sph_status_string(int status);
+/* Text of the last CUDA error a context saw ("" if none). */
+const char* sph_last_error(const sph_ctx* ctx);
+
+/* ---- host-side parameter rules (no device needed) -------------------- */
+
+/* physics::deriveFluidParams (fluid_sph.cpp:65-100); no colliders or fields. */
+int sph_derive_params(const sph_fluid_settings* settings,
+                      const float emitter_world[16],
+                      uint32_t particle_count,
+                      uint32_t cell_count,
+                      sph_params* out);
+/* physics::fluidSubsteps (fluid_sph.cpp:128-136). */
+int sph_fluid_substeps(const sph_params* params, float delta_seconds, uint32_t* substeps);
+/* gfx::cellCountFor (src/gfx/fluid.cpp:50-52): clamp(bit_ceil(2n), 1024, 65536). */
+uint32_t sph_cell_count_for(uint32_t particles);
+/* Same rule without the 65536 ceiling, for tanks beyond the reference's cap. */
+uint32_t sph_cell_count_uncapped(uint32_t particles);
+
+/* ---- context lifetime ------------------------------------------------- */
+
+/* Allocates device state for up to `capacity` particles on `device`. */
+int sph_create(const sph_params* params, uint32_t capacity, int device, sph_ctx** out);
+int sph_destroy(sph_ctx* ctx);
+/* Replaces the constants; the bucket count may change (up to the context's
+ * bucket capacity, chosen at create as max(lattice[3], uncapped(capacity))). */
+int sph_set_params(sph_ctx* ctx, const sph_params* params);
+int sph_particle_count(const sph_ctx* ctx, uint32_t* count);
+
+/* ---- physics::FluidSolver surface ------------------------------------- */
+
+/* FluidSolver::emit (fluid_sph.cpp:138-154), on the device. */
+int sph_emit(sph_ctx* ctx, uint32_t count);
+/* Uploads `count` particles (host AoS float4). `velocities` may be NULL (zeros). */
+int sph_upload(sph_ctx* ctx, const float* positions, const float* velocities, uint32_t count);
+/* Downloads the current state (host AoS float4). Either pointer may be NULL. */
+int sph_download(sph_ctx* ctx, float* positions, float* velocities);
+/* FluidSolver::step (fluid_sph.cpp:311-321): splits the frame with fluidSubsteps. */
+int sph_step(sph_ctx* ctx, float delta_seconds);
+/* FluidSolver::substep (fluid_sph.cpp:190-309): one grid + density + integrate pass. */
+int sph_substep(sph_ctx* ctx, float dt);
+/* FluidSolver::keepRendered (fluid_sph.cpp:156-158). */
+int sph_keep_rendered(sph_ctx* ctx);
+/* FluidSolver::previousParticles (fluid_sph.h:112): host AoS float4. */
+int sph_download_previous(sph_ctx* ctx, float* positions);
+/* Waits for all work queued on the context stream. */
+int sph_synchronize(sph_ctx* ctx);
+
+/* ---- grid of the last substep, in physics::FluidGrid form ------------- */
+
+/*
+ * FluidGrid::build output (fluid_sph.cpp:160-188) for the positions the last
+ * substep started from: cell_of[n], cell_counts[C] (un-truncated) and
+ * cell_particles[C*32] (ids ascending per bucket, first 32 kept; slots past
+ * a bucket's count are left untouched). Any pointer may be NULL.
+ */
+int sph_grid_download(sph_ctx* ctx, uint32_t* cell_of, uint32_t* cell_counts, uint32_t* cell_particles);
+/* Builds the grid for the current positions without stepping. */
+int sph_grid_build(sph_ctx* ctx);
+
+/* ---- statistics -------------------------------------------------------- */
+
+/* Reduces statistics of the current state (FP64 on the device). */
+int sph_stats_compute(sph_ctx* ctx, sph_stats* out);
+
+/* ---- device-resident access (for callers that keep data in HBM) ------- */
+
+/* The context's cudaStream_t, as an opaque pointer. */
+int sph_stream(sph_ctx* ctx, void** stream);
+/* Device pointers to the current positions and velocities (AoS float4,
+ * id order). They change after every substep (ping-pong); fetch again. */
+int sph_device_state(sph_ctx* ctx, void** positions, void** velocities);
+/* Enqueues `substeps` substeps of `dt` without host synchronisation. */
+int sph_run(sph_ctx* ctx, float dt, uint32_t substeps);
+/* Runs `substeps` substeps without the CUDA graph and adds the device time of
+ * each phase, measured with CUDA events on the context stream, to
+ * phase_ms[0..4]: keys, radix sort, bounds + gather, density, integrate.
+ * Synchronises. Results are identical to sph_run. */
+#define SPH_PROFILE_PHASES 5
+int sph_profile_substeps(sph_ctx* ctx, float dt, uint32_t substeps, double* phase_ms);
+/* Number of kernel launches one substep enqueues. */
+int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches);
+/* Bytes of device memory the context holds. */
+int sph_device_bytes(const sph_ctx* ctx, uint64_t* bytes);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* SPH_C_H */

@@ -1,0 +1,679 @@
+// sph_oracle.cpp — CPU oracle of the reference's SPH fluid step.
+//
+// TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+// baseline. Every function names the reference lines it restates. Built with
+// -ffp-contract=off -fno-fast-math so that each float operation is rounded
+// once, in the order the reference writes it (GCC on aarch64 would otherwise
+// fuse a*b+c into one FMA).
+#include "sph_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// std::numbers::pi_v<float> (fluid_sph.cpp:20).
+constexpr float PI = 3.14159265358979323846F;
+// fluid_sph.cpp:22: chunk size of every parallel loop.
+constexpr uint32_t GRANULARITY = 256;
+constexpr uint32_t CAPACITY = SPH_CELL_CAPACITY;
+
+struct V3 {
+    float x, y, z;
+};
+
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 scale(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline V3 divide(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+// glm::dot for vec3: (x*x' + y*y') + z*z'.
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// glm::length: sqrt(dot(v, v)).
+inline float length(V3 a) { return std::sqrt(dot(a, a)); }
+inline V3 xyz(const float* v4) { return {v4[0], v4[1], v4[2]}; }
+
+struct Cell {
+    int32_t x, y, z;
+};
+
+// spatial_hash.h:12-14: ivec3(floor(p / h)), division per component.
+inline Cell spatialCell(V3 p, float h) {
+    return {static_cast<int32_t>(std::floor(p.x / h)), static_cast<int32_t>(std::floor(p.y / h)),
+            static_cast<int32_t>(std::floor(p.z / h))};
+}
+
+// spatial_hash.h:16-20.
+inline uint32_t spatialHash(Cell c, uint32_t cellCount) {
+    uint32_t hashed = static_cast<uint32_t>(c.x) * 73856093U ^ static_cast<uint32_t>(c.y) * 19349663U ^
+                      static_cast<uint32_t>(c.z) * 83492791U;
+    return hashed & (cellCount - 1U);
+}
+
+// fluid_sph.cpp:24-31.
+inline float poly6(float squaredDistance, float h) {
+    float h2 = h * h;
+    if (squaredDistance >= h2) {
+        return 0.0F;
+    }
+    float d = h2 - squaredDistance;
+    return 315.0F / (64.0F * PI * std::pow(h, 9.0F)) * d * d * d;
+}
+
+// fluid_sph.cpp:33-39.
+inline V3 spikyGradient(V3 delta, float len, float h) {
+    if (len >= h || len <= 1e-6F) {
+        return {0.0F, 0.0F, 0.0F};
+    }
+    float d = h - len;
+    return scale(-45.0F / (PI * std::pow(h, 6.0F)) * d * d, divide(delta, len));
+}
+
+// fluid_sph.cpp:41-46.
+inline float viscosityLaplacian(float len, float h) {
+    if (len >= h) {
+        return 0.0F;
+    }
+    return 45.0F / (PI * std::pow(h, 6.0F)) * (h - len);
+}
+
+// force_field.h:31-60.
+V3 forceFieldAcceleration(const sph_force_field& field, V3 position) {
+    V3 offset = sub(position, {field.position_radius[0], field.position_radius[1], field.position_radius[2]});
+    float distance = length(offset);
+    float weight = 1.0F;
+    float radius = field.position_radius[3];
+    if (radius > 0.0F) {
+        float t = std::clamp(1.0F - distance / radius, 0.0F, 1.0F);
+        weight = t <= 0.0F ? 0.0F : std::pow(t, field.falloff);
+    }
+    if (weight <= 0.0F) {
+        return {0.0F, 0.0F, 0.0F};
+    }
+    V3 axis{field.axis_strength[0], field.axis_strength[1], field.axis_strength[2]};
+    float strength = field.axis_strength[3];
+    switch (field.type) {
+    case 0:
+        return scale(strength * weight, axis);
+    case 1: {
+        V3 radial = sub(offset, scale(dot(offset, axis), axis));
+        float r = length(radial);
+        if (r < 1.0e-4F) {
+            return {0.0F, 0.0F, 0.0F};
+        }
+        V3 u = divide(radial, r);
+        V3 c{axis.y * u.z - u.y * axis.z, axis.z * u.x - u.z * axis.x, axis.x * u.y - u.x * axis.y};
+        return scale(strength * weight, c);
+    }
+    case 2:
+        if (distance < 1.0e-4F) {
+            return {0.0F, 0.0F, 0.0F};
+        }
+        return scale(strength * weight, divide({-offset.x, -offset.y, -offset.z}, distance));
+    default:
+        return {0.0F, 0.0F, 0.0F};
+    }
+}
+
+// force_field.h:62-70: starts from vec3{0} and adds every field.
+V3 forceFieldsAcceleration(const sph_params& params, V3 position) {
+    V3 total{0.0F, 0.0F, 0.0F};
+    for (uint32_t i = 0; i < params.field_count && i < SPH_MAX_FORCE_FIELDS; ++i) {
+        total = add(total, forceFieldAcceleration(params.fields[i], position));
+    }
+    return total;
+}
+
+// A small persistent pool with the chunking of core::JobSystem::parallelFor
+// (job_system.cpp:80-117): ranges of `GRANULARITY` ids, any worker may take
+// any chunk. Results never depend on which worker ran a chunk.
+class Pool {
+public:
+    explicit Pool(uint32_t threads) {
+        for (uint32_t t = 1; t < threads; ++t) {
+            workers.emplace_back([this] { loop(); });
+        }
+    }
+    ~Pool() {
+        {
+            std::lock_guard<std::mutex> lock(mutex);
+            stop = true;
+            ++generation;
+        }
+        wake.notify_all();
+        for (std::thread& w : workers) {
+            w.join();
+        }
+    }
+    uint32_t size() const { return static_cast<uint32_t>(workers.size()) + 1; }
+
+    void parallelFor(uint32_t count, const std::function<void(uint32_t, uint32_t)>& body) {
+        if (workers.empty() || count <= GRANULARITY) {
+            body(0, count);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lock(mutex);
+            task = &body;
+            total = count;
+            next.store(0);
+            active = static_cast<uint32_t>(workers.size());
+            ++generation;
+        }
+        wake.notify_all();
+        drain();
+        std::unique_lock<std::mutex> lock(mutex);
+        done.wait(lock, [this] { return active == 0; });
+        task = nullptr;
+    }
+
+private:
+    void drain() {
+        for (;;) {
+            uint32_t begin = next.fetch_add(GRANULARITY);
+            if (begin >= total) {
+                return;
+            }
+            (*task)(begin, std::min(begin + GRANULARITY, total));
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> lock(mutex);
+                wake.wait(lock, [&] { return generation != seen; });
+                seen = generation;
+                if (stop) {
+                    return;
+                }
+            }
+            drain();
+            {
+                std::lock_guard<std::mutex> lock(mutex);
+                if (--active == 0) {
+                    done.notify_all();
+                }
+            }
+        }
+    }
+
+    std::vector<std::thread> workers;
+    std::mutex mutex;
+    std::condition_variable wake;
+    std::condition_variable done;
+    const std::function<void(uint32_t, uint32_t)>* task = nullptr;
+    std::atomic<uint32_t> next{0};
+    uint32_t total = 0;
+    uint32_t active = 0;
+    uint64_t generation = 0;
+    bool stop = false;
+};
+
+Pool& poolFor(uint32_t threads) {
+    static std::mutex guard;
+    static std::unique_ptr<Pool> pool;
+    std::lock_guard<std::mutex> lock(guard);
+    threads = std::max(threads, 1U);
+    if (!pool || pool->size() != threads) {
+        pool.reset();
+        pool = std::make_unique<Pool>(threads);
+    }
+    return *pool;
+}
+
+// fluid_sph.cpp:55-61.
+void forRange(uint32_t threads, uint32_t count, const std::function<void(uint32_t, uint32_t)>& body) {
+    if (threads > 1 && count > GRANULARITY) {
+        poolFor(threads).parallelFor(count, body);
+    } else {
+        body(0, count);
+    }
+}
+
+struct Grid {
+    std::vector<uint32_t> cellOf;
+    std::vector<uint32_t> cellCounts;
+    std::vector<uint32_t> cellParticles;
+    uint32_t bucketCount(uint32_t b) const { return std::min(cellCounts[b], CAPACITY); }
+    uint32_t particleAt(uint32_t b, uint32_t k) const { return cellParticles[static_cast<size_t>(b) * CAPACITY + k]; }
+};
+
+// fluid_sph.cpp:160-188.
+void buildGrid(Grid& grid, const sph_params& params, const float* positions, uint32_t count, uint32_t threads) {
+    uint32_t cells = params.lattice[3];
+    float h = params.smoothing_radius;
+    grid.cellCounts.assign(cells, 0U);
+    grid.cellParticles.resize(static_cast<size_t>(cells) * CAPACITY);
+    grid.cellOf.resize(count);
+    forRange(threads, count, [&](uint32_t begin, uint32_t end) {
+        for (uint32_t i = begin; i < end; ++i) {
+            grid.cellOf[i] = spatialHash(spatialCell(xyz(positions + 4 * static_cast<size_t>(i)), h), cells);
+        }
+    });
+    // Serial insert in ascending id: ids within a bucket stay ascending and
+    // only the first CAPACITY are kept (fluid_sph.cpp:181-187).
+    for (uint32_t i = 0; i < count; ++i) {
+        uint32_t cell = grid.cellOf[i];
+        uint32_t slot = grid.cellCounts[cell]++;
+        if (slot < CAPACITY) {
+            grid.cellParticles[static_cast<size_t>(cell) * CAPACITY + slot] = i;
+        }
+    }
+}
+
+bool validParams(const sph_params* params) {
+    if (params == nullptr) {
+        return false;
+    }
+    uint32_t cells = params->lattice[3];
+    return cells != 0 && (cells & (cells - 1)) == 0 && params->smoothing_radius > 0.0F;
+}
+
+// fluid_sph.cpp:200-222.
+void densityPass(const sph_params& params, const Grid& grid, float* pos, float* vel, uint32_t count, uint32_t threads) {
+    float h = params.smoothing_radius;
+    float mass = params.gravity[3];
+    uint32_t cells = params.lattice[3];
+    forRange(threads, count, [&](uint32_t begin, uint32_t end) {
+        for (uint32_t i = begin; i < end; ++i) {
+            V3 position = xyz(pos + 4 * static_cast<size_t>(i));
+            Cell cell = spatialCell(position, h);
+            float density = 0.0F;
+            for (int dz = -1; dz <= 1; ++dz) {
+                for (int dy = -1; dy <= 1; ++dy) {
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        uint32_t bucket = spatialHash({cell.x + dx, cell.y + dy, cell.z + dz}, cells);
+                        uint32_t n = grid.bucketCount(bucket);
+                        for (uint32_t k = 0; k < n; ++k) {
+                            uint32_t j = grid.particleAt(bucket, k);
+                            V3 delta = sub(position, xyz(pos + 4 * static_cast<size_t>(j)));
+                            density += mass * poly6(dot(delta, delta), h);
+                        }
+                    }
+                }
+            }
+            density = std::max(density, 1e-6F);
+            pos[4 * static_cast<size_t>(i) + 3] = density;
+            vel[4 * static_cast<size_t>(i) + 3] = std::max(params.stiffness * (density - params.rest_density), 0.0F);
+        }
+    });
+}
+
+// fluid_sph.cpp:225-305 (shape colliders excluded).
+void integratePass(const sph_params& params,
+                   const Grid& grid,
+                   const float* pos,
+                   const float* vel,
+                   float* nextPos,
+                   float* nextVel,
+                   uint32_t count,
+                   float dt,
+                   uint32_t threads) {
+    float h = params.smoothing_radius;
+    float mass = params.gravity[3];
+    uint32_t cells = params.lattice[3];
+    V3 gravity{params.gravity[0], params.gravity[1], params.gravity[2]};
+    float radius = params.container_min[3];
+    float restitution = params.container_max[3];
+    forRange(threads, count, [&](uint32_t begin, uint32_t end) {
+        for (uint32_t i = begin; i < end; ++i) {
+            const float* self = pos + 4 * static_cast<size_t>(i);
+            V3 position = xyz(self);
+            float density = std::max(self[3], 1e-6F);
+            V3 velocity = xyz(vel + 4 * static_cast<size_t>(i));
+            float pressure = vel[4 * static_cast<size_t>(i) + 3];
+            Cell cell = spatialCell(position, h);
+
+            V3 force{0.0F, 0.0F, 0.0F};
+            for (int dz = -1; dz <= 1; ++dz) {
+                for (int dy = -1; dy <= 1; ++dy) {
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        uint32_t bucket = spatialHash({cell.x + dx, cell.y + dy, cell.z + dz}, cells);
+                        uint32_t n = grid.bucketCount(bucket);
+                        for (uint32_t k = 0; k < n; ++k) {
+                            uint32_t j = grid.particleAt(bucket, k);
+                            if (j == i) {
+                                continue;
+                            }
+                            const float* other = pos + 4 * static_cast<size_t>(j);
+                            const float* otherVel = vel + 4 * static_cast<size_t>(j);
+                            V3 delta = sub(position, xyz(other));
+                            float distance = length(delta);
+                            if (distance >= h || distance <= 1e-6F) {
+                                continue;
+                            }
+                            float otherDensity = std::max(other[3], 1e-6F);
+                            float pressureScale = -mass * (pressure + otherVel[3]) / (2.0F * otherDensity);
+                            force = add(force, scale(pressureScale, spikyGradient(delta, distance, h)));
+                            V3 viscous = divide(scale(params.viscosity * mass, sub(xyz(otherVel), velocity)), otherDensity);
+                            float lap = viscosityLaplacian(distance, h);
+                            force = add(force, {viscous.x * lap, viscous.y * lap, viscous.z * lap});
+                        }
+                    }
+                }
+            }
+
+            V3 acceleration = add(add(divide(force, density), gravity), forceFieldsAcceleration(params, position));
+            velocity = add(velocity, {acceleration.x * dt, acceleration.y * dt, acceleration.z * dt});
+            float maxSpeed = 0.4F * h / dt;
+            float speed = length(velocity);
+            if (speed > maxSpeed) {
+                float s = maxSpeed / speed;
+                velocity = {velocity.x * s, velocity.y * s, velocity.z * s};
+            }
+            position = add(position, {velocity.x * dt, velocity.y * dt, velocity.z * dt});
+
+            float p[3] = {position.x, position.y, position.z};
+            float v[3] = {velocity.x, velocity.y, velocity.z};
+            for (int axis = 0; axis < 3; ++axis) {
+                float low = params.container_min[axis] + radius;
+                float high = params.container_max[axis] - radius;
+                if (p[axis] < low) {
+                    p[axis] = low;
+                    if (v[axis] < 0.0F) {
+                        v[axis] = -v[axis] * restitution;
+                    }
+                } else if (p[axis] > high) {
+                    p[axis] = high;
+                    if (v[axis] > 0.0F) {
+                        v[axis] = -v[axis] * restitution;
+                    }
+                }
+            }
+            float* np = nextPos + 4 * static_cast<size_t>(i);
+            float* nv = nextVel + 4 * static_cast<size_t>(i);
+            np[0] = p[0];
+            np[1] = p[1];
+            np[2] = p[2];
+            np[3] = density;
+            nv[0] = v[0];
+            nv[1] = v[1];
+            nv[2] = v[2];
+            nv[3] = pressure;
+        }
+    });
+}
+
+} // namespace
+
+extern "C" {
+
+int oracle_abi(void) { return SPH_ABI_VERSION; }
+
+uint32_t oracle_spatial_hash(int32_t cx, int32_t cy, int32_t cz, uint32_t cell_count) {
+    return spatialHash({cx, cy, cz}, cell_count);
+}
+
+void oracle_spatial_cell(const float position[3], float cell_size, int32_t out[3]) {
+    Cell c = spatialCell({position[0], position[1], position[2]}, cell_size);
+    out[0] = c.x;
+    out[1] = c.y;
+    out[2] = c.z;
+}
+
+// fluid_sph.cpp:65-100 (colliders and force fields come from a scene; none here).
+int oracle_derive_params(const sph_fluid_settings* settings,
+                         const float emitter_world[16],
+                         uint32_t particle_count,
+                         uint32_t cell_count,
+                         sph_params* out) {
+    if (settings == nullptr || emitter_world == nullptr || out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::memset(out, 0, sizeof(*out));
+    float spacing = settings->particle_radius * 2.0F;
+    std::memcpy(out->emitter_world, emitter_world, sizeof(out->emitter_world));
+    for (int a = 0; a < 3; ++a) {
+        out->emitter_half_extents[a] = settings->emitter_half_extents[a];
+        out->container_min[a] = settings->container_min[a];
+        out->container_max[a] = settings->container_max[a];
+        out->gravity[a] = settings->gravity[a];
+    }
+    out->emitter_half_extents[3] = spacing;
+    out->container_min[3] = settings->particle_radius;
+    out->container_max[3] = 0.3F;
+    out->gravity[3] = settings->rest_density * spacing * spacing * spacing;
+    out->smoothing_radius = std::max(settings->smoothing_radius, spacing);
+    out->rest_density = settings->rest_density;
+    out->stiffness = settings->stiffness;
+    out->viscosity = settings->viscosity;
+    auto along = [spacing](float half) {
+        return std::max(1U, static_cast<uint32_t>(std::floor(half * 2.0F / spacing)));
+    };
+    uint32_t nx = along(settings->emitter_half_extents[0]);
+    uint32_t ny = along(settings->emitter_half_extents[1]);
+    uint32_t nz = std::max(1U, (particle_count + nx * ny - 1) / (nx * ny));
+    out->lattice[0] = nx;
+    out->lattice[1] = ny;
+    out->lattice[2] = nz;
+    out->lattice[3] = cell_count;
+    return SPH_OK;
+}
+
+// fluid_sph.cpp:128-136.
+uint32_t oracle_fluid_substeps(const sph_params* params, float delta_seconds) {
+    float h = params->smoothing_radius;
+    float gravity = std::max(length({params->gravity[0], params->gravity[1], params->gravity[2]}), 0.1F);
+    float stable = std::min(0.4F * h / std::sqrt(std::max(params->stiffness, 1.0F)), 0.25F * std::sqrt(h / gravity));
+    float frameStep = std::min(std::max(delta_seconds, 0.0F), SPH_MAX_FRAME_STEP);
+    auto steps = static_cast<uint32_t>(std::ceil(frameStep / std::max(stable, 1e-5F)));
+    return std::clamp(steps, 1U, 8U);
+}
+
+// fluid_sph.cpp:138-154. glm's mat4 * vec4 sums the columns as
+// (c0*x + c1*y) + (c2*z + c3*w).
+void oracle_emit(const sph_params* params, uint32_t count, float* positions, float* velocities) {
+    uint32_t cx = std::max(params->lattice[0], 1U);
+    uint32_t cy = std::max(params->lattice[1], 1U);
+    uint32_t cz = std::max(params->lattice[2], 1U);
+    float spacing = params->emitter_half_extents[3];
+    float extent[3] = {static_cast<float>(cx - 1U) * spacing * 0.5F, static_cast<float>(cy - 1U) * spacing * 0.5F,
+                       static_cast<float>(cz - 1U) * spacing * 0.5F};
+    const float* m = params->emitter_world;
+    for (uint32_t i = 0; i < count; ++i) {
+        uint32_t index[3] = {i % cx, (i / cx) % cy, i / (cx * cy)};
+        float local[4];
+        for (int a = 0; a < 3; ++a) {
+            local[a] = static_cast<float>(index[a]) * spacing - extent[a];
+        }
+        local[3] = 1.0F;
+        float* p = positions + 4 * static_cast<size_t>(i);
+        for (int r = 0; r < 3; ++r) {
+            float add0 = m[0 * 4 + r] * local[0] + m[1 * 4 + r] * local[1];
+            float add1 = m[2 * 4 + r] * local[2] + m[3 * 4 + r] * local[3];
+            p[r] = add0 + add1;
+        }
+        p[3] = params->rest_density;
+        if (velocities != nullptr) {
+            float* v = velocities + 4 * static_cast<size_t>(i);
+            v[0] = v[1] = v[2] = v[3] = 0.0F;
+        }
+    }
+}
+
+int oracle_grid_build(const sph_params* params,
+                      const float* positions,
+                      uint32_t count,
+                      uint32_t* cell_of,
+                      uint32_t* cell_counts,
+                      uint32_t* cell_particles,
+                      uint32_t threads) {
+    if (!validParams(params) || (count > 0 && positions == nullptr)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    Grid grid;
+    buildGrid(grid, *params, positions, count, threads);
+    if (cell_of != nullptr) {
+        std::memcpy(cell_of, grid.cellOf.data(), grid.cellOf.size() * sizeof(uint32_t));
+    }
+    if (cell_counts != nullptr) {
+        std::memcpy(cell_counts, grid.cellCounts.data(), grid.cellCounts.size() * sizeof(uint32_t));
+    }
+    if (cell_particles != nullptr) {
+        uint32_t cells = params->lattice[3];
+        for (uint32_t b = 0; b < cells; ++b) {
+            uint32_t n = grid.bucketCount(b);
+            for (uint32_t k = 0; k < n; ++k) {
+                cell_particles[static_cast<size_t>(b) * CAPACITY + k] = grid.particleAt(b, k);
+            }
+        }
+    }
+    return SPH_OK;
+}
+
+int oracle_density(const sph_params* params, float* positions, float* velocities, uint32_t count, uint32_t threads) {
+    if (!validParams(params)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    Grid grid;
+    buildGrid(grid, *params, positions, count, threads);
+    densityPass(*params, grid, positions, velocities, count, threads);
+    return SPH_OK;
+}
+
+// fluid_sph.cpp:190-309.
+int oracle_substep(const sph_params* params, float* positions, float* velocities, uint32_t count, float dt, uint32_t threads) {
+    if (!validParams(params)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (count == 0) {
+        return SPH_OK;
+    }
+    Grid grid;
+    buildGrid(grid, *params, positions, count, threads);
+    densityPass(*params, grid, positions, velocities, count, threads);
+    std::vector<float> nextPos(4 * static_cast<size_t>(count));
+    std::vector<float> nextVel(4 * static_cast<size_t>(count));
+    integratePass(*params, grid, positions, velocities, nextPos.data(), nextVel.data(), count, dt, threads);
+    std::memcpy(positions, nextPos.data(), nextPos.size() * sizeof(float));
+    std::memcpy(velocities, nextVel.data(), nextVel.size() * sizeof(float));
+    return SPH_OK;
+}
+
+// fluid_sph.cpp:311-321.
+int oracle_step(const sph_params* params,
+                float* positions,
+                float* velocities,
+                uint32_t count,
+                float delta_seconds,
+                uint32_t threads) {
+    if (!validParams(params)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (count == 0 || delta_seconds <= 0.0F) {
+        return SPH_OK;
+    }
+    uint32_t substeps = oracle_fluid_substeps(params, delta_seconds);
+    float frameStep = std::min(delta_seconds, SPH_MAX_FRAME_STEP);
+    float dt = frameStep / static_cast<float>(substeps);
+    for (uint32_t s = 0; s < substeps; ++s) {
+        int status = oracle_substep(params, positions, velocities, count, dt, threads);
+        if (status != SPH_OK) {
+            return status;
+        }
+    }
+    return SPH_OK;
+}
+
+int oracle_pair_counts(const sph_params* params,
+                       const float* positions,
+                       uint32_t count,
+                       uint64_t* candidates,
+                       uint64_t* in_range,
+                       uint32_t threads) {
+    if (!validParams(params)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    Grid grid;
+    buildGrid(grid, *params, positions, count, threads);
+    float h = params->smoothing_radius;
+    float h2 = h * h;
+    uint32_t cells = params->lattice[3];
+    std::atomic<uint64_t> p{0};
+    std::atomic<uint64_t> q{0};
+    forRange(threads, count, [&](uint32_t begin, uint32_t end) {
+        uint64_t lp = 0;
+        uint64_t lq = 0;
+        for (uint32_t i = begin; i < end; ++i) {
+            V3 position = xyz(positions + 4 * static_cast<size_t>(i));
+            Cell cell = spatialCell(position, h);
+            for (int dz = -1; dz <= 1; ++dz) {
+                for (int dy = -1; dy <= 1; ++dy) {
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        uint32_t bucket = spatialHash({cell.x + dx, cell.y + dy, cell.z + dz}, cells);
+                        uint32_t n = grid.bucketCount(bucket);
+                        lp += n;
+                        for (uint32_t k = 0; k < n; ++k) {
+                            V3 delta = sub(position, xyz(positions + 4 * static_cast<size_t>(grid.particleAt(bucket, k))));
+                            lq += dot(delta, delta) < h2 ? 1 : 0;
+                        }
+                    }
+                }
+            }
+        }
+        p += lp;
+        q += lq;
+    });
+    if (candidates != nullptr) {
+        *candidates = p.load();
+    }
+    if (in_range != nullptr) {
+        *in_range = q.load();
+    }
+    return SPH_OK;
+}
+
+int oracle_stats(const sph_params* params, const float* positions, const float* velocities, uint32_t count, sph_stats* out) {
+    if (params == nullptr || out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::memset(out, 0, sizeof(*out));
+    out->particles = count;
+    out->buckets = params->lattice[3];
+    double rho0 = params->rest_density;
+    double mass = params->gravity[3];
+    double sumRho = 0.0;
+    double sumCompression = 0.0;
+    double maxRho = 0.0;
+    double com[3] = {0.0, 0.0, 0.0};
+    double kinetic = 0.0;
+    uint32_t nonfinite = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* p = positions + 4 * static_cast<size_t>(i);
+        const float* v = velocities + 4 * static_cast<size_t>(i);
+        bool finite = std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]) && std::isfinite(v[0]) &&
+                      std::isfinite(v[1]) && std::isfinite(v[2]);
+        nonfinite += finite ? 0 : 1;
+        double rho = p[3];
+        sumRho += rho;
+        sumCompression += std::max(0.0, rho - rho0) / rho0;
+        maxRho = std::max(maxRho, rho);
+        for (int a = 0; a < 3; ++a) {
+            com[a] += p[a];
+        }
+        kinetic += 0.5 * mass * (static_cast<double>(v[0]) * v[0] + static_cast<double>(v[1]) * v[1] +
+                                 static_cast<double>(v[2]) * v[2]);
+    }
+    if (count > 0) {
+        out->mean_density = sumRho / count;
+        out->mean_compression = sumCompression / count;
+        for (int a = 0; a < 3; ++a) {
+            out->centre_of_mass[a] = com[a] / count;
+        }
+    }
+    out->max_density = maxRho;
+    out->kinetic_energy = kinetic;
+    out->nonfinite = nonfinite;
+    return SPH_OK;
+}
+
+uint32_t oracle_hardware_threads(void) { return std::max(1U, std::thread::hardware_concurrency()); }
+
+} // extern "C"

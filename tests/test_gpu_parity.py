@@ -1,0 +1,246 @@
+"""CUDA path vs the CPU oracle, through the C ABI (libsph_gb300.so).
+
+Bar: bit-exact. Grid keys, bucket counts and bucket order are integer work;
+density, pressure, positions and velocities are compared by their IEEE bit
+patterns, because the kernels perform the reference's float operations in
+the reference's order (src/physics/fluid_sph.cpp:190-309).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from computer_graphics_lab_00_gb300 import abi
+from computer_graphics_lab_00_gb300 import workloads as W
+from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def assert_bit_exact(gpu, ref, what: str) -> None:
+    g, r = bits(gpu), bits(ref)
+    if not np.array_equal(g, r):
+        bad = np.argwhere(g != r)
+        i = tuple(bad[0])
+        raise AssertionError(
+            f"{what}: {len(bad)} words differ; first at {i}: gpu {np.asarray(gpu)[i]!r} oracle {np.asarray(ref)[i]!r}"
+        )
+
+
+def assert_grid_equal(gpu_grid, ref_grid) -> None:
+    cell_of, counts, slots = gpu_grid
+    o_cell_of, o_counts, o_slots = ref_grid
+    np.testing.assert_array_equal(cell_of, o_cell_of)
+    np.testing.assert_array_equal(counts, o_counts)
+    filled = np.minimum(counts, 32)
+    used = (np.arange(32)[None, :] < filled[:, None]).reshape(-1)
+    np.testing.assert_array_equal(slots[used], o_slots[used])
+
+
+def small_block(n: int, lattice, box=(0.6, 0.6, 0.6), cells=None, seed=1):
+    params = W.make_params(
+        container_min=(0.0, 0.0, 0.0),
+        container_max=box,
+        lattice=lattice,
+        cell_count=cells or W.cell_count_for(n),
+    )
+    pos, vel = W.jittered_block(params, n, seed)
+    return params, pos, vel
+
+
+@pytest.fixture(scope="module")
+def case16k():
+    case = W.dam_break_16k()
+    pos, vel = case.initial_state()
+    return case, pos, vel
+
+
+def test_grid_bit_exact_16k(native, oracle, case16k):
+    case, pos, vel = case16k
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        solver.build_grid()
+        assert_grid_equal(solver.grid(), oracle.grid_build(case.params, pos))
+
+
+def test_one_substep_bit_exact_16k(native, oracle, case16k):
+    case, pos, vel = case16k
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        solver.substep(case.dt)
+        gp, gv = solver.state()
+        # The grid the substep used is the one built from its start positions.
+        assert_grid_equal(solver.grid(), oracle.grid_build(case.params, pos))
+    op, ov = oracle.substep(case.params, pos, vel, case.dt, threads=oracle.hardware_threads)
+    assert_bit_exact(gp[:, 3], op[:, 3], "density")
+    assert_bit_exact(gv[:, 3], ov[:, 3], "pressure")
+    assert_bit_exact(gp, op, "positions")
+    assert_bit_exact(gv, ov, "velocities")
+
+
+def test_dam_break_16k_600_steps_bit_exact(native, oracle, case16k):
+    """The whole 16,384-particle dam break (dt = 1/600, 600 steps) stays
+    bit-identical to the oracle, so its density and centre-of-mass
+    statistics are identical too."""
+    case, pos, vel = case16k
+    threads = oracle.hardware_threads
+    op, ov = pos, vel
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        for chunk in range(6):
+            solver.run(case.dt, 100)
+            op, ov = oracle.run_substeps(case.params, op, ov, case.dt, 100, threads=threads)
+            gp, gv = solver.state()
+            assert_bit_exact(gp, op, f"positions after {(chunk + 1) * 100} steps")
+            assert_bit_exact(gv, ov, f"velocities after {(chunk + 1) * 100} steps")
+        gs = solver.stats()
+    os_ = oracle.stats(case.params, op, ov)
+    assert gs.mean_density == pytest.approx(os_.mean_density, rel=1e-12)
+    for a in range(3):
+        assert gs.centre_of_mass[a] == pytest.approx(os_.centre_of_mass[a], rel=1e-12)
+    assert gs.nonfinite == 0
+
+
+def test_reference_scene_emit_and_frames(native, oracle):
+    """tests/fluid_test.cpp:130-150 scene: emit, then frames of 1/60 s (3 substeps each)."""
+    params = W.reference_test_scene(1024)
+    with FluidSolverGpu(params, 1024) as solver:
+        solver.emit(params, 1024)
+        gp, gv = solver.state()
+        op, ov = oracle.emit(params, 1024)
+        assert_bit_exact(gp, op, "emit positions")
+        assert_bit_exact(solver.previous_particles()[:, :3], op[:, :3], "previous after emit")
+        for _ in range(30):
+            solver.step(params, 1.0 / 60.0)
+        gp, gv = solver.state()
+    op, ov = oracle.step(params, op, ov, 1.0 / 60.0, frames=30)
+    assert_bit_exact(gp, op, "positions after 30 frames")
+    assert_bit_exact(gv, ov, "velocities after 30 frames")
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 33, 127, 4095, 4096, 4097, 10007])
+def test_ragged_counts_bit_exact(native, oracle, n):
+    lattice = (16, 16, max(1, (n + 255) // 256))
+    params, pos, vel = small_block(n, lattice)
+    with FluidSolverGpu(params, n) as solver:
+        solver.upload(pos, vel)
+        solver.run(1.0 / 600.0, 3)
+        gp, gv = solver.state()
+        assert_grid_equal(solver.grid(), oracle.grid_build(params, oracle.run_substeps(params, pos, vel, 1 / 600.0, 2)[0]))
+    op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 3)
+    assert_bit_exact(gp, op, f"positions n={n}")
+    assert_bit_exact(gv, ov, f"velocities n={n}")
+
+
+def test_overflowing_bucket_keeps_first_32_ids(native, oracle):
+    """More than 32 particles in one cell: only the first 32 by id are
+    neighbours (fluid_sph.cpp:179-187); counts stay un-truncated."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
+                           lattice=(4, 4, 8), cell_count=1024)
+    rng = np.random.default_rng(7)
+    n = 300
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = (0.5 + rng.uniform(0.0, 0.039, size=(n, 3))).astype(np.float32)  # one 0.04 m cell
+    pos[200:, :3] = rng.uniform(0.1, 0.9, size=(100, 3)).astype(np.float32)
+    pos[:, 3] = 1000.0
+    vel = np.zeros((n, 4), np.float32)
+    with FluidSolverGpu(params, n) as solver:
+        solver.upload(pos, vel)
+        solver.build_grid()
+        grid = solver.grid()
+        ref = oracle.grid_build(params, pos)
+        assert_grid_equal(grid, ref)
+        assert grid[1].max() >= 200
+        solver.substep(1.0 / 600.0)
+        gp, gv = solver.state()
+    op, ov = oracle.substep(params, pos, vel, 1.0 / 600.0)
+    assert_bit_exact(gp, op, "positions with an overflowing bucket")
+    assert_bit_exact(gv, ov, "velocities with an overflowing bucket")
+
+
+def test_hash_collisions_and_duplicate_buckets(native, oracle):
+    """With few buckets, neighbour cells collide and the same bucket is
+    visited twice for one particle; the reference counts it twice and so
+    must the kernels."""
+    n = 8192
+    params, pos, vel = small_block(n, (16, 16, 32), box=(0.5, 0.8, 0.8), cells=1024)
+    with FluidSolverGpu(params, n) as solver:
+        solver.upload(pos, vel)
+        solver.run(1.0 / 600.0, 5)
+        gp, gv = solver.state()
+    op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 5, threads=oracle.hardware_threads)
+    assert_bit_exact(gp, op, "positions with collisions")
+    assert_bit_exact(gv, ov, "velocities with collisions")
+
+
+def test_pair_counts_match_oracle(native, oracle, case16k):
+    case, pos, vel = case16k
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        st = solver.stats()
+    p, q = oracle.pair_counts(case.params, pos)
+    assert st.candidates == p
+    assert st.pairs_in_range == q
+
+
+def test_1m_grid_and_two_substeps_bit_exact(native, oracle):
+    """The 1,048,576-particle dam break (C = 2^21): grid and two substeps."""
+    case = W.dam_break_1m()
+    pos, vel = case.initial_state()
+    threads = oracle.hardware_threads
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        solver.build_grid()
+        assert_grid_equal(solver.grid(), oracle.grid_build(case.params, pos, threads=threads))
+        solver.run(case.dt, 2)
+        gp, gv = solver.state()
+    op, ov = oracle.run_substeps(case.params, pos, vel, case.dt, 2, threads=threads)
+    assert_bit_exact(gp, op, "1M positions")
+    assert_bit_exact(gv, ov, "1M velocities")
+
+
+def test_gpu_runs_are_deterministic(native):
+    case = W.dam_break_16k()
+    pos, vel = case.initial_state()
+    out = []
+    for _ in range(2):
+        with FluidSolverGpu(case.params, case.count) as solver:
+            solver.upload(pos, vel)
+            solver.run(case.dt, 50)
+            out.append(solver.state())
+    assert_bit_exact(out[0][0], out[1][0], "run-to-run positions")
+    assert_bit_exact(out[0][1], out[1][1], "run-to-run velocities")
+
+
+def test_errors_are_status_codes(native):
+    case = W.dam_break_16k()
+    bad = case.params.copy()
+    bad.lattice[3] = 1000  # not a power of two
+    with pytest.raises(abi.SphError) as e:
+        FluidSolverGpu(bad, 16)
+    assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
+    with FluidSolverGpu(case.params, 16) as solver:
+        pos = np.zeros((17, 4), np.float32)
+        with pytest.raises(abi.SphError) as e:
+            solver.upload(pos)
+        assert e.value.status == abi.SPH_ERR_CAPACITY
+        pos = np.zeros((4, 4), np.float32)
+        pos[2, 1] = np.nan
+        with pytest.raises(abi.SphError) as e:
+            solver.upload(pos)
+        assert e.value.status == abi.SPH_ERR_NONFINITE
+        solver.upload(np.zeros((0, 4), np.float32))
+        solver.step(case.params, 1.0 / 60.0)  # empty: no-op, like FluidSolver::step
+        assert solver.particles().shape == (0, 4)
+        with pytest.raises(abi.SphError) as e:
+            solver.substep(-1.0)
+        assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
+    coll = case.params.copy()
+    coll.collider_count = 1
+    with pytest.raises(abi.SphError) as e:
+        FluidSolverGpu(coll, 16)
+    assert e.value.status == abi.SPH_ERR_UNSUPPORTED

@@ -1,0 +1,102 @@
+"""Pins the oracle to the reference itself: the reference's unmodified
+src/physics/fluid_sph.cpp, compiled here against the glm/scene stand-ins
+(oracle/ref), must produce the oracle's bits exactly. Skipped where the
+reference tree is absent."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from computer_graphics_lab_00_gb300 import abi
+from computer_graphics_lab_00_gb300 import workloads as W
+
+
+@pytest.fixture(scope="module")
+def reference(reference_available):
+    if not reference_available:
+        pytest.skip("reference tree not present; the oracle is pinned by tests/golden instead")
+    from oracle.bind import Reference
+
+    return Reference
+
+
+def same_bits(a, b) -> bool:
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
+
+
+def test_grid_matches_reference_16k(oracle, reference):
+    case = W.dam_break_16k()
+    pos, _ = case.initial_state()
+    got = oracle.grid_build(case.params, pos, threads=4)
+    want = reference().grid_build(case.params, pos, threads=4)
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g, w)
+
+
+def test_substeps_match_reference_16k(oracle, reference):
+    case = W.dam_break_16k()
+    pos, vel = case.initial_state()
+    ref = reference()
+    ref.set_state(pos, vel)
+    for _ in range(8):
+        ref.substep(case.params, case.dt, threads=4)
+    op, ov = oracle.run_substeps(case.params, pos, vel, case.dt, 8, threads=4)
+    rp, rv = ref.state()
+    assert same_bits(op, rp)
+    assert same_bits(ov, rv)
+
+
+def test_reference_scene_frames_and_emit(oracle, reference):
+    """tests/fluid_test.cpp's scene: emit, then 150 frames of 1/60 s."""
+    params = W.reference_test_scene(1024)
+    ref = reference()
+    ref.emit(params, 1024)
+    op, ov = oracle.emit(params, 1024)
+    rp, rv = ref.state()
+    assert same_bits(op, rp) and same_bits(ov, rv)
+    assert same_bits(ref.previous()[:, :3], op[:, :3])
+    ref.step(params, 1.0 / 60.0, threads=1, frames=150)
+    op, ov = oracle.step(params, op, ov, 1.0 / 60.0, threads=4, frames=150)
+    rp, rv = ref.state()
+    assert same_bits(op, rp)
+    assert same_bits(ov, rv)
+
+
+def test_collisions_and_overflow_match_reference(oracle, reference):
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(0.5, 0.8, 0.8),
+                           lattice=(16, 16, 32), cell_count=1024)
+    pos, vel = W.jittered_block(params, 8192, seed=5)
+    pos[:300, :3] = (0.25 + np.random.default_rng(1).uniform(0, 0.039, (300, 3))).astype(np.float32)
+    ref = reference()
+    ref.set_state(pos, vel)
+    for _ in range(3):
+        ref.substep(params, 1.0 / 600.0, threads=2)
+    op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 3, threads=3)
+    rp, rv = ref.state()
+    assert same_bits(op, rp) and same_bits(ov, rv)
+
+
+@pytest.mark.parametrize("dt", [0.0, 1 / 1200, 1 / 600, 1 / 240, 1 / 60, 1.0])
+def test_substep_rule_matches_reference(oracle, reference, dt):
+    for case in (W.dam_break_16k(), ):
+        assert oracle.fluid_substeps(case.params, dt) == reference().fluid_substeps(case.params, dt)
+    params = W.reference_test_scene(1024)
+    assert oracle.fluid_substeps(params, dt) == reference().fluid_substeps(params, dt)
+
+
+def test_derive_params_matches_reference(oracle, reference):
+    s = abi.SphFluidSettings()
+    for a in range(3):
+        s.emitter_half_extents[a] = 0.4
+        s.container_min[a] = -1.0
+        s.container_max[a] = 1.0
+    s.container_min[1] = 0.0
+    s.container_max[1] = 2.0
+    s.particle_radius, s.smoothing_radius, s.rest_density = 0.025, 0.1, 1000.0
+    s.stiffness, s.viscosity = 50.0, 0.5
+    s.gravity[1] = -9.81
+    world = W.translation((0.0, 1.0, 0.0))
+    for count in (100, 512, 1024, 5000):
+        got = oracle.derive_params(s, world, count, 1024)
+        want = reference().derive_params(s, np.array(world, np.float32), count, 1024)
+        assert bytes(got) == bytes(want)
