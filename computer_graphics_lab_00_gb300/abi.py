@@ -116,6 +116,19 @@ class SphFluidSettings(ctypes.Structure):
     ]
 
 
+class SphTuning(ctypes.Structure):
+    _fields_ = [
+        ("radix_bits", ctypes.c_uint32),
+        ("neighbour_kernel", ctypes.c_uint32),
+        ("block_size", ctypes.c_uint32),
+        ("queue_depth", ctypes.c_uint32),
+        ("schedule", ctypes.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+
 class SphStats(ctypes.Structure):
     _fields_ = [
         ("particles", ctypes.c_uint32),
@@ -210,6 +223,9 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_device_state": (c_int, [c_void_p, P(c_void_p), P(c_void_p)]),
         "sph_run": (c_int, [c_void_p, c_f32, c_u32]),
         "sph_profile_substeps": (c_int, [c_void_p, c_f32, c_u32, P(ctypes.c_double)]),
+        "sph_get_tuning": (c_int, [c_void_p, P(SphTuning)]),
+        "sph_set_tuning": (c_int, [c_void_p, P(SphTuning)]),
+        "sph_selftest_division": (c_int, [c_void_p, ctypes.c_uint64, ctypes.c_uint64, c_int, P(ctypes.c_uint64)]),
         "sph_launches_per_substep": (c_int, [c_void_p, u32p]),
         "sph_device_bytes": (c_int, [c_void_p, P(ctypes.c_uint64)]),
     }

@@ -272,6 +272,48 @@ int sph_profile_substeps(sph_ctx* ctx, float dt, uint32_t substeps, double* phas
     return ctx->engine.profile(dt, substeps, phase_ms);
 }
 
+int sph_get_tuning(const sph_ctx* ctx, sph_tuning* out) {
+    if (ctx == nullptr || out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    const sph::NeighbourTuning& t = ctx->engine.tuning();
+    out->radix_bits = ctx->engine.radix_bits();
+    out->neighbour_kernel = t.variant;
+    out->block_size = t.block;
+    out->queue_depth = t.queue;
+    out->schedule = ctx->engine.schedule_on() ? 1u : 0u;
+    return SPH_OK;
+}
+
+int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning) {
+    if (ctx == nullptr || tuning == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    sph::NeighbourTuning t;
+    t.variant = tuning->neighbour_kernel;
+    t.block = tuning->block_size;
+    t.queue = tuning->queue_depth;
+    if (tuning->schedule > 1) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    int status = ctx->engine.set_tuning(t);
+    if (status != SPH_OK) {
+        return status;
+    }
+    status = ctx->engine.set_schedule(tuning->schedule != 0);
+    if (status != SPH_OK) {
+        return status;
+    }
+    return ctx->engine.set_radix_bits(tuning->radix_bits);
+}
+
+int sph_selftest_division(sph_ctx* ctx, uint64_t seed, uint64_t count, int mode, uint64_t* mismatches) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.selftest_division(seed, count, mode, mismatches);
+}
+
 int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches) {
     if (ctx == nullptr || launches == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;

@@ -31,6 +31,8 @@ struct alignas(16) TankConst {
     float stiffness;
     float dt;          // substep length
     float max_speed;   // 0.4 * h / dt
+    float r2_far;      // smallest r^2 whose rounded square root is >= h
+    float r2_near;     // largest r^2 whose rounded square root is <= 1e-6
     float gravity[3];
     float restitution;
     float low[3];      // container_min + particle radius

@@ -34,6 +34,47 @@ uint32_t fluid_substeps(const sph_params& params, float delta_seconds) {
     return std::clamp(steps, 1U, 8U);
 }
 
+// Smallest x >= 0 with sqrtf(x) >= v: since the correctly rounded square root
+// is monotone, sqrtf(r2) >= v exactly when r2 >= this threshold.
+float sqrt_at_least(float v) {
+    uint32_t lo = 0;
+    uint32_t hi = 0x7F800000u;  // +inf
+    while (lo < hi) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        float x;
+        std::memcpy(&x, &mid, sizeof(x));
+        if (std::sqrt(x) >= v) {
+            hi = mid;
+        } else {
+            lo = mid + 1;
+        }
+    }
+    float out;
+    std::memcpy(&out, &lo, sizeof(out));
+    return out;
+}
+
+// Largest x >= 0 with sqrtf(x) <= v (sqrtf(r2) <= v exactly when r2 <= it).
+float sqrt_at_most(float v) {
+    uint32_t lo = 0;
+    uint32_t hi = 0x7F800000u;
+    // Smallest x with sqrtf(x) > v, minus one.
+    while (lo < hi) {
+        uint32_t mid = lo + (hi - lo) / 2;
+        float x;
+        std::memcpy(&x, &mid, sizeof(x));
+        if (std::sqrt(x) > v) {
+            hi = mid;
+        } else {
+            lo = mid + 1;
+        }
+    }
+    uint32_t bits = lo == 0 ? 0 : lo - 1;
+    float out;
+    std::memcpy(&out, &bits, sizeof(out));
+    return out;
+}
+
 // The per-particle constants of fluid_sph.cpp:24-46 and :194-285, each from
 // the reference's own float expression (std::pow(float, float) is powf).
 TankConst make_tank_const(const sph_params& p, float dt) {
@@ -51,6 +92,9 @@ TankConst make_tank_const(const sph_params& p, float dt) {
     t.stiffness = p.stiffness;
     t.dt = dt;
     t.max_speed = dt > 0.0F ? 0.4F * h / dt : 0.0F;
+    // fluid_sph.cpp:245-248 skips a pair when length >= h or length <= 1e-6.
+    t.r2_far = sqrt_at_least(h);
+    t.r2_near = sqrt_at_most(1e-6F);
     for (int a = 0; a < 3; ++a) {
         t.gravity[a] = p.gravity[a];
         t.low[a] = p.container_min[a] + p.container_min[3];
@@ -122,7 +166,8 @@ void Engine::release() {
     void* buffers[] = {d_tanks_,       pos_,          vel_,         prev_,        tank_of_,   stank_,
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
-                       bucket_stats_};
+                       bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
+                       schedule_.tile_of, schedule_.order, schedule_.tile_hist};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -191,7 +236,16 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         (status = alloc(&spos2_, n)) != SPH_OK || (status = alloc(&svel_, n)) != SPH_OK ||
         (status = alloc(&counters_, 1)) != SPH_OK ||
         (status = alloc(&stats_acc_, tanks_.size() * kStatsPerTank)) != SPH_OK ||
-        (status = alloc(&bucket_stats_, 2)) != SPH_OK) {
+        (status = alloc(&bucket_stats_, 2)) != SPH_OK ||
+        (status = alloc(&tuning_.pair_list, static_cast<size_t>(n) * tuning_.list_cap)) != SPH_OK ||
+        (status = alloc(&tuning_.pair_count, n)) != SPH_OK ||
+        (status = alloc(&tuning_.masks, static_cast<size_t>(n) * 27)) != SPH_OK) {
+        return status;
+    }
+    schedule_.tile_bits = tanks_.size() == 1 ? 5u : 3u;
+    schedule_.bins = static_cast<uint32_t>(tanks_.size()) << (3 * schedule_.tile_bits);
+    if ((status = alloc(&schedule_.tile_of, n)) != SPH_OK || (status = alloc(&schedule_.order, n)) != SPH_OK ||
+        (status = alloc(&schedule_.tile_hist, schedule_.bins)) != SPH_OK) {
         return status;
     }
     if (tanks_.size() > 1) {
@@ -357,10 +411,30 @@ int Engine::enqueue_grid(uint32_t* launches) {
     SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
     SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
     SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, launches));
-    SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_, svel_,
-                                  stank_, stream_));
+    int status = enqueue_bounds(launches);
+    if (status != SPH_OK) {
+        return status;
+    }
     if (launches != nullptr) {
-        *launches += 2;
+        *launches += 1;
+    }
+    return SPH_OK;
+}
+
+int Engine::enqueue_bounds(uint32_t* launches) {
+    uint32_t n = total_count_;
+    Schedule schedule = schedule_;
+    if (!use_schedule_) {
+        schedule.tile_of = nullptr;
+    } else {
+        SPH_CUDA(cudaMemsetAsync(schedule.tile_hist, 0, sizeof(uint32_t) * schedule.bins, stream_));
+    }
+    SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_, svel_,
+                                  stank_, d_tanks_, schedule, stream_));
+    SPH_CUDA(launch_schedule(n, schedule, stream_));
+    tuning_.order = use_schedule_ ? schedule_.order : nullptr;
+    if (launches != nullptr) {
+        *launches += use_schedule_ ? 3 : 1;
     }
     return SPH_OK;
 }
@@ -371,8 +445,9 @@ int Engine::enqueue_substep(uint32_t* launches) {
         return status;
     }
     uint32_t n = total_count_;
-    SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_));
-    SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_));
+    SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning_));
+    SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
+                                  tuning_));
     if (launches != nullptr) {
         *launches += 2;
     }
@@ -517,7 +592,7 @@ int Engine::stats(uint32_t tank, sph_stats* out, bool with_pairs) {
         }
         grid_valid_ = true;
         SPH_CUDA(cudaMemsetAsync(counters_, 0, sizeof(StepCounters), stream_));
-        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, counters_, stream_));
+        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, counters_, stream_, tuning_));
         SPH_CUDA(cudaMemsetAsync(bucket_stats_, 0, 2 * sizeof(uint32_t), stream_));
         SPH_CUDA(launch_bucket_stats(bucket_ + tanks_[tank].bucket_base, params_[tank].lattice[3], bucket_stats_,
                                      stream_));
@@ -567,6 +642,53 @@ int Engine::set_active(const std::vector<uint8_t>& active) {
     return SPH_OK;
 }
 
+int Engine::selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t* mismatches) {
+    if (mismatches == nullptr || mode < 0 || mode > 5) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaMemsetAsync(counters_, 0, sizeof(StepCounters), stream_));
+    SPH_CUDA(launch_division_selftest(seed, count, mode, &counters_->candidates, stream_));
+    unsigned long long bad = 0;
+    SPH_CUDA(cudaMemcpyAsync(&bad, &counters_->candidates, sizeof(bad), cudaMemcpyDeviceToHost, stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    *mismatches = bad;
+    return SPH_OK;
+}
+
+int Engine::set_tuning(const NeighbourTuning& tuning) {
+    bool queue_ok = tuning.queue == 8 || tuning.queue == 16 || tuning.queue == 24 || tuning.queue == 32;
+    if (tuning.variant > 4 || tuning.block < 32 || tuning.block > 512 || tuning.block % 32 != 0 || !queue_ok ||
+        static_cast<size_t>(tuning.queue) * tuning.block * sizeof(uint32_t) > 48 * 1024) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (tuning.variant >= 2 && tuning.block != 64 && tuning.block != 128 && tuning.block != 256) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    NeighbourTuning kept = tuning_;
+    tuning_ = tuning;
+    tuning_.pair_list = kept.pair_list;
+    tuning_.pair_count = kept.pair_count;
+    tuning_.list_cap = kept.list_cap;
+    tuning_.masks = kept.masks;
+    tuning_.order = kept.order;
+    if (graph_ != nullptr) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    return SPH_OK;
+}
+
+int Engine::set_schedule(bool on) {
+    use_schedule_ = on;
+    if (graph_ != nullptr) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    grid_valid_ = false;
+    return SPH_OK;
+}
+
 int Engine::set_radix_bits(uint32_t bits) {
     if (bits < 1 || bits > kRadixMaxBits) {
         return SPH_ERR_INVALID_ARGUMENT;
@@ -611,12 +733,15 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
         SPH_CUDA(cudaEventRecord(events_[1], stream_));
         SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, nullptr));
         SPH_CUDA(cudaEventRecord(events_[2], stream_));
-        SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_,
-                                      svel_, stank_, stream_));
+        status = enqueue_bounds(nullptr);
+        if (status != SPH_OK) {
+            return status;
+        }
         SPH_CUDA(cudaEventRecord(events_[3], stream_));
-        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_));
+        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning_));
         SPH_CUDA(cudaEventRecord(events_[4], stream_));
-        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_));
+        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
+                                  tuning_));
         SPH_CUDA(cudaEventRecord(events_[5], stream_));
         SPH_CUDA(cudaEventSynchronize(events_[5]));
         for (uint32_t k = 0; k < kProfilePhases; ++k) {

@@ -22,6 +22,8 @@ namespace sph {
 // Host restatements of the reference's parameter rules.
 uint32_t fluid_substeps(const sph_params& params, float delta_seconds);  // fluid_sph.cpp:128-136
 TankConst make_tank_const(const sph_params& params, float dt);           // constants of one tank
+float sqrt_at_least(float v);  // smallest x >= 0 with sqrtf(x) >= v
+float sqrt_at_most(float v);   // largest x >= 0 with sqrtf(x) <= v
 int validate_params(const sph_params& params);
 
 class Engine {
@@ -48,6 +50,12 @@ public:
     int synchronize();
     int set_active(const std::vector<uint8_t>& active);
     int set_radix_bits(uint32_t bits);
+    int set_tuning(const NeighbourTuning& tuning);
+    int set_schedule(bool on);
+    bool schedule_on() const { return use_schedule_; }
+    int selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
+    const NeighbourTuning& tuning() const { return tuning_; }
+    uint32_t radix_bits() const { return radix_bits_; }
     // Runs substeps without the graph, timing each phase with CUDA events on
     // the context stream: keys, sort, bounds+gather, density, integrate.
     static constexpr uint32_t kProfilePhases = 5;
@@ -68,6 +76,7 @@ public:
 
 private:
     int enqueue_grid(uint32_t* launches);
+    int enqueue_bounds(uint32_t* launches);
     int enqueue_substep(uint32_t* launches);
     int refresh_constants(float dt);
     int ensure_graph();
@@ -82,8 +91,11 @@ private:
     uint32_t total_capacity_ = 0;
     uint32_t total_count_ = 0;
     uint32_t total_buckets_ = 0;
-    uint32_t radix_bits_ = 7;
+    uint32_t radix_bits_ = 6;
     RadixPlan plan_{};
+    NeighbourTuning tuning_{};
+    Schedule schedule_{};
+    bool use_schedule_ = false;
     float const_dt_ = -1.0f;
     bool consts_dirty_ = true;
 

@@ -24,9 +24,12 @@ template <bool kCount>
 __global__ void __launch_bounds__(128) density_kernel(const float4* __restrict__ spos, float4* __restrict__ svel,
                                                       float4* __restrict__ spos2, const uint2* __restrict__ bucket,
                                                       const TankConst* __restrict__ tanks,
-                                                      const uint16_t* __restrict__ stank, uint32_t n,
+                                                      const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
                                                       StepCounters* __restrict__ counters) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
     if (p >= n) {
         return;
     }
@@ -98,9 +101,12 @@ __global__ void __launch_bounds__(128) integrate_kernel(const float4* __restrict
                                                         const uint32_t* __restrict__ sorted_ids,
                                                         const uint2* __restrict__ bucket,
                                                         const TankConst* __restrict__ tanks,
-                                                        const uint16_t* __restrict__ stank, uint32_t n,
+                                                        const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
                                                         float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
     if (p >= n) {
         return;
     }
@@ -209,6 +215,264 @@ __global__ void __launch_bounds__(128) integrate_kernel(const float4* __restrict
     uint32_t i = sorted_ids[p];
     pos_out[i] = make_float4(pp[0], pp[1], pp[2], density);
     vel_out[i] = make_float4(vv[0], vv[1], vv[2], pressure);
+}
+
+// The 27 neighbour buckets of a cell, in the reference's (dz, dy, dx) order
+// (fluid_sph.cpp:205-207): walk index b = 9 (dz + 1) + 3 (dy + 1) + (dx + 1).
+__device__ __forceinline__ uint2 neighbour_range(const uint2* __restrict__ bucket, uint32_t cx, uint32_t cy,
+                                                 uint32_t cz, uint32_t b, uint32_t mask, uint32_t base) {
+    uint32_t dz = b / 9u;
+    uint32_t dy = (b / 3u) % 3u;
+    uint32_t dx = b % 3u;
+    uint32_t key = base + spatial_hash(cx + dx - 1u, cy + dy - 1u, cz + dz - 1u, mask);
+    uint2 range = __ldg(&bucket[key]);
+    return make_uint2(range.x, range.x + min(range.y - range.x, kCellCapacity));
+}
+
+// Density with one flat loop over the concatenated 27-bucket candidate
+// stream, so lanes whose cells have different bucket sizes stay converged
+// for as long as their streams last.
+template <bool kCount>
+__global__ void density_flat_kernel(const float4* __restrict__ spos, float4* __restrict__ svel,
+                                    float4* __restrict__ spos2, const uint2* __restrict__ bucket,
+                                    const TankConst* __restrict__ tanks, const uint16_t* __restrict__ stank,
+                                    uint32_t n, const uint32_t* __restrict__ order, StepCounters* __restrict__ counters) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    bool valid = p < n;
+    const TankConst* t = tanks + (valid && stank != nullptr ? stank[p] : 0);
+    const float h = __ldg(&t->h);
+    const float h2 = __ldg(&t->h2);
+    const float c6 = __ldg(&t->c_poly6);
+    const float mass = __ldg(&t->mass);
+    const uint32_t mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+    const float4 self = valid ? spos[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, h));
+    float density = 0.0f;
+    uint32_t candidates = 0;
+    uint32_t in_range = 0;
+    uint32_t b = valid ? 0u : 27u;
+    uint32_t cur = 0;
+    uint32_t end = 0;
+    for (;;) {
+        while (cur == end && b < 27u) {
+            uint2 r = neighbour_range(bucket, cx, cy, cz, b, mask, base);
+            cur = r.x;
+            end = r.y;
+            ++b;
+            if (kCount) {
+                candidates += end - cur;
+            }
+        }
+        if (cur == end) {
+            break;
+        }
+        float4 other = __ldg(&spos[cur]);
+        ++cur;
+        float ex = __fsub_rn(self.x, other.x);
+        float ey = __fsub_rn(self.y, other.y);
+        float ez = __fsub_rn(self.z, other.z);
+        float r2 = dot3(ex, ey, ez);
+        if (r2 < h2) {
+            // poly6 (fluid_sph.cpp:24-31) times mass, added in candidate order.
+            float d = __fsub_rn(h2, r2);
+            float w = __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d);
+            density = __fadd_rn(density, __fmul_rn(mass, w));
+            if (kCount) {
+                ++in_range;
+            }
+        }
+    }
+    if (kCount) {
+        unsigned long long c = candidates;
+        unsigned long long r = in_range;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+            r += __shfl_down_sync(0xFFFFFFFFu, r, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&counters->candidates, c);
+            atomicAdd(&counters->in_range, r);
+        }
+    }
+    if (!valid) {
+        return;
+    }
+    density = max_like_std(density, 1e-6f);
+    float pressure =
+        max_like_std(__fmul_rn(__ldg(&t->stiffness), __fsub_rn(density, __ldg(&t->rest_density))), 0.0f);
+    spos2[p] = make_float4(self.x, self.y, self.z, density);
+    reinterpret_cast<float*>(svel)[4 * static_cast<size_t>(p) + 3] = pressure;
+}
+
+struct PairConst {
+    float h, c_spiky, c_visc, neg_mass, visc_mass;
+};
+
+// Pressure and viscosity force of one in-range pair, added to f in the
+// reference's order (fluid_sph.cpp:244-254).
+__device__ __forceinline__ void add_pair_force(const PairConst& k, const float4& self, float vx, float vy, float vz,
+                                               float pressure, const float4& other, const float4& ov, float& fx,
+                                               float& fy, float& fz) {
+    float ex = __fsub_rn(self.x, other.x);
+    float ey = __fsub_rn(self.y, other.y);
+    float ez = __fsub_rn(self.z, other.z);
+    float distance = __fsqrt_rn(dot3(ex, ey, ez));
+    float other_density = max_like_std(other.w, 1e-6f);
+    float ps = __fdiv_rn(__fmul_rn(k.neg_mass, __fadd_rn(pressure, ov.w)), __fmul_rn(2.0f, other_density));
+    float d = __fsub_rn(k.h, distance);
+    float gs = __fmul_rn(__fmul_rn(k.c_spiky, d), d);
+    fx = __fadd_rn(fx, __fmul_rn(ps, __fmul_rn(gs, __fdiv_rn(ex, distance))));
+    fy = __fadd_rn(fy, __fmul_rn(ps, __fmul_rn(gs, __fdiv_rn(ey, distance))));
+    fz = __fadd_rn(fz, __fmul_rn(ps, __fmul_rn(gs, __fdiv_rn(ez, distance))));
+    float lap = __fmul_rn(k.c_visc, d);
+    fx = __fadd_rn(fx, __fmul_rn(__fdiv_rn(__fmul_rn(k.visc_mass, __fsub_rn(ov.x, vx)), other_density), lap));
+    fy = __fadd_rn(fy, __fmul_rn(__fdiv_rn(__fmul_rn(k.visc_mass, __fsub_rn(ov.y, vy)), other_density), lap));
+    fz = __fadd_rn(fz, __fmul_rn(__fdiv_rn(__fmul_rn(k.visc_mass, __fsub_rn(ov.z, vz)), other_density), lap));
+}
+
+// Semi-implicit Euler, speed clamp and walls (fluid_sph.cpp:260-285), then
+// the id-order write.
+__device__ __forceinline__ void finish_particle(const TankConst* t, const float4& self, float density, float vx,
+                                                float vy, float vz, float pressure, float fx, float fy, float fz,
+                                                uint32_t i, float4* __restrict__ pos_out,
+                                                float4* __restrict__ vel_out) {
+    // The force-field sum starts at vec3{0} and is added even when there are
+    // no fields, which maps -0 to +0.
+    const float dt = __ldg(&t->dt);
+    float ax = __fadd_rn(__fadd_rn(__fdiv_rn(fx, density), __ldg(&t->gravity[0])), 0.0f);
+    float ay = __fadd_rn(__fadd_rn(__fdiv_rn(fy, density), __ldg(&t->gravity[1])), 0.0f);
+    float az = __fadd_rn(__fadd_rn(__fdiv_rn(fz, density), __ldg(&t->gravity[2])), 0.0f);
+    vx = __fadd_rn(vx, __fmul_rn(ax, dt));
+    vy = __fadd_rn(vy, __fmul_rn(ay, dt));
+    vz = __fadd_rn(vz, __fmul_rn(az, dt));
+    const float max_speed = __ldg(&t->max_speed);
+    float speed = __fsqrt_rn(dot3(vx, vy, vz));
+    if (speed > max_speed) {
+        float s = __fdiv_rn(max_speed, speed);
+        vx = __fmul_rn(vx, s);
+        vy = __fmul_rn(vy, s);
+        vz = __fmul_rn(vz, s);
+    }
+    float pp[3] = {__fadd_rn(self.x, __fmul_rn(vx, dt)), __fadd_rn(self.y, __fmul_rn(vy, dt)),
+                   __fadd_rn(self.z, __fmul_rn(vz, dt))};
+    float vv[3] = {vx, vy, vz};
+    const float restitution = __ldg(&t->restitution);
+#pragma unroll
+    for (int axis = 0; axis < 3; ++axis) {
+        float low = __ldg(&t->low[axis]);
+        float high = __ldg(&t->high[axis]);
+        if (pp[axis] < low) {
+            pp[axis] = low;
+            if (vv[axis] < 0.0f) {
+                vv[axis] = __fmul_rn(-vv[axis], restitution);
+            }
+        } else if (pp[axis] > high) {
+            pp[axis] = high;
+            if (vv[axis] > 0.0f) {
+                vv[axis] = __fmul_rn(-vv[axis], restitution);
+            }
+        }
+    }
+    pos_out[i] = make_float4(pp[0], pp[1], pp[2], density);
+    vel_out[i] = make_float4(vv[0], vv[1], vv[2], pressure);
+}
+
+// Integrate in two phases per lane. The scan walks the candidate stream and
+// keeps only in-range pairs, testing r^2 against the thresholds whose square
+// roots round to h and 1e-6 (so `distance >= h || distance <= 1e-6` needs no
+// square root per candidate); their sorted positions queue up in shared
+// memory in stream order. When any lane's queue fills, the whole warp drains
+// its queues, so the long per-pair force code runs with all lanes busy
+// instead of once per candidate with most lanes masked off. Forces still add
+// in the reference's order.
+template <int kQueue>
+__global__ void integrate_queued_kernel(const float4* __restrict__ spos2, const float4* __restrict__ svel,
+                                        const uint32_t* __restrict__ sorted_ids, const uint2* __restrict__ bucket,
+                                        const TankConst* __restrict__ tanks, const uint16_t* __restrict__ stank,
+                                        uint32_t n, const uint32_t* __restrict__ order, float4* __restrict__ pos_out, float4* __restrict__ vel_out) {
+    extern __shared__ uint32_t queue_smem[];
+    uint32_t* queue = queue_smem + threadIdx.x;
+    const uint32_t stride = blockDim.x;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    bool valid = p < n;
+    const TankConst* t = tanks + (valid && stank != nullptr ? stank[p] : 0);
+    valid = valid && __ldg(&t->active) != 0;
+    PairConst k;
+    k.h = __ldg(&t->h);
+    k.c_spiky = __ldg(&t->c_spiky);
+    k.c_visc = __ldg(&t->c_visc);
+    k.neg_mass = __ldg(&t->neg_mass);
+    k.visc_mass = __ldg(&t->visc_mass);
+    const float r2_far = __ldg(&t->r2_far);
+    const float r2_near = __ldg(&t->r2_near);
+    const uint32_t mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+
+    const float4 self = valid ? spos2[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 self_vel = valid ? svel[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, k.h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, k.h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, k.h));
+    float fx = 0.0f;
+    float fy = 0.0f;
+    float fz = 0.0f;
+    uint32_t b = valid ? 0u : 27u;
+    uint32_t cur = 0;
+    uint32_t end = 0;
+    uint32_t queued = 0;
+    for (;;) {
+        while (cur == end && b < 27u) {
+            uint2 r = neighbour_range(bucket, cx, cy, cz, b, mask, base);
+            cur = r.x;
+            end = r.y;
+            ++b;
+        }
+        bool has = cur < end;
+        if (!__any_sync(0xFFFFFFFFu, has)) {
+            break;
+        }
+        if (has) {
+            float4 other = __ldg(&spos2[cur]);
+            float ex = __fsub_rn(self.x, other.x);
+            float ey = __fsub_rn(self.y, other.y);
+            float ez = __fsub_rn(self.z, other.z);
+            float r2 = dot3(ex, ey, ez);
+            // Kept exactly when j != i and !(sqrt(r2) >= h || sqrt(r2) <= 1e-6).
+            if (cur != p && !(r2 >= r2_far || r2 <= r2_near)) {
+                queue[queued * stride] = cur;
+                ++queued;
+            }
+            ++cur;
+        }
+        if (__any_sync(0xFFFFFFFFu, queued == static_cast<uint32_t>(kQueue))) {
+            for (uint32_t e = 0; e < queued; ++e) {
+                uint32_t q = queue[e * stride];
+                add_pair_force(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                               __ldg(&svel[q]), fx, fy, fz);
+            }
+            queued = 0;
+        }
+    }
+    for (uint32_t e = 0; e < queued; ++e) {
+        uint32_t q = queue[e * stride];
+        add_pair_force(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]), __ldg(&svel[q]),
+                       fx, fy, fz);
+    }
+    if (!valid) {
+        return;
+    }
+    finish_particle(t, self, max_like_std(self.w, 1e-6f), self_vel.x, self_vel.y, self_vel.z, self_vel.w, fx, fy, fz,
+                    sorted_ids[p], pos_out, vel_out);
 }
 
 // FluidSolver::emit (fluid_sph.cpp:138-154); glm's mat4 * vec4 adds the
@@ -360,29 +624,663 @@ __global__ void bucket_stats_kernel(const uint2* __restrict__ bucket, uint32_t b
     }
 }
 
+// ---- list-driven variant ---------------------------------------------------
+//
+// Density walks the candidate stream two candidates at a time with packed
+// f32x2 arithmetic (each lane of a packed add/sub/mul is rounded like the
+// scalar operation) and adds the poly6 terms without branches: a candidate
+// out of range adds +0, which leaves the non-negative running sum unchanged,
+// so the sum is the reference's bit for bit. On the same pass it records, per
+// particle, which candidates integrate will use (j != i and
+// !(sqrt(r2) >= h || sqrt(r2) <= 1e-6), tested on r2 against exact square-root
+// thresholds), as 16-bit codes (bucket index << 5 | slot) in stream order.
+// Integrate then runs only the recorded pairs, so every lane of a warp spends
+// its time in the force code instead of in a candidate scan where most lanes
+// idle. A particle with more pairs than the list holds is flagged and
+// integrate scans its candidates directly (same order, same bits).
+
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ void unpack2(unsigned long long v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+template <bool kCount, bool kPacked>
+__global__ void __launch_bounds__(128) density_list_kernel(const float4* __restrict__ spos, float4* __restrict__ svel,
+                                                           float4* __restrict__ spos2, const uint2* __restrict__ bucket,
+                                                           const TankConst* __restrict__ tanks,
+                                                           const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
+                                                           uint16_t* __restrict__ pair_list,
+                                                           uint16_t* __restrict__ pair_count, uint32_t cap,
+                                                           StepCounters* __restrict__ counters) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    if (p >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    const float h = __ldg(&t->h);
+    const float h2 = __ldg(&t->h2);
+    const float r2_far = __ldg(&t->r2_far);
+    const float r2_near = __ldg(&t->r2_near);
+    const uint32_t mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+    const float c6 = __ldg(&t->c_poly6);
+    const float mass = __ldg(&t->mass);
+    const unsigned long long h2x2 = pack2(h2, h2);
+    const unsigned long long c6x2 = pack2(c6, c6);
+    const unsigned long long massx2 = pack2(mass, mass);
+    const float4 self = spos[p];
+    const unsigned long long sx = pack2(self.x, self.x);
+    const unsigned long long sy = pack2(self.y, self.y);
+    const unsigned long long sz = pack2(self.z, self.z);
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, h));
+    uint16_t* list = pair_list + static_cast<size_t>(p) * cap;
+    float density = 0.0f;
+    uint32_t listed = 0;
+    uint32_t candidates = 0;
+    uint32_t in_range = 0;
+    for (uint32_t b = 0; b < 27u; ++b) {
+        uint2 r = neighbour_range(bucket, cx, cy, cz, b, mask, base);
+        uint32_t count = r.y - r.x;
+        if (kCount) {
+            candidates += count;
+        }
+        for (uint32_t k = 0; k < count; k += 2) {
+            uint32_t qa = r.x + k;
+            bool has_b = k + 1 < count;
+            uint32_t qb = has_b ? qa + 1 : qa;
+            float4 oa = __ldg(&spos[qa]);
+            float4 ob = __ldg(&spos[qb]);
+            float r2a, r2b, wa, wb;
+            if constexpr (kPacked) {
+                unsigned long long ex = sub2(sx, pack2(oa.x, ob.x));
+                unsigned long long ey = sub2(sy, pack2(oa.y, ob.y));
+                unsigned long long ez = sub2(sz, pack2(oa.z, ob.z));
+                unsigned long long r2 = add2(add2(mul2(ex, ex), mul2(ey, ey)), mul2(ez, ez));
+                unsigned long long d = sub2(h2x2, r2);
+                unsigned long long w = mul2(massx2, mul2(mul2(mul2(c6x2, d), d), d));
+                unpack2(r2, r2a, r2b);
+                unpack2(w, wa, wb);
+            } else {
+                r2a = dot3(__fsub_rn(self.x, oa.x), __fsub_rn(self.y, oa.y), __fsub_rn(self.z, oa.z));
+                r2b = dot3(__fsub_rn(self.x, ob.x), __fsub_rn(self.y, ob.y), __fsub_rn(self.z, ob.z));
+                float da = __fsub_rn(h2, r2a);
+                float db = __fsub_rn(h2, r2b);
+                wa = __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, da), da), da));
+                wb = __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, db), db), db));
+            }
+            bool in_a = r2a < h2;
+            bool in_b = has_b && r2b < h2;
+            density = __fadd_rn(density, in_a ? wa : 0.0f);
+            density = __fadd_rn(density, in_b ? wb : 0.0f);
+            if (kCount) {
+                in_range += (in_a ? 1u : 0u) + (in_b ? 1u : 0u);
+            }
+            bool keep_a = qa != p && !(r2a >= r2_far || r2a <= r2_near);
+            bool keep_b = has_b && qb != p && !(r2b >= r2_far || r2b <= r2_near);
+            if (keep_a) {
+                if (listed < cap) {
+                    list[listed] = static_cast<uint16_t>((b << 5) | k);
+                }
+                ++listed;
+            }
+            if (keep_b) {
+                if (listed < cap) {
+                    list[listed] = static_cast<uint16_t>((b << 5) | (k + 1));
+                }
+                ++listed;
+            }
+        }
+    }
+    pair_count[p] = static_cast<uint16_t>(min(listed, 0xFFFFu));
+    if (kCount) {
+        unsigned long long c = candidates;
+        unsigned long long rr = in_range;
+        unsigned int active = __activemask();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c += __shfl_down_sync(active, c, o);
+            rr += __shfl_down_sync(active, rr, o);
+        }
+        if ((threadIdx.x & 31) == static_cast<uint32_t>(__ffs(active) - 1)) {
+            atomicAdd(&counters->candidates, c);
+            atomicAdd(&counters->in_range, rr);
+        }
+    }
+    density = max_like_std(density, 1e-6f);
+    float pressure =
+        max_like_std(__fmul_rn(__ldg(&t->stiffness), __fsub_rn(density, __ldg(&t->rest_density))), 0.0f);
+    spos2[p] = make_float4(self.x, self.y, self.z, density);
+    reinterpret_cast<float*>(svel)[4 * static_cast<size_t>(p) + 3] = pressure;
+}
+
+// Correctly rounded x / y given r = RN(1/y): q = RN(x r) is within one ulp of
+// x / y, the residual x - q y is exact in one FMA, and one more FMA rounds
+// q + (x - q y) r to the correctly rounded quotient (Markstein's division
+// theorem; P. Markstein, IBM J. Res. Dev. 34(1), 1990). Holds for the
+// magnitudes of this solver (no overflow or subnormal intermediates). A zero
+// dividend yields +0 where IEEE division gives the dividend's signed zero; the
+// force sums it feeds start at +0 and so never change bits because of it.
+__device__ __forceinline__ float div_by(float x, float y, float r) {
+    float q = __fmul_rn(x, r);
+    float e = __fmaf_rn(-q, y, x);
+    return __fmaf_rn(e, r, q);
+}
+
+// Pair force with the two shared reciprocals (1/distance, 1/rho_j); the same
+// operations and order as add_pair_force.
+__device__ __forceinline__ void add_pair_force_rcp(const PairConst& k, const float4& self, float vx, float vy, float vz,
+                                                   float pressure, const float4& other, const float4& ov, float& fx,
+                                                   float& fy, float& fz) {
+    float ex = __fsub_rn(self.x, other.x);
+    float ey = __fsub_rn(self.y, other.y);
+    float ez = __fsub_rn(self.z, other.z);
+    float distance = __fsqrt_rn(dot3(ex, ey, ez));
+    float inv_distance = __frcp_rn(distance);
+    float other_density = max_like_std(other.w, 1e-6f);
+    float inv_density = __frcp_rn(other_density);
+    // 1 / (2 rho_j) is RN(1/rho_j) / 2 exactly (a power-of-two scaling).
+    float ps = div_by(__fmul_rn(k.neg_mass, __fadd_rn(pressure, ov.w)), __fmul_rn(2.0f, other_density),
+                      __fmul_rn(0.5f, inv_density));
+    float d = __fsub_rn(k.h, distance);
+    float gs = __fmul_rn(__fmul_rn(k.c_spiky, d), d);
+    fx = __fadd_rn(fx, __fmul_rn(ps, __fmul_rn(gs, div_by(ex, distance, inv_distance))));
+    fy = __fadd_rn(fy, __fmul_rn(ps, __fmul_rn(gs, div_by(ey, distance, inv_distance))));
+    fz = __fadd_rn(fz, __fmul_rn(ps, __fmul_rn(gs, div_by(ez, distance, inv_distance))));
+    float lap = __fmul_rn(k.c_visc, d);
+    fx = __fadd_rn(fx, __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.x, vx)), other_density, inv_density), lap));
+    fy = __fadd_rn(fy, __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.y, vy)), other_density, inv_density), lap));
+    fz = __fadd_rn(fz, __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.z, vz)), other_density, inv_density), lap));
+}
+
+template <int kBlock, bool kRcp>
+__global__ void __launch_bounds__(kBlock) integrate_list_kernel(const float4* __restrict__ spos2,
+                                                                const float4* __restrict__ svel,
+                                                                const uint32_t* __restrict__ sorted_ids,
+                                                                const uint2* __restrict__ bucket,
+                                                                const TankConst* __restrict__ tanks,
+                                                                const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
+                                                                const uint16_t* __restrict__ pair_list,
+                                                                const uint16_t* __restrict__ pair_count, uint32_t cap,
+                                                                float4* __restrict__ pos_out,
+                                                                float4* __restrict__ vel_out) {
+    __shared__ uint32_t starts[27][kBlock];
+    uint32_t p = blockIdx.x * kBlock + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    if (p >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    if (__ldg(&t->active) == 0) {
+        return;
+    }
+    PairConst k;
+    k.h = __ldg(&t->h);
+    k.c_spiky = __ldg(&t->c_spiky);
+    k.c_visc = __ldg(&t->c_visc);
+    k.neg_mass = __ldg(&t->neg_mass);
+    k.visc_mass = __ldg(&t->visc_mass);
+    const uint32_t mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+    const float4 self = spos2[p];
+    const float4 self_vel = svel[p];
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, k.h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, k.h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, k.h));
+    float fx = 0.0f;
+    float fy = 0.0f;
+    float fz = 0.0f;
+    uint32_t pairs = pair_count[p];
+    if (pairs <= cap) {
+        for (uint32_t b = 0; b < 27u; ++b) {
+            starts[b][threadIdx.x] = neighbour_range(bucket, cx, cy, cz, b, mask, base).x;
+        }
+        const uint16_t* list = pair_list + static_cast<size_t>(p) * cap;
+        for (uint32_t e = 0; e < pairs; ++e) {
+            uint32_t code = list[e];
+            uint32_t q = starts[code >> 5][threadIdx.x] + (code & 31u);
+            if (kRcp) {
+                add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                                   __ldg(&svel[q]), fx, fy, fz);
+            } else {
+                add_pair_force(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                               __ldg(&svel[q]), fx, fy, fz);
+            }
+        }
+    } else {
+        // More pairs than the list holds: scan the candidates (rare).
+        const float r2_far = __ldg(&t->r2_far);
+        const float r2_near = __ldg(&t->r2_near);
+        for (uint32_t b = 0; b < 27u; ++b) {
+            uint2 r = neighbour_range(bucket, cx, cy, cz, b, mask, base);
+            for (uint32_t q = r.x; q < r.y; ++q) {
+                float4 other = __ldg(&spos2[q]);
+                float r2 = dot3(__fsub_rn(self.x, other.x), __fsub_rn(self.y, other.y), __fsub_rn(self.z, other.z));
+                if (q != p && !(r2 >= r2_far || r2 <= r2_near)) {
+                    if (kRcp) {
+                        add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, other,
+                                           __ldg(&svel[q]), fx, fy, fz);
+                    } else {
+                        add_pair_force(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, other,
+                                       __ldg(&svel[q]), fx, fy, fz);
+                    }
+                }
+            }
+        }
+    }
+    finish_particle(t, self, max_like_std(self.w, 1e-6f), self_vel.x, self_vel.y, self_vel.z, self_vel.w, fx, fy, fz,
+                    sorted_ids[p], pos_out, vel_out);
+}
+
+// ---- mask-driven variant ---------------------------------------------------
+//
+// Density keeps the nested bucket loops (all lanes of a warp step through the
+// 27 buckets together) and, per bucket, ORs into one 32-bit word the slots
+// integrate will use (j != i and !(sqrt(r2) >= h || sqrt(r2) <= 1e-6), via the
+// exact r2 thresholds). The word is stored bucket-major, masks[b * n + p], so
+// each store of a warp is one contiguous 128-byte line. Integrate reads its 27
+// words (again one line per warp and bucket), expands the set bits into a
+// list of sorted positions in shared memory in stream order, and runs the
+// pair forces over that list with all lanes busy.
+template <bool kCount>
+__global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restrict__ spos, float4* __restrict__ svel,
+                                                           float4* __restrict__ spos2, const uint2* __restrict__ bucket,
+                                                           const TankConst* __restrict__ tanks,
+                                                           const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
+                                                           uint32_t* __restrict__ masks,
+                                                           StepCounters* __restrict__ counters) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    if (p >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    const float h = __ldg(&t->h);
+    const float h2 = __ldg(&t->h2);
+    const float c6 = __ldg(&t->c_poly6);
+    const float mass = __ldg(&t->mass);
+    const float r2_far = __ldg(&t->r2_far);
+    const float r2_near = __ldg(&t->r2_near);
+    const uint32_t cell_mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+    const float4 self = spos[p];
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, h));
+    float density = 0.0f;
+    uint32_t candidates = 0;
+    uint32_t in_range = 0;
+    for (uint32_t b = 0; b < 27u; ++b) {
+        uint2 r = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base);
+        uint32_t word = 0;
+        if (kCount) {
+            candidates += r.y - r.x;
+        }
+        for (uint32_t q = r.x; q < r.y; ++q) {
+            float4 other = __ldg(&spos[q]);
+            float r2 = dot3(__fsub_rn(self.x, other.x), __fsub_rn(self.y, other.y), __fsub_rn(self.z, other.z));
+            if (r2 < h2) {
+                // poly6 (fluid_sph.cpp:24-31) times mass, added in candidate order.
+                float d = __fsub_rn(h2, r2);
+                density = __fadd_rn(density, __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d)));
+                if (kCount) {
+                    ++in_range;
+                }
+            }
+            bool keep = q != p && !(r2 >= r2_far || r2 <= r2_near);
+            word |= static_cast<uint32_t>(keep) << (q - r.x);
+        }
+        masks[static_cast<size_t>(b) * n + p] = word;
+    }
+    if (kCount) {
+        unsigned long long c = candidates;
+        unsigned long long rr = in_range;
+        unsigned int active = __activemask();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c += __shfl_down_sync(active, c, o);
+            rr += __shfl_down_sync(active, rr, o);
+        }
+        if ((threadIdx.x & 31) == static_cast<uint32_t>(__ffs(active) - 1)) {
+            atomicAdd(&counters->candidates, c);
+            atomicAdd(&counters->in_range, rr);
+        }
+    }
+    density = max_like_std(density, 1e-6f);
+    float pressure =
+        max_like_std(__fmul_rn(__ldg(&t->stiffness), __fsub_rn(density, __ldg(&t->rest_density))), 0.0f);
+    spos2[p] = make_float4(self.x, self.y, self.z, density);
+    reinterpret_cast<float*>(svel)[4 * static_cast<size_t>(p) + 3] = pressure;
+}
+
+template <int kBlock, int kList>
+__global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __restrict__ spos2,
+                                                                const float4* __restrict__ svel,
+                                                                const uint32_t* __restrict__ sorted_ids,
+                                                                const uint2* __restrict__ bucket,
+                                                                const TankConst* __restrict__ tanks,
+                                                                const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
+                                                                const uint32_t* __restrict__ masks,
+                                                                float4* __restrict__ pos_out,
+                                                                float4* __restrict__ vel_out) {
+    __shared__ uint32_t list[kList][kBlock];
+    uint32_t p = blockIdx.x * kBlock + threadIdx.x;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    if (p >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    if (__ldg(&t->active) == 0) {
+        return;
+    }
+    PairConst k;
+    k.h = __ldg(&t->h);
+    k.c_spiky = __ldg(&t->c_spiky);
+    k.c_visc = __ldg(&t->c_visc);
+    k.neg_mass = __ldg(&t->neg_mass);
+    k.visc_mass = __ldg(&t->visc_mass);
+    const uint32_t cell_mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+    const float4 self = spos2[p];
+    const float4 self_vel = svel[p];
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, k.h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, k.h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, k.h));
+    float fx = 0.0f;
+    float fy = 0.0f;
+    float fz = 0.0f;
+    uint32_t listed = 0;
+    for (uint32_t b = 0; b < 27u; ++b) {
+        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + p]);
+        if (word == 0) {
+            continue;
+        }
+        uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
+        while (word != 0) {
+            uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
+            word &= word - 1;
+            if (listed == static_cast<uint32_t>(kList)) {
+                // Drain a full list, in order, before taking more.
+                for (uint32_t e = 0; e < listed; ++e) {
+                    uint32_t q = list[e][threadIdx.x];
+                    add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                                       __ldg(&svel[q]), fx, fy, fz);
+                }
+                listed = 0;
+            }
+            list[listed][threadIdx.x] = start + slot;
+            ++listed;
+        }
+    }
+    for (uint32_t e = 0; e < listed; ++e) {
+        uint32_t q = list[e][threadIdx.x];
+        add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]), __ldg(&svel[q]),
+                           fx, fy, fz);
+    }
+    finish_particle(t, self, max_like_std(self.w, 1e-6f), self_vel.x, self_vel.y, self_vel.z, self_vel.w, fx, fy, fz,
+                    sorted_ids[p], pos_out, vel_out);
+}
+
+// Division self-test: counts x / y where the reciprocal-based quotient and
+// IEEE division differ in value (signed zeros compare equal).
+__global__ void division_selftest_kernel(uint64_t seed, uint64_t count, int mode, unsigned long long* mismatches) {
+    uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    unsigned long long bad = 0;
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
+        float x;
+        float y;
+        if (mode == 0) {
+            // Every divisor mantissa in [1, 2) against dividends from a mixer.
+            uint32_t ym = static_cast<uint32_t>(i & 0x7FFFFFu);
+            uint64_t z = (i >> 23) * 0x9E3779B97F4A7C15ULL + seed;
+            z = (z ^ (z >> 31)) * 0xBF58476D1CE4E5B9ULL;
+            uint32_t xb = 0x3F800000u | static_cast<uint32_t>((z >> 20) & 0x7FFFFFu);
+            x = __uint_as_float(xb);
+            y = __uint_as_float(0x3F800000u | ym);
+        } else {
+            // Random signs, mantissas and exponents over 2^-60 .. 2^60.
+            uint64_t z = i * 0x9E3779B97F4A7C15ULL + seed;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+            z ^= z >> 31;
+            uint32_t ex = 67u + static_cast<uint32_t>((z >> 8) % 121u);
+            uint32_t ey = 67u + static_cast<uint32_t>((z >> 16) % 121u);
+            x = __uint_as_float((static_cast<uint32_t>(z >> 63) << 31) | (ex << 23) |
+                                static_cast<uint32_t>((z >> 24) & 0x7FFFFFu));
+            y = __uint_as_float((static_cast<uint32_t>((z >> 62) & 1u) << 31) | (ey << 23) |
+                                static_cast<uint32_t>((z >> 40) & 0x7FFFFFu));
+        }
+        float want;
+        float got;
+        if (mode <= 1) {
+            want = __fdiv_rn(x, y);
+            got = div_by(x, y, __frcp_rn(y));
+        } else {
+            // Packed f32x2 arithmetic against the scalar operations.
+            float u = __fmul_rn(x, 0.75f);
+            float v = __fadd_rn(y, 0.125f);
+            unsigned long long px = pack2(x, u);
+            unsigned long long py = pack2(y, v);
+            float lo;
+            float hi;
+            if (mode == 2) {
+                unpack2(mul2(px, py), lo, hi);
+                want = __fmul_rn(x, y);
+                got = lo;
+                if (hi != __fmul_rn(u, v)) {
+                    ++bad;
+                }
+            } else if (mode == 3) {
+                unpack2(add2(px, py), lo, hi);
+                want = __fadd_rn(x, y);
+                got = lo;
+                if (hi != __fadd_rn(u, v)) {
+                    ++bad;
+                }
+            } else if (mode == 4) {
+                unpack2(sub2(px, py), lo, hi);
+                want = __fsub_rn(x, y);
+                got = lo;
+                if (hi != __fsub_rn(u, v)) {
+                    ++bad;
+                }
+            } else {
+                // The squared-distance chain (x*x + y*y) + u*u.
+                unsigned long long pu = pack2(u, v);
+                unpack2(add2(add2(mul2(px, px), mul2(py, py)), mul2(pu, pu)), lo, hi);
+                want = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(u, u));
+                got = lo;
+            }
+        }
+        if (want != got) {
+            ++bad;
+        }
+    }
+    if (bad != 0) {
+        atomicAdd(mismatches, bad);
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, const uint2* bucket, const TankConst* tanks,
-                           const uint16_t* stank, uint32_t n, StepCounters* counters, cudaStream_t stream) {
+                           const uint16_t* stank, uint32_t n, StepCounters* counters, cudaStream_t stream,
+                           const NeighbourTuning& tuning) {
     if (n == 0) {
         return cudaSuccess;
     }
-    uint32_t blocks = (n + 127) / 128;
+    if (tuning.variant == 0) {
+        uint32_t blocks = (n + 127) / 128;
+        if (counters != nullptr) {
+            density_kernel<true><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n, tuning.order, counters);
+        } else {
+            density_kernel<false><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n, tuning.order, nullptr);
+        }
+        return cudaGetLastError();
+    }
+    if (tuning.variant == 4) {
+        uint32_t blocks = (n + 127) / 128;
+        if (counters != nullptr) {
+            density_mask_kernel<true><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
+                                                                  tuning.order, tuning.masks, counters);
+        } else {
+            density_mask_kernel<false><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
+                                                                   tuning.order, tuning.masks, nullptr);
+        }
+        return cudaGetLastError();
+    }
+    if (tuning.variant >= 2) {
+        uint32_t blocks = (n + 127) / 128;
+        if (counters != nullptr) {
+            density_list_kernel<true, false><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
+                                                                  tuning.order, tuning.pair_list, tuning.pair_count, tuning.list_cap,
+                                                                  counters);
+        } else {
+            density_list_kernel<false, false><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
+                                                                   tuning.order, tuning.pair_list, tuning.pair_count,
+                                                                   tuning.list_cap, nullptr);
+        }
+        return cudaGetLastError();
+    }
+    uint32_t threads = tuning.block;
+    uint32_t blocks = (n + threads - 1) / threads;
     if (counters != nullptr) {
-        density_kernel<true><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n, counters);
+        density_flat_kernel<true><<<blocks, threads, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n, tuning.order, counters);
     } else {
-        density_kernel<false><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n, nullptr);
+        density_flat_kernel<false><<<blocks, threads, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n, tuning.order, nullptr);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
                              const TankConst* tanks, const uint16_t* stank, uint32_t n, float4* pos, float4* vel,
-                             cudaStream_t stream) {
+                             cudaStream_t stream, const NeighbourTuning& tuning) {
     if (n == 0) {
         return cudaSuccess;
     }
-    integrate_kernel<<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n, pos, vel);
+    if (tuning.variant == 0) {
+        integrate_kernel<<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, pos,
+                                                              vel);
+        return cudaGetLastError();
+    }
+    if (tuning.variant == 4) {
+        switch (tuning.block) {
+        case 64:
+            integrate_mask_kernel<64, 48><<<(n + 63) / 64, 64, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks,
+                                                                            stank, n, tuning.order, tuning.masks, pos, vel);
+            break;
+        case 256:
+            if (tuning.queue <= 24) {
+                integrate_mask_kernel<256, 24><<<(n + 255) / 256, 256, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
+            } else if (tuning.queue == 32) {
+                integrate_mask_kernel<256, 32><<<(n + 255) / 256, 256, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
+            } else {
+                integrate_mask_kernel<256, 40><<<(n + 255) / 256, 256, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
+            }
+            break;
+        default:
+            integrate_mask_kernel<128, 48><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks,
+                                                                                stank, n, tuning.order, tuning.masks, pos, vel);
+            break;
+        }
+        return cudaGetLastError();
+    }
+    if (tuning.variant >= 2) {
+        bool rcp = tuning.variant == 3;
+        switch (tuning.block) {
+        case 64:
+            if (rcp) {
+                integrate_list_kernel<64, true><<<(n + 63) / 64, 64, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.pair_list, tuning.pair_count,
+                    tuning.list_cap, pos, vel);
+            } else {
+                integrate_list_kernel<64, false><<<(n + 63) / 64, 64, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.pair_list, tuning.pair_count,
+                    tuning.list_cap, pos, vel);
+            }
+            break;
+        case 256:
+            if (rcp) {
+                integrate_list_kernel<256, true><<<(n + 255) / 256, 256, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.pair_list, tuning.pair_count,
+                    tuning.list_cap, pos, vel);
+            } else {
+                integrate_list_kernel<256, false><<<(n + 255) / 256, 256, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.pair_list, tuning.pair_count,
+                    tuning.list_cap, pos, vel);
+            }
+            break;
+        default:
+            if (rcp) {
+                integrate_list_kernel<128, true><<<(n + 127) / 128, 128, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.pair_list, tuning.pair_count,
+                    tuning.list_cap, pos, vel);
+            } else {
+                integrate_list_kernel<128, false><<<(n + 127) / 128, 128, 0, stream>>>(
+                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.pair_list, tuning.pair_count,
+                    tuning.list_cap, pos, vel);
+            }
+            break;
+        }
+        return cudaGetLastError();
+    }
+    uint32_t threads = tuning.block;
+    uint32_t blocks = (n + threads - 1) / threads;
+    size_t smem = static_cast<size_t>(tuning.queue) * threads * sizeof(uint32_t);
+    switch (tuning.queue) {
+    case 8:
+        integrate_queued_kernel<8><<<blocks, threads, smem, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
+                                                                      tuning.order, pos, vel);
+        break;
+    case 16:
+        integrate_queued_kernel<16><<<blocks, threads, smem, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank,
+                                                                       n, tuning.order, pos, vel);
+        break;
+    case 32:
+        integrate_queued_kernel<32><<<blocks, threads, smem, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank,
+                                                                       n, tuning.order, pos, vel);
+        break;
+    default:
+        integrate_queued_kernel<24><<<blocks, threads, smem, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank,
+                                                                       n, tuning.order, pos, vel);
+        break;
+    }
     return cudaGetLastError();
 }
 
@@ -413,6 +1311,12 @@ cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_
         return cudaSuccess;
     }
     nonfinite_kernel<<<(n + 255) / 256, 256, 0, stream>>>(pos, vel, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_division_selftest(uint64_t seed, uint64_t count, int mode, unsigned long long* mismatches,
+                                     cudaStream_t stream) {
+    division_selftest_kernel<<<152 * 8, 256, 0, stream>>>(seed, count, mode, mismatches);
     return cudaGetLastError();
 }
 

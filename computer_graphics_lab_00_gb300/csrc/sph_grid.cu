@@ -71,49 +71,63 @@ __global__ void __launch_bounds__(kRadixThreads) radix_upsweep(const uint32_t* _
     }
 }
 
-// Exclusive scan of m counters in one block (m is bins x tiles, at most a
-// few hundred thousand).
+// Exclusive scan of m counters in one block of 1024 threads (m is bins x
+// tiles, at most a few hundred thousand). Each pass scans 8192 counters:
+// every thread loads 8 consecutive ones (a warp reads 1 KB contiguous), the
+// thread totals are scanned across the block, and a carry links the passes.
 __global__ void __launch_bounds__(1024) scan_exclusive_block(uint32_t* __restrict__ data, uint32_t m) {
     __shared__ uint32_t warp_sums[32];
-    uint32_t per = (m + blockDim.x - 1) / blockDim.x;
-    uint32_t begin = threadIdx.x * per;
-    uint32_t end = min(begin + per, m);
-    uint32_t sum = 0;
-    for (uint32_t i = begin; i < end; ++i) {
-        sum += data[i];
-    }
-    uint32_t lane = threadIdx.x & 31;
-    uint32_t warp = threadIdx.x >> 5;
-    uint32_t inclusive = sum;
+    __shared__ uint32_t block_total;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = threadIdx.x >> 5;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < m; base += 8 * 1024) {
+        uint32_t first = base + threadIdx.x * 8;
+        uint32_t v[8];
+        uint32_t local = 0;
 #pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
-        if (lane >= o) {
-            inclusive += v;
+        for (int k = 0; k < 8; ++k) {
+            v[k] = first + k < m ? data[first + k] : 0;
+            local += v[k];
         }
-    }
-    if (lane == 31) {
-        warp_sums[warp] = inclusive;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t v = lane < (blockDim.x >> 5) ? warp_sums[lane] : 0;
-        uint32_t inc = v;
+        uint32_t inclusive = local;
 #pragma unroll
         for (uint32_t o = 1; o < 32; o <<= 1) {
-            uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
             if (lane >= o) {
-                inc += u;
+                inclusive += u;
             }
         }
-        warp_sums[lane] = inc - v;
-    }
-    __syncthreads();
-    uint32_t run = warp_sums[warp] + inclusive - sum;
-    for (uint32_t i = begin; i < end; ++i) {
-        uint32_t v = data[i];
-        data[i] = run;
-        run += v;
+        if (lane == 31) {
+            warp_sums[warp] = inclusive;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane];
+            uint32_t inc = w;
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                if (lane >= o) {
+                    inc += u;
+                }
+            }
+            warp_sums[lane] = inc - w;
+            if (lane == 31) {
+                block_total = inc;
+            }
+        }
+        __syncthreads();
+        uint32_t run = carry + warp_sums[warp] + inclusive - local;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            if (first + k < m) {
+                data[first + k] = run;
+            }
+            run += v[k];
+        }
+        carry += block_total;
+        __syncthreads();
     }
 }
 
@@ -180,6 +194,15 @@ __global__ void __launch_bounds__(kRadixThreads) radix_downsweep(const uint32_t*
     }
 }
 
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
 __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __restrict__ sorted_keys,
                                                             const uint32_t* __restrict__ sorted_ids, uint32_t n,
                                                             uint32_t* __restrict__ bucket_words,
@@ -187,23 +210,68 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
                                                             const float4* __restrict__ vel,
                                                             const uint16_t* __restrict__ tank_of,
                                                             float4* __restrict__ spos, float4* __restrict__ svel,
-                                                            uint16_t* __restrict__ stank) {
+                                                            uint16_t* __restrict__ stank,
+                                                            const TankConst* __restrict__ tanks, Schedule schedule) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) {
+    bool valid = p < n;
+    uint32_t i = 0;
+    uint32_t tank = 0;
+    float4 position = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (valid) {
+        uint32_t key = sorted_keys[p];
+        if (p == 0 || sorted_keys[p - 1] != key) {
+            bucket_words[2 * static_cast<size_t>(key)] = p;
+        }
+        if (p + 1 == n || sorted_keys[p + 1] != key) {
+            bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
+        }
+        i = sorted_ids[p];
+        position = pos[i];
+        spos[p] = position;
+        svel[p] = vel[i];
+        if (tank_of != nullptr) {
+            tank = tank_of[i];
+            stank[p] = static_cast<uint16_t>(tank);
+        }
+    }
+    if (schedule.tile_of == nullptr) {
         return;
     }
-    uint32_t key = sorted_keys[p];
-    if (p == 0 || sorted_keys[p - 1] != key) {
-        bucket_words[2 * static_cast<size_t>(key)] = p;
+    // Processing order: cells grouped into 4 x 4 x 4 tiles, tiles in Morton
+    // order, so the particles a block works on sit next to each other.
+    uint32_t bin = 0xFFFFFFFFu;
+    if (valid) {
+        float h = __ldg(&tanks[tank].h);
+        uint32_t axis_mask = (1u << schedule.tile_bits) - 1u;
+        uint32_t tx = (static_cast<uint32_t>(cell_coord(position.x, h)) >> 2) & axis_mask;
+        uint32_t ty = (static_cast<uint32_t>(cell_coord(position.y, h)) >> 2) & axis_mask;
+        uint32_t tz = (static_cast<uint32_t>(cell_coord(position.z, h)) >> 2) & axis_mask;
+        bin = (tank << (3 * schedule.tile_bits)) + (spread3(tx) | (spread3(ty) << 1) | (spread3(tz) << 2));
+        schedule.tile_of[p] = bin;
     }
-    if (p + 1 == n || sorted_keys[p + 1] != key) {
-        bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
+    uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
+    if (valid && (threadIdx.x & 31) == static_cast<uint32_t>(__ffs(peers) - 1)) {
+        atomicAdd(&schedule.tile_hist[bin], static_cast<uint32_t>(__popc(peers)));
     }
-    uint32_t i = sorted_ids[p];
-    spos[p] = pos[i];
-    svel[p] = vel[i];
-    if (tank_of != nullptr) {
-        stank[p] = tank_of[i];
+}
+
+// Scatters sorted positions into the processing order: lanes with the same
+// tile take one contiguous range (one atomic per group), keeping a cell's
+// particles adjacent.
+__global__ void __launch_bounds__(256) schedule_scatter_kernel(uint32_t n, Schedule schedule) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool valid = p < n;
+    uint32_t bin = valid ? schedule.tile_of[p] : 0xFFFFFFFFu;
+    uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
+    uint32_t leader = static_cast<uint32_t>(__ffs(peers) - 1);
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (valid && lane == leader) {
+        base = atomicAdd(&schedule.tile_hist[bin], static_cast<uint32_t>(__popc(peers)));
+    }
+    base = __shfl_sync(0xFFFFFFFFu, base, static_cast<int>(leader));
+    if (valid) {
+        schedule.order[base + static_cast<uint32_t>(__popc(peers & lanemask_lt()))] = p;
     }
 }
 
@@ -279,13 +347,23 @@ cudaError_t launch_radix_sort(GridScratch& s, uint32_t n, const RadixPlan& plan,
 
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
-                                 float4* svel, uint16_t* stank, cudaStream_t stream) {
+                                 float4* svel, uint16_t* stank, const TankConst* tanks, const Schedule& schedule,
+                                 cudaStream_t stream) {
     if (n == 0) {
         return cudaSuccess;
     }
     bounds_gather_kernel<<<(n + 255) / 256, 256, 0, stream>>>(sorted_keys, sorted_ids, n,
                                                               reinterpret_cast<uint32_t*>(bucket), pos, vel, tank_of,
-                                                              spos, svel, stank);
+                                                              spos, svel, stank, tanks, schedule);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_schedule(uint32_t n, const Schedule& schedule, cudaStream_t stream) {
+    if (n == 0 || schedule.tile_of == nullptr) {
+        return cudaSuccess;
+    }
+    scan_exclusive_block<<<1, 1024, 0, stream>>>(schedule.tile_hist, schedule.bins);
+    schedule_scatter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, schedule);
     return cudaGetLastError();
 }
 

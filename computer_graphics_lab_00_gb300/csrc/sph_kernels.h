@@ -55,22 +55,60 @@ cudaError_t launch_keys(const float4* pos, const uint16_t* tank_of, const TankCo
 cudaError_t launch_radix_sort(GridScratch& scratch, uint32_t n, const RadixPlan& plan, cudaStream_t stream,
                               uint32_t* launches);
 
-// Bucket table (start, end) from sorted keys (table pre-zeroed) and the
-// cell-ordered copies of position, velocity and tank id.
+// Processing order of the neighbour passes. When tile_of is null the passes
+// run in sorted (bucket) order; otherwise bounds_gather bins every particle
+// into a Morton-ordered tile of 4 x 4 x 4 cells (tile_bits bits per axis,
+// per tank) and launch_schedule turns the bins into `order`.
+struct Schedule {
+    uint32_t* tile_of = nullptr;    // n: bin of each sorted position
+    uint32_t* tile_hist = nullptr;  // bins: counts, then running offsets
+    uint32_t* order = nullptr;      // n: sorted positions in processing order
+    uint32_t tile_bits = 5;
+    uint32_t bins = 0;
+};
+
+// Bucket table (start, end) from sorted keys (table pre-zeroed), the
+// cell-ordered copies of position, velocity and tank id, and (optionally) the
+// tile histogram of the processing order (tile_hist pre-zeroed).
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
-                                 float4* svel, uint16_t* stank, cudaStream_t stream);
+                                 float4* svel, uint16_t* stank, const TankConst* tanks, const Schedule& schedule,
+                                 cudaStream_t stream);
+// Scan of the tile histogram and scatter into schedule.order.
+cudaError_t launch_schedule(uint32_t n, const Schedule& schedule, cudaStream_t stream);
+
+// Shape of the neighbour passes. variant 0: one thread per particle with
+// nested bucket loops; 1: flat candidate stream (density) and the queued pair
+// pass (integrate); 2: density records each particle's in-range pairs and
+// integrate runs only those; 3: as 2 with divisions through a shared
+// correctly rounded reciprocal; 4: density stores per-bucket 32-bit masks
+// of the pairs integrate uses (bucket-major, coalesced) and integrate expands
+// them (reciprocal divisions). block: threads per block of integrate
+// (64/128/256 for variants 2-3); queue: in-range pairs buffered per thread
+// (variant 1: 8, 16, 24 or 32). pair_list / pair_count / list_cap: the
+// per-particle pair lists of variants 2-3 (device buffers the engine owns).
+struct NeighbourTuning {
+    uint32_t variant = 4;
+    uint32_t block = 256;
+    uint32_t queue = 32;
+    uint16_t* pair_list = nullptr;
+    uint16_t* pair_count = nullptr;
+    uint32_t list_cap = 64;
+    uint32_t* masks = nullptr;  // 27 words per particle, bucket-major (variant 4)
+    const uint32_t* order = nullptr;  // processing order (null: sorted order)
+};
 
 // Density and pressure (fluid_sph.cpp:200-222). Writes spos2 = (xyz, rho)
 // and svel[p].w = pressure. `counters` may be null (no pair counting).
 cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, const uint2* bucket, const TankConst* tanks,
-                           const uint16_t* stank, uint32_t n, StepCounters* counters, cudaStream_t stream);
+                           const uint16_t* stank, uint32_t n, StepCounters* counters, cudaStream_t stream,
+                           const NeighbourTuning& tuning);
 
 // Forces, semi-implicit Euler, speed clamp and walls (fluid_sph.cpp:225-305).
 // Writes the id-order state.
 cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
                              const TankConst* tanks, const uint16_t* stank, uint32_t n, float4* pos, float4* vel,
-                             cudaStream_t stream);
+                             cudaStream_t stream, const NeighbourTuning& tuning);
 
 // FluidSolver::emit lattice (fluid_sph.cpp:138-154) for particles
 // [first, first + count) of one tank.
@@ -85,6 +123,11 @@ cudaError_t launch_stats(const float4* pos, const float4* vel, const uint16_t* t
                          uint32_t n, double* acc, cudaStream_t stream);
 // Counts particles whose position or velocity xyz is not finite (adds to *out).
 cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_t n, uint32_t* out, cudaStream_t stream);
+// Counts x / y (over `count` generated pairs) where division through a
+// correctly rounded reciprocal differs from IEEE division. mode 0: every
+// divisor mantissa; mode 1: random signs, mantissas, exponents.
+cudaError_t launch_division_selftest(uint64_t seed, uint64_t count, int mode, unsigned long long* mismatches,
+                                     cudaStream_t stream);
 // Largest bucket count and number of buckets above capacity.
 cudaError_t launch_bucket_stats(const uint2* bucket, uint32_t buckets, uint32_t* out2, cudaStream_t stream);
 

@@ -189,6 +189,18 @@ class FluidSolverGpu:
         self._check(self._lib.sph_device_state(self._ctx, ctypes.byref(pos), ctypes.byref(vel)), "sph_device_state")
         return int(pos.value or 0), int(vel.value or 0)
 
+    def tuning(self) -> dict:
+        out = abi.SphTuning()
+        self._check(self._lib.sph_get_tuning(self._ctx, ctypes.byref(out)), "sph_get_tuning")
+        return out.as_dict()
+
+    def set_tuning(self, **knobs) -> None:
+        """Changes the launch shape (radix_bits, neighbour_kernel, block_size, queue_depth)."""
+        current = self.tuning()
+        current.update(knobs)
+        t = abi.SphTuning(**current)
+        self._check(self._lib.sph_set_tuning(self._ctx, ctypes.byref(t)), "sph_set_tuning")
+
     PROFILE_PHASES = ("keys", "sort", "bounds_gather", "density", "integrate")
 
     def profile(self, dt: float, substeps: int) -> dict:

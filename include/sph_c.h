@@ -122,6 +122,18 @@ typedef struct sph_stats {
     uint32_t pad;
 } sph_stats;
 
+/* Launch shape of the step; results do not depend on it. */
+typedef struct sph_tuning {
+    uint32_t radix_bits;       /* digit width of the grid sort, 1..8 */
+    uint32_t neighbour_kernel; /* 0: nested per-candidate loops; 1: flat stream + queued pair pass;
+                                  2: density records in-range pairs, integrate runs them;
+                                  3: as 2, divisions through a shared correctly rounded reciprocal;
+                                  4: density stores per-bucket pair masks, integrate expands them */
+    uint32_t block_size;       /* threads per block of integrate (32..512, multiple of 32; 64/128/256 for 2-4) */
+    uint32_t queue_depth;      /* in-range pairs buffered per thread: 8, 16, 24 or 32 */
+    uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 Morton order of 4x4x4-cell tiles */
+} sph_tuning;
+
 typedef struct sph_ctx sph_ctx;
 
 /* ---- version and diagnostics ---------------------------------------- */
@@ -209,6 +221,14 @@ int sph_run(sph_ctx* ctx, float dt, uint32_t substeps);
  * Synchronises. Results are identical to sph_run. */
 #define SPH_PROFILE_PHASES 5
 int sph_profile_substeps(sph_ctx* ctx, float dt, uint32_t substeps, double* phase_ms);
+/* Reads / replaces the launch shape (an autotuner's knobs). */
+int sph_get_tuning(const sph_ctx* ctx, sph_tuning* out);
+int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning);
+/* Diagnostic: counts, over `count` generated (x, y), the quotients where
+ * division through a correctly rounded reciprocal (the integrate pass of
+ * neighbour_kernel 3) differs from IEEE x / y. mode 0: every divisor mantissa
+ * in [1, 2); mode 1: random signs, mantissas and exponents 2^-60..2^60. */
+int sph_selftest_division(sph_ctx* ctx, uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
 /* Number of kernel launches one substep enqueues. */
 int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches);
 /* Bytes of device memory the context holds. */

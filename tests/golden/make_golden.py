@@ -1,0 +1,94 @@
+"""Generates the golden vectors in tests/golden/ from the reference itself.
+
+The reference's unmodified src/physics/fluid_sph.cpp is compiled in place
+(oracle/ref/Makefile -> oracle/_ref/libsph_ref.so) and run on small seeded
+cases; its outputs are frozen here so that machines without the reference
+tree (the GPU host) can still pin the oracle and the CUDA path to it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from computer_graphics_lab_00_gb300 import workloads as W  # noqa: E402
+from oracle.bind import Reference, build_reference  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def params_bytes(params) -> np.ndarray:
+    return np.frombuffer(bytes(params), dtype=np.uint8).copy()
+
+
+def compact_slots(counts: np.ndarray, slots: np.ndarray) -> np.ndarray:
+    filled = np.minimum(counts, 32)
+    used = (np.arange(32)[None, :] < filled[:, None]).reshape(-1)
+    return slots[used]
+
+
+def scene_frames() -> dict:
+    """tests/fluid_test.cpp's scene: emit 1024, then 30 frames of 1/60 s."""
+    params = W.reference_test_scene(1024)
+    ref = Reference()
+    ref.emit(params, 1024)
+    emit_pos, emit_vel = ref.state()
+    ref.step(params, 1.0 / 60.0, frames=30)
+    pos, vel = ref.state()
+    return {"params": params_bytes(params), "emit_pos": emit_pos, "emit_vel": emit_vel, "pos_30": pos, "vel_30": vel}
+
+
+def dam_break_small() -> dict:
+    """2,048 jittered particles (16 x 16 x 8) in a 0.6 m box, 4,096 buckets."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(0.6, 0.6, 0.6), lattice=(16, 16, 8),
+                           cell_count=4096)
+    pos, vel = W.jittered_block(params, 2048, seed=11)
+    ref = Reference()
+    cell_of, counts, slots = ref.grid_build(params, pos)
+    ref.set_state(pos, vel)
+    ref.substep(params, 1.0 / 600.0)
+    pos1, vel1 = ref.state()
+    for _ in range(19):
+        ref.substep(params, 1.0 / 600.0)
+    pos20, vel20 = ref.state()
+    return {"params": params_bytes(params), "pos": pos, "vel": vel, "cell_of": cell_of, "cell_counts": counts,
+            "cell_slots": compact_slots(counts, slots), "pos_1": pos1, "vel_1": vel1, "pos_20": pos20,
+            "vel_20": vel20}
+
+
+def collisions_overflow() -> dict:
+    """1,024 particles with 1,024 buckets (colliding neighbour cells), 200 of
+    them packed into one cell (an overflowing bucket)."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(0.5, 0.5, 0.5), lattice=(8, 8, 16),
+                           cell_count=1024)
+    pos, vel = W.jittered_block(params, 1024, seed=21)
+    u = W.uniform01(99, np.arange(600, dtype=np.uint64)).reshape(200, 3)
+    pos[:200, :3] = np.float32(0.2) + u * np.float32(0.039)
+    ref = Reference()
+    cell_of, counts, slots = ref.grid_build(params, pos)
+    ref.set_state(pos, vel)
+    for _ in range(5):
+        ref.substep(params, 1.0 / 600.0)
+    pos5, vel5 = ref.state()
+    return {"params": params_bytes(params), "pos": pos, "vel": vel, "cell_of": cell_of, "cell_counts": counts,
+            "cell_slots": compact_slots(counts, slots), "pos_5": pos5, "vel_5": vel5}
+
+
+def main() -> None:
+    if build_reference() is None:
+        raise SystemExit("the reference tree is needed to regenerate the golden vectors")
+    for name, make in (("scene_frames", scene_frames), ("dam_break_small", dam_break_small),
+                       ("collisions_overflow", collisions_overflow)):
+        data = make()
+        np.savez_compressed(OUT / f"{name}.npz", **data)
+        print(name, {k: v.shape for k, v in data.items()})
+
+
+if __name__ == "__main__":
+    main()

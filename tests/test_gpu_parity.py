@@ -144,7 +144,7 @@ def test_overflowing_bucket_keeps_first_32_ids(native, oracle):
     rng = np.random.default_rng(7)
     n = 300
     pos = np.zeros((n, 4), np.float32)
-    pos[:, :3] = (0.5 + rng.uniform(0.0, 0.039, size=(n, 3))).astype(np.float32)  # one 0.04 m cell
+    pos[:, :3] = (0.481 + rng.uniform(0.0, 0.038, size=(n, 3))).astype(np.float32)  # inside cell [0.48, 0.52)
     pos[200:, :3] = rng.uniform(0.1, 0.9, size=(100, 3)).astype(np.float32)
     pos[:, 3] = 1000.0
     vel = np.zeros((n, 4), np.float32)
@@ -244,3 +244,86 @@ def test_errors_are_status_codes(native):
     with pytest.raises(abi.SphError) as e:
         FluidSolverGpu(coll, 16)
     assert e.value.status == abi.SPH_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("tuning", [
+    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=7, schedule=0),
+    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=7, schedule=1),
+    dict(neighbour_kernel=1, block_size=64, queue_depth=8, radix_bits=8, schedule=1),
+    dict(neighbour_kernel=1, block_size=128, queue_depth=16, radix_bits=7, schedule=0),
+    dict(neighbour_kernel=1, block_size=256, queue_depth=24, radix_bits=5, schedule=1),
+    dict(neighbour_kernel=1, block_size=128, queue_depth=32, radix_bits=3, schedule=0),
+    dict(neighbour_kernel=2, block_size=64, queue_depth=16, radix_bits=7, schedule=1),
+    dict(neighbour_kernel=2, block_size=128, queue_depth=16, radix_bits=8, schedule=0),
+    dict(neighbour_kernel=3, block_size=128, queue_depth=16, radix_bits=7, schedule=1),
+    dict(neighbour_kernel=3, block_size=256, queue_depth=16, radix_bits=6, schedule=0),
+    dict(neighbour_kernel=4, block_size=64, queue_depth=16, radix_bits=7, schedule=0),
+    dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=1),
+    dict(neighbour_kernel=4, block_size=256, queue_depth=16, radix_bits=8, schedule=1),
+])
+def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
+    """Every launch shape the autotuner may pick gives the oracle's bits."""
+    n = 8192
+    params, pos, vel = small_block(n, (16, 16, 32), box=(0.5, 0.8, 0.8), cells=W.cell_count_for(n))
+    with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(**tuning)
+        assert solver.tuning() == tuning
+        solver.upload(pos, vel)
+        solver.run(1.0 / 600.0, 4)
+        gp, gv = solver.state()
+    op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 4, threads=oracle.hardware_threads)
+    assert_bit_exact(gp, op, f"positions {tuning}")
+    assert_bit_exact(gv, ov, f"velocities {tuning}")
+
+
+def test_bad_tuning_is_rejected(native):
+    case = W.dam_break_16k()
+    with FluidSolverGpu(case.params, 16) as solver:
+        for bad in (dict(block_size=100), dict(queue_depth=12), dict(neighbour_kernel=7), dict(radix_bits=0),
+                    dict(radix_bits=9), dict(schedule=2)):
+            with pytest.raises(abi.SphError) as e:
+                solver.set_tuning(**bad)
+            assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("mode,count", [(0, 1 << 29), (1, 1 << 30), (2, 1 << 26), (3, 1 << 26), (4, 1 << 26),
+                                        pytest.param(5, 1 << 26, marks=pytest.mark.xfail(
+                                            reason="ptxas contracts packed f32x2 mul+add into a fused "
+                                                   "multiply-add even under --fmad=false, so the exact passes "
+                                                   "use scalar arithmetic", strict=False))])
+def test_reciprocal_division_matches_ieee(native, mode, count):
+    """Arithmetic the exact passes rely on, against IEEE scalar operations:
+    division through a correctly rounded reciprocal (modes 0-1: every divisor
+    mantissa; random operands over 2^-60..2^60), and packed f32x2 mul, add and
+    sub lane by lane (modes 2-4). Mode 5 records that a packed squared-distance
+    chain does not round like the scalar chain."""
+    import ctypes
+
+    case = W.dam_break_16k()
+    with FluidSolverGpu(case.params, 16) as solver:
+        bad = ctypes.c_uint64()
+        status = native.sph_selftest_division(solver._ctx, 12345, count, mode, ctypes.byref(bad))
+        assert status == 0
+        assert bad.value == 0
+
+
+def test_pair_list_overflow_falls_back_bit_exact(native, oracle):
+    """Particles with more in-range pairs than a list holds (64) are scanned
+    directly by integrate; a compressed clump forces that path."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
+                           lattice=(4, 4, 8), cell_count=4096)
+    rng = np.random.default_rng(3)
+    n = 2000
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = (0.4 + rng.uniform(0.0, 0.12, size=(n, 3))).astype(np.float32)
+    pos[:, 3] = 1000.0
+    vel = np.zeros((n, 4), np.float32)
+    for variant, schedule in ((2, 0), (3, 1), (4, 0), (4, 1)):
+        with FluidSolverGpu(params, n) as solver:
+            solver.set_tuning(neighbour_kernel=variant, schedule=schedule)
+            solver.upload(pos, vel)
+            solver.run(1.0 / 600.0, 2)
+            gp, gv = solver.state()
+        op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 2)
+        assert_bit_exact(gp, op, f"positions with list overflow, variant {variant}")
+        assert_bit_exact(gv, ov, f"velocities with list overflow, variant {variant}")
