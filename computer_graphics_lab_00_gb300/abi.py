@@ -19,6 +19,8 @@ SPH_ABI_VERSION = 1
 SPH_CELL_CAPACITY = 32
 SPH_MAX_COLLIDERS = 8
 SPH_MAX_FORCE_FIELDS = 8
+SPH_STATIC_MAX_PARTICLES = 65536
+SPH_STATIC_MAX_CELLS = 65536
 
 SPH_OK = 0
 SPH_ERR_INVALID_ARGUMENT = -1
@@ -218,6 +220,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_synchronize": (c_int, [c_void_p]),
         "sph_grid_download": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
         "sph_grid_build": (c_int, [c_void_p]),
+        "sph_grid_build_static": (c_int, [P(SphParams), c_void_p, c_u32, c_void_p, c_void_p, c_void_p, c_void_p]),
         "sph_stats_compute": (c_int, [c_void_p, P(SphStats)]),
         "sph_stream": (c_int, [c_void_p, P(c_void_p)]),
         "sph_device_state": (c_int, [c_void_p, P(c_void_p), P(c_void_p)]),

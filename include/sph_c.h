@@ -201,6 +201,41 @@ int sph_grid_download(sph_ctx* ctx, uint32_t* cell_of, uint32_t* cell_counts, ui
 /* Builds the grid for the current positions without stepping. */
 int sph_grid_build(sph_ctx* ctx);
 
+/*
+ * Grid build that allocates nothing. This entry point has no counterpart in
+ * the reference. It is for callers that cannot allocate device memory at the
+ * point where they build the grid: a render loop that records a frame's GPU
+ * work under a fixed device-memory budget (its engine hands all memory to its
+ * own allocator up front), or a latency-critical loop that cannot afford the
+ * implicit device synchronisation a cudaMalloc may bring.
+ *
+ * The caller passes device buffers: `positions` (count AoS float4, id order),
+ * and receives `cell_of` (count u32), `cell_counts` (C u32, un-truncated) and
+ * `cell_particles` (C * 32 u32: the first 32 ids of each bucket, ascending;
+ * slots past a bucket's count are left untouched) — the arrays of
+ * FluidGrid::build for C = params->lattice[3]. Work is enqueued on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream) and is complete when
+ * that stream reaches it.
+ *
+ * The sort's scratch is a static device array inside the library, sized for
+ * at most SPH_STATIC_MAX_PARTICLES particles and SPH_STATIC_MAX_CELLS buckets
+ * (about 1.6 MB, held on every GPU that uses this call until the process
+ * exits); larger requests return SPH_ERR_CAPACITY. The first call on a device
+ * looks the array's device address up (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture. All calls share
+ * the one array, so calls whose work overlaps on the GPU (on different
+ * streams, or from different threads) race with each other: serialise them.
+ */
+#define SPH_STATIC_MAX_PARTICLES 65536u
+#define SPH_STATIC_MAX_CELLS 65536u
+int sph_grid_build_static(const sph_params* params,
+                          const void* positions,
+                          uint32_t count,
+                          void* cell_of,
+                          void* cell_counts,
+                          void* cell_particles,
+                          void* stream);
+
 /* ---- statistics -------------------------------------------------------- */
 
 /* Reduces statistics of the current state (FP64 on the device). */
