@@ -57,6 +57,8 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=None, help="steps of the end-to-end leg (default: --steps)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--batched-steps", type=int, default=20,
+                   help="substeps of the 256-tank leg (0 skips it)")
     return p.parse_args()
 
 
@@ -169,6 +171,45 @@ def cpu_baseline(case, seconds: float) -> dict:
         "sample": f"{steps} substeps of the full {case.count}-particle tank from its initial state ({wall:.1f} s)",
         "ms_per_step": 1e3 * wall / steps,
     }
+
+
+def batched_leg(steps: int, flush, device: int) -> dict:
+    """256 independent tanks (about 5M particles, uneven sizes) advanced by one
+    CUDA graph launch per substep; launch shape from the autotuner."""
+    import torch
+
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.batch import BatchSolverGpu
+
+    ts = W.batched_tanks()
+    solver = BatchSolverGpu(ts.params, ts.counts, device=device)
+    for t in range(len(ts.counts)):
+        solver.upload(t, *ts.initial_state(t))
+    tune = solver.autotune(ts.dt, 3)
+    stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
+    solver.run(ts.dt, 3)
+    solver.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            starts[k].record(stream)
+        solver.run(ts.dt, 1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
+    phases = solver.profile(ts.dt, 3)
+    n = ts.total_particles
+    out = {
+        "workload": ts.name, "tanks": len(ts.counts), "particles": n, "dt": ts.dt, "steps": steps,
+        "ms_per_step": ms, "value": n * ts.dt / (ms / 1e3), "unit": UNIT,
+        "particle_steps_per_s": n / (ms / 1e3), "tuning": tune["tuning"],
+        "phase_ms": {k: v / 3 for k, v in phases.items()},
+        "launches_per_substep": solver.launches_per_substep(),
+    }
+    solver.close()
+    return out
 
 
 def run_reference(args) -> None:
@@ -361,6 +402,8 @@ def run_gb300(args) -> None:
         "clocks": clocks,
         "wall_s_timed": wall,
     }
+    if args.batched_steps > 0 and world == 1:
+        out["batched"] = batched_leg(args.batched_steps, flush, local)
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, args.cpu_seconds)
     solver.close()

@@ -31,6 +31,7 @@ SPH_ERR_UNSUPPORTED = -5
 SPH_ERR_TIMEOUT = -6
 SPH_ERR_NO_DEVICE = -7
 SPH_ERR_NONFINITE = -8
+SPH_ALL_TANKS = 0xFFFFFFFF
 
 
 class SphCollider(ctypes.Structure):
@@ -232,6 +233,33 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_launches_per_substep": (c_int, [c_void_p, u32p]),
         "sph_device_bytes": (c_int, [c_void_p, P(ctypes.c_uint64)]),
     }
+    u8p = P(ctypes.c_uint8)
+    f64p = P(ctypes.c_double)
+    tp = P(SphTuning)
+    sigs.update({
+        "sph_autotune": (c_int, [c_void_p, c_f32, c_u32, tp, f32p]),
+        "sph_batch_create": (c_int, [P(SphParams), u32p, c_u32, c_int, P(c_void_p)]),
+        "sph_batch_destroy": (c_int, [c_void_p]),
+        "sph_batch_last_error": (ctypes.c_char_p, [c_void_p]),
+        "sph_batch_tank_count": (c_int, [c_void_p, u32p]),
+        "sph_batch_particle_count": (c_int, [c_void_p, c_u32, u32p]),
+        "sph_batch_upload": (c_int, [c_void_p, c_u32, c_void_p, c_void_p]),
+        "sph_batch_download": (c_int, [c_void_p, c_u32, c_void_p, c_void_p]),
+        "sph_batch_emit": (c_int, [c_void_p, c_u32]),
+        "sph_batch_set_active": (c_int, [c_void_p, u8p]),
+        "sph_batch_run": (c_int, [c_void_p, c_f32, c_u32]),
+        "sph_batch_run_per_tank": (c_int, [c_void_p, f32p, u32p]),
+        "sph_batch_step": (c_int, [c_void_p, c_f32]),
+        "sph_batch_stats": (c_int, [c_void_p, P(SphStats)]),
+        "sph_batch_synchronize": (c_int, [c_void_p]),
+        "sph_batch_stream": (c_int, [c_void_p, P(c_void_p)]),
+        "sph_batch_get_tuning": (c_int, [c_void_p, tp]),
+        "sph_batch_set_tuning": (c_int, [c_void_p, tp]),
+        "sph_batch_autotune": (c_int, [c_void_p, c_f32, c_u32, tp, f32p]),
+        "sph_batch_profile_substeps": (c_int, [c_void_p, c_f32, c_u32, f64p]),
+        "sph_batch_launches_per_substep": (c_int, [c_void_p, u32p]),
+        "sph_batch_device_bytes": (c_int, [c_void_p, P(ctypes.c_uint64)]),
+    })
     for name, (restype, argtypes) in sigs.items():
         fn = getattr(lib, name)
         fn.restype = restype

@@ -7,11 +7,16 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/sph_c.h"
 #include "sph_engine.h"
 
 struct sph_ctx {
+    sph::Engine engine;
+};
+
+struct sph_batch {
     sph::Engine engine;
 };
 
@@ -26,6 +31,29 @@ uint32_t bit_ceil(uint32_t x) {
         v <<= 1;
     }
     return v;
+}
+
+void to_api(const sph::TuneChoice& c, sph_tuning* out) {
+    out->radix_bits = c.radix_bits;
+    out->neighbour_kernel = c.tuning.variant;
+    out->block_size = c.tuning.block;
+    out->queue_depth = c.tuning.queue;
+    out->schedule = c.schedule ? 1u : 0u;
+}
+
+int autotune(sph::Engine& engine, float dt, uint32_t substeps, sph_tuning* best, float* best_ms) {
+    if (best == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    sph::TuneChoice choice;
+    int status = engine.autotune(dt, substeps, &choice, nullptr);
+    if (status == SPH_OK) {
+        to_api(choice, best);
+        if (best_ms != nullptr) {
+            *best_ms = choice.ms;
+        }
+    }
+    return status;
 }
 
 }  // namespace
@@ -327,6 +355,222 @@ int sph_device_bytes(const sph_ctx* ctx, uint64_t* bytes) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     *bytes = ctx->engine.device_bytes();
+    return SPH_OK;
+}
+
+int sph_autotune(sph_ctx* ctx, float dt, uint32_t substeps_per_trial, sph_tuning* best, float* best_ms) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return autotune(ctx->engine, dt, substeps_per_trial, best, best_ms);
+}
+
+// ---- batched tanks ----------------------------------------------------------
+
+int sph_batch_create(const sph_params* params, const uint32_t* counts, uint32_t tanks, int device, sph_batch** out) {
+    if (params == nullptr || counts == nullptr || out == nullptr || tanks == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    std::vector<sph_params> p(params, params + tanks);
+    std::vector<uint32_t> n(counts, counts + tanks);
+    for (uint32_t c : n) {
+        if (c == 0) {
+            return SPH_ERR_INVALID_ARGUMENT;
+        }
+    }
+    sph_batch* batch = new (std::nothrow) sph_batch();
+    if (batch == nullptr) {
+        return SPH_ERR_OUT_OF_MEMORY;
+    }
+    int status = batch->engine.init(device, p, n);
+    if (status != SPH_OK) {
+        delete batch;
+        return status;
+    }
+    *out = batch;
+    return SPH_OK;
+}
+
+int sph_batch_destroy(sph_batch* batch) {
+    delete batch;
+    return SPH_OK;
+}
+
+const char* sph_batch_last_error(const sph_batch* batch) { return batch == nullptr ? "" : batch->engine.last_error(); }
+
+int sph_batch_tank_count(const sph_batch* batch, uint32_t* tanks) {
+    if (batch == nullptr || tanks == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *tanks = batch->engine.tank_count();
+    return SPH_OK;
+}
+
+int sph_batch_particle_count(const sph_batch* batch, uint32_t tank, uint32_t* count) {
+    if (batch == nullptr || count == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (tank == SPH_ALL_TANKS) {
+        *count = batch->engine.total_count();
+        return SPH_OK;
+    }
+    if (tank >= batch->engine.tank_count()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *count = batch->engine.count(tank);
+    return SPH_OK;
+}
+
+int sph_batch_upload(sph_batch* batch, uint32_t tank, const float* positions, const float* velocities) {
+    if (batch == nullptr || tank >= batch->engine.tank_count()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.upload(tank, positions, velocities, batch->engine.capacity(tank));
+}
+
+int sph_batch_download(sph_batch* batch, uint32_t tank, float* positions, float* velocities) {
+    if (batch == nullptr || tank >= batch->engine.tank_count()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.download(tank, positions, velocities);
+}
+
+int sph_batch_emit(sph_batch* batch, uint32_t tank) {
+    if (batch == nullptr || tank >= batch->engine.tank_count()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.emit(tank, batch->engine.capacity(tank));
+}
+
+int sph_batch_set_active(sph_batch* batch, const uint8_t* active) {
+    if (batch == nullptr || active == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<uint8_t> a(active, active + batch->engine.tank_count());
+    return batch->engine.set_active(a);
+}
+
+int sph_batch_run(sph_batch* batch, float dt, uint32_t substeps) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.run(dt, substeps);
+}
+
+int sph_batch_run_per_tank(sph_batch* batch, const float* dt, const uint32_t* substeps) {
+    if (batch == nullptr || dt == nullptr || substeps == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    uint32_t tanks = batch->engine.tank_count();
+    return batch->engine.run_per_tank(std::vector<float>(dt, dt + tanks),
+                                      std::vector<uint32_t>(substeps, substeps + tanks));
+}
+
+// FluidSolver::step for every tank: each tank splits the frame with its own
+// fluidSubsteps (fluid_sph.cpp:311-321).
+int sph_batch_step(sph_batch* batch, float delta_seconds) {
+    if (batch == nullptr || std::isnan(delta_seconds)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (delta_seconds <= 0.0F) {
+        return SPH_OK;
+    }
+    uint32_t tanks = batch->engine.tank_count();
+    std::vector<float> dt(tanks);
+    std::vector<uint32_t> n(tanks);
+    float frame_step = std::min(delta_seconds, SPH_MAX_FRAME_STEP);
+    for (uint32_t t = 0; t < tanks; ++t) {
+        n[t] = sph::fluid_substeps(batch->engine.params(t), delta_seconds);
+        dt[t] = frame_step / static_cast<float>(n[t]);
+    }
+    return batch->engine.run_per_tank(dt, n);
+}
+
+int sph_batch_stats(sph_batch* batch, sph_stats* out) {
+    if (batch == nullptr || out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<sph_stats> all;
+    int status = batch->engine.stats_all(all);
+    if (status == SPH_OK) {
+        std::copy(all.begin(), all.end(), out);
+    }
+    return status;
+}
+
+int sph_batch_synchronize(sph_batch* batch) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.synchronize();
+}
+
+int sph_batch_stream(sph_batch* batch, void** stream) {
+    if (batch == nullptr || stream == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *stream = static_cast<void*>(batch->engine.stream());
+    return SPH_OK;
+}
+
+int sph_batch_get_tuning(const sph_batch* batch, sph_tuning* out) {
+    if (batch == nullptr || out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    sph::TuneChoice c;
+    c.tuning = batch->engine.tuning();
+    c.radix_bits = batch->engine.radix_bits();
+    c.schedule = batch->engine.schedule_on();
+    to_api(c, out);
+    return SPH_OK;
+}
+
+int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
+    if (batch == nullptr || tuning == nullptr || tuning->schedule > 1) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    sph::NeighbourTuning t = batch->engine.tuning();
+    t.variant = tuning->neighbour_kernel;
+    t.block = tuning->block_size;
+    t.queue = tuning->queue_depth;
+    int status = batch->engine.set_tuning(t);
+    if (status == SPH_OK) {
+        status = batch->engine.set_schedule(tuning->schedule != 0);
+    }
+    if (status == SPH_OK) {
+        status = batch->engine.set_radix_bits(tuning->radix_bits);
+    }
+    return status;
+}
+
+int sph_batch_autotune(sph_batch* batch, float dt, uint32_t substeps_per_trial, sph_tuning* best, float* best_ms) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return autotune(batch->engine, dt, substeps_per_trial, best, best_ms);
+}
+
+int sph_batch_profile_substeps(sph_batch* batch, float dt, uint32_t substeps, double* phase_ms) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.profile(dt, substeps, phase_ms);
+}
+
+int sph_batch_launches_per_substep(const sph_batch* batch, uint32_t* launches) {
+    if (batch == nullptr || launches == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *launches = batch->engine.launches_per_substep();
+    return SPH_OK;
+}
+
+int sph_batch_device_bytes(const sph_batch* batch, uint64_t* bytes) {
+    if (batch == nullptr || bytes == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *bytes = batch->engine.device_bytes();
     return SPH_OK;
 }
 

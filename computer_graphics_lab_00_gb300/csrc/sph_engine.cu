@@ -167,7 +167,7 @@ void Engine::release() {
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
-                       schedule_.tile_of, schedule_.order, schedule_.tile_hist};
+                       schedule_.tile_of, schedule_.order, schedule_.tile_hist, snap_pos_, snap_vel_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -510,6 +510,216 @@ int Engine::run(float dt, uint32_t substeps) {
     return SPH_OK;
 }
 
+int Engine::run_per_tank(const std::vector<float>& dt, const std::vector<uint32_t>& substeps) {
+    if (dt.size() != tanks_.size() || substeps.size() != tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    uint32_t rounds = 0;
+    for (size_t t = 0; t < tanks_.size(); ++t) {
+        if (substeps[t] > 0 && (!(dt[t] > 0.0F) || !std::isfinite(dt[t]))) {
+            return SPH_ERR_INVALID_ARGUMENT;
+        }
+        rounds = std::max(rounds, substeps[t]);
+    }
+    if (total_count_ == 0 || rounds == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = ensure_graph();
+    if (status != SPH_OK) {
+        return status;
+    }
+    std::vector<uint32_t> chosen(tanks_.size());
+    for (size_t t = 0; t < tanks_.size(); ++t) {
+        chosen[t] = user_active_.empty() ? 1U : user_active_[t];
+    }
+    for (uint32_t r = 0; r < rounds; ++r) {
+        // Tank t runs substeps[t] substeps of dt[t]; afterwards it sits out.
+        for (size_t t = 0; t < tanks_.size(); ++t) {
+            TankConst& k = tanks_[t];
+            k.active = (r < substeps[t] && chosen[t] != 0) ? 1U : 0U;
+            k.dt = dt[t];
+            k.max_speed = dt[t] > 0.0F ? 0.4F * k.h / dt[t] : 0.0F;
+        }
+        SPH_CUDA(cudaMemcpyAsync(d_tanks_, tanks_.data(), tanks_.size() * sizeof(TankConst), cudaMemcpyHostToDevice,
+                                 stream_));
+        SPH_CUDA(cudaGraphLaunch(graph_, stream_));
+    }
+    for (size_t t = 0; t < tanks_.size(); ++t) {
+        tanks_[t].active = chosen[t];
+    }
+    consts_dirty_ = true;
+    grid_valid_ = true;
+    return SPH_OK;
+}
+
+int Engine::stats_all(std::vector<sph_stats>& out) {
+    out.assign(tanks_.size(), sph_stats{});
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = refresh_constants(const_dt_ < 0.0F ? 0.0F : const_dt_);
+    if (status != SPH_OK) {
+        return status;
+    }
+    SPH_CUDA(cudaMemsetAsync(stats_acc_, 0, sizeof(double) * kStatsPerTank * tanks_.size(), stream_));
+    SPH_CUDA(launch_stats(pos_, vel_, tank_of_, d_tanks_, total_count_, stats_acc_, stream_));
+    std::vector<double> acc(kStatsPerTank * tanks_.size());
+    SPH_CUDA(cudaMemcpyAsync(acc.data(), stats_acc_, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    for (size_t t = 0; t < tanks_.size(); ++t) {
+        const double* a = acc.data() + t * kStatsPerTank;
+        sph_stats& o = out[t];
+        o.particles = tanks_[t].particle_count;
+        o.buckets = params_[t].lattice[3];
+        double count = a[8];
+        if (count > 0) {
+            o.mean_density = a[0] / count;
+            o.mean_compression = a[1] / count;
+            o.centre_of_mass[0] = a[3] / count;
+            o.centre_of_mass[1] = a[4] / count;
+            o.centre_of_mass[2] = a[5] / count;
+        }
+        std::memcpy(&o.max_density, &a[2], sizeof(double));
+        o.kinetic_energy = a[6];
+        o.nonfinite = static_cast<uint32_t>(a[7]);
+    }
+    return SPH_OK;
+}
+
+int Engine::snapshot(bool save) {
+    SPH_CUDA(cudaSetDevice(device_));
+    if (snap_pos_ == nullptr) {
+        int status = SPH_OK;
+        if ((status = alloc(&snap_pos_, total_capacity_)) != SPH_OK ||
+            (status = alloc(&snap_vel_, total_capacity_)) != SPH_OK) {
+            return status;
+        }
+    }
+    size_t bytes = sizeof(float4) * total_count_;
+    if (bytes == 0) {
+        return SPH_OK;
+    }
+    if (save) {
+        SPH_CUDA(cudaMemcpyAsync(snap_pos_, pos_, bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(snap_vel_, vel_, bytes, cudaMemcpyDeviceToDevice, stream_));
+    } else {
+        SPH_CUDA(cudaMemcpyAsync(pos_, snap_pos_, bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(vel_, snap_vel_, bytes, cudaMemcpyDeviceToDevice, stream_));
+        grid_valid_ = false;
+    }
+    return SPH_OK;
+}
+
+int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<TuneChoice>* tried) {
+    if (best == nullptr || !(dt > 0.0F) || substeps == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (total_count_ == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    cudaEvent_t start = nullptr;
+    cudaEvent_t stop = nullptr;
+    SPH_CUDA(cudaEventCreate(&start));
+    SPH_CUDA(cudaEventCreate(&stop));
+    int status = snapshot(true);
+    const NeighbourTuning original = tuning_;
+    const uint32_t original_bits = radix_bits_;
+    const bool original_schedule = use_schedule_;
+    auto measure = [&](const TuneChoice& c, float* ms) -> int {
+        int st = set_tuning(c.tuning);
+        if (st == SPH_OK) {
+            st = set_schedule(c.schedule);
+        }
+        if (st == SPH_OK) {
+            st = set_radix_bits(c.radix_bits);
+        }
+        if (st == SPH_OK) {
+            st = snapshot(false);
+        }
+        if (st == SPH_OK) {
+            st = run(dt, 1);  // captures the graph, warms caches
+        }
+        if (st != SPH_OK) {
+            return st;
+        }
+        SPH_CUDA(cudaEventRecord(start, stream_));
+        st = run(dt, substeps);
+        if (st != SPH_OK) {
+            return st;
+        }
+        SPH_CUDA(cudaEventRecord(stop, stream_));
+        SPH_CUDA(cudaEventSynchronize(stop));
+        SPH_CUDA(cudaEventElapsedTime(ms, start, stop));
+        *ms /= static_cast<float>(substeps);
+        return SPH_OK;
+    };
+    // Stage 1: neighbour kernel, block size and processing order; stage 2:
+    // the radix digit width for the winner.
+    std::vector<TuneChoice> stage1;
+    for (uint32_t variant : {3u, 4u}) {
+        for (uint32_t block : {128u, 256u}) {
+            for (bool schedule : {false, true}) {
+                TuneChoice c;
+                c.tuning = original;
+                c.tuning.variant = variant;
+                c.tuning.block = block;
+                c.tuning.queue = 32;
+                c.schedule = schedule;
+                c.radix_bits = original_bits;
+                stage1.push_back(c);
+            }
+        }
+    }
+    TuneChoice winner;
+    winner.ms = 1e30F;
+    for (TuneChoice& c : stage1) {
+        if (status == SPH_OK) {
+            status = measure(c, &c.ms);
+        }
+        if (status == SPH_OK && c.ms < winner.ms) {
+            winner = c;
+        }
+        if (tried != nullptr) {
+            tried->push_back(c);
+        }
+    }
+    for (uint32_t bits : {5u, 6u, 7u, 8u}) {
+        if (status != SPH_OK || bits == winner.radix_bits) {
+            continue;
+        }
+        TuneChoice c = winner;
+        c.radix_bits = bits;
+        status = measure(c, &c.ms);
+        if (status == SPH_OK && c.ms < winner.ms) {
+            winner = c;
+        }
+        if (tried != nullptr) {
+            tried->push_back(c);
+        }
+    }
+    int restore = snapshot(false);
+    if (status == SPH_OK) {
+        status = restore;
+    }
+    if (status == SPH_OK) {
+        status = set_tuning(winner.tuning);
+        if (status == SPH_OK) {
+            status = set_schedule(winner.schedule);
+        }
+        if (status == SPH_OK) {
+            status = set_radix_bits(winner.radix_bits);
+        }
+        *best = winner;
+    } else {
+        set_tuning(original);
+        set_schedule(original_schedule);
+        set_radix_bits(original_bits);
+    }
+    cudaEventDestroy(start);
+    cudaEventDestroy(stop);
+    return status;
+}
+
 int Engine::build_grid() {
     SPH_CUDA(cudaSetDevice(device_));
     int status = refresh_constants(const_dt_ < 0.0F ? 0.0F : const_dt_);
@@ -635,6 +845,7 @@ int Engine::set_active(const std::vector<uint8_t>& active) {
     if (active.size() != tanks_.size()) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
+    user_active_ = active;
     for (size_t t = 0; t < tanks_.size(); ++t) {
         tanks_[t].active = active[t] != 0 ? 1U : 0U;
     }

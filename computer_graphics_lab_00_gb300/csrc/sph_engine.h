@@ -26,6 +26,14 @@ float sqrt_at_least(float v);  // smallest x >= 0 with sqrtf(x) >= v
 float sqrt_at_most(float v);   // largest x >= 0 with sqrtf(x) <= v
 int validate_params(const sph_params& params);
 
+// One launch shape and its measured time per substep.
+struct TuneChoice {
+    NeighbourTuning tuning{};
+    uint32_t radix_bits = 6;
+    bool schedule = false;
+    float ms = 0.0F;
+};
+
 class Engine {
 public:
     ~Engine();
@@ -43,6 +51,16 @@ public:
 
     // Enqueues `substeps` substeps of length dt for every active tank.
     int run(float dt, uint32_t substeps);
+    // Tank t runs substeps[t] substeps of length dt[t] (tanks that finish
+    // early sit out the remaining rounds).
+    int run_per_tank(const std::vector<float>& dt, const std::vector<uint32_t>& substeps);
+    // FP64 statistics of every tank.
+    int stats_all(std::vector<sph_stats>& out);
+    // Times candidate launch shapes on the current state (restored after)
+    // and keeps the fastest. Results never depend on the shape.
+    int autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<TuneChoice>* tried);
+    // Saves (true) or restores (false) the particle state in device memory.
+    int snapshot(bool save);
     // Grid build only (for inspection).
     int build_grid();
     int grid_download(uint32_t tank, uint32_t* cell_of, uint32_t* cell_counts, uint32_t* cell_particles);
@@ -63,6 +81,7 @@ public:
 
     uint32_t tank_count() const { return static_cast<uint32_t>(tanks_.size()); }
     uint32_t count(uint32_t tank) const { return tanks_[tank].particle_count; }
+    uint32_t capacity(uint32_t tank) const { return capacity_[tank]; }
     uint32_t total_count() const { return total_count_; }
     const sph_params& params(uint32_t tank) const { return params_[tank]; }
     uint32_t launches_per_substep() const { return launches_per_substep_; }
@@ -120,6 +139,9 @@ private:
     uint32_t launches_per_substep_ = 0;
     bool grid_valid_ = false;
     uint32_t nonfinite_host_ = 0;
+    std::vector<uint8_t> user_active_;
+    float4* snap_pos_ = nullptr;
+    float4* snap_vel_ = nullptr;
     cudaEvent_t events_[kProfilePhases + 1] = {};
     std::string last_error_;
 };

@@ -222,3 +222,73 @@ def reference_test_scene(count: int = 1024, cell_count: int = 1024) -> SphParams
         smoothing_radius=0.1,
         emitter_world=translation((0.0, 1.0, 0.0)),
     )
+
+
+@dataclass
+class TankSet:
+    """Many independent tanks: per-tank constants, counts and initial states."""
+
+    name: str
+    params: list
+    counts: list
+    dt: float
+    steps: int
+    seed: int
+    notes: str = ""
+
+    def initial_state(self, tank: int):
+        return jittered_block(self.params[tank], self.counts[tank], self.seed * 1_000_003 + tank)
+
+    @property
+    def total_particles(self) -> int:
+        return int(sum(self.counts))
+
+
+def _draws(seed: int, stream: int, count: int) -> np.ndarray:
+    """`count` uniforms in [0, 1) from splitmix64, one stream per purpose."""
+    return uniform01(seed * 7919 + stream, np.arange(count, dtype=np.uint64)).astype(np.float64)
+
+
+def tank_lattice(n: int, extent, fill: float, spacing: float):
+    """Block of `n` particles for one tank: nx = floor(f Lx / s),
+    nz = floor(f Lz / s), ny = ceil(n / (nx nz)); while the block is taller
+    than the tank allows (ny s > Ly - 2 s), nx and nz grow (within the walls)."""
+    s = spacing
+    nx = max(1, int(np.floor(fill * extent[0] / s)))
+    nz = max(1, int(np.floor(fill * extent[2] / s)))
+    max_x = max(1, int(np.floor((extent[0] - 2 * s) / s)))
+    max_z = max(1, int(np.floor((extent[2] - 2 * s) / s)))
+    ny = -(-n // (nx * nz))
+    while ny * s > extent[1] - 2 * s and (nx < max_x or nz < max_z):
+        if nx < max_x:
+            nx += 1
+        if nz < max_z:
+            nz += 1
+        ny = -(-n // (nx * nz))
+    # The emit rule fills x, then y, then z (fluid_sph.cpp:147-149).
+    layers = -(-n // (nx * ny))
+    return nx, ny, layers
+
+
+def batched_tanks(tanks: int = 256, seed: int = 0, spacing: float = 0.02) -> TankSet:
+    """Independent dam-break tanks with uneven particle counts.
+
+    Per tank: N log-uniform in [2048, 65536], extents uniform in [0.5, 2] m per
+    axis, initial block fill fraction uniform in [0.2, 0.6], s = 0.02 m,
+    h = 0.04 m, dt = 1/600 s, and the reference's bucket rule
+    (gfx::cellCountFor). All draws are seeded splitmix64 streams.
+    """
+    u_n = _draws(seed, 1, tanks)
+    u_l = _draws(seed, 2, 3 * tanks).reshape(tanks, 3)
+    u_f = _draws(seed, 3, tanks)
+    params, counts = [], []
+    for t in range(tanks):
+        n = int(round(np.exp(np.log(2048.0) + u_n[t] * (np.log(65536.0) - np.log(2048.0)))))
+        extent = [float(np.float32(0.5 + 1.5 * u_l[t, a])) for a in range(3)]
+        fill = 0.2 + 0.4 * u_f[t]
+        lattice = tank_lattice(n, extent, fill, spacing)
+        params.append(make_params(container_min=(0.0, 0.0, 0.0), container_max=extent, lattice=lattice,
+                                  cell_count=cell_count_for(n), spacing=spacing))
+        counts.append(n)
+    return TankSet("batched_256_tanks", params, counts, 1.0 / 600.0, 300, seed,
+                   "N_t log-uniform [2048, 65536], extents U[0.5, 2] m, fill U[0.2, 0.6]")

@@ -269,6 +269,53 @@ int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches);
 /* Bytes of device memory the context holds. */
 int sph_device_bytes(const sph_ctx* ctx, uint64_t* bytes);
 
+/* Times candidate launch shapes (neighbour kernel, block size, processing
+ * order, radix digit width) on the current state, which is restored
+ * afterwards, and keeps the fastest. Results are bit-identical for every
+ * shape. */
+int sph_autotune(sph_ctx* ctx, float dt, uint32_t substeps_per_trial, sph_tuning* best, float* best_ms);
+
+/* ---- batched tanks ------------------------------------------------------
+ *
+ * Many independent fluids ("tanks", each a physics::FluidSolver) advanced by
+ * the same kernel launches: one CUDA graph launch per substep covers every
+ * tank. Tank t has its own sph_params (container, lattice, bucket count) and a
+ * particle count fixed at create. There is no reference counterpart beyond
+ * the per-tank FluidSolver semantics (fluid_sph.cpp:190-321), which each tank
+ * keeps bit for bit. */
+#define SPH_ALL_TANKS 0xFFFFFFFFu
+typedef struct sph_batch sph_batch;
+
+int sph_batch_create(const sph_params* params, const uint32_t* counts, uint32_t tanks, int device, sph_batch** out);
+int sph_batch_destroy(sph_batch* batch);
+const char* sph_batch_last_error(const sph_batch* batch);
+int sph_batch_tank_count(const sph_batch* batch, uint32_t* tanks);
+/* Particles of one tank, or of all tanks with SPH_ALL_TANKS. */
+int sph_batch_particle_count(const sph_batch* batch, uint32_t tank, uint32_t* count);
+/* Host AoS float4 arrays of the tank's fixed particle count; velocities may be NULL. */
+int sph_batch_upload(sph_batch* batch, uint32_t tank, const float* positions, const float* velocities);
+int sph_batch_download(sph_batch* batch, uint32_t tank, float* positions, float* velocities);
+/* FluidSolver::emit for one tank. */
+int sph_batch_emit(sph_batch* batch, uint32_t tank);
+/* Tanks with active[t] == 0 keep their state through later substeps. */
+int sph_batch_set_active(sph_batch* batch, const uint8_t* active);
+/* `substeps` substeps of `dt` for every active tank. */
+int sph_batch_run(sph_batch* batch, float dt, uint32_t substeps);
+/* Tank t runs substeps[t] substeps of dt[t]; tanks done early sit out. */
+int sph_batch_run_per_tank(sph_batch* batch, const float* dt, const uint32_t* substeps);
+/* FluidSolver::step for every tank (each with its own fluidSubsteps). */
+int sph_batch_step(sph_batch* batch, float delta_seconds);
+/* FP64 statistics of every tank into out[tanks]. */
+int sph_batch_stats(sph_batch* batch, sph_stats* out);
+int sph_batch_synchronize(sph_batch* batch);
+int sph_batch_stream(sph_batch* batch, void** stream);
+int sph_batch_get_tuning(const sph_batch* batch, sph_tuning* out);
+int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning);
+int sph_batch_autotune(sph_batch* batch, float dt, uint32_t substeps_per_trial, sph_tuning* best, float* best_ms);
+int sph_batch_profile_substeps(sph_batch* batch, float dt, uint32_t substeps, double* phase_ms);
+int sph_batch_launches_per_substep(const sph_batch* batch, uint32_t* launches);
+int sph_batch_device_bytes(const sph_batch* batch, uint64_t* bytes);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

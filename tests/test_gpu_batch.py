@@ -1,0 +1,123 @@
+"""Batched tanks through the C ABI: every tank must give exactly the bits
+the oracle gives for that tank alone (the batch shares launches, not
+physics)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from computer_graphics_lab_00_gb300 import workloads as W
+from computer_graphics_lab_00_gb300.batch import BatchSolverGpu
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b) -> bool:
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
+
+
+def small_set(tanks=6, seed=4):
+    """A few tanks of the batched generator's shape, with small counts."""
+    full = W.batched_tanks(tanks=tanks, seed=seed)
+    params, counts = [], []
+    for t in range(tanks):
+        n = 400 + 611 * t
+        extent = [full.params[t].container_max[a] for a in range(3)]
+        lattice = W.tank_lattice(n, extent, 0.4, 0.02)
+        params.append(W.make_params(container_min=(0, 0, 0), container_max=extent, lattice=lattice,
+                                    cell_count=W.cell_count_for(n)))
+        counts.append(n)
+    return W.TankSet("small", params, counts, 1.0 / 600.0, 10, seed)
+
+
+@pytest.fixture(scope="module")
+def tanks():
+    return small_set()
+
+
+def load(ts):
+    solver = BatchSolverGpu(ts.params, ts.counts)
+    for t in range(len(ts.counts)):
+        solver.upload(t, *ts.initial_state(t))
+    return solver
+
+
+def test_each_tank_matches_the_oracle(native, oracle, tanks):
+    with load(tanks) as solver:
+        solver.run(tanks.dt, 5)
+        for t in range(len(tanks.counts)):
+            gp, gv = solver.download(t)
+            op, ov = oracle.run_substeps(tanks.params[t], *tanks.initial_state(t), tanks.dt, 5)
+            assert same(gp, op) and same(gv, ov), f"tank {t}"
+
+
+def test_per_tank_step_lengths_and_frozen_tanks(native, oracle, tanks):
+    n = len(tanks.counts)
+    dt = [1.0 / 600.0 if t % 2 == 0 else 1.0 / 1200.0 for t in range(n)]
+    substeps = [t % 3 for t in range(n)]  # 0, 1, 2, 0, 1, 2
+    with load(tanks) as solver:
+        active = [1] * n
+        active[1] = 0
+        solver.set_active(active)
+        solver.run_per_tank(dt, substeps)
+        for t in range(n):
+            gp, gv = solver.download(t)
+            runs = 0 if t == 1 else substeps[t]
+            op, ov = oracle.run_substeps(tanks.params[t], *tanks.initial_state(t), dt[t], runs)
+            assert same(gp, op) and same(gv, ov), f"tank {t}"
+
+
+def test_batch_step_matches_fluid_solver_step(native, oracle, tanks):
+    with load(tanks) as solver:
+        for _ in range(3):
+            solver.step(1.0 / 60.0)
+        for t in range(len(tanks.counts)):
+            gp, gv = solver.download(t)
+            op, ov = oracle.step(tanks.params[t], *tanks.initial_state(t), 1.0 / 60.0, frames=3)
+            assert same(gp, op) and same(gv, ov), f"tank {t}"
+
+
+def test_per_tank_statistics(native, oracle, tanks):
+    with load(tanks) as solver:
+        solver.run(tanks.dt, 3)
+        stats = solver.stats()
+        for t in range(len(tanks.counts)):
+            op, ov = oracle.run_substeps(tanks.params[t], *tanks.initial_state(t), tanks.dt, 3)
+            ref = oracle.stats(tanks.params[t], op, ov)
+            assert stats[t].particles == tanks.counts[t]
+            assert stats[t].mean_density == pytest.approx(ref.mean_density, rel=1e-12)
+            assert stats[t].mean_compression == pytest.approx(ref.mean_compression, rel=1e-9, abs=1e-15)
+            for a in range(3):
+                assert stats[t].centre_of_mass[a] == pytest.approx(ref.centre_of_mass[a], rel=1e-12)
+
+
+def test_autotune_restores_state_and_keeps_bits(native, oracle, tanks, tmp_path):
+    with load(tanks) as solver:
+        before = [solver.download(t) for t in range(len(tanks.counts))]
+        result = solver.autotune(tanks.dt, 2, cache=tmp_path / "tune.json", key="small")
+        assert result["ms_per_substep"] > 0
+        for t, (p, v) in enumerate(before):
+            gp, gv = solver.download(t)
+            assert same(gp, p) and same(gv, v), f"autotune changed tank {t}"
+        solver.run(tanks.dt, 2)
+        for t in range(len(tanks.counts)):
+            gp, gv = solver.download(t)
+            op, ov = oracle.run_substeps(tanks.params[t], *tanks.initial_state(t), tanks.dt, 2)
+            assert same(gp, op) and same(gv, ov), f"tank {t} after autotune"
+        cached = solver.autotune(tanks.dt, 2, cache=tmp_path / "tune.json", key="small")
+        assert cached["tuning"] == result["tuning"]
+
+
+def test_256_tank_workload_spot_checks(native, oracle):
+    """The full 256-tank set (about 5M particles): two substeps, four tanks
+    checked against the oracle."""
+    ts = W.batched_tanks()
+    with BatchSolverGpu(ts.params, ts.counts) as solver:
+        for t in range(len(ts.counts)):
+            solver.upload(t, *ts.initial_state(t))
+        solver.run(ts.dt, 2)
+        for t in (0, 17, 128, 255):
+            gp, gv = solver.download(t)
+            op, ov = oracle.run_substeps(ts.params[t], *ts.initial_state(t), ts.dt, 2,
+                                         threads=oracle.hardware_threads)
+            assert same(gp, op) and same(gv, ov), f"tank {t}"
