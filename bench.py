@@ -46,6 +46,7 @@ METRIC = "sim-s×particles/s @1M: plain vs learned 5×dt (≤1% density err); % 
 UNIT = "sim-s*particles/s"
 FALLBACK_HBM_GBS = 6800.0
 FLUSH_BYTES = 256 << 20
+WEIGHTS = ROOT / "computer_graphics_lab_00_gb300" / "weights" / "sph_correction.npz"
 
 
 def parse_args():
@@ -59,6 +60,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batched-steps", type=int, default=20,
                    help="substeps of the 256-tank leg (0 skips it)")
+    p.add_argument("--learned-steps", type=int, default=20,
+                   help="coarse steps of the learned 5x-dt leg at 1M (0 skips it)")
     return p.parse_args()
 
 
@@ -209,6 +212,61 @@ def batched_leg(steps: int, flush, device: int) -> dict:
         "launches_per_substep": solver.launches_per_substep(),
     }
     solver.close()
+    return out
+
+
+def learned_leg(steps: int, flush, device: int, plain_ms: float) -> dict:
+    """The learned 5x-dt form on the same 1,048,576-particle tank: coarse
+    steps of 1/240 s (plain force + tensor-core MLP correction), timed like
+    the plain leg; accuracy against the plain fine run (1/1200 s) over 0.1 s."""
+    import torch
+
+    from computer_graphics_lab_00_gb300 import training as T
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    case = W.dam_break_1m()
+    n = case.count
+    mlp = MlpGpu(device=device)
+    T.load_model(mlp, WEIGHTS)
+    pos, vel = case.initial_state()
+    solver = FluidSolverGpu(case.params, n, device=device)
+    solver.upload(pos, vel)
+    stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
+    solver.run_learned(T.COARSE_DT, 3, mlp)
+    solver.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            starts[k].record(stream)
+        solver.run_learned(T.COARSE_DT, 1, mlp)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
+    # Accuracy over 0.1 s from the initial state.
+    fine = FluidSolverGpu(case.params, n, device=device)
+    fine.upload(pos, vel)
+    fine.run(T.FINE_DT, 120)
+    solver.upload(pos, vel)
+    solver.run_learned(T.COARSE_DT, 24, mlp)
+    sf = fine.stats()
+    sl = solver.stats()
+    value = n * T.COARSE_DT / (ms / 1e3)
+    plain_fine_value = n * T.FINE_DT / (plain_ms / 1e3)
+    out = {
+        "dt": T.COARSE_DT, "steps": steps, "ms_per_step": ms, "value": value, "unit": UNIT,
+        "speedup_vs_plain_fine_step": value / plain_fine_value,
+        "speedup_vs_plain_1_600": value / (n * case.dt / (plain_ms / 1e3)),
+        "density_error_0p1s": abs(sl.mean_compression - sf.mean_compression),
+        "fine_mean_compression_0p1s": sf.mean_compression,
+        "com_drift_0p1s_m": float(np.linalg.norm(np.array(sl.centre_of_mass[:]) - np.array(sf.centre_of_mass[:]))),
+        "weights": str(WEIGHTS.relative_to(ROOT)),
+    }
+    for s in (solver, fine, mlp):
+        s.close()
     return out
 
 
@@ -404,6 +462,8 @@ def run_gb300(args) -> None:
     }
     if args.batched_steps > 0 and world == 1:
         out["batched"] = batched_leg(args.batched_steps, flush, local)
+    if args.learned_steps > 0 and world == 1 and WEIGHTS.exists():
+        out["learned"] = learned_leg(args.learned_steps, flush, local, step_ms)
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, args.cpu_seconds)
     solver.close()

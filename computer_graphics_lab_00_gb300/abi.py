@@ -259,6 +259,15 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_batch_profile_substeps": (c_int, [c_void_p, c_f32, c_u32, f64p]),
         "sph_batch_launches_per_substep": (c_int, [c_void_p, u32p]),
         "sph_batch_device_bytes": (c_int, [c_void_p, P(ctypes.c_uint64)]),
+        "sph_run_learned": (c_int, [c_void_p, c_f32, c_u32, c_void_p]),
+        "sph_batch_run_learned": (c_int, [c_void_p, c_f32, c_u32, c_void_p]),
+        "sph_batch_learned_features": (c_int, [c_void_p, c_f32, c_void_p]),
+        "sph_batch_learned_check": (c_int, [c_void_p]),
+        "sph_batch_snapshot": (c_int, [c_void_p, c_u32, c_int]),
+        "sph_batch_restore_tanks": (c_int, [c_void_p, c_u32, u8p]),
+        "sph_batch_device_state": (c_int, [c_void_p, P(c_void_p), P(c_void_p)]),
+        "sph_batch_tank_offset": (c_int, [c_void_p, c_u32, u32p]),
+        "sph_batch_copy_state": (c_int, [c_void_p, c_void_p, c_void_p]),
     })
     for name, (restype, argtypes) in sigs.items():
         fn = getattr(lib, name)

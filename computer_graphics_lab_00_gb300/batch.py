@@ -162,6 +162,48 @@ class BatchSolverGpu:
                     "sph_batch_profile_substeps")
         return dict(zip(self.PROFILE_PHASES, list(out)))
 
+    # -- learned coarse step --------------------------------------------------------
+    def run_learned(self, dt: float, substeps: int, mlp=None) -> None:
+        """Learned coarse substeps (mlp None: zero correction, = plain bits)."""
+        handle = None if mlp is None else mlp.handle
+        self._check(self._lib.sph_batch_run_learned(self._handle, ctypes.c_float(dt), substeps, handle),
+                    "sph_batch_run_learned")
+
+    def learned_features(self, dt: float, features_ptr: int) -> None:
+        self._check(self._lib.sph_batch_learned_features(self._handle, ctypes.c_float(dt),
+                                                         ctypes.c_void_p(features_ptr)), "sph_batch_learned_features")
+
+    def learned_check(self) -> None:
+        self._check(self._lib.sph_batch_learned_check(self._handle), "sph_batch_learned_check")
+
+    def snapshot(self, slot: int = 0, save: bool = True) -> None:
+        self._check(self._lib.sph_batch_snapshot(self._handle, slot, 1 if save else 0), "sph_batch_snapshot")
+
+    def restore_tanks(self, slot: int, which) -> None:
+        w = np.ascontiguousarray(np.asarray(which, dtype=np.uint8))
+        self._check(self._lib.sph_batch_restore_tanks(self._handle, slot,
+                                                      w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))),
+                    "sph_batch_restore_tanks")
+
+    def device_state(self):
+        pos = ctypes.c_void_p()
+        vel = ctypes.c_void_p()
+        self._check(self._lib.sph_batch_device_state(self._handle, ctypes.byref(pos), ctypes.byref(vel)),
+                    "sph_batch_device_state")
+        return int(pos.value or 0), int(vel.value or 0)
+
+    def copy_state(self, positions_ptr: int | None, velocities_ptr: int | None) -> None:
+        """Device-to-device copy of all tanks' state (id order) on the batch stream."""
+        self._check(self._lib.sph_batch_copy_state(self._handle,
+                                                   None if positions_ptr is None else ctypes.c_void_p(positions_ptr),
+                                                   None if velocities_ptr is None else ctypes.c_void_p(velocities_ptr)),
+                    "sph_batch_copy_state")
+
+    def tank_offset(self, tank: int) -> int:
+        out = ctypes.c_uint32()
+        self._check(self._lib.sph_batch_tank_offset(self._handle, tank, ctypes.byref(out)), "sph_batch_tank_offset")
+        return int(out.value)
+
     def launches_per_substep(self) -> int:
         out = ctypes.c_uint32()
         self._check(self._lib.sph_batch_launches_per_substep(self._handle, ctypes.byref(out)),

@@ -11,6 +11,7 @@
 
 #include "../../include/sph_c.h"
 #include "sph_engine.h"
+#include "sph_mlp.cuh"
 
 struct sph_ctx {
     sph::Engine engine;
@@ -571,6 +572,98 @@ int sph_batch_device_bytes(const sph_batch* batch, uint64_t* bytes) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     *bytes = batch->engine.device_bytes();
+    return SPH_OK;
+}
+
+}  // extern "C"
+
+// ---- learned coarse step --------------------------------------------------------
+
+namespace {
+
+int run_learned(sph::Engine& engine, float dt, uint32_t substeps, const sph_mlp* mlp) {
+    sph::mlp::ModelView view{};
+    const sph::mlp::ModelView* model = nullptr;
+    if (mlp != nullptr) {
+        if (!sph_mlp_model_view(mlp, &view)) {
+            return SPH_ERR_INVALID_ARGUMENT;
+        }
+        model = &view;
+    }
+    return engine.run_learned(dt, substeps, model);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sph_run_learned(sph_ctx* ctx, float dt, uint32_t substeps, const sph_mlp* mlp) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return run_learned(ctx->engine, dt, substeps, mlp);
+}
+
+int sph_batch_run_learned(sph_batch* batch, float dt, uint32_t substeps, const sph_mlp* mlp) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return run_learned(batch->engine, dt, substeps, mlp);
+}
+
+int sph_batch_learned_features(sph_batch* batch, float dt, void* features) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.learned_features(dt, static_cast<float*>(features));
+}
+
+int sph_batch_learned_check(sph_batch* batch) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.learned_error();
+}
+
+int sph_batch_snapshot(sph_batch* batch, uint32_t slot, int save) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.snapshot(save != 0, slot);
+}
+
+int sph_batch_restore_tanks(sph_batch* batch, uint32_t slot, const uint8_t* which) {
+    if (batch == nullptr || which == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.restore_tanks(slot, std::vector<uint8_t>(which, which + batch->engine.tank_count()));
+}
+
+int sph_batch_device_state(sph_batch* batch, void** positions, void** velocities) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (positions != nullptr) {
+        *positions = batch->engine.positions();
+    }
+    if (velocities != nullptr) {
+        *velocities = batch->engine.velocities();
+    }
+    return SPH_OK;
+}
+
+int sph_batch_copy_state(sph_batch* batch, void* positions, void* velocities) {
+    if (batch == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.copy_state(static_cast<float4*>(positions), static_cast<float4*>(velocities));
+}
+
+int sph_batch_tank_offset(const sph_batch* batch, uint32_t tank, uint32_t* first) {
+    if (batch == nullptr || first == nullptr || tank >= batch->engine.tank_count()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *first = batch->engine.particle_base(tank);
     return SPH_OK;
 }
 

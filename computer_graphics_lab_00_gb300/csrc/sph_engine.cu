@@ -1,6 +1,8 @@
 // sph_engine.cu — device state, the substep pipeline and its CUDA graph.
 #include "sph_engine.h"
 
+#include "sph_mlp.cuh"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -157,6 +159,10 @@ void Engine::release() {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    if (learned_graph_ != nullptr) {
+        cudaGraphExecDestroy(learned_graph_);
+        learned_graph_ = nullptr;
+    }
     for (cudaEvent_t& e : events_) {
         if (e != nullptr) {
             cudaEventDestroy(e);
@@ -167,7 +173,8 @@ void Engine::release() {
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
-                       schedule_.tile_of, schedule_.order, schedule_.tile_hist, snap_pos_, snap_vel_};
+                       schedule_.tile_of, schedule_.order, schedule_.tile_hist, snap_pos_[0], snap_vel_[0],
+                       snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -585,12 +592,15 @@ int Engine::stats_all(std::vector<sph_stats>& out) {
     return SPH_OK;
 }
 
-int Engine::snapshot(bool save) {
+int Engine::snapshot(bool save, uint32_t slot) {
+    if (slot >= kSnapshotSlots) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
     SPH_CUDA(cudaSetDevice(device_));
-    if (snap_pos_ == nullptr) {
+    if (snap_pos_[slot] == nullptr) {
         int status = SPH_OK;
-        if ((status = alloc(&snap_pos_, total_capacity_)) != SPH_OK ||
-            (status = alloc(&snap_vel_, total_capacity_)) != SPH_OK) {
+        if ((status = alloc(&snap_pos_[slot], total_capacity_)) != SPH_OK ||
+            (status = alloc(&snap_vel_[slot], total_capacity_)) != SPH_OK) {
             return status;
         }
     }
@@ -599,13 +609,43 @@ int Engine::snapshot(bool save) {
         return SPH_OK;
     }
     if (save) {
-        SPH_CUDA(cudaMemcpyAsync(snap_pos_, pos_, bytes, cudaMemcpyDeviceToDevice, stream_));
-        SPH_CUDA(cudaMemcpyAsync(snap_vel_, vel_, bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(snap_pos_[slot], pos_, bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(snap_vel_[slot], vel_, bytes, cudaMemcpyDeviceToDevice, stream_));
     } else {
-        SPH_CUDA(cudaMemcpyAsync(pos_, snap_pos_, bytes, cudaMemcpyDeviceToDevice, stream_));
-        SPH_CUDA(cudaMemcpyAsync(vel_, snap_vel_, bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(pos_, snap_pos_[slot], bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(vel_, snap_vel_[slot], bytes, cudaMemcpyDeviceToDevice, stream_));
         grid_valid_ = false;
     }
+    return SPH_OK;
+}
+
+int Engine::copy_state(float4* positions, float4* velocities) {
+    SPH_CUDA(cudaSetDevice(device_));
+    size_t bytes = sizeof(float4) * total_count_;
+    if (positions != nullptr && bytes > 0) {
+        SPH_CUDA(cudaMemcpyAsync(positions, pos_, bytes, cudaMemcpyDeviceToDevice, stream_));
+    }
+    if (velocities != nullptr && bytes > 0) {
+        SPH_CUDA(cudaMemcpyAsync(velocities, vel_, bytes, cudaMemcpyDeviceToDevice, stream_));
+    }
+    return SPH_OK;
+}
+
+int Engine::restore_tanks(uint32_t slot, const std::vector<uint8_t>& which) {
+    if (slot >= kSnapshotSlots || snap_pos_[slot] == nullptr || which.size() != tanks_.size()) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    for (size_t t = 0; t < tanks_.size(); ++t) {
+        if (which[t] == 0) {
+            continue;
+        }
+        size_t first = tanks_[t].particle_base;
+        size_t bytes = sizeof(float4) * tanks_[t].particle_count;
+        SPH_CUDA(cudaMemcpyAsync(pos_ + first, snap_pos_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(vel_ + first, snap_vel_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
+    }
+    grid_valid_ = false;
     return SPH_OK;
 }
 
@@ -718,6 +758,146 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
     cudaEventDestroy(start);
     cudaEventDestroy(stop);
     return status;
+}
+
+int Engine::ensure_learned_buffers() {
+    if (sforce_ != nullptr) {
+        return SPH_OK;
+    }
+    int status = SPH_OK;
+    if ((status = alloc(&sforce_, total_capacity_)) != SPH_OK ||
+        (status = alloc(&scorrection_, total_capacity_)) != SPH_OK ||
+        (status = alloc(&sfeatures_, static_cast<size_t>(total_capacity_) * 32)) != SPH_OK) {
+        return status;
+    }
+    SPH_CUDA(mlp::prepare_forward());
+    return SPH_OK;
+}
+
+// One learned substep: grid, density (with the pair masks), force +
+// features, MLP, finish. model == nullptr runs the same split path with a
+// zero correction (bit-identical to the plain substep).
+int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launches) {
+    int status = enqueue_grid(launches);
+    if (status != SPH_OK) {
+        return status;
+    }
+    uint32_t n = total_count_;
+    NeighbourTuning masked = tuning_;
+    masked.variant = 4;
+    SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
+    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.masks, sforce_,
+                             sfeatures_, false, stream_));
+    if (model != nullptr) {
+        SPH_CUDA(mlp::launch_forward(*model, sfeatures_, n, reinterpret_cast<float*>(scorrection_), nullptr,
+                                     &counters_->error_flags, stream_));
+    }
+    SPH_CUDA(launch_finish_learned(spos2_, svel_, grid_.sorted_ids, d_tanks_, stank_, n, sforce_,
+                                   model != nullptr ? scorrection_ : nullptr, pos_, vel_, stream_));
+    if (launches != nullptr) {
+        *launches += model != nullptr ? 4 : 3;
+    }
+    return SPH_OK;
+}
+
+int Engine::run_learned(float dt, uint32_t substeps, const mlp::ModelView* model) {
+    if (!(dt > 0.0F) || !std::isfinite(dt)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (total_count_ == 0 || substeps == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = ensure_learned_buffers();
+    if (status != SPH_OK) {
+        return status;
+    }
+    status = refresh_constants(dt);
+    if (status != SPH_OK) {
+        return status;
+    }
+    bool same_model = (model == nullptr && !learned_graph_has_model_) ||
+                      (model != nullptr && learned_graph_has_model_ &&
+                       std::memcmp(model, &learned_graph_model_, sizeof(mlp::ModelView)) == 0);
+    if (learned_graph_ == nullptr || learned_graph_count_ != total_count_ || !same_model) {
+        if (learned_graph_ != nullptr) {
+            cudaGraphExecDestroy(learned_graph_);
+            learned_graph_ = nullptr;
+        }
+        SPH_CUDA(cudaMemsetAsync(&counters_->error_flags, 0, sizeof(unsigned int), stream_));
+        cudaGraph_t graph = nullptr;
+        SPH_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        uint32_t launches = 0;
+        status = enqueue_learned_substep(model, &launches);
+        cudaError_t end = cudaStreamEndCapture(stream_, &graph);
+        if (status != SPH_OK) {
+            if (graph != nullptr) {
+                cudaGraphDestroy(graph);
+            }
+            return status;
+        }
+        if (end != cudaSuccess) {
+            return fail(end, "cudaStreamEndCapture");
+        }
+        cudaError_t inst = cudaGraphInstantiate(&learned_graph_, graph, 0);
+        cudaGraphDestroy(graph);
+        if (inst != cudaSuccess) {
+            learned_graph_ = nullptr;
+            return fail(inst, "cudaGraphInstantiate");
+        }
+        learned_graph_count_ = total_count_;
+        learned_graph_has_model_ = model != nullptr;
+        if (model != nullptr) {
+            learned_graph_model_ = *model;
+        }
+        learned_launches_ = launches;
+    }
+    for (uint32_t s = 0; s < substeps; ++s) {
+        SPH_CUDA(cudaGraphLaunch(learned_graph_, stream_));
+    }
+    grid_valid_ = true;
+    return SPH_OK;
+}
+
+int Engine::learned_error() {
+    unsigned int flag = 0;
+    SPH_CUDA(cudaMemcpyAsync(&flag, &counters_->error_flags, sizeof(flag), cudaMemcpyDeviceToHost, stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    if (flag != 0) {
+        last_error_ = "tensor-core completion wait timed out";
+        return SPH_ERR_TIMEOUT;
+    }
+    return SPH_OK;
+}
+
+// Features of the current state (id order), for training sets; the state
+// itself does not change.
+int Engine::learned_features(float dt, float* features) {
+    if (features == nullptr || !(dt > 0.0F)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (total_count_ == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = ensure_learned_buffers();
+    if (status == SPH_OK) {
+        status = refresh_constants(dt);
+    }
+    if (status == SPH_OK) {
+        status = enqueue_grid(nullptr);
+    }
+    if (status != SPH_OK) {
+        return status;
+    }
+    uint32_t n = total_count_;
+    NeighbourTuning masked = tuning_;
+    masked.variant = 4;
+    SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
+    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.masks, sforce_,
+                             features, true, stream_));
+    grid_valid_ = true;
+    return SPH_OK;
 }
 
 int Engine::build_grid() {

@@ -16,6 +16,7 @@
 
 #include "../../include/sph_c.h"
 #include "sph_kernels.h"
+#include "sph_mlp.cuh"
 
 namespace sph {
 
@@ -59,8 +60,22 @@ public:
     // Times candidate launch shapes on the current state (restored after)
     // and keeps the fastest. Results never depend on the shape.
     int autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<TuneChoice>* tried);
-    // Saves (true) or restores (false) the particle state in device memory.
-    int snapshot(bool save);
+    // Learned coarse substeps: plain force + MLP correction (model may be
+    // null: zero correction, bit-identical to the plain substep).
+    int run_learned(float dt, uint32_t substeps, const mlp::ModelView* model);
+    // Correction features of the current state, id order, n x 32 (device).
+    int learned_features(float dt, float* features);
+    // SPH_ERR_TIMEOUT if a tensor-core wait gave up since the last check.
+    int learned_error();
+    uint32_t learned_launches_per_substep() const { return learned_launches_; }
+    // Saves (true) or restores (false) the particle state in device memory,
+    // in one of kSnapshotSlots slots; restore_tanks copies back only the
+    // particles of the tanks with which[t] != 0.
+    static constexpr uint32_t kSnapshotSlots = 2;
+    int snapshot(bool save, uint32_t slot = 0);
+    int restore_tanks(uint32_t slot, const std::vector<uint8_t>& which);
+    // Device-to-device copy of the whole state (id order) into caller buffers.
+    int copy_state(float4* positions, float4* velocities);
     // Grid build only (for inspection).
     int build_grid();
     int grid_download(uint32_t tank, uint32_t* cell_of, uint32_t* cell_counts, uint32_t* cell_particles);
@@ -82,6 +97,7 @@ public:
     uint32_t tank_count() const { return static_cast<uint32_t>(tanks_.size()); }
     uint32_t count(uint32_t tank) const { return tanks_[tank].particle_count; }
     uint32_t capacity(uint32_t tank) const { return capacity_[tank]; }
+    uint32_t particle_base(uint32_t tank) const { return tanks_[tank].particle_base; }
     uint32_t total_count() const { return total_count_; }
     const sph_params& params(uint32_t tank) const { return params_[tank]; }
     uint32_t launches_per_substep() const { return launches_per_substep_; }
@@ -96,6 +112,8 @@ public:
 private:
     int enqueue_grid(uint32_t* launches);
     int enqueue_bounds(uint32_t* launches);
+    int enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launches);
+    int ensure_learned_buffers();
     int enqueue_substep(uint32_t* launches);
     int refresh_constants(float dt);
     int ensure_graph();
@@ -140,8 +158,16 @@ private:
     bool grid_valid_ = false;
     uint32_t nonfinite_host_ = 0;
     std::vector<uint8_t> user_active_;
-    float4* snap_pos_ = nullptr;
-    float4* snap_vel_ = nullptr;
+    float4* snap_pos_[kSnapshotSlots] = {nullptr, nullptr};
+    float4* snap_vel_[kSnapshotSlots] = {nullptr, nullptr};
+    float4* sforce_ = nullptr;
+    float4* scorrection_ = nullptr;
+    float* sfeatures_ = nullptr;
+    cudaGraphExec_t learned_graph_ = nullptr;
+    uint32_t learned_graph_count_ = 0xFFFFFFFFu;
+    bool learned_graph_has_model_ = false;
+    mlp::ModelView learned_graph_model_{};
+    uint32_t learned_launches_ = 0;
     cudaEvent_t events_[kProfilePhases + 1] = {};
     std::string last_error_;
 };

@@ -342,13 +342,14 @@ __device__ __forceinline__ void add_pair_force(const PairConst& k, const float4&
 __device__ __forceinline__ void finish_particle(const TankConst* t, const float4& self, float density, float vx,
                                                 float vy, float vz, float pressure, float fx, float fy, float fz,
                                                 uint32_t i, float4* __restrict__ pos_out,
-                                                float4* __restrict__ vel_out) {
+                                                float4* __restrict__ vel_out, float4 learned = {0.0f, 0.0f, 0.0f, 0.0f}) {
     // The force-field sum starts at vec3{0} and is added even when there are
-    // no fields, which maps -0 to +0.
+    // no fields, which maps -0 to +0. A learned correction, when present, is
+    // one more acceleration term; +0 leaves the plain step's bits unchanged.
     const float dt = __ldg(&t->dt);
-    float ax = __fadd_rn(__fadd_rn(__fdiv_rn(fx, density), __ldg(&t->gravity[0])), 0.0f);
-    float ay = __fadd_rn(__fadd_rn(__fdiv_rn(fy, density), __ldg(&t->gravity[1])), 0.0f);
-    float az = __fadd_rn(__fadd_rn(__fdiv_rn(fz, density), __ldg(&t->gravity[2])), 0.0f);
+    float ax = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fx, density), __ldg(&t->gravity[0])), 0.0f), learned.x);
+    float ay = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fy, density), __ldg(&t->gravity[1])), 0.0f), learned.y);
+    float az = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fz, density), __ldg(&t->gravity[2])), 0.0f), learned.z);
     vx = __fadd_rn(vx, __fmul_rn(ax, dt));
     vy = __fadd_rn(vy, __fmul_rn(ay, dt));
     vz = __fadd_rn(vz, __fmul_rn(az, dt));
@@ -1054,6 +1055,175 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
                     sorted_ids[p], pos_out, vel_out);
 }
 
+// ---- learned coarse step ------------------------------------------------------
+//
+// The learned step splits integrate in two: `features_kernel` computes the
+// plain SPH force of each particle exactly as integrate_mask_kernel does and,
+// over the same pairs, the 32 features the correction MLP reads; the MLP
+// turns features into an acceleration correction; `finish_learned_kernel`
+// adds it to the plain acceleration and advances the particle exactly as the
+// plain integrate does. With a zero correction the result is bit-identical to
+// the plain substep.
+//
+// Features of particle i (h the kernel radius, D the substep, rho0 and k the
+// rest density and stiffness; sums over the in-range pairs j, u = (x_j -
+// x_i) / h, w = (1 - |u|)^2):
+//   0  (rho_i - rho0) / rho0          1  p_i / (k rho0)
+//   2-4  v_i D / h                    5-7  (F_i / rho_i) D^2 / h
+//   8  pairs / 32                     9  sum w
+//   10-12  sum w u                    13-15  sum w (v_j - v_i) D / h
+//   16-21  sum w u_a u_b (xx yy zz xy xz yz)
+//   22-24  sum w (p_j - p_i) / (k rho0) u
+//   25  sum w (rho_j - rho_i) / rho0
+//   26-28  min(max((x_i - wall_low) / h, 0), 4)   29-31  same for the high walls
+constexpr int kFeatures = 32;
+
+template <int kBlock, int kList>
+__global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restrict__ spos2,
+                                                          const float4* __restrict__ svel,
+                                                          const uint32_t* __restrict__ sorted_ids,
+                                                          const uint2* __restrict__ bucket,
+                                                          const TankConst* __restrict__ tanks,
+                                                          const uint16_t* __restrict__ stank, uint32_t n,
+                                                          const uint32_t* __restrict__ masks,
+                                                          float4* __restrict__ force_out,
+                                                          float* __restrict__ features_out, int id_order) {
+    __shared__ uint32_t list[kList][kBlock];
+    uint32_t p = blockIdx.x * kBlock + threadIdx.x;
+    if (p >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    PairConst k;
+    k.h = __ldg(&t->h);
+    k.c_spiky = __ldg(&t->c_spiky);
+    k.c_visc = __ldg(&t->c_visc);
+    k.neg_mass = __ldg(&t->neg_mass);
+    k.visc_mass = __ldg(&t->visc_mass);
+    const uint32_t cell_mask = __ldg(&t->cell_mask);
+    const uint32_t base = __ldg(&t->bucket_base);
+    const float4 self = spos2[p];
+    const float4 sv = svel[p];
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(self.x, k.h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(self.y, k.h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(self.z, k.h));
+    const float rho0 = __ldg(&t->rest_density);
+    const float stiff = __ldg(&t->stiffness);
+    const float dt = __ldg(&t->dt);
+    const float inv_h = 1.0f / k.h;
+    const float vscale = dt * inv_h;
+    const float inv_prho = 1.0f / (stiff * rho0);
+    float fx = 0.0f;
+    float fy = 0.0f;
+    float fz = 0.0f;
+    float f[kFeatures];
+#pragma unroll
+    for (int q = 0; q < kFeatures; ++q) {
+        f[q] = 0.0f;
+    }
+    uint32_t pairs = 0;
+    auto visit = [&](uint32_t q) {
+        float4 other = __ldg(&spos2[q]);
+        float4 ov = __ldg(&svel[q]);
+        add_pair_force_rcp(k, self, sv.x, sv.y, sv.z, sv.w, other, ov, fx, fy, fz);
+        float ux = (other.x - self.x) * inv_h;
+        float uy = (other.y - self.y) * inv_h;
+        float uz = (other.z - self.z) * inv_h;
+        float r = sqrtf(ux * ux + uy * uy + uz * uz);
+        float w = (1.0f - r) * (1.0f - r);
+        f[9] += w;
+        f[10] += w * ux;
+        f[11] += w * uy;
+        f[12] += w * uz;
+        f[13] += w * (ov.x - sv.x) * vscale;
+        f[14] += w * (ov.y - sv.y) * vscale;
+        f[15] += w * (ov.z - sv.z) * vscale;
+        f[16] += w * ux * ux;
+        f[17] += w * uy * uy;
+        f[18] += w * uz * uz;
+        f[19] += w * ux * uy;
+        f[20] += w * ux * uz;
+        f[21] += w * uy * uz;
+        float dp = (ov.w - sv.w) * inv_prho;
+        f[22] += w * dp * ux;
+        f[23] += w * dp * uy;
+        f[24] += w * dp * uz;
+        f[25] += w * (other.w - self.w) / rho0;
+        ++pairs;
+    };
+    uint32_t listed = 0;
+    for (uint32_t b = 0; b < 27u; ++b) {
+        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + p]);
+        if (word == 0) {
+            continue;
+        }
+        uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
+        while (word != 0) {
+            uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
+            word &= word - 1;
+            if (listed == static_cast<uint32_t>(kList)) {
+                for (uint32_t e = 0; e < listed; ++e) {
+                    visit(list[e][threadIdx.x]);
+                }
+                listed = 0;
+            }
+            list[listed][threadIdx.x] = start + slot;
+            ++listed;
+        }
+    }
+    for (uint32_t e = 0; e < listed; ++e) {
+        visit(list[e][threadIdx.x]);
+    }
+    const float density = max_like_std(self.w, 1e-6f);
+    f[0] = (self.w - rho0) / rho0;
+    f[1] = sv.w * inv_prho;
+    f[2] = sv.x * vscale;
+    f[3] = sv.y * vscale;
+    f[4] = sv.z * vscale;
+    f[5] = fx / density * dt * vscale;
+    f[6] = fy / density * dt * vscale;
+    f[7] = fz / density * dt * vscale;
+    f[8] = pairs * (1.0f / 32.0f);
+    const float pos[3] = {self.x, self.y, self.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        f[26 + a] = fminf(fmaxf((pos[a] - __ldg(&t->low[a])) * inv_h, 0.0f), 4.0f);
+        f[29 + a] = fminf(fmaxf((__ldg(&t->high[a]) - pos[a]) * inv_h, 0.0f), 4.0f);
+    }
+    force_out[p] = make_float4(fx, fy, fz, 0.0f);
+    uint32_t row = id_order ? sorted_ids[p] : p;
+    float4* dst = reinterpret_cast<float4*>(features_out + static_cast<size_t>(row) * kFeatures);
+#pragma unroll
+    for (int q = 0; q < kFeatures / 4; ++q) {
+        dst[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+    }
+}
+
+__global__ void __launch_bounds__(256) finish_learned_kernel(const float4* __restrict__ spos2,
+                                                             const float4* __restrict__ svel,
+                                                             const uint32_t* __restrict__ sorted_ids,
+                                                             const TankConst* __restrict__ tanks,
+                                                             const uint16_t* __restrict__ stank, uint32_t n,
+                                                             const float4* __restrict__ force,
+                                                             const float4* __restrict__ correction,
+                                                             float4* __restrict__ pos_out,
+                                                             float4* __restrict__ vel_out) {
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    if (__ldg(&t->active) == 0) {
+        return;
+    }
+    const float4 self = spos2[p];
+    const float4 sv = svel[p];
+    const float4 fo = force[p];
+    const float4 da = correction != nullptr ? correction[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    finish_particle(t, self, max_like_std(self.w, 1e-6f), sv.x, sv.y, sv.z, sv.w, fo.x, fo.y, fo.z, sorted_ids[p],
+                    pos_out, vel_out, da);
+}
+
 // Division self-test: counts x / y where the reciprocal-based quotient and
 // IEEE division differ in value (signed zeros compare equal).
 __global__ void division_selftest_kernel(uint64_t seed, uint64_t count, int mode, unsigned long long* mismatches) {
@@ -1311,6 +1481,28 @@ cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_
         return cudaSuccess;
     }
     nonfinite_kernel<<<(n + 255) / 256, 256, 0, stream>>>(pos, vel, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_features(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
+                            const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* masks,
+                            float4* force, float* features, bool id_order, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    features_kernel<128, 48><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
+                                                                  masks, force, features, id_order ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,
+                                  const TankConst* tanks, const uint16_t* stank, uint32_t n, const float4* force,
+                                  const float4* correction, float4* pos, float4* vel, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    finish_learned_kernel<<<(n + 255) / 256, 256, 0, stream>>>(spos2, svel, sorted_ids, tanks, stank, n, force,
+                                                                correction, pos, vel);
     return cudaGetLastError();
 }
 

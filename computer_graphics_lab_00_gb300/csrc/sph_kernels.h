@@ -123,6 +123,17 @@ cudaError_t launch_stats(const float4* pos, const float4* vel, const uint16_t* t
                          uint32_t n, double* acc, cudaStream_t stream);
 // Counts particles whose position or velocity xyz is not finite (adds to *out).
 cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_t n, uint32_t* out, cudaStream_t stream);
+// Learned coarse step, first half: the plain SPH force per particle
+// (force[p], sorted order) and the 32 correction features (row p, or row
+// sorted_ids[p] when id_order). Needs the variant-4 pair masks of density.
+cudaError_t launch_features(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
+                            const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* masks,
+                            float4* force, float* features, bool id_order, cudaStream_t stream);
+// Second half: acceleration = plain + correction[p] (null: none), then the
+// plain step's velocity update, clamp, walls and id-order write.
+cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,
+                                  const TankConst* tanks, const uint16_t* stank, uint32_t n, const float4* force,
+                                  const float4* correction, float4* pos, float4* vel, cudaStream_t stream);
 // Counts x / y (over `count` generated pairs) where division through a
 // correctly rounded reciprocal differs from IEEE division. mode 0: every
 // divisor mantissa; mode 1: random signs, mantissas, exponents.

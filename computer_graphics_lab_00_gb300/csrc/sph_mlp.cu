@@ -1,0 +1,1030 @@
+// sph_mlp.cu — the learned correction's MLP: tcgen05 forward, FP32 backward,
+// Adam, and its C ABI (sph_mlp_* in include/sph_c.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sph_c.h"
+#include "sph_mlp.cuh"
+
+namespace sph {
+namespace mlp {
+
+namespace {
+
+// ---- tcgen05 / mbarrier helpers (inline PTX, sm_100-family) -----------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major canonical layout of
+// 8-row x 16-byte core matrices. lbo: byte stride between core matrices along
+// K; sbo: byte stride between 8-row groups along M/N. Bits 46-47 hold the
+// descriptor version (1 on sm_100-family tensor cores).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+    d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= static_cast<uint64_t>(1) << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: D = F32, A = B = BF16, both K-major,
+// dense, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t instr_desc(uint32_t m, uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait: gives up after ~2^22 polls instead of hanging.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+    for (uint32_t i = 0; i < (1u << 22); ++i) {
+        if (mbar_try_wait(mbar, parity)) {
+            return true;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_load16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        v[k] = __uint_as_float(r[k]);
+    }
+}
+
+// GELU, erf form (Hendrycks & Gimpel 2016).
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+// Byte offset of (row, 8-element chunk) in a K-major no-swizzle tile whose
+// rows hold `k` BF16 elements.
+__device__ __forceinline__ uint32_t tile_offset(uint32_t row, uint32_t chunk, uint32_t k) {
+    return (row >> 3) * (k / 8u) * 128u + chunk * 128u + (row & 7u) * 16u;
+}
+
+constexpr uint32_t kSmemW1 = 0;
+constexpr uint32_t kSmemW2 = kSmemW1 + kHidden * kIn * 2;        // 8 KB
+constexpr uint32_t kSmemW3 = kSmemW2 + kHidden * kHidden * 2;    // +32 KB
+constexpr uint32_t kSmemX = kSmemW3 + kOutPad * kHidden * 2;     // +4 KB
+constexpr uint32_t kSmemH = kSmemX + kTile * kIn * 2;            // +8 KB
+constexpr uint32_t kSmemBar = kSmemH + kTile * kHidden * 2;      // +32 KB
+constexpr uint32_t kSmemBytes = kSmemBar + 64;
+constexpr uint32_t kTmemCols = 128;
+
+__device__ __forceinline__ void store_chunk(uint8_t* base, uint32_t offset, const float* v8) {
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(v8[0], v8[1]);
+    __nv_bfloat162 p1 = __floats2bfloat162_rn(v8[2], v8[3]);
+    __nv_bfloat162 p2 = __floats2bfloat162_rn(v8[4], v8[5]);
+    __nv_bfloat162 p3 = __floats2bfloat162_rn(v8[6], v8[7]);
+    uint4 q;
+    q.x = *reinterpret_cast<uint32_t*>(&p0);
+    q.y = *reinterpret_cast<uint32_t*>(&p1);
+    q.z = *reinterpret_cast<uint32_t*>(&p2);
+    q.w = *reinterpret_cast<uint32_t*>(&p3);
+    *reinterpret_cast<uint4*>(base + offset) = q;
+}
+
+// One CTA of 128 threads owns 128 TMEM columns and runs 128-particle tiles:
+// X (normalised features, BF16) -> [MMA W1] -> +b1, GELU -> H1 (BF16) ->
+// [MMA W2] -> +b2, GELU -> H2 -> [MMA W3] -> +b3 -> scaled output. Thread t
+// is row t of the tile and TMEM lane t. One thread issues the MMAs; an
+// mbarrier reports their completion.
+__global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, const float* __restrict__ features,
+                                                             uint32_t n, float* __restrict__ out, ForwardSaves saves,
+                                                             int save, unsigned int* __restrict__ error_flag) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmemBar);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kSmemBar + 8);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5;
+
+    // Weights into the canonical K-major layout (16-byte chunks).
+    for (uint32_t c = tid; c < kHidden * (kIn / 8); c += blockDim.x) {
+        uint32_t row = c / (kIn / 8);
+        uint32_t chunk = c % (kIn / 8);
+        *reinterpret_cast<uint4*>(smem + kSmemW1 + tile_offset(row, chunk, kIn)) =
+            *reinterpret_cast<const uint4*>(model.w1 + row * kIn + chunk * 8);
+    }
+    for (uint32_t c = tid; c < kHidden * (kHidden / 8); c += blockDim.x) {
+        uint32_t row = c / (kHidden / 8);
+        uint32_t chunk = c % (kHidden / 8);
+        *reinterpret_cast<uint4*>(smem + kSmemW2 + tile_offset(row, chunk, kHidden)) =
+            *reinterpret_cast<const uint4*>(model.w2 + row * kHidden + chunk * 8);
+    }
+    for (uint32_t c = tid; c < kOutPad * (kHidden / 8); c += blockDim.x) {
+        uint32_t row = c / (kHidden / 8);
+        uint32_t chunk = c % (kHidden / 8);
+        *reinterpret_cast<uint4*>(smem + kSmemW3 + tile_offset(row, chunk, kHidden)) =
+            *reinterpret_cast<const uint4*>(model.w3 + row * kHidden + chunk * 8);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_base = (warp * 32u) << 16;
+    const float* b1 = model.params + kB1;
+    const float* b2 = model.params + kB2;
+    const float* b3 = model.params + kB3;
+    const uint32_t sX = smem_u32(smem + kSmemX);
+    const uint32_t sH = smem_u32(smem + kSmemH);
+    const uint32_t sW1 = smem_u32(smem + kSmemW1);
+    const uint32_t sW2 = smem_u32(smem + kSmemW2);
+    const uint32_t sW3 = smem_u32(smem + kSmemW3);
+    constexpr uint32_t idesc_hidden = instr_desc(kTile, kHidden);
+    constexpr uint32_t idesc_out = instr_desc(kTile, kOutPad);
+    uint32_t parity = 0;
+    bool failed = false;
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint32_t row = tile * kTile + tid;
+        const bool valid = row < n;
+        // Normalised features -> BF16 tile.
+        const float4* frow = reinterpret_cast<const float4*>(features + static_cast<size_t>(row) * kIn);
+#pragma unroll
+        for (uint32_t chunk = 0; chunk < kIn / 8; ++chunk) {
+            float v[8];
+            float4 a = valid ? frow[2 * chunk] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float4 b = valid ? frow[2 * chunk + 1] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float raw[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k) {
+                uint32_t f = chunk * 8 + k;
+                v[k] = valid ? (raw[k] - model.in_mean[f]) * model.in_inv_std[f] : 0.0f;
+            }
+            store_chunk(smem + kSmemX, tile_offset(tid, chunk, kIn), v);
+            if (save && valid) {
+#pragma unroll
+                for (uint32_t k = 0; k < 8; ++k) {
+                    saves.x[static_cast<size_t>(row) * kIn + chunk * 8 + k] = __float2bfloat16_rn(v[k]);
+                }
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+
+        // ---- layer 1: [128 x 32] x [32 x 128] ----
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t k = 0; k < kIn / 16; ++k) {
+                mma_bf16(tmem, smem_desc(sX + k * 256u, 128u, (kIn / 8) * 128u),
+                         smem_desc(sW1 + k * 256u, 128u, (kIn / 8) * 128u), idesc_hidden, k > 0 ? 1u : 0u);
+            }
+            mma_commit(mbar);
+        }
+        bool ok = mbar_wait(mbar, parity);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        for (uint32_t c = 0; c < kHidden / 16; ++c) {
+            float v[16];
+            tmem_load16(tmem + lane_base + c * 16u, v);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                float z = v[k] + b1[c * 16 + k];
+                if (save && valid) {
+                    saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
+                }
+                v[k] = gelu(z);
+            }
+            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c, kHidden), v);
+            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c + 1, kHidden), v + 8);
+            if (save && valid) {
+#pragma unroll
+                for (uint32_t k = 0; k < 16; ++k) {
+                    saves.h1[static_cast<size_t>(row) * kHidden + c * 16 + k] = __float2bfloat16_rn(v[k]);
+                }
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+
+        // ---- layer 2: [128 x 128] x [128 x 128] ----
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t k = 0; k < kHidden / 16; ++k) {
+                mma_bf16(tmem, smem_desc(sH + k * 256u, 128u, (kHidden / 8) * 128u),
+                         smem_desc(sW2 + k * 256u, 128u, (kHidden / 8) * 128u), idesc_hidden, k > 0 ? 1u : 0u);
+            }
+            mma_commit(mbar);
+        }
+        ok = mbar_wait(mbar, parity);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        for (uint32_t c = 0; c < kHidden / 16; ++c) {
+            float v[16];
+            tmem_load16(tmem + lane_base + c * 16u, v);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                float z = v[k] + b2[c * 16 + k];
+                if (save && valid) {
+                    saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
+                }
+                v[k] = gelu(z);
+            }
+            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c, kHidden), v);
+            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c + 1, kHidden), v + 8);
+            if (save && valid) {
+#pragma unroll
+                for (uint32_t k = 0; k < 16; ++k) {
+                    saves.h2[static_cast<size_t>(row) * kHidden + c * 16 + k] = __float2bfloat16_rn(v[k]);
+                }
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+
+        // ---- layer 3: [128 x 128] x [128 x 16] ----
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t k = 0; k < kHidden / 16; ++k) {
+                mma_bf16(tmem, smem_desc(sH + k * 256u, 128u, (kHidden / 8) * 128u),
+                         smem_desc(sW3 + k * 256u, 128u, (kHidden / 8) * 128u), idesc_out, k > 0 ? 1u : 0u);
+            }
+            mma_commit(mbar);
+        }
+        ok = mbar_wait(mbar, parity);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        {
+            float v[16];
+            tmem_load16(tmem + lane_base, v);
+            if (valid) {
+                float y0 = v[0] + b3[0];
+                float y1 = v[1] + b3[1];
+                float y2 = v[2] + b3[2];
+                if (save) {
+                    float4* ys = reinterpret_cast<float4*>(saves.y);
+                    ys[row] = make_float4(y0, y1, y2, 0.0f);
+                }
+                if (out != nullptr) {
+                    reinterpret_cast<float4*>(out)[row] =
+                        make_float4(y0 * model.out_scale[0], y1 * model.out_scale[1], y2 * model.out_scale[2], 0.0f);
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(error_flag, 1u);
+        }
+        // Let an MMA still in flight finish (bounded) before the columns go.
+        mbar_wait(mbar, parity);
+        tc_fence_before();
+        __syncthreads();
+    }
+    tc_fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// ---- backward on the CUDA cores (FP32) ---------------------------------------
+
+constexpr uint32_t kRowsPerChunk = 1024;
+
+// Per row: dY from the loss, dH2 = dY W3, dZ2 = dH2 * GELU'(z2), dH1 = dZ2 W2,
+// dZ1 = dH1 * GELU'(z1). Weights as the forward saw them (BF16 values).
+__global__ void __launch_bounds__(128) backward_rows_kernel(ModelView model, ForwardSaves saves,
+                                                            const float* __restrict__ targets, uint32_t n,
+                                                            float* __restrict__ dz1, float* __restrict__ dz2,
+                                                            float* __restrict__ dy_out, float* __restrict__ loss_parts) {
+    extern __shared__ float sm[];
+    float* w2 = sm;                          // [128][128]
+    float* w3 = w2 + kHidden * kHidden;      // [3][128]
+    float* rows = w3 + kOut * kHidden;       // [128 threads][128] dZ2 rows
+    __shared__ float block_loss[4];
+    for (uint32_t i = threadIdx.x; i < kHidden * kHidden; i += blockDim.x) {
+        w2[i] = __bfloat162float(model.w2[i]);
+    }
+    for (uint32_t i = threadIdx.x; i < kOut * kHidden; i += blockDim.x) {
+        w3[i] = __bfloat162float(model.w3[i]);
+    }
+    __syncthreads();
+    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    float local_loss = 0.0f;
+    if (m < n) {
+        float4 y = reinterpret_cast<const float4*>(saves.y)[m];
+        float yv[3] = {y.x, y.y, y.z};
+        float dy[3];
+        const float inv = 2.0f / (static_cast<float>(n) * kOut);
+#pragma unroll
+        for (int o = 0; o < kOut; ++o) {
+            float t = targets[static_cast<size_t>(m) * kOut + o] / model.out_scale[o];
+            float e = yv[o] - t;
+            local_loss += e * e;
+            dy[o] = inv * e;
+            dy_out[static_cast<size_t>(m) * 4 + o] = dy[o];
+        }
+        float* row = rows + threadIdx.x * kHidden;
+        for (int k = 0; k < kHidden; ++k) {
+            float dh2 = dy[0] * w3[k] + dy[1] * w3[kHidden + k] + dy[2] * w3[2 * kHidden + k];
+            float d = dh2 * gelu_grad(saves.z2[static_cast<size_t>(m) * kHidden + k]);
+            row[k] = d;
+            dz2[static_cast<size_t>(m) * kHidden + k] = d;
+        }
+        for (int k = 0; k < kHidden; ++k) {
+            float acc = 0.0f;
+            for (int j = 0; j < kHidden; ++j) {
+                acc += row[j] * w2[j * kHidden + k];
+            }
+            dz1[static_cast<size_t>(m) * kHidden + k] = acc * gelu_grad(saves.z1[static_cast<size_t>(m) * kHidden + k]);
+        }
+        local_loss /= static_cast<float>(n) * kOut;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        local_loss += __shfl_down_sync(0xFFFFFFFFu, local_loss, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        block_loss[threadIdx.x >> 5] = local_loss;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        loss_parts[blockIdx.x] = block_loss[0] + block_loss[1] + block_loss[2] + block_loss[3];
+    }
+}
+
+// partial[chunk][o][k] = sum over the chunk's rows of dz[m][o] * in[m][k]
+// (k == in_dim stands for the bias input 1). One 32 x 32 (o, k) tile per
+// block; fixed order, so the result is deterministic.
+__global__ void __launch_bounds__(256) weight_grad_kernel(const float* __restrict__ dz, uint32_t dz_stride,
+                                                          const __nv_bfloat16* __restrict__ in, uint32_t in_dim,
+                                                          uint32_t out_dim, uint32_t n, float* __restrict__ partial) {
+    __shared__ float sdz[32][33];
+    __shared__ float sin[32][33];
+    const uint32_t chunk = blockIdx.x;
+    const uint32_t o0 = blockIdx.y * 32;
+    const uint32_t k0 = blockIdx.z * 32;
+    const uint32_t tx = threadIdx.x & 31;  // k
+    const uint32_t ty = threadIdx.x >> 5;  // 0..7 -> o = ty + 8 j
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const uint32_t first = chunk * kRowsPerChunk;
+    const uint32_t last = min(first + kRowsPerChunk, n);
+    for (uint32_t base = first; base < last; base += 32) {
+        for (uint32_t e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
+            uint32_t r = e >> 5;
+            uint32_t c = e & 31;
+            uint32_t m = base + r;
+            bool row_ok = m < last;
+            sdz[r][c] = (row_ok && o0 + c < out_dim) ? dz[static_cast<size_t>(m) * dz_stride + o0 + c] : 0.0f;
+            float x = 0.0f;
+            if (row_ok) {
+                uint32_t k = k0 + c;
+                x = k < in_dim ? __bfloat162float(in[static_cast<size_t>(m) * in_dim + k]) : (k == in_dim ? 1.0f : 0.0f);
+            }
+            sin[r][c] = x;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (uint32_t r = 0; r < 32; ++r) {
+            float x = sin[r][tx];
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+                acc[j] += sdz[r][ty + 8 * j] * x;
+            }
+        }
+        __syncthreads();
+    }
+    const uint32_t cols = in_dim + 1;
+#pragma unroll
+    for (uint32_t j = 0; j < 4; ++j) {
+        uint32_t o = o0 + ty + 8 * j;
+        uint32_t k = k0 + tx;
+        if (o < out_dim && k < cols) {
+            partial[(static_cast<size_t>(chunk) * out_dim + o) * cols + k] = acc[j];
+        }
+    }
+}
+
+// Sums the chunk partials in chunk order into the parameter gradient: W part
+// at grad[w_off + o * in_dim + k], bias at grad[b_off + o].
+__global__ void reduce_grad_kernel(const float* __restrict__ partial, uint32_t chunks, uint32_t out_dim, uint32_t in_dim,
+                                   float* __restrict__ grad, uint32_t w_off, uint32_t b_off) {
+    uint32_t cols = in_dim + 1;
+    uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= out_dim * cols) {
+        return;
+    }
+    float s = 0.0f;
+    for (uint32_t c = 0; c < chunks; ++c) {
+        s += partial[static_cast<size_t>(c) * out_dim * cols + idx];
+    }
+    uint32_t o = idx / cols;
+    uint32_t k = idx % cols;
+    if (k < in_dim) {
+        grad[w_off + o * in_dim + k] = s;
+    } else {
+        grad[b_off + o] = s;
+    }
+}
+
+__global__ void loss_sum_kernel(const float* __restrict__ parts, uint32_t count, float* __restrict__ loss) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        float s = 0.0f;
+        for (uint32_t i = 0; i < count; ++i) {
+            s += parts[i];
+        }
+        *loss = s;
+    }
+}
+
+__global__ void quantise_kernel(const float* __restrict__ params, __nv_bfloat16* __restrict__ w1,
+                                __nv_bfloat16* __restrict__ w2, __nv_bfloat16* __restrict__ w3) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kHidden * kIn) {
+        w1[i] = __float2bfloat16_rn(params[kW1 + i]);
+    }
+    if (i < kHidden * kHidden) {
+        w2[i] = __float2bfloat16_rn(params[kW2 + i]);
+    }
+    if (i < kOutPad * kHidden) {
+        w3[i] = i < kOut * kHidden ? __float2bfloat16_rn(params[kW3 + i]) : __float2bfloat16_rn(0.0f);
+    }
+}
+
+// adamStep (src/gfx/neural_math.cpp:1188-1208), moments stored [first | second].
+__global__ void adam_kernel(float* __restrict__ params, const float* __restrict__ grads, float* __restrict__ moments,
+                            float lr, float beta1, float beta2, float epsilon, float first_correction,
+                            float second_correction) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) {
+        return;
+    }
+    float g = grads[i];
+    float* first = moments;
+    float* second = moments + kParams;
+    first[i] = beta1 * first[i] + (1.0f - beta1) * g;
+    second[i] = beta2 * second[i] + (1.0f - beta2) * g * g;
+    float corrected_first = first[i] / first_correction;
+    float corrected_second = second[i] / second_correction;
+    params[i] -= lr * corrected_first / (sqrtf(corrected_second) + epsilon);
+}
+
+}  // namespace
+
+cudaError_t launch_forward(const ModelView& model, const float* features, uint32_t n, float* out_accel,
+                           const ForwardSaves* saves, unsigned int* error_flag, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    cudaError_t prepared = prepare_forward();
+    if (prepared != cudaSuccess) {
+        return prepared;
+    }
+    uint32_t tiles = (n + kTile - 1) / kTile;
+    int device = 0;
+    cudaGetDevice(&device);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(sms) * 2u);
+    ForwardSaves none{};
+    mlp_forward_kernel<<<grid, 128, kSmemBytes, stream>>>(model, features, n, out_accel, saves ? *saves : none,
+                                                          saves ? 1 : 0, error_flag);
+    return cudaGetLastError();
+}
+
+cudaError_t prepare_forward() {
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(kSmemBytes));
+        if (e != cudaSuccess) {
+            return e;
+        }
+        configured = true;
+    }
+    return cudaSuccess;
+}
+
+size_t backward_scratch_floats(uint32_t n) {
+    uint32_t chunks = (n + kRowsPerChunk - 1) / kRowsPerChunk;
+    size_t partial = static_cast<size_t>(chunks) * kHidden * (kHidden + 1);
+    return 2 * static_cast<size_t>(n) * kHidden + 4 * static_cast<size_t>(n) + partial + (n + 127) / 128 + 64;
+}
+
+cudaError_t launch_backward(const ModelView& model, const ForwardSaves& saves, const float* targets, uint32_t n,
+                            float* d_params, float* loss, float* scratch, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    float* dz1 = scratch;
+    float* dz2 = dz1 + static_cast<size_t>(n) * kHidden;
+    float* dy = dz2 + static_cast<size_t>(n) * kHidden;
+    uint32_t chunks = (n + kRowsPerChunk - 1) / kRowsPerChunk;
+    float* partial = dy + 4 * static_cast<size_t>(n);
+    float* loss_parts = partial + static_cast<size_t>(chunks) * kHidden * (kHidden + 1);
+    uint32_t blocks = (n + 127) / 128;
+    size_t smem = (kHidden * kHidden + kOut * kHidden + 128 * kHidden) * sizeof(float);
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(backward_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) {
+            return e;
+        }
+        configured = true;
+    }
+    backward_rows_kernel<<<blocks, 128, smem, stream>>>(model, saves, targets, n, dz1, dz2, dy, loss_parts);
+    loss_sum_kernel<<<1, 32, 0, stream>>>(loss_parts, blocks, loss);
+    struct Layer {
+        const float* dz;
+        uint32_t stride;
+        const __nv_bfloat16* in;
+        uint32_t in_dim;
+        uint32_t out_dim;
+        uint32_t w_off;
+        uint32_t b_off;
+    };
+    const Layer layers[3] = {
+        {dy, 4, saves.h2, static_cast<uint32_t>(kHidden), static_cast<uint32_t>(kOut), static_cast<uint32_t>(kW3),
+         static_cast<uint32_t>(kB3)},
+        {dz2, static_cast<uint32_t>(kHidden), saves.h1, static_cast<uint32_t>(kHidden),
+         static_cast<uint32_t>(kHidden), static_cast<uint32_t>(kW2), static_cast<uint32_t>(kB2)},
+        {dz1, static_cast<uint32_t>(kHidden), saves.x, static_cast<uint32_t>(kIn), static_cast<uint32_t>(kHidden),
+         static_cast<uint32_t>(kW1), static_cast<uint32_t>(kB1)},
+    };
+    for (const Layer& l : layers) {
+        dim3 grid(chunks, (l.out_dim + 31) / 32, (l.in_dim + 1 + 31) / 32);
+        weight_grad_kernel<<<grid, 256, 0, stream>>>(l.dz, l.stride, l.in, l.in_dim, l.out_dim, n, partial);
+        uint32_t entries = l.out_dim * (l.in_dim + 1);
+        reduce_grad_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(partial, chunks, l.out_dim, l.in_dim, d_params,
+                                                                      l.w_off, l.b_off);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quantise(const float* params, __nv_bfloat16* w1, __nv_bfloat16* w2, __nv_bfloat16* w3,
+                            cudaStream_t stream) {
+    quantise_kernel<<<(kHidden * kHidden + 255) / 256, 256, 0, stream>>>(params, w1, w2, w3);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float* params, const float* grads, float* moments, uint32_t step, float lr, float beta1,
+                        float beta2, float epsilon, __nv_bfloat16* w1, __nv_bfloat16* w2, __nv_bfloat16* w3,
+                        cudaStream_t stream) {
+    // adamCorrections (neural_math.cpp:1177-1186), step counted from 1.
+    float first = 1.0F - std::pow(beta1, static_cast<float>(step));
+    float second = 1.0F - std::pow(beta2, static_cast<float>(step));
+    if (step == 0 || !(first > 0.0F) || !(second > 0.0F)) {
+        return cudaSuccess;
+    }
+    adam_kernel<<<(kParams + 255) / 256, 256, 0, stream>>>(params, grads, moments, lr, beta1, beta2, epsilon, first,
+                                                           second);
+    return launch_quantise(params, w1, w2, w3, stream);
+}
+
+}  // namespace mlp
+}  // namespace sph
+
+// ---- C ABI --------------------------------------------------------------------
+
+
+struct sph_mlp {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    float* params = nullptr;   // FP32 vector
+    float* grads = nullptr;
+    float* moments = nullptr;  // first | second
+    __nv_bfloat16* w1 = nullptr;
+    __nv_bfloat16* w2 = nullptr;
+    __nv_bfloat16* w3 = nullptr;
+    float* norm = nullptr;     // mean[32] | inv_std[32] | out_scale[3]
+    float* loss = nullptr;
+    unsigned int* error = nullptr;
+    // Training buffers, grown to the largest batch.
+    uint32_t capacity = 0;
+    float* z1 = nullptr;
+    float* z2 = nullptr;
+    __nv_bfloat16* x = nullptr;
+    __nv_bfloat16* h1 = nullptr;
+    __nv_bfloat16* h2 = nullptr;
+    float* y = nullptr;
+    float* scratch = nullptr;
+    uint32_t step = 0;
+    float beta1 = 0.9F;
+    float beta2 = 0.999F;
+    float epsilon = 1e-8F;
+    std::string last_error;
+};
+
+namespace {
+
+using sph::mlp::kHidden;
+using sph::mlp::kIn;
+using sph::mlp::kOut;
+using sph::mlp::kOutPad;
+using sph::mlp::kParams;
+
+int mlp_fail(sph_mlp* m, cudaError_t e, const char* what) {
+    if (m != nullptr) {
+        m->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;
+}
+
+#define MLP_CUDA(m, call)                            \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) {                     \
+            return mlp_fail((m), e_, #call);         \
+        }                                            \
+    } while (0)
+
+sph::mlp::ModelView view(const sph_mlp* m) {
+    sph::mlp::ModelView v;
+    v.w1 = m->w1;
+    v.w2 = m->w2;
+    v.w3 = m->w3;
+    v.params = m->params;
+    v.in_mean = m->norm;
+    v.in_inv_std = m->norm + kIn;
+    v.out_scale = m->norm + 2 * kIn;
+    return v;
+}
+
+uint64_t splitmix(uint64_t v) {
+    v += 0x9E3779B97F4A7C15ULL;
+    v = (v ^ (v >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    v = (v ^ (v >> 27)) * 0x94D049BB133111EBULL;
+    return v ^ (v >> 31);
+}
+
+// Standard normal from two splitmix64 uniforms (Box-Muller).
+float gaussian(uint64_t seed, uint64_t index) {
+    double u1 = (static_cast<double>(splitmix(seed * 0x9E3779B97F4A7C15ULL + 2 * index) >> 11) + 1.0) * 0x1.0p-53;
+    double u2 = static_cast<double>(splitmix(seed * 0x9E3779B97F4A7C15ULL + 2 * index + 1) >> 11) * 0x1.0p-53;
+    return static_cast<float>(std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+}
+
+int grow(sph_mlp* m, uint32_t n) {
+    if (n <= m->capacity) {
+        return SPH_OK;
+    }
+    void* bufs[] = {m->z1, m->z2, m->x, m->h1, m->h2, m->y, m->scratch};
+    for (void* b : bufs) {
+        if (b != nullptr) {
+            cudaFree(b);
+        }
+    }
+    size_t rows = n;
+    MLP_CUDA(m, cudaMalloc(&m->z1, rows * kHidden * sizeof(float)));
+    MLP_CUDA(m, cudaMalloc(&m->z2, rows * kHidden * sizeof(float)));
+    MLP_CUDA(m, cudaMalloc(&m->x, rows * kIn * sizeof(__nv_bfloat16)));
+    MLP_CUDA(m, cudaMalloc(&m->h1, rows * kHidden * sizeof(__nv_bfloat16)));
+    MLP_CUDA(m, cudaMalloc(&m->h2, rows * kHidden * sizeof(__nv_bfloat16)));
+    MLP_CUDA(m, cudaMalloc(&m->y, rows * 4 * sizeof(float)));
+    MLP_CUDA(m, cudaMalloc(&m->scratch, sph::mlp::backward_scratch_floats(n) * sizeof(float)));
+    m->capacity = n;
+    return SPH_OK;
+}
+
+int gradients(sph_mlp* m, const void* features, const void* targets, uint32_t n) {
+    int status = grow(m, n);
+    if (status != SPH_OK) {
+        return status;
+    }
+    sph::mlp::ForwardSaves saves{m->z1, m->z2, m->x, m->h1, m->h2, m->y};
+    sph::mlp::ModelView v = view(m);
+    MLP_CUDA(m, cudaMemsetAsync(m->error, 0, sizeof(unsigned int), m->stream));
+    MLP_CUDA(m, sph::mlp::launch_forward(v, static_cast<const float*>(features), n, nullptr, &saves, m->error,
+                                         m->stream));
+    MLP_CUDA(m, sph::mlp::launch_backward(v, saves, static_cast<const float*>(targets), n, m->grads, m->loss,
+                                          m->scratch, m->stream));
+    return SPH_OK;
+}
+
+int check_error_flag(sph_mlp* m) {
+    unsigned int flag = 0;
+    MLP_CUDA(m, cudaMemcpyAsync(&flag, m->error, sizeof(flag), cudaMemcpyDeviceToHost, m->stream));
+    MLP_CUDA(m, cudaStreamSynchronize(m->stream));
+    if (flag != 0) {
+        m->last_error = "tensor-core completion wait timed out";
+        return SPH_ERR_TIMEOUT;
+    }
+    return SPH_OK;
+}
+
+}  // namespace
+
+bool sph_mlp_model_view(const sph_mlp* m, sph::mlp::ModelView* out) {
+    if (m == nullptr || out == nullptr) {
+        return false;
+    }
+    *out = view(m);
+    return true;
+}
+
+extern "C" {
+
+int sph_mlp_create(int device, uint64_t seed, sph_mlp** out) {
+    if (out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) {
+        cudaGetLastError();
+        return SPH_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= devices) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    sph_mlp* m = new (std::nothrow) sph_mlp();
+    if (m == nullptr) {
+        return SPH_ERR_OUT_OF_MEMORY;
+    }
+    m->device = device;
+    auto cleanup = [&](int status) {
+        sph_mlp_destroy(m);
+        return status;
+    };
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&m->params, kParams * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->grads, kParams * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->moments, 2 * kParams * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->w1, kHidden * kIn * sizeof(__nv_bfloat16)) != cudaSuccess ||
+        cudaMalloc(&m->w2, kHidden * kHidden * sizeof(__nv_bfloat16)) != cudaSuccess ||
+        cudaMalloc(&m->w3, kOutPad * kHidden * sizeof(__nv_bfloat16)) != cudaSuccess ||
+        cudaMalloc(&m->norm, (2 * kIn + kOut + 1) * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->loss, sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->error, sizeof(unsigned int)) != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(SPH_ERR_OUT_OF_MEMORY);
+    }
+    // He-normal weights (std sqrt(2 / fan_in)), zero biases; the last layer is
+    // scaled down so an untrained model starts near "no correction".
+    std::vector<float> p(kParams, 0.0F);
+    uint64_t stream_id = 0;
+    auto fill = [&](int offset, int count, int fan_in, float extra) {
+        float deviation = std::sqrt(2.0F / static_cast<float>(fan_in)) * extra;
+        for (int i = 0; i < count; ++i) {
+            p[offset + i] = deviation * gaussian(seed + stream_id, static_cast<uint64_t>(i));
+        }
+        ++stream_id;
+    };
+    fill(sph::mlp::kW1, kHidden * kIn, kIn, 1.0F);
+    fill(sph::mlp::kW2, kHidden * kHidden, kHidden, 1.0F);
+    fill(sph::mlp::kW3, kOut * kHidden, kHidden, 0.1F);
+    std::vector<float> norm(2 * kIn + kOut + 1, 0.0F);
+    for (int i = 0; i < kIn; ++i) {
+        norm[kIn + i] = 1.0F;
+    }
+    for (int o = 0; o < kOut; ++o) {
+        norm[2 * kIn + o] = 1.0F;
+    }
+    if (cudaMemcpy(m->params, p.data(), kParams * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(m->norm, norm.data(), norm.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(m->moments, 0, 2 * kParams * sizeof(float)) != cudaSuccess ||
+        sph::mlp::launch_quantise(m->params, m->w1, m->w2, m->w3, m->stream) != cudaSuccess ||
+        cudaStreamSynchronize(m->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(SPH_ERR_CUDA);
+    }
+    *out = m;
+    return SPH_OK;
+}
+
+int sph_mlp_destroy(sph_mlp* m) {
+    if (m == nullptr) {
+        return SPH_OK;
+    }
+    cudaSetDevice(m->device);
+    void* bufs[] = {m->params, m->grads, m->moments, m->w1, m->w2, m->w3, m->norm, m->loss, m->error,
+                    m->z1,     m->z2,    m->x,       m->h1, m->h2, m->y,  m->scratch};
+    for (void* b : bufs) {
+        if (b != nullptr) {
+            cudaFree(b);
+        }
+    }
+    if (m->stream != nullptr) {
+        cudaStreamDestroy(m->stream);
+    }
+    delete m;
+    return SPH_OK;
+}
+
+const char* sph_mlp_last_error(const sph_mlp* m) { return m == nullptr ? "" : m->last_error.c_str(); }
+
+int sph_mlp_get_params(sph_mlp* m, float* params) {
+    if (m == nullptr || params == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaStreamSynchronize(m->stream));
+    MLP_CUDA(m, cudaMemcpy(params, m->params, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+    return SPH_OK;
+}
+
+int sph_mlp_set_params(sph_mlp* m, const float* params) {
+    if (m == nullptr || params == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < kParams; ++i) {
+        if (!std::isfinite(params[i])) {
+            return SPH_ERR_NONFINITE;
+        }
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaMemcpyAsync(m->params, params, kParams * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    MLP_CUDA(m, sph::mlp::launch_quantise(m->params, m->w1, m->w2, m->w3, m->stream));
+    MLP_CUDA(m, cudaMemsetAsync(m->moments, 0, 2 * kParams * sizeof(float), m->stream));
+    MLP_CUDA(m, cudaStreamSynchronize(m->stream));
+    m->step = 0;
+    return SPH_OK;
+}
+
+int sph_mlp_set_normalisation(sph_mlp* m, const float* feature_mean, const float* feature_std,
+                              const float* output_scale) {
+    if (m == nullptr || feature_mean == nullptr || feature_std == nullptr || output_scale == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<float> norm(2 * kIn + kOut + 1, 0.0F);
+    for (int i = 0; i < kIn; ++i) {
+        if (!(feature_std[i] > 0.0F) || !std::isfinite(feature_mean[i])) {
+            return SPH_ERR_INVALID_ARGUMENT;
+        }
+        norm[i] = feature_mean[i];
+        norm[kIn + i] = 1.0F / feature_std[i];
+    }
+    for (int o = 0; o < kOut; ++o) {
+        if (!(output_scale[o] > 0.0F)) {
+            return SPH_ERR_INVALID_ARGUMENT;
+        }
+        norm[2 * kIn + o] = output_scale[o];
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaMemcpy(m->norm, norm.data(), norm.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return SPH_OK;
+}
+
+int sph_mlp_get_normalisation(sph_mlp* m, float* feature_mean, float* feature_std, float* output_scale) {
+    if (m == nullptr || feature_mean == nullptr || feature_std == nullptr || output_scale == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<float> norm(2 * kIn + kOut + 1);
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaMemcpy(norm.data(), m->norm, norm.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < kIn; ++i) {
+        feature_mean[i] = norm[i];
+        feature_std[i] = 1.0F / norm[kIn + i];
+    }
+    for (int o = 0; o < kOut; ++o) {
+        output_scale[o] = norm[2 * kIn + o];
+    }
+    return SPH_OK;
+}
+
+int sph_mlp_forward(sph_mlp* m, const void* features, uint32_t count, void* accel, void* stream) {
+    if (m == nullptr || (count > 0 && (features == nullptr || accel == nullptr))) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    cudaStream_t s = stream != nullptr ? static_cast<cudaStream_t>(stream) : m->stream;
+    MLP_CUDA(m, cudaMemsetAsync(m->error, 0, sizeof(unsigned int), s));
+    MLP_CUDA(m, sph::mlp::launch_forward(view(m), static_cast<const float*>(features), count,
+                                         static_cast<float*>(accel), nullptr, m->error, s));
+    if (stream == nullptr) {
+        return check_error_flag(m);
+    }
+    return SPH_OK;
+}
+
+int sph_mlp_gradients(sph_mlp* m, const void* features, const void* targets, uint32_t count, float* grads,
+                      float* loss) {
+    if (m == nullptr || features == nullptr || targets == nullptr || count == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    int status = gradients(m, features, targets, count);
+    if (status != SPH_OK) {
+        return status;
+    }
+    status = check_error_flag(m);
+    if (status != SPH_OK) {
+        return status;
+    }
+    if (grads != nullptr) {
+        MLP_CUDA(m, cudaMemcpy(grads, m->grads, kParams * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    if (loss != nullptr) {
+        MLP_CUDA(m, cudaMemcpy(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    return SPH_OK;
+}
+
+int sph_mlp_set_adam(sph_mlp* m, float beta1, float beta2, float epsilon) {
+    if (m == nullptr || !(beta1 >= 0.0F && beta1 < 1.0F) || !(beta2 >= 0.0F && beta2 < 1.0F) || !(epsilon > 0.0F)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    m->beta1 = beta1;
+    m->beta2 = beta2;
+    m->epsilon = epsilon;
+    return SPH_OK;
+}
+
+int sph_mlp_train_step(sph_mlp* m, const void* features, const void* targets, uint32_t count, float learning_rate,
+                       float* loss) {
+    if (m == nullptr || features == nullptr || targets == nullptr || count == 0 || !(learning_rate > 0.0F)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    int status = gradients(m, features, targets, count);
+    if (status != SPH_OK) {
+        return status;
+    }
+    m->step += 1;
+    MLP_CUDA(m, sph::mlp::launch_adam(m->params, m->grads, m->moments, m->step, learning_rate, m->beta1, m->beta2,
+                                      m->epsilon, m->w1, m->w2, m->w3, m->stream));
+    if (loss != nullptr) {
+        MLP_CUDA(m, cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
+    }
+    return check_error_flag(m);
+}
+
+int sph_mlp_stream(sph_mlp* m, void** stream) {
+    if (m == nullptr || stream == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *stream = static_cast<void*>(m->stream);
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -102,6 +102,11 @@ class FluidSolverGpu:
         """Enqueues substeps without waiting for them."""
         self._check(self._lib.sph_run(self._ctx, ctypes.c_float(dt), substeps), "sph_run")
 
+    def run_learned(self, dt: float, substeps: int, mlp=None) -> None:
+        """Learned coarse substeps (mlp None: zero correction, the plain bits)."""
+        self._check(self._lib.sph_run_learned(self._ctx, ctypes.c_float(dt), substeps,
+                                              None if mlp is None else mlp.handle), "sph_run_learned")
+
     def particle_count(self) -> int:
         out = ctypes.c_uint32()
         self._check(self._lib.sph_particle_count(self._ctx, ctypes.byref(out)), "sph_particle_count")

@@ -316,6 +316,71 @@ int sph_batch_profile_substeps(sph_batch* batch, float dt, uint32_t substeps, do
 int sph_batch_launches_per_substep(const sph_batch* batch, uint32_t* launches);
 int sph_batch_device_bytes(const sph_batch* batch, uint64_t* bytes);
 
+/* ---- learned acceleration correction (MLP) ------------------------------
+ *
+ * No counterpart in the reference. A 32 -> 128 -> 128 -> 3 MLP with GELU
+ * (erf form), BF16 weights and FP32 accumulation; forward on the tensor cores
+ * (tcgen05), backward and Adam (src/gfx/neural_math.cpp:1177-1208) on the CUDA
+ * cores. Inputs are 32 FP32 features per particle (sph_batch_learned_sample
+ * documents them); outputs are accelerations (m/s^2) in an n x 4 array
+ * (xyz, w = 0). Feature and target arrays are device pointers. */
+#define SPH_MLP_INPUTS 32
+#define SPH_MLP_HIDDEN 128
+#define SPH_MLP_OUTPUTS 3
+/* FP32 parameter vector: W1[128][32], b1[128], W2[128][128], b2[128], W3[3][128], b3[3]. */
+#define SPH_MLP_PARAMS 21123
+typedef struct sph_mlp sph_mlp;
+
+/* He-normal weights from a seeded splitmix64 stream, zero biases. */
+int sph_mlp_create(int device, uint64_t seed, sph_mlp** out);
+int sph_mlp_destroy(sph_mlp* mlp);
+const char* sph_mlp_last_error(const sph_mlp* mlp);
+int sph_mlp_get_params(sph_mlp* mlp, float* params);
+/* Replaces the FP32 parameters (BF16 copies refreshed, Adam state reset). */
+int sph_mlp_set_params(sph_mlp* mlp, const float* params);
+/* Inputs are normalised as (f - mean) / std; outputs are network * scale. */
+int sph_mlp_set_normalisation(sph_mlp* mlp, const float* feature_mean, const float* feature_std,
+                              const float* output_scale);
+int sph_mlp_get_normalisation(sph_mlp* mlp, float* feature_mean, float* feature_std, float* output_scale);
+/* accel[n][4] = MLP(features[n][32]). With stream == NULL the call runs on
+ * the model's stream and synchronises; otherwise it is enqueued on `stream`. */
+int sph_mlp_forward(sph_mlp* mlp, const void* features, uint32_t count, void* accel, void* stream);
+/* Gradient of the mean squared error between the normalised output and
+ * targets[n][3] / output_scale, into grads[SPH_MLP_PARAMS] (host); no update. */
+int sph_mlp_gradients(sph_mlp* mlp, const void* features, const void* targets, uint32_t count, float* grads,
+                      float* loss);
+int sph_mlp_set_adam(sph_mlp* mlp, float beta1, float beta2, float epsilon);
+/* One Adam step on a batch; loss (host, may be NULL) is the batch's loss. */
+int sph_mlp_train_step(sph_mlp* mlp, const void* features, const void* targets, uint32_t count, float learning_rate,
+                       float* loss);
+int sph_mlp_stream(sph_mlp* mlp, void** stream);
+
+/* Learned coarse substeps (no counterpart in the reference): the plain SPH
+ * force as in sph_step, plus the MLP's acceleration correction, then the
+ * plain velocity update, speed clamp and walls. mlp == NULL runs the same
+ * path with a zero correction, which is bit-identical to the plain substep. */
+int sph_run_learned(sph_ctx* ctx, float dt, uint32_t substeps, const sph_mlp* mlp);
+int sph_batch_run_learned(sph_batch* batch, float dt, uint32_t substeps, const sph_mlp* mlp);
+/* The 32 correction features of every particle of the current state (device
+ * array, all tanks, id order, n x 32 floats) for a substep of length dt; the
+ * state does not change. Feature definitions: csrc/sph_forces.cu. */
+int sph_batch_learned_features(sph_batch* batch, float dt, void* features);
+/* SPH_ERR_TIMEOUT if a tensor-core completion wait gave up since the last
+ * check (the step's results are then not valid). Synchronises. */
+int sph_batch_learned_check(sph_batch* batch);
+/* Saves (save != 0) or restores the whole particle state in device memory,
+ * in slot 0 or 1; sph_batch_restore_tanks copies back only the tanks with
+ * which[t] != 0. */
+int sph_batch_snapshot(sph_batch* batch, uint32_t slot, int save);
+int sph_batch_restore_tanks(sph_batch* batch, uint32_t slot, const uint8_t* which);
+/* Device pointers to all tanks' state (AoS float4, id order); tank t starts
+ * at particle sph_batch_tank_offset(t). */
+int sph_batch_device_state(sph_batch* batch, void** positions, void** velocities);
+int sph_batch_tank_offset(const sph_batch* batch, uint32_t tank, uint32_t* first);
+/* Copies the whole state (id order, AoS float4) into caller device buffers,
+ * enqueued on the batch's stream; either pointer may be NULL. */
+int sph_batch_copy_state(sph_batch* batch, void* positions, void* velocities);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

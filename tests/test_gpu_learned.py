@@ -1,0 +1,76 @@
+"""The learned coarse step through the C ABI: with no correction it is the
+plain substep bit for bit; features are finite; the training and
+fallback pipeline runs end to end on a small set."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from computer_graphics_lab_00_gb300 import training as T
+from computer_graphics_lab_00_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b) -> bool:
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def small():
+    return T.learned_tanks(tanks=4, particles=4096, seed=2)
+
+
+def test_zero_correction_is_the_plain_step(native, oracle, small):
+    a = T.load_tanks(small)
+    b = T.load_tanks(small)
+    a.run_learned(T.COARSE_DT, 3, None)
+    b.run(T.COARSE_DT, 3)
+    for t in range(small.counts.__len__()):
+        pa, va = a.download(t)
+        pb, vb = b.download(t)
+        assert same(pa, pb) and same(va, vb), t
+        op, ov = oracle.run_substeps(small.params[t], *small.initial_state(t), T.COARSE_DT, 3)
+        assert same(pa, op) and same(va, ov), t
+    a.close()
+    b.close()
+
+
+def test_features_are_finite_and_plausible(native, small):
+    import torch
+
+    s = T.load_tanks(small)
+    s.run(T.FINE_DT, 50)
+    n = s.total_particles
+    f = torch.empty((n, 32), dtype=torch.float32, device="cuda")
+    before = [s.download(t) for t in range(len(small.counts))]
+    s.learned_features(T.COARSE_DT, f.data_ptr())
+    s.synchronize()
+    for t in range(len(small.counts)):
+        p, v = s.download(t)
+        assert same(p, before[t][0]) and same(v, before[t][1])
+    f = f.cpu().numpy()
+    assert np.isfinite(f).all()
+    pairs = f[:, 8] * 32
+    assert 5 < np.median(pairs) < 60
+    assert (f[:, 26:] >= 0).all() and (f[:, 26:] <= 4).all()
+    s.close()
+
+
+def test_pipeline_end_to_end(native, small, tmp_path):
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    feats, targs = T.generate(small, snapshots=4, duration=0.1)
+    assert feats.shape == (4 * sum(small.counts), 32) and targs.shape == (4 * sum(small.counts), 3)
+    with MlpGpu(seed=4) as mlp:
+        rep = T.train(mlp, feats, targs, steps=60, batch=8192, lr=1e-3, log_every=20)
+        assert rep["losses"][-1][1] < rep["losses"][0][1]
+        T.save_model(mlp, tmp_path / "m.npz")
+        with MlpGpu(seed=9) as other:
+            T.load_model(other, tmp_path / "m.npz")
+            assert np.array_equal(other.params(), mlp.params())
+        cmp = T.compare_with_fine(small, mlp, duration=0.1, every=0.05)
+        assert set(cmp) == {"learned", "plain"}
+        fb = T.run_with_fallback(small, mlp, coarse_steps=12, check_every=4)
+        assert fb["coarse_steps"] == 12 and fb["checks"] >= 1
+        assert 0.0 <= fb["fallback_fraction"] <= 1.0
