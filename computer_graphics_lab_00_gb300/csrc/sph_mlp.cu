@@ -131,19 +131,44 @@ __device__ __forceinline__ void store_chunk(uint8_t* base, uint32_t offset, cons
     *reinterpret_cast<uint4*>(base + offset) = q;
 }
 
-// One CTA of 128 threads owns 128 TMEM columns and runs 128-particle tiles:
+// erf by Abramowitz & Stegun 7.1.26 (Handbook of Mathematical Functions,
+// 1964): 1 - (a1 t + ... + a5 t^5) exp(-x^2), t = 1 / (1 + p |x|), absolute
+// error at most 1.5e-7 — far below the BF16 rounding the activations get
+// next (plus a few ulp of __expf). Checked against erff by
+// sph_mlp_selftest_erf.
+__device__ __forceinline__ float erf_as(float x) {
+    float ax = fabsf(x);
+    float t = __frcp_rn(fmaf(0.3275911f, ax, 1.0f));
+    float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f),
+                          0.254829592f);
+    float y = 1.0f - poly * __expf(-ax * ax);
+    return copysignf(y, x);
+}
+
+// GELU of the forward pass (erf form through erf_as).
+__device__ __forceinline__ float gelu_fast(float z) { return 0.5f * z * (1.0f + erf_as(z * 0.70710678118654752f)); }
+
+constexpr uint32_t kForwardThreads = 256;
+
+// One CTA of 256 threads owns 128 TMEM columns and runs 128-particle tiles:
 // X (normalised features, BF16) -> [MMA W1] -> +b1, GELU -> H1 (BF16) ->
-// [MMA W2] -> +b2, GELU -> H2 -> [MMA W3] -> +b3 -> scaled output. Thread t
-// is row t of the tile and TMEM lane t. One thread issues the MMAs; an
-// mbarrier reports their completion.
-__global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, const float* __restrict__ features,
-                                                             uint32_t n, float* __restrict__ out, ForwardSaves saves,
-                                                             int save, unsigned int* __restrict__ error_flag) {
+// [MMA W2] -> +b2, GELU -> H2 -> [MMA W3] -> +b3 -> scaled output. Row r of a
+// tile is TMEM lane r; warp w reads the lane quarter w % 4 and, for the hidden
+// layers, the column half w / 4, so two threads share each row's epilogue.
+// One thread issues the MMAs; an mbarrier reports their completion.
+__global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelView model,
+                                                                         const float* __restrict__ features,
+                                                                         uint32_t n, float* __restrict__ out,
+                                                                         ForwardSaves saves, int save,
+                                                                         unsigned int* __restrict__ error_flag) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmemBar);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kSmemBar + 8);
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5;
+    const uint32_t quarter = warp & 3u;
+    const uint32_t half = warp >> 2;
+    const uint32_t local_row = quarter * 32u + (tid & 31u);
 
     // Weights into the canonical K-major layout (16-byte chunks).
     for (uint32_t c = tid; c < kHidden * (kIn / 8); c += blockDim.x) {
@@ -179,7 +204,7 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t lane_base = (warp * 32u) << 16;
+    const uint32_t lane_base = (quarter * 32u) << 16;
     const float* b1 = model.params + kB1;
     const float* b2 = model.params + kB2;
     const float* b3 = model.params + kB3;
@@ -195,12 +220,13 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
     const uint32_t tiles = (n + kTile - 1) / kTile;
 
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
-        const uint32_t row = tile * kTile + tid;
+        const uint32_t row = tile * kTile + local_row;
         const bool valid = row < n;
-        // Normalised features -> BF16 tile.
+        // Normalised features -> BF16 tile; each thread converts 16 of its row's 32.
         const float4* frow = reinterpret_cast<const float4*>(features + static_cast<size_t>(row) * kIn);
 #pragma unroll
-        for (uint32_t chunk = 0; chunk < kIn / 8; ++chunk) {
+        for (uint32_t j = 0; j < 2; ++j) {
+            uint32_t chunk = half * 2u + j;
             float v[8];
             float4 a = valid ? frow[2 * chunk] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             float4 b = valid ? frow[2 * chunk + 1] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -210,7 +236,7 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
                 uint32_t f = chunk * 8 + k;
                 v[k] = valid ? (raw[k] - model.in_mean[f]) * model.in_inv_std[f] : 0.0f;
             }
-            store_chunk(smem + kSmemX, tile_offset(tid, chunk, kIn), v);
+            store_chunk(smem + kSmemX, tile_offset(local_row, chunk, kIn), v);
             if (save && valid) {
 #pragma unroll
                 for (uint32_t k = 0; k < 8; ++k) {
@@ -239,7 +265,9 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
         }
         parity ^= 1u;
         tc_fence_after();
-        for (uint32_t c = 0; c < kHidden / 16; ++c) {
+#pragma unroll 1
+        for (uint32_t j = 0; j < 4; ++j) {
+            uint32_t c = half * 4u + j;
             float v[16];
             tmem_load16(tmem + lane_base + c * 16u, v);
 #pragma unroll
@@ -248,10 +276,10 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
                 if (save && valid) {
                     saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
                 }
-                v[k] = gelu(z);
+                v[k] = gelu_fast(z);
             }
-            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c, kHidden), v);
-            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c + 1, kHidden), v + 8);
+            store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c, kHidden), v);
+            store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
             if (save && valid) {
 #pragma unroll
                 for (uint32_t k = 0; k < 16; ++k) {
@@ -280,7 +308,9 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
         }
         parity ^= 1u;
         tc_fence_after();
-        for (uint32_t c = 0; c < kHidden / 16; ++c) {
+#pragma unroll 1
+        for (uint32_t j = 0; j < 4; ++j) {
+            uint32_t c = half * 4u + j;
             float v[16];
             tmem_load16(tmem + lane_base + c * 16u, v);
 #pragma unroll
@@ -289,10 +319,10 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
                 if (save && valid) {
                     saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
                 }
-                v[k] = gelu(z);
+                v[k] = gelu_fast(z);
             }
-            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c, kHidden), v);
-            store_chunk(smem + kSmemH, tile_offset(tid, 2 * c + 1, kHidden), v + 8);
+            store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c, kHidden), v);
+            store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
             if (save && valid) {
 #pragma unroll
                 for (uint32_t k = 0; k < 16; ++k) {
@@ -321,7 +351,7 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
         }
         parity ^= 1u;
         tc_fence_after();
-        {
+        if (half == 0) {
             float v[16];
             tmem_load16(tmem + lane_base, v);
             if (valid) {
@@ -329,8 +359,7 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
                 float y1 = v[1] + b3[1];
                 float y2 = v[2] + b3[2];
                 if (save) {
-                    float4* ys = reinterpret_cast<float4*>(saves.y);
-                    ys[row] = make_float4(y0, y1, y2, 0.0f);
+                    reinterpret_cast<float4*>(saves.y)[row] = make_float4(y0, y1, y2, 0.0f);
                 }
                 if (out != nullptr) {
                     reinterpret_cast<float4*>(out)[row] =
@@ -354,6 +383,17 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_kernel(ModelView model, co
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
     }
+}
+
+// max |erf_as(x) - erff(x)| over `count` points spread on [-6, 6] (as float
+// bits in *out).
+__global__ void erf_selftest_kernel(uint32_t count, unsigned int* out) {
+    float worst = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        float x = -6.0f + 12.0f * (static_cast<float>(i) / static_cast<float>(count));
+        worst = fmaxf(worst, fabsf(erf_as(x) - erff(x)));
+    }
+    atomicMax(out, __float_as_uint(worst));
 }
 
 // ---- backward on the CUDA cores (FP32) ---------------------------------------
@@ -555,9 +595,13 @@ cudaError_t launch_forward(const ModelView& model, const float* features, uint32
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(sms) * 2u);
     ForwardSaves none{};
-    mlp_forward_kernel<<<grid, 128, kSmemBytes, stream>>>(model, features, n, out_accel, saves ? *saves : none,
+    mlp_forward_kernel<<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel, saves ? *saves : none,
                                                           saves ? 1 : 0, error_flag);
     return cudaGetLastError();
+}
+
+void launch_erf_selftest(uint32_t count, unsigned int* out, cudaStream_t stream) {
+    erf_selftest_kernel<<<152 * 4, 256, 0, stream>>>(count, out);
 }
 
 cudaError_t prepare_forward() {
@@ -1017,6 +1061,21 @@ int sph_mlp_train_step(sph_mlp* m, const void* features, const void* targets, ui
         MLP_CUDA(m, cudaMemcpyAsync(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, m->stream));
     }
     return check_error_flag(m);
+}
+
+int sph_mlp_selftest_erf(sph_mlp* m, uint32_t count, float* max_abs_error) {
+    if (m == nullptr || max_abs_error == nullptr || count == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaMemsetAsync(m->error, 0, sizeof(unsigned int), m->stream));
+    sph::mlp::launch_erf_selftest(count, m->error, m->stream);
+    unsigned int bits = 0;
+    MLP_CUDA(m, cudaMemcpyAsync(&bits, m->error, sizeof(bits), cudaMemcpyDeviceToHost, m->stream));
+    MLP_CUDA(m, cudaStreamSynchronize(m->stream));
+    std::memcpy(max_abs_error, &bits, sizeof(float));
+    MLP_CUDA(m, cudaMemsetAsync(m->error, 0, sizeof(unsigned int), m->stream));
+    return SPH_OK;
 }
 
 int sph_mlp_stream(sph_mlp* m, void** stream) {

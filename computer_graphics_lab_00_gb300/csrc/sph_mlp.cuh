@@ -75,6 +75,8 @@ cudaError_t launch_quantise(const float* params, __nv_bfloat16* w1, __nv_bfloat1
 // Sets the forward kernel's shared-memory limit; call once per device before
 // any stream capture that contains a forward launch.
 cudaError_t prepare_forward();
+// max |erf_as - erff| over [-6, 6] as float bits in *out (pre-zeroed).
+void launch_erf_selftest(uint32_t count, unsigned int* out, cudaStream_t stream);
 
 }  // namespace mlp
 }  // namespace sph

@@ -46,6 +46,7 @@ def _declare(lib):
         "sph_mlp_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                               ctypes.c_float, f32p]),
         "sph_mlp_stream": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p)]),
+        "sph_mlp_selftest_erf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, f32p]),
     }
     for name, (restype, argtypes) in sigs.items():
         fn = getattr(lib, name)
@@ -139,6 +140,11 @@ class MlpGpu:
         self._check(self._lib.sph_mlp_train_step(self._h, ctypes.c_void_p(features_ptr), ctypes.c_void_p(targets_ptr),
                                                  count, lr, _fp(loss)), "sph_mlp_train_step")
         return float(loss[0])
+
+    def selftest_erf(self, count: int = 1 << 24) -> float:
+        out = np.zeros(1, np.float32)
+        self._check(self._lib.sph_mlp_selftest_erf(self._h, count, _fp(out)), "sph_mlp_selftest_erf")
+        return float(out[0])
 
     # -- checkpoints: FP32 weights + normalisation, JSON ----------------------------
     def save(self, path) -> None:

@@ -354,6 +354,9 @@ int sph_mlp_set_adam(sph_mlp* mlp, float beta1, float beta2, float epsilon);
 int sph_mlp_train_step(sph_mlp* mlp, const void* features, const void* targets, uint32_t count, float learning_rate,
                        float* loss);
 int sph_mlp_stream(sph_mlp* mlp, void** stream);
+/* Diagnostic: largest |erf(x) - erff(x)| of the forward pass's erf
+ * (Abramowitz & Stegun 7.1.26) over `count` points on [-6, 6]. */
+int sph_mlp_selftest_erf(sph_mlp* mlp, uint32_t count, float* max_abs_error);
 
 /* Learned coarse substeps (no counterpart in the reference): the plain SPH
  * force as in sph_step, plus the MLP's acceleration correction, then the

@@ -121,3 +121,14 @@ def test_training_fits_a_smooth_target(native, torch_cuda):
         for _ in range(300):
             last = mlp.train_step(d_f.data_ptr(), d_t.data_ptr(), n, lr=1e-3)
     assert last < 0.1 * first, (first, last)
+
+
+def test_forward_erf_is_within_its_published_bound(native):
+    """The forward pass evaluates GELU's erf by Abramowitz & Stegun 7.1.26
+    (absolute error 1.5e-7) with the fast exponential (__expf, a few ulp);
+    against erff the sum must stay below 1e-6, four orders under the BF16
+    rounding the activation gets next."""
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    with MlpGpu() as mlp:
+        assert mlp.selftest_erf() < 1e-6
