@@ -176,42 +176,59 @@ def cpu_baseline(case, seconds: float) -> dict:
     }
 
 
-def batched_leg(steps: int, flush, device: int) -> dict:
+def batched_leg(steps: int, flush, device: int, world: int = 1) -> dict:
     """256 independent tanks (about 5M particles, uneven sizes) advanced by one
-    CUDA graph launch per substep; launch shape from the autotuner."""
+    CUDA graph launch per substep; launch shape from the autotuner. With N
+    ranks the tanks are sharded by particle count (no exchange between
+    ranks); the time is the slowest rank's and the work is fixed ("strong")."""
     import torch
 
     from computer_graphics_lab_00_gb300 import workloads as W
-    from computer_graphics_lab_00_gb300.batch import BatchSolverGpu
+    from computer_graphics_lab_00_gb300.sharding import ShardedBatch
 
     ts = W.batched_tanks()
-    solver = BatchSolverGpu(ts.params, ts.counts, device=device)
-    for t in range(len(ts.counts)):
-        solver.upload(t, *ts.initial_state(t))
-    tune = solver.autotune(ts.dt, 3)
-    stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
-    solver.run(ts.dt, 3)
-    solver.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
-    for k in range(steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            starts[k].record(stream)
-        solver.run(ts.dt, 1)
-        ends[k].record(stream)
-    torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
-    phases = solver.profile(ts.dt, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    shard = ShardedBatch(ts, rank, world, device=device)
+    solver = shard.solver
+    ms = 0.0
+    tune = {"tuning": None}
+    phases = {}
+    launches = 0
+    if solver is not None:
+        tune = solver.autotune(ts.dt, 3)
+        stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
+        solver.run(ts.dt, 3)
+        solver.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                starts[k].record(stream)
+            solver.run(ts.dt, 1)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
+        phases = solver.profile(ts.dt, 3)
+        launches = solver.launches_per_substep()
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
     n = ts.total_particles
     out = {
         "workload": ts.name, "tanks": len(ts.counts), "particles": n, "dt": ts.dt, "steps": steps,
         "ms_per_step": ms, "value": n * ts.dt / (ms / 1e3), "unit": UNIT,
         "particle_steps_per_s": n / (ms / 1e3), "tuning": tune["tuning"],
         "phase_ms": {k: v / 3 for k, v in phases.items()},
-        "launches_per_substep": solver.launches_per_substep(),
+        "launches_per_substep": launches,
+        "scaling": "strong",
+        "sharding": f"{world} ranks, tanks by greedy particle balance" if world > 1 else "one GPU",
+        "rank0_tanks": len(shard.tanks), "rank0_particles": shard.particles,
     }
-    solver.close()
+    shard.close()
     return out
 
 
@@ -397,6 +414,7 @@ def run_gb300(args) -> None:
 
         dist.all_reduce(times, op=dist.ReduceOp.MAX)
     device_ms, e2e_wall = float(times[0]), float(times[1])
+    batched = batched_leg(args.batched_steps, flush, local, world) if args.batched_steps > 0 else None
     if rank != 0:
         solver.close()
         return
@@ -460,8 +478,8 @@ def run_gb300(args) -> None:
         "clocks": clocks,
         "wall_s_timed": wall,
     }
-    if args.batched_steps > 0 and world == 1:
-        out["batched"] = batched_leg(args.batched_steps, flush, local)
+    if batched is not None:
+        out["batched"] = batched
     if args.learned_steps > 0 and world == 1 and WEIGHTS.exists():
         out["learned"] = learned_leg(args.learned_steps, flush, local, step_ms)
     if world == 1 and not args.no_cpu_baseline:

@@ -1063,6 +1063,19 @@ int sph_mlp_train_step(sph_mlp* m, const void* features, const void* targets, ui
     return check_error_flag(m);
 }
 
+int sph_mlp_apply_gradients(sph_mlp* m, const float* grads, float learning_rate) {
+    if (m == nullptr || grads == nullptr || !(learning_rate > 0.0F)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaMemcpyAsync(m->grads, grads, kParams * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+    m->step += 1;
+    MLP_CUDA(m, sph::mlp::launch_adam(m->params, m->grads, m->moments, m->step, learning_rate, m->beta1, m->beta2,
+                                      m->epsilon, m->w1, m->w2, m->w3, m->stream));
+    MLP_CUDA(m, cudaStreamSynchronize(m->stream));
+    return check_error_flag(m);
+}
+
 int sph_mlp_selftest_erf(sph_mlp* m, uint32_t count, float* max_abs_error) {
     if (m == nullptr || max_abs_error == nullptr || count == 0) {
         return SPH_ERR_INVALID_ARGUMENT;

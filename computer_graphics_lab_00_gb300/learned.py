@@ -47,6 +47,7 @@ def _declare(lib):
                                               ctypes.c_float, f32p]),
         "sph_mlp_stream": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p)]),
         "sph_mlp_selftest_erf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, f32p]),
+        "sph_mlp_apply_gradients": (ctypes.c_int, [ctypes.c_void_p, f32p, ctypes.c_float]),
     }
     for name, (restype, argtypes) in sigs.items():
         fn = getattr(lib, name)
@@ -140,6 +141,13 @@ class MlpGpu:
         self._check(self._lib.sph_mlp_train_step(self._h, ctypes.c_void_p(features_ptr), ctypes.c_void_p(targets_ptr),
                                                  count, lr, _fp(loss)), "sph_mlp_train_step")
         return float(loss[0])
+
+    def apply_gradients(self, grads, lr: float = 1e-3) -> None:
+        """Adam with an externally reduced gradient (data-parallel training)."""
+        g = np.ascontiguousarray(grads, dtype=np.float32)
+        if g.shape != (PARAMS,):
+            raise ValueError(f"expected {PARAMS} gradient entries")
+        self._check(self._lib.sph_mlp_apply_gradients(self._h, _fp(g), lr), "sph_mlp_apply_gradients")
 
     def selftest_erf(self, count: int = 1 << 24) -> float:
         out = np.zeros(1, np.float32)

@@ -354,6 +354,11 @@ int sph_mlp_set_adam(sph_mlp* mlp, float beta1, float beta2, float epsilon);
 int sph_mlp_train_step(sph_mlp* mlp, const void* features, const void* targets, uint32_t count, float learning_rate,
                        float* loss);
 int sph_mlp_stream(sph_mlp* mlp, void** stream);
+/* One Adam step with a gradient supplied by the caller (host, SPH_MLP_PARAMS
+ * floats), e.g. the average of several GPUs' sph_mlp_gradients in
+ * data-parallel training. No counterpart in the reference (it has no learned
+ * fluid path); the update rule is adamStep (src/gfx/neural_math.cpp:1177-1208). */
+int sph_mlp_apply_gradients(sph_mlp* mlp, const float* grads, float learning_rate);
 /* Diagnostic: largest |erf(x) - erff(x)| of the forward pass's erf
  * (Abramowitz & Stegun 7.1.26) over `count` points on [-6, 6]. */
 int sph_mlp_selftest_erf(sph_mlp* mlp, uint32_t count, float* max_abs_error);
