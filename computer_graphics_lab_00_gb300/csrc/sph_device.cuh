@@ -10,6 +10,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/sph_c.h"
+
 namespace sph {
 
 constexpr uint32_t kCellCapacity = 32;  // fluid_sph.h:23
@@ -46,6 +48,13 @@ struct alignas(16) TankConst {
     uint32_t lattice[3];
     uint32_t active;         // 0: the tank is frozen this substep
     float emitter_world[16];
+    float radius;                      // particle radius (container_min.w)
+    uint32_t collider_count;           // shape colliders of this tank (<= SPH_MAX_COLLIDERS)
+    uint32_t field_count;              // force fields of this tank (<= SPH_MAX_FORCE_FIELDS)
+    uint32_t pad_extra;
+    const sph_collider* colliders;     // this tank's colliders in device memory
+    const sph_force_field* fields;     // this tank's force fields in device memory
+    const float4* field_accel;         // field accelerations of all particles (id order), if any tank has fields
 };
 
 struct StepCounters {

@@ -109,6 +109,12 @@ TankConst make_tank_const(const sph_params& p, float dt) {
     t.cell_mask = p.lattice[3] - 1U;
     t.active = 1;
     std::memcpy(t.emitter_world, p.emitter_world, sizeof(t.emitter_world));
+    t.radius = p.container_min[3];
+    // Colliders and force fields are attached by the engine, which owns their device copies.
+    t.collider_count = 0;
+    t.field_count = 0;
+    t.colliders = nullptr;
+    t.fields = nullptr;
     return t;
 }
 
@@ -120,9 +126,13 @@ int validate_params(const sph_params& p) {
     if (!(p.smoothing_radius > 0.0F) || !std::isfinite(p.smoothing_radius)) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
-    if (p.collider_count != 0 || p.field_count != 0) {
-        // Shape colliders and force fields are not on the device path.
-        return SPH_ERR_UNSUPPORTED;
+    if (p.collider_count > SPH_MAX_COLLIDERS || p.field_count > SPH_MAX_FORCE_FIELDS) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    for (uint32_t c = 0; c < p.collider_count; ++c) {
+        if (p.colliders[c].type > 5) {  // scene::ColliderShape: sphere .. mesh
+            return SPH_ERR_INVALID_ARGUMENT;
+        }
     }
     return SPH_OK;
 }
@@ -169,7 +179,7 @@ void Engine::release() {
             e = nullptr;
         }
     }
-    void* buffers[] = {d_tanks_,       pos_,          vel_,         prev_,        tank_of_,   stank_,
+    void* buffers[] = {d_tanks_,       d_colliders_,  d_fields_,    field_accel_, pos_,          vel_,         prev_,        tank_of_,   stank_,
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
@@ -233,7 +243,10 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
 
     uint32_t n = total_capacity_;
     int status = SPH_OK;
-    if ((status = alloc(&d_tanks_, tanks_.size())) != SPH_OK || (status = alloc(&pos_, n)) != SPH_OK ||
+    if ((status = alloc(&d_tanks_, tanks_.size())) != SPH_OK ||
+        (status = alloc(&d_colliders_, tanks_.size() * SPH_MAX_COLLIDERS)) != SPH_OK ||
+        (status = alloc(&d_fields_, tanks_.size() * SPH_MAX_FORCE_FIELDS)) != SPH_OK ||
+        (status = alloc(&pos_, n)) != SPH_OK ||
         (status = alloc(&vel_, n)) != SPH_OK || (status = alloc(&prev_, n)) != SPH_OK ||
         (status = alloc(&grid_.keys, n)) != SPH_OK || (status = alloc(&grid_.keys_a, n)) != SPH_OK ||
         (status = alloc(&grid_.vals_a, n)) != SPH_OK || (status = alloc(&grid_.keys_b, n)) != SPH_OK ||
@@ -269,8 +282,27 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
     SPH_CUDA(cudaMemsetAsync(pos_, 0, sizeof(float4) * n, stream_));
     SPH_CUDA(cudaMemsetAsync(vel_, 0, sizeof(float4) * n, stream_));
     SPH_CUDA(cudaMemsetAsync(prev_, 0, sizeof(float4) * n, stream_));
+    colliders_host_.assign(tanks_.size() * SPH_MAX_COLLIDERS, sph_collider{});
+    fields_host_.assign(tanks_.size() * SPH_MAX_FORCE_FIELDS, sph_force_field{});
+    for (uint32_t t = 0; t < tanks_.size(); ++t) {
+        attach_shapes(t);
+    }
     consts_dirty_ = true;
-    return SPH_OK;
+    return update_shape_flags();
+}
+
+void Engine::attach_shapes(uint32_t tank) {
+    const sph_params& p = params_[tank];
+    TankConst& k = tanks_[tank];
+    k.collider_count = p.collider_count;
+    k.field_count = p.field_count;
+    k.colliders = d_colliders_ + static_cast<size_t>(tank) * SPH_MAX_COLLIDERS;
+    k.fields = d_fields_ + static_cast<size_t>(tank) * SPH_MAX_FORCE_FIELDS;
+    k.field_accel = field_accel_;
+    std::copy(p.colliders, p.colliders + SPH_MAX_COLLIDERS,
+              colliders_host_.begin() + static_cast<size_t>(tank) * SPH_MAX_COLLIDERS);
+    std::copy(p.fields, p.fields + SPH_MAX_FORCE_FIELDS,
+              fields_host_.begin() + static_cast<size_t>(tank) * SPH_MAX_FORCE_FIELDS);
 }
 
 int Engine::set_params(uint32_t tank, const sph_params& params) {
@@ -292,7 +324,60 @@ int Engine::set_params(uint32_t tank, const sph_params& params) {
     fresh.active = tanks_[tank].active;
     tanks_[tank] = fresh;
     params_[tank] = params;
+    attach_shapes(tank);
     consts_dirty_ = true;
+    return update_shape_flags();
+}
+
+int Engine::update_shape_flags() {
+    bool fields = false;
+    bool colliders = false;
+    for (const TankConst& t : tanks_) {
+        fields = fields || t.field_count != 0;
+        colliders = colliders || t.collider_count != 0;
+    }
+    if (fields && field_accel_ == nullptr) {
+        int status = alloc(&field_accel_, total_capacity_);
+        if (status != SPH_OK) {
+            return status;
+        }
+        for (TankConst& t : tanks_) {
+            t.field_accel = field_accel_;
+        }
+    }
+    if (fields != has_fields_ || colliders != has_colliders_) {
+        // The substep's launch list changes: capture the graphs again.
+        if (graph_ != nullptr) {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
+        if (learned_graph_ != nullptr) {
+            cudaGraphExecDestroy(learned_graph_);
+            learned_graph_ = nullptr;
+        }
+    }
+    has_fields_ = fields;
+    has_colliders_ = colliders;
+    return SPH_OK;
+}
+
+int Engine::enqueue_fields(uint32_t* launches) {
+    if (has_fields_) {
+        SPH_CUDA(launch_fields(pos_, tank_of_, d_tanks_, total_count_, field_accel_, stream_));
+        if (launches != nullptr) {
+            *launches += 1;
+        }
+    }
+    return SPH_OK;
+}
+
+int Engine::enqueue_colliders(uint32_t* launches) {
+    if (has_colliders_) {
+        SPH_CUDA(launch_colliders(pos_, vel_, tank_of_, d_tanks_, total_count_, stream_));
+        if (launches != nullptr) {
+            *launches += 1;
+        }
+    }
     return SPH_OK;
 }
 
@@ -306,6 +391,12 @@ int Engine::refresh_constants(float dt) {
     }
     SPH_CUDA(cudaMemcpyAsync(d_tanks_, tanks_.data(), tanks_.size() * sizeof(TankConst), cudaMemcpyHostToDevice,
                              stream_));
+    if (consts_dirty_) {
+        SPH_CUDA(cudaMemcpyAsync(d_colliders_, colliders_host_.data(), colliders_host_.size() * sizeof(sph_collider),
+                                 cudaMemcpyHostToDevice, stream_));
+        SPH_CUDA(cudaMemcpyAsync(d_fields_, fields_host_.data(), fields_host_.size() * sizeof(sph_force_field),
+                                 cudaMemcpyHostToDevice, stream_));
+    }
     const_dt_ = dt;
     consts_dirty_ = false;
     return SPH_OK;
@@ -452,13 +543,16 @@ int Engine::enqueue_substep(uint32_t* launches) {
         return status;
     }
     uint32_t n = total_count_;
+    if ((status = enqueue_fields(launches)) != SPH_OK) {
+        return status;
+    }
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning_));
     SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
                                   tuning_));
     if (launches != nullptr) {
         *launches += 2;
     }
-    return SPH_OK;
+    return enqueue_colliders(launches);
 }
 
 int Engine::ensure_graph() {
@@ -785,6 +879,9 @@ int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launc
     uint32_t n = total_count_;
     NeighbourTuning masked = tuning_;
     masked.variant = 4;
+    if ((status = enqueue_fields(launches)) != SPH_OK) {
+        return status;
+    }
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
     SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.masks, sforce_,
                              sfeatures_, false, stream_));
@@ -797,7 +894,7 @@ int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launc
     if (launches != nullptr) {
         *launches += model != nullptr ? 4 : 3;
     }
-    return SPH_OK;
+    return enqueue_colliders(launches);
 }
 
 int Engine::run_learned(float dt, uint32_t substeps, const mlp::ModelView* model) {
@@ -1131,8 +1228,15 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
         SPH_CUDA(cudaEventRecord(events_[3], stream_));
         SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning_));
         SPH_CUDA(cudaEventRecord(events_[4], stream_));
+        // Force fields and colliders, when present, count as integrate.
+        if ((status = enqueue_fields(nullptr)) != SPH_OK) {
+            return status;
+        }
         SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
                                   tuning_));
+        if ((status = enqueue_colliders(nullptr)) != SPH_OK) {
+            return status;
+        }
         SPH_CUDA(cudaEventRecord(events_[5], stream_));
         SPH_CUDA(cudaEventSynchronize(events_[5]));
         for (uint32_t k = 0; k < kProfilePhases; ++k) {

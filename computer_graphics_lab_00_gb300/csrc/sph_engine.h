@@ -116,6 +116,10 @@ private:
     int ensure_learned_buffers();
     int enqueue_substep(uint32_t* launches);
     int refresh_constants(float dt);
+    void attach_shapes(uint32_t tank);  // copies tank's colliders and fields to staging, sets pointers
+    int update_shape_flags();           // has_fields_ / has_colliders_; graphs recaptured on change
+    int enqueue_fields(uint32_t* launches);
+    int enqueue_colliders(uint32_t* launches);
     int ensure_graph();
     void release();
     template <typename T> int alloc(T** ptr, size_t count);
@@ -137,6 +141,13 @@ private:
     bool consts_dirty_ = true;
 
     TankConst* d_tanks_ = nullptr;
+    sph_collider* d_colliders_ = nullptr;        // SPH_MAX_COLLIDERS per tank
+    sph_force_field* d_fields_ = nullptr;        // SPH_MAX_FORCE_FIELDS per tank
+    std::vector<sph_collider> colliders_host_;   // staging copies of the same
+    std::vector<sph_force_field> fields_host_;
+    float4* field_accel_ = nullptr;              // per particle, allocated once some tank has fields
+    bool has_fields_ = false;
+    bool has_colliders_ = false;
     float4* pos_ = nullptr;
     float4* vel_ = nullptr;
     float4* prev_ = nullptr;

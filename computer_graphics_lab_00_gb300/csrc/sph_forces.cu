@@ -20,6 +20,12 @@ namespace {
 // std::max(a, b) returns b only when a < b.
 __device__ __forceinline__ float max_like_std(float a, float b) { return a < b ? b : a; }
 
+__device__ __forceinline__ void finish_particle(const TankConst* t, const float4& self, float density, float vx,
+                                                float vy, float vz, float pressure, float fx, float fy, float fz,
+                                                uint32_t i, float4* __restrict__ pos_out,
+                                                float4* __restrict__ vel_out,
+                                                float4 learned = {0.0f, 0.0f, 0.0f, 0.0f});
+
 template <bool kCount>
 __global__ void __launch_bounds__(128) density_kernel(const float4* __restrict__ spos, float4* __restrict__ svel,
                                                       float4* __restrict__ spos2, const uint2* __restrict__ bucket,
@@ -175,46 +181,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(const float4* __restrict
         }
     }
 
-    // fluid_sph.cpp:260-285. The force-field sum starts at vec3{0} and is
-    // added even when there are no fields, which maps -0 to +0.
-    const float dt = __ldg(&t->dt);
-    float ax = __fadd_rn(__fadd_rn(__fdiv_rn(fx, density), __ldg(&t->gravity[0])), 0.0f);
-    float ay = __fadd_rn(__fadd_rn(__fdiv_rn(fy, density), __ldg(&t->gravity[1])), 0.0f);
-    float az = __fadd_rn(__fadd_rn(__fdiv_rn(fz, density), __ldg(&t->gravity[2])), 0.0f);
-    vx = __fadd_rn(vx, __fmul_rn(ax, dt));
-    vy = __fadd_rn(vy, __fmul_rn(ay, dt));
-    vz = __fadd_rn(vz, __fmul_rn(az, dt));
-    const float max_speed = __ldg(&t->max_speed);
-    float speed = __fsqrt_rn(dot3(vx, vy, vz));
-    if (speed > max_speed) {
-        float s = __fdiv_rn(max_speed, speed);
-        vx = __fmul_rn(vx, s);
-        vy = __fmul_rn(vy, s);
-        vz = __fmul_rn(vz, s);
-    }
-    float pp[3] = {__fadd_rn(self.x, __fmul_rn(vx, dt)), __fadd_rn(self.y, __fmul_rn(vy, dt)),
-                   __fadd_rn(self.z, __fmul_rn(vz, dt))};
-    float vv[3] = {vx, vy, vz};
-    const float restitution = __ldg(&t->restitution);
-#pragma unroll
-    for (int axis = 0; axis < 3; ++axis) {
-        float low = __ldg(&t->low[axis]);
-        float high = __ldg(&t->high[axis]);
-        if (pp[axis] < low) {
-            pp[axis] = low;
-            if (vv[axis] < 0.0f) {
-                vv[axis] = __fmul_rn(-vv[axis], restitution);
-            }
-        } else if (pp[axis] > high) {
-            pp[axis] = high;
-            if (vv[axis] > 0.0f) {
-                vv[axis] = __fmul_rn(-vv[axis], restitution);
-            }
-        }
-    }
-    uint32_t i = sorted_ids[p];
-    pos_out[i] = make_float4(pp[0], pp[1], pp[2], density);
-    vel_out[i] = make_float4(vv[0], vv[1], vv[2], pressure);
+    finish_particle(t, self, density, vx, vy, vz, pressure, fx, fy, fz, sorted_ids[p], pos_out, vel_out);
 }
 
 // The 27 neighbour buckets of a cell, in the reference's (dz, dy, dx) order
@@ -337,19 +304,358 @@ __device__ __forceinline__ void add_pair_force(const PairConst& k, const float4&
     fz = __fadd_rn(fz, __fmul_rn(__fdiv_rn(__fmul_rn(k.visc_mass, __fsub_rn(ov.z, vz)), other_density), lap));
 }
 
+// ---- force fields and shape colliders -------------------------------------------
+//
+// Both follow the reference operation by operation: force_field.h:31-70 and
+// collider_shapes.h:27-134 with fluid_sph.cpp:48-53 and :287-300. They sit
+// in kernels of their own, launched only when some tank has fields or
+// colliders: `fields_kernel` sums the field accelerations at the substep's
+// start positions before integrate reads them, and `colliders_kernel`
+// pushes particles out after integrate has applied the walls, which is where
+// the reference's collider loop sits. The neighbour kernels carry no trace of
+// either beyond one uniform branch.
+
+// std::clamp(v, lo, hi) and std::min / std::max.
+__device__ __forceinline__ float clamp_like_std(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }
+__device__ __forceinline__ float min_like_std(float a, float b) { return b < a ? b : a; }
+
+// std::pow(float, float) of the reference, used for the field falloff. The
+// power is evaluated in double and rounded once to float: the correctly
+// rounded powf (except where the double result falls within its own error of
+// a float rounding boundary). The host's glibc powf is not correctly rounded:
+// on about 0.1 % of arguments in (0, 1) it returns the neighbouring float, so
+// a falloff other than 1 agrees with the reference to 1 ulp in the weight;
+// a falloff of 1 or a radius of 0 (no power) is bit-exact.
+__device__ __forceinline__ float pow_float(float x, float y) {
+    return __double2float_rn(pow(static_cast<double>(x), static_cast<double>(y)));
+}
+
+// forceFieldsAcceleration (force_field.h:62-70): +0 plus every field in order.
+__device__ __forceinline__ float3 fields_acceleration(const sph_force_field* __restrict__ fields, uint32_t count,
+                                                   float x, float y, float z) {
+    float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+    for (uint32_t i = 0; i < count; ++i) {
+        const sph_force_field& f = fields[i];
+        float ox = __fsub_rn(x, f.position_radius[0]);
+        float oy = __fsub_rn(y, f.position_radius[1]);
+        float oz = __fsub_rn(z, f.position_radius[2]);
+        float distance = __fsqrt_rn(dot3(ox, oy, oz));
+        float weight = 1.0f;
+        float radius = f.position_radius[3];
+        if (radius > 0.0f) {
+            float t = clamp_like_std(__fsub_rn(1.0f, __fdiv_rn(distance, radius)), 0.0f, 1.0f);
+            weight = t <= 0.0f ? 0.0f : pow_float(t, f.falloff);
+        }
+        float ax = 0.0f, ay = 0.0f, az = 0.0f;
+        if (!(weight <= 0.0f)) {
+            float s = __fmul_rn(f.axis_strength[3], weight);
+            float kx = f.axis_strength[0], ky = f.axis_strength[1], kz = f.axis_strength[2];
+            if (f.type == 0) {
+                ax = __fmul_rn(kx, s);
+                ay = __fmul_rn(ky, s);
+                az = __fmul_rn(kz, s);
+            } else if (f.type == 1) {
+                float along = __fadd_rn(__fadd_rn(__fmul_rn(ox, kx), __fmul_rn(oy, ky)), __fmul_rn(oz, kz));
+                float rx = __fsub_rn(ox, __fmul_rn(kx, along));
+                float ry = __fsub_rn(oy, __fmul_rn(ky, along));
+                float rz = __fsub_rn(oz, __fmul_rn(kz, along));
+                float r = __fsqrt_rn(dot3(rx, ry, rz));
+                if (!(r < 1.0e-4f)) {
+                    float ux = __fdiv_rn(rx, r), uy = __fdiv_rn(ry, r), uz = __fdiv_rn(rz, r);
+                    // glm::cross(axis, u).
+                    ax = __fmul_rn(__fsub_rn(__fmul_rn(ky, uz), __fmul_rn(uy, kz)), s);
+                    ay = __fmul_rn(__fsub_rn(__fmul_rn(kz, ux), __fmul_rn(uz, kx)), s);
+                    az = __fmul_rn(__fsub_rn(__fmul_rn(kx, uy), __fmul_rn(ux, ky)), s);
+                }
+            } else if (f.type == 2) {
+                if (!(distance < 1.0e-4f)) {
+                    ax = __fmul_rn(__fdiv_rn(-ox, distance), s);
+                    ay = __fmul_rn(__fdiv_rn(-oy, distance), s);
+                    az = __fmul_rn(__fdiv_rn(-oz, distance), s);
+                }
+            }
+        }
+        tx = __fadd_rn(tx, ax);
+        ty = __fadd_rn(ty, ay);
+        tz = __fadd_rn(tz, az);
+    }
+    return make_float3(tx, ty, tz);
+}
+
+struct SurfacePoint {
+    float p[3];
+    float n[3];
+    float d;
+};
+
+// closestOnSphereLocal (collider_shapes.h:33-41).
+__device__ __forceinline__ SurfacePoint closest_on_sphere(float radius, float x, float y, float z) {
+    SurfacePoint r;
+    float d = __fsqrt_rn(dot3(x, y, z));
+    if (d > 1.0e-6f) {
+        r.n[0] = __fdiv_rn(x, d);
+        r.n[1] = __fdiv_rn(y, d);
+        r.n[2] = __fdiv_rn(z, d);
+    } else {
+        r.n[0] = 0.0f;
+        r.n[1] = 1.0f;
+        r.n[2] = 0.0f;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        r.p[a] = __fmul_rn(r.n[a], radius);
+    }
+    r.d = __fsub_rn(d, radius);
+    return r;
+}
+
+// closestOnBoxLocal (collider_shapes.h:44-66); glm::clamp = min(max(v, lo), hi).
+__device__ __forceinline__ SurfacePoint closest_on_box(const float* e, const float* p) {
+    SurfacePoint r;
+    float c[3], dl[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c[a] = min_like_std(max_like_std(p[a], -e[a]), e[a]);
+        dl[a] = __fsub_rn(p[a], c[a]);
+    }
+    float dist_sq = dot3(dl[0], dl[1], dl[2]);
+    if (dist_sq > 1.0e-10f) {
+        float dist = __fsqrt_rn(dist_sq);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            r.n[a] = __fdiv_rn(dl[a], dist);
+            r.p[a] = c[a];
+        }
+        r.d = dist;
+        return r;
+    }
+    float gap[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        gap[a] = __fsub_rn(e[a], fabsf(p[a]));
+    }
+    int axis = gap[0] < gap[1] ? (gap[0] < gap[2] ? 0 : 2) : (gap[1] < gap[2] ? 1 : 2);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        r.n[a] = 0.0f;
+        r.p[a] = p[a];
+    }
+    float sign = p[axis] >= 0.0f ? 1.0f : -1.0f;
+    r.n[axis] = sign;
+    r.p[axis] = __fmul_rn(sign, e[axis]);
+    r.d = -gap[axis];
+    return r;
+}
+
+// closestOnCylinderLocal (collider_shapes.h:85-115).
+__device__ __forceinline__ SurfacePoint closest_on_cylinder(float radius, float half_height, const float* p) {
+    SurfacePoint r;
+    float d = __fsqrt_rn(dot3(p[0], 0.0f, p[2]));
+    float dir[3];
+    if (d > 1.0e-6f) {
+        dir[0] = __fdiv_rn(p[0], d);
+        dir[1] = __fdiv_rn(0.0f, d);
+        dir[2] = __fdiv_rn(p[2], d);
+    } else {
+        dir[0] = 1.0f;
+        dir[1] = 0.0f;
+        dir[2] = 0.0f;
+    }
+    bool inside = fabsf(p[1]) <= half_height && d <= radius;
+    if (inside) {
+        float gap_y = __fsub_rn(half_height, fabsf(p[1]));
+        float gap_r = __fsub_rn(radius, d);
+        if (gap_y < gap_r) {
+            float side = p[1] >= 0.0f ? 1.0f : -1.0f;
+            r.n[0] = 0.0f;
+            r.n[1] = side;
+            r.n[2] = 0.0f;
+            r.p[0] = p[0];
+            r.p[1] = __fmul_rn(side, half_height);
+            r.p[2] = p[2];
+            r.d = -gap_y;
+        } else {
+            const float add[3] = {0.0f, p[1], 0.0f};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                r.n[a] = dir[a];
+                r.p[a] = __fadd_rn(__fmul_rn(dir[a], radius), add[a]);
+            }
+            r.d = -gap_r;
+        }
+        return r;
+    }
+    float reach = min_like_std(d, radius);
+    float c[3] = {__fmul_rn(dir[0], reach), __fmul_rn(dir[1], reach), __fmul_rn(dir[2], reach)};
+    c[1] = clamp_like_std(p[1], -half_height, half_height);
+    float dl[3] = {__fsub_rn(p[0], c[0]), __fsub_rn(p[1], c[1]), __fsub_rn(p[2], c[2])};
+    float dist = __fsqrt_rn(dot3(dl[0], dl[1], dl[2]));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        r.p[a] = c[a];
+    }
+    if (dist > 1.0e-6f) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            r.n[a] = __fdiv_rn(dl[a], dist);
+        }
+    } else {
+        r.n[0] = 0.0f;
+        r.n[1] = 1.0f;
+        r.n[2] = 0.0f;
+    }
+    r.d = dist;
+    return r;
+}
+
+// closestOnColliderLocal (collider_shapes.h:118-134).
+__device__ __forceinline__ SurfacePoint closest_on_collider(const sph_collider& c, const float* p) {
+    const float radius = c.data0[3];
+    switch (c.type) {
+    case 0:
+        return closest_on_sphere(radius, p[0], p[1], p[2]);
+    case 1:
+        return closest_on_box(c.data0, p);
+    case 2: {
+        SurfacePoint r;  // closestOnPlaneLocal (collider_shapes.h:68-74)
+        r.n[0] = 0.0f;
+        r.n[1] = 1.0f;
+        r.n[2] = 0.0f;
+        r.p[0] = p[0];
+        r.p[1] = 0.0f;
+        r.p[2] = p[2];
+        r.d = p[1];
+        return r;
+    }
+    case 3:
+        return closest_on_cylinder(radius, c.data0[1], p);
+    case 4: {
+        // closestOnCapsuleLocal (collider_shapes.h:77-82).
+        float hh = c.data0[1];
+        float seg = clamp_like_std(p[1], -hh, hh);
+        SurfacePoint r = closest_on_sphere(radius, __fsub_rn(p[0], 0.0f), __fsub_rn(p[1], seg), __fsub_rn(p[2], 0.0f));
+        r.p[0] = __fadd_rn(r.p[0], 0.0f);
+        r.p[1] = __fadd_rn(r.p[1], seg);
+        r.p[2] = __fadd_rn(r.p[2], 0.0f);
+        return r;
+    }
+    default:
+        return closest_on_sphere(0.0f, p[0], p[1], p[2]);
+    }
+}
+
+// glm mat4 * vec4(v, w) for column-major m: (c0 x + c1 y) + (c2 z + c3 w).
+__device__ __forceinline__ float mat4_row(const float* m, int r, const float* v, float w) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(m[r], v[0]), __fmul_rn(m[4 + r], v[1])),
+                     __fadd_rn(__fmul_rn(m[8 + r], v[2]), __fmul_rn(m[12 + r], w)));
+}
+
+// One-way shape colliders (fluid_sph.cpp:287-300), in order, each seeing the
+// position the previous one left; bounce is fluid_sph.cpp:48-53.
+__device__ __forceinline__ void apply_colliders(const sph_collider* __restrict__ colliders, uint32_t count,
+                                                float particle_radius, float restitution, float* pp, float* vv) {
+    for (uint32_t c = 0; c < count; ++c) {
+        const sph_collider& col = colliders[c];
+        float local[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            local[r] = mat4_row(col.inverse_world, r, pp, 1.0f);
+        }
+        SurfacePoint s = closest_on_collider(col, local);
+        if (s.d < particle_radius) {
+            // glm::normalize(mat3(world) * n) = v * (1 / sqrt(dot(v, v))).
+            float nv[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                nv[r] = __fadd_rn(__fadd_rn(__fmul_rn(col.world[r], s.n[0]), __fmul_rn(col.world[4 + r], s.n[1])),
+                                  __fmul_rn(col.world[8 + r], s.n[2]));
+            }
+            float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(nv[0], nv[1], nv[2])));
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                nv[r] = __fmul_rn(nv[r], inv);
+            }
+            float moved[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                moved[r] = __fadd_rn(mat4_row(col.world, r, s.p, 1.0f), __fmul_rn(nv[r], particle_radius));
+            }
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                pp[r] = moved[r];
+            }
+            float along = __fadd_rn(__fadd_rn(__fmul_rn(vv[0], nv[0]), __fmul_rn(vv[1], nv[1])), __fmul_rn(vv[2], nv[2]));
+            if (along < 0.0f) {
+                float k = __fmul_rn(__fadd_rn(1.0f, restitution), along);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    vv[r] = __fsub_rn(vv[r], __fmul_rn(k, nv[r]));
+                }
+            }
+        }
+    }
+}
+
+// forceFieldsAcceleration at each particle's position (id order), for the
+// tanks that have fields.
+__global__ void fields_kernel(const float4* __restrict__ pos, const uint16_t* __restrict__ tank_of,
+                              const TankConst* __restrict__ tanks, uint32_t n, float4* __restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (tank_of != nullptr ? tank_of[i] : 0);
+    uint32_t count = t->field_count;
+    if (count == 0 || t->active == 0) {
+        return;
+    }
+    float4 p = pos[i];
+    float3 a = fields_acceleration(t->fields, count, p.x, p.y, p.z);
+    out[i] = make_float4(a.x, a.y, a.z, 0.0f);
+}
+
+// The collider loop of fluid_sph.cpp:287-300 on the integrated state (id
+// order), for the tanks that have colliders.
+__global__ void colliders_kernel(float4* __restrict__ pos, float4* __restrict__ vel,
+                                 const uint16_t* __restrict__ tank_of, const TankConst* __restrict__ tanks,
+                                 uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (tank_of != nullptr ? tank_of[i] : 0);
+    uint32_t count = t->collider_count;
+    if (count == 0 || t->active == 0) {
+        return;
+    }
+    float4 p = pos[i];
+    float4 v = vel[i];
+    float pp[3] = {p.x, p.y, p.z};
+    float vv[3] = {v.x, v.y, v.z};
+    apply_colliders(t->colliders, count, t->radius, t->restitution, pp, vv);
+    pos[i] = make_float4(pp[0], pp[1], pp[2], p.w);
+    vel[i] = make_float4(vv[0], vv[1], vv[2], v.w);
+}
+
 // Semi-implicit Euler, speed clamp and walls (fluid_sph.cpp:260-285), then
 // the id-order write.
 __device__ __forceinline__ void finish_particle(const TankConst* t, const float4& self, float density, float vx,
                                                 float vy, float vz, float pressure, float fx, float fy, float fz,
                                                 uint32_t i, float4* __restrict__ pos_out,
-                                                float4* __restrict__ vel_out, float4 learned = {0.0f, 0.0f, 0.0f, 0.0f}) {
+                                                float4* __restrict__ vel_out, float4 learned) {
     // The force-field sum starts at vec3{0} and is added even when there are
     // no fields, which maps -0 to +0. A learned correction, when present, is
     // one more acceleration term; +0 leaves the plain step's bits unchanged.
     const float dt = __ldg(&t->dt);
-    float ax = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fx, density), __ldg(&t->gravity[0])), 0.0f), learned.x);
-    float ay = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fy, density), __ldg(&t->gravity[1])), 0.0f), learned.y);
-    float az = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fz, density), __ldg(&t->gravity[2])), 0.0f), learned.z);
+    // Force fields (when the tank has any) were summed at the substep's start
+    // positions by fields_kernel; otherwise the sum is the +0 of vec3{0}.
+    float4 field = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (__ldg(&t->field_count) != 0) {
+        field = __ldg(&t->field_accel[i]);
+    }
+    float ax = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fx, density), __ldg(&t->gravity[0])), field.x), learned.x);
+    float ay = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fy, density), __ldg(&t->gravity[1])), field.y), learned.y);
+    float az = __fadd_rn(__fadd_rn(__fadd_rn(__fdiv_rn(fz, density), __ldg(&t->gravity[2])), field.z), learned.z);
     vx = __fadd_rn(vx, __fmul_rn(ax, dt));
     vy = __fadd_rn(vy, __fmul_rn(ay, dt));
     vz = __fadd_rn(vz, __fmul_rn(az, dt));
@@ -1451,6 +1757,18 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
                                                                        n, tuning.order, pos, vel);
         break;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fields(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                          float4* out, cudaStream_t stream) {
+    fields_kernel<<<(n + 255) / 256, 256, 0, stream>>>(pos, tank_of, tanks, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_colliders(float4* pos, float4* vel, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                             cudaStream_t stream) {
+    colliders_kernel<<<(n + 255) / 256, 256, 0, stream>>>(pos, vel, tank_of, tanks, n);
     return cudaGetLastError();
 }
 

@@ -112,6 +112,12 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
 
 // FluidSolver::emit lattice (fluid_sph.cpp:138-154) for particles
 // [first, first + count) of one tank.
+// Force-field accelerations at the substep's start (id order) for tanks with
+// fields; shape colliders on the integrated state for tanks with colliders.
+cudaError_t launch_fields(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                          float4* out, cudaStream_t stream);
+cudaError_t launch_colliders(float4* pos, float4* vel, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                             cudaStream_t stream);
 cudaError_t launch_emit(const TankConst* tank, uint32_t first, uint32_t count, float4* pos, float4* vel, float4* prev,
                         cudaStream_t stream);
 

@@ -224,6 +224,112 @@ def reference_test_scene(count: int = 1024, cell_count: int = 1024) -> SphParams
     )
 
 
+# -- shape colliders and force fields (scene::ColliderShape, scene::ForceFieldType) ---------------
+
+SPHERE, BOX, PLANE, CYLINDER, CAPSULE, MESH = range(6)
+WIND, VORTEX, POINT = range(3)
+
+
+def pose(position, axis_angle=None) -> np.ndarray:
+    """Column-major float32 mat4 of a rotation (axis, angle in radians) then
+    a translation: the world matrix of a collider."""
+    m = np.eye(4, dtype=np.float64)
+    if axis_angle is not None:
+        axis = np.asarray(axis_angle[0], np.float64)
+        axis = axis / np.linalg.norm(axis)
+        c, s_ = math.cos(axis_angle[1]), math.sin(axis_angle[1])
+        x, y, z = axis
+        m[:3, :3] = [[c + x * x * (1 - c), x * y * (1 - c) - z * s_, x * z * (1 - c) + y * s_],
+                     [y * x * (1 - c) + z * s_, c + y * y * (1 - c), y * z * (1 - c) - x * s_],
+                     [z * x * (1 - c) - y * s_, z * y * (1 - c) + x * s_, c + z * z * (1 - c)]]
+    m[:3, 3] = position
+    return m.astype(np.float32)
+
+
+def add_collider(params: SphParams, shape: int, world: np.ndarray, half_extents=(0.0, 0.0, 0.0),
+                 radius: float = 0.0) -> None:
+    """Appends a shape collider (gfx::GpuFluidCollider layout: world and
+    inverse-world matrices, half extents, radius; y of the half extents is
+    the half height of a cylinder or capsule)."""
+    from .abi import SPH_MAX_COLLIDERS
+
+    k = params.collider_count
+    if k >= SPH_MAX_COLLIDERS:
+        raise ValueError("at most 8 colliders")
+    c = params.colliders[k]
+    w = np.asarray(world, np.float32)
+    inv = np.linalg.inv(w.astype(np.float64)).astype(np.float32)
+    for col in range(4):
+        for r in range(4):
+            c.world[col * 4 + r] = float(w[r, col])
+            c.inverse_world[col * 4 + r] = float(inv[r, col])
+    for a in range(3):
+        c.data0[a] = float(half_extents[a])
+    c.data0[3] = float(radius)
+    c.type = int(shape)
+    params.collider_count = k + 1
+
+
+def add_force_field(params: SphParams, kind: int, position, axis, strength: float, radius: float = 0.0,
+                    falloff: float = 1.0) -> None:
+    """Appends a force field (physics::ForceFieldSample in world space)."""
+    from .abi import SPH_MAX_FORCE_FIELDS
+
+    k = params.field_count
+    if k >= SPH_MAX_FORCE_FIELDS:
+        raise ValueError("at most 8 force fields")
+    f = params.fields[k]
+    for a in range(3):
+        f.position_radius[a] = float(position[a])
+        f.axis_strength[a] = float(axis[a])
+    f.position_radius[3] = float(radius)
+    f.axis_strength[3] = float(strength)
+    f.falloff = float(falloff)
+    f.type = int(kind)
+    params.field_count = k + 1
+
+
+def obstacle_course(seed: int = 0, count: int = 16384) -> Case:
+    """The 16k dam break with one collider of every shape in its path and
+    three force fields: a tilted plane ramp, a rotated box, a sphere, an
+    upright cylinder and a lying capsule; a bounded wind, an unbounded vortex
+    about y and a bounded point attractor. Falloffs are 1, where the
+    reference's powf is exact."""
+    case = dam_break_16k(seed)
+    p = case.params
+    add_collider(p, PLANE, pose((0.55, 0.05, 0.35), ((0.0, 0.0, 1.0), 0.35)))
+    add_collider(p, BOX, pose((0.55, 0.12, 0.7), ((0.3, 1.0, 0.2), 0.6)), half_extents=(0.08, 0.1, 0.06))
+    add_collider(p, SPHERE, pose((0.3, 0.1, 0.2)), radius=0.09)
+    add_collider(p, CYLINDER, pose((0.8, 0.15, 0.5)), half_extents=(0.0, 0.15, 0.0), radius=0.07)
+    add_collider(p, CAPSULE, pose((0.45, 0.08, 0.5), ((1.0, 0.0, 0.0), 1.5707964)), half_extents=(0.0, 0.12, 0.0),
+                 radius=0.05)
+    add_force_field(p, WIND, (0.5, 0.3, 0.5), (1.0, 0.0, 0.0), 3.0, radius=0.6, falloff=1.0)
+    add_force_field(p, VORTEX, (0.5, 0.0, 0.5), (0.0, 1.0, 0.0), 4.0, radius=0.0)
+    add_force_field(p, POINT, (0.7, 0.4, 0.5), (0.0, 0.0, 0.0), 5.0, radius=0.5, falloff=1.0)
+    return Case("obstacle_course_16k", p, case.count, case.dt, case.steps, seed, case.notes)
+
+
+def obstacles_small() -> SphParams:
+    """2,048 particles (16 x 16 x 8) in a 0.6 m box with one collider of each
+    shape and one field of each kind close to the block, so that every
+    collider and field acts within a few substeps. Falloffs are 1, where the
+    reference's powf is exact."""
+    p = make_params(container_min=(0.0, 0.0, 0.0), container_max=(0.6, 0.6, 0.6), lattice=(16, 16, 8),
+                    cell_count=4096)
+    # The block spans about [0.02, 0.32] x [0.02, 0.32] x [0.02, 0.16].
+    add_collider(p, SPHERE, pose((0.17, 0.17, 0.09)), radius=0.05)
+    add_collider(p, BOX, pose((0.3, 0.05, 0.1), ((0.2, 1.0, 0.4), 0.7)), half_extents=(0.05, 0.04, 0.06))
+    add_collider(p, PLANE, pose((0.3, 0.02, 0.3), ((1.0, 0.0, 1.0), 0.3)))
+    add_collider(p, CYLINDER, pose((0.05, 0.1, 0.12)), half_extents=(0.0, 0.06, 0.0), radius=0.03)
+    add_collider(p, CAPSULE, pose((0.25, 0.25, 0.05), ((0.0, 0.0, 1.0), 1.2)), half_extents=(0.0, 0.05, 0.0),
+                 radius=0.025)
+    add_collider(p, MESH, pose((0.5, 0.5, 0.5)))  # falls through to a point sphere, as in the reference
+    add_force_field(p, WIND, (0.1, 0.2, 0.1), (0.0, 0.0, 1.0), 2.0, radius=0.3, falloff=1.0)
+    add_force_field(p, VORTEX, (0.17, 0.0, 0.09), (0.0, 1.0, 0.0), 3.0, radius=0.0)
+    add_force_field(p, POINT, (0.2, 0.3, 0.1), (0.0, 0.0, 0.0), 4.0, radius=0.25, falloff=1.0)
+    return p
+
+
 @dataclass
 class TankSet:
     """Many independent tanks: per-tank constants, counts and initial states."""

@@ -61,7 +61,20 @@ physics::FluidParams toReference(const sph_params& p) {
     out.viscosity = p.viscosity;
     out.lattice = glm::uvec3{p.lattice[0], p.lattice[1], p.lattice[2]};
     out.cellCount = p.lattice[3];
-    out.colliderCount = 0;
+    out.colliderCount = std::min<uint32_t>(p.collider_count, physics::FLUID_MAX_COLLIDERS);
+    for (uint32_t c = 0; c < out.colliderCount; ++c) {
+        const sph_collider& src = p.colliders[c];
+        physics::FluidCollider& dst = out.colliders[c];
+        dst.shape = static_cast<scene::ColliderShape>(src.type);
+        dst.radius = src.data0[3];
+        dst.halfExtents = glm::vec3{src.data0[0], src.data0[1], src.data0[2]};
+        for (int col = 0; col < 4; ++col) {
+            for (int r = 0; r < 4; ++r) {
+                dst.world[col][r] = src.world[col * 4 + r];
+                dst.inverseWorld[col][r] = src.inverse_world[col * 4 + r];
+            }
+        }
+    }
     out.fieldCount = std::min<uint32_t>(p.field_count, physics::MAX_FORCE_FIELDS);
     for (uint32_t f = 0; f < out.fieldCount; ++f) {
         const sph_force_field& src = p.fields[f];

@@ -130,6 +130,169 @@ V3 forceFieldsAcceleration(const sph_params& params, V3 position) {
     return total;
 }
 
+// ---- shape colliders (collider_shapes.h:27-137, fluid_sph.cpp:48-53, :287-300)
+
+struct Surface {
+    V3 point{0.0F, 0.0F, 0.0F};
+    V3 normal{0.0F, 1.0F, 0.0F};
+    float distance = 0.0F;
+};
+
+inline float clampf(float v, float lo, float hi) { return v < lo ? lo : (hi < v ? hi : v); }  // std::clamp
+inline float minf(float a, float b) { return b < a ? b : a; }                                  // std::min
+inline float maxf(float a, float b) { return a < b ? b : a; }                                  // std::max
+
+// collider_shapes.h:33-41.
+Surface closestOnSphere(float radius, V3 p) {
+    Surface r;
+    float d = length(p);
+    r.normal = d > 1.0e-6F ? divide(p, d) : V3{0.0F, 1.0F, 0.0F};
+    r.point = scale(radius, r.normal);
+    r.distance = d - radius;
+    return r;
+}
+
+// collider_shapes.h:44-66; glm::clamp is min(max(v, lo), hi) per component.
+Surface closestOnBox(V3 extent, V3 p) {
+    Surface r;
+    V3 clamped{minf(maxf(p.x, -extent.x), extent.x), minf(maxf(p.y, -extent.y), extent.y),
+               minf(maxf(p.z, -extent.z), extent.z)};
+    V3 delta = sub(p, clamped);
+    float distanceSq = dot(delta, delta);
+    if (distanceSq > 1.0e-10F) {
+        float distance = std::sqrt(distanceSq);
+        r.normal = divide(delta, distance);
+        r.point = clamped;
+        r.distance = distance;
+        return r;
+    }
+    float gap[3] = {extent.x - std::fabs(p.x), extent.y - std::fabs(p.y), extent.z - std::fabs(p.z)};
+    int axis = gap[0] < gap[1] ? (gap[0] < gap[2] ? 0 : 2) : (gap[1] < gap[2] ? 1 : 2);
+    float pa[3] = {p.x, p.y, p.z};
+    float ea[3] = {extent.x, extent.y, extent.z};
+    float n[3] = {0.0F, 0.0F, 0.0F};
+    n[axis] = pa[axis] >= 0.0F ? 1.0F : -1.0F;
+    float q[3] = {p.x, p.y, p.z};
+    q[axis] = n[axis] * ea[axis];
+    r.point = {q[0], q[1], q[2]};
+    r.normal = {n[0], n[1], n[2]};
+    r.distance = -gap[axis];
+    return r;
+}
+
+// collider_shapes.h:68-74.
+Surface closestOnPlane(V3 p) {
+    Surface r;
+    r.normal = {0.0F, 1.0F, 0.0F};
+    r.point = {p.x, 0.0F, p.z};
+    r.distance = p.y;
+    return r;
+}
+
+// collider_shapes.h:77-82.
+Surface closestOnCapsule(float radius, float halfHeight, V3 p) {
+    V3 onSegment{0.0F, clampf(p.y, -halfHeight, halfHeight), 0.0F};
+    Surface r = closestOnSphere(radius, sub(p, onSegment));
+    r.point = add(r.point, onSegment);
+    return r;
+}
+
+// collider_shapes.h:85-115.
+Surface closestOnCylinder(float radius, float halfHeight, V3 p) {
+    Surface r;
+    V3 radial{p.x, 0.0F, p.z};
+    float d = length(radial);
+    V3 direction = d > 1.0e-6F ? divide(radial, d) : V3{1.0F, 0.0F, 0.0F};
+    bool inside = std::fabs(p.y) <= halfHeight && d <= radius;
+    if (inside) {
+        float gapY = halfHeight - std::fabs(p.y);
+        float gapR = radius - d;
+        if (gapY < gapR) {
+            float side = p.y >= 0.0F ? 1.0F : -1.0F;
+            r.normal = {0.0F, side, 0.0F};
+            r.point = {p.x, side * halfHeight, p.z};
+            r.distance = -gapY;
+        } else {
+            r.normal = direction;
+            r.point = add(scale(radius, direction), V3{0.0F, p.y, 0.0F});
+            r.distance = -gapR;
+        }
+        return r;
+    }
+    V3 closest = scale(minf(d, radius), direction);
+    closest.y = clampf(p.y, -halfHeight, halfHeight);
+    V3 delta = sub(p, closest);
+    float distance = length(delta);
+    r.point = closest;
+    r.normal = distance > 1.0e-6F ? divide(delta, distance) : V3{0.0F, 1.0F, 0.0F};
+    r.distance = distance;
+    return r;
+}
+
+// collider_shapes.h:118-134 (scene::ColliderShape: 0 sphere, 1 box, 2 plane,
+// 3 cylinder, 4 capsule; a mesh falls through to a sphere of radius 0).
+Surface closestOnColliderLocal(const sph_collider& c, V3 p) {
+    float radius = c.data0[3];
+    V3 half{c.data0[0], c.data0[1], c.data0[2]};
+    switch (c.type) {
+    case 0:
+        return closestOnSphere(radius, p);
+    case 1:
+        return closestOnBox(half, p);
+    case 2:
+        return closestOnPlane(p);
+    case 3:
+        return closestOnCylinder(radius, half.y, p);
+    case 4:
+        return closestOnCapsule(radius, half.y, p);
+    default:
+        return closestOnSphere(0.0F, p);
+    }
+}
+
+// glm mat4 * vec4(p, 1): (c0 x + c1 y) + (c2 z + c3 w), column-major.
+inline V3 transformPoint(const float* m, V3 p) {
+    float out[3];
+    for (int r = 0; r < 3; ++r) {
+        out[r] = (m[0 * 4 + r] * p.x + m[1 * 4 + r] * p.y) + (m[2 * 4 + r] * p.z + m[3 * 4 + r] * 1.0F);
+    }
+    return {out[0], out[1], out[2]};
+}
+
+// glm mat3(m) * vec3: (c0 x + c1 y) + c2 z.
+inline V3 rotateVector(const float* m, V3 v) {
+    float out[3];
+    for (int r = 0; r < 3; ++r) {
+        out[r] = (m[0 * 4 + r] * v.x + m[1 * 4 + r] * v.y) + m[2 * 4 + r] * v.z;
+    }
+    return {out[0], out[1], out[2]};
+}
+
+// glm::normalize: v * inversesqrt(dot(v, v)), inversesqrt(x) = 1 / sqrt(x).
+inline V3 normalize(V3 v) { return scale(1.0F / std::sqrt(dot(v, v)), v); }
+
+// fluid_sph.cpp:48-53.
+inline void bounce(V3& velocity, V3 normal, float restitution) {
+    float along = dot(velocity, normal);
+    if (along < 0.0F) {
+        velocity = sub(velocity, scale((1.0F + restitution) * along, normal));
+    }
+}
+
+// fluid_sph.cpp:287-300: one-way push-out from every shape collider, in order.
+void applyColliders(const sph_params& params, float radius, float restitution, V3& position, V3& velocity) {
+    for (uint32_t c = 0; c < params.collider_count && c < SPH_MAX_COLLIDERS; ++c) {
+        const sph_collider& collider = params.colliders[c];
+        V3 local = transformPoint(collider.inverse_world, position);
+        Surface surface = closestOnColliderLocal(collider, local);
+        if (surface.distance < radius) {
+            V3 normal = normalize(rotateVector(collider.world, surface.normal));
+            position = add(transformPoint(collider.world, surface.point), scale(radius, normal));
+            bounce(velocity, normal, restitution);
+        }
+    }
+}
+
 // A small persistent pool with the chunking of core::JobSystem::parallelFor
 // (job_system.cpp:80-117): ranges of `GRANULARITY` ids, any worker may take
 // any chunk. Results never depend on which worker ran a chunk.
@@ -306,7 +469,7 @@ void densityPass(const sph_params& params, const Grid& grid, float* pos, float* 
     });
 }
 
-// fluid_sph.cpp:225-305 (shape colliders excluded).
+// fluid_sph.cpp:225-305.
 void integratePass(const sph_params& params,
                    const Grid& grid,
                    const float* pos,
@@ -387,6 +550,15 @@ void integratePass(const sph_params& params,
                     }
                 }
             }
+            position = {p[0], p[1], p[2]};
+            velocity = {v[0], v[1], v[2]};
+            applyColliders(params, radius, restitution, position, velocity);
+            p[0] = position.x;
+            p[1] = position.y;
+            p[2] = position.z;
+            v[0] = velocity.x;
+            v[1] = velocity.y;
+            v[2] = velocity.z;
             float* np = nextPos + 4 * static_cast<size_t>(i);
             float* nv = nextVel + 4 * static_cast<size_t>(i);
             np[0] = p[0];

@@ -12,9 +12,10 @@
  *   src/physics/fluid_sph.cpp:128-136      fluidSubsteps
  *   src/physics/fluid_sph.cpp:138-154      FluidSolver::emit
  *   src/physics/fluid_sph.cpp:160-188      FluidGrid::build
- *   src/physics/fluid_sph.cpp:190-309      FluidSolver::substep (no colliders)
+ *   src/physics/fluid_sph.cpp:190-309      FluidSolver::substep
  *   src/physics/fluid_sph.cpp:311-321      FluidSolver::step
  *   src/physics/force_field.h:31-70        forceFieldsAcceleration
+ *   src/physics/collider_shapes.h:27-134   closestOnColliderLocal (shape colliders)
  *   src/core/job_system.cpp:80-117         parallelFor chunking (granularity 256)
  * and is pinned against the unmodified reference sources compiled here
  * (oracle/ref, output in oracle/_ref) by tests/test_oracle_vs_reference.py.

@@ -80,11 +80,27 @@ def collisions_overflow() -> dict:
             "cell_slots": compact_slots(counts, slots), "pos_5": pos5, "vel_5": vel5}
 
 
+def obstacles_small() -> dict:
+    """2,048 particles with one collider of every shape and one field of
+    every kind (workloads.obstacles_small), 1 and 40 substeps."""
+    params = W.obstacles_small()
+    pos, vel = W.jittered_block(params, 2048, seed=13)
+    ref = Reference()
+    ref.set_state(pos, vel)
+    ref.substep(params, 1.0 / 600.0)
+    pos1, vel1 = ref.state()
+    for _ in range(39):
+        ref.substep(params, 1.0 / 600.0)
+    pos40, vel40 = ref.state()
+    return {"params": params_bytes(params), "pos": pos, "vel": vel, "pos_1": pos1, "vel_1": vel1, "pos_40": pos40,
+            "vel_40": vel40}
+
+
 def main() -> None:
     if build_reference() is None:
         raise SystemExit("the reference tree is needed to regenerate the golden vectors")
     for name, make in (("scene_frames", scene_frames), ("dam_break_small", dam_break_small),
-                       ("collisions_overflow", collisions_overflow)):
+                       ("collisions_overflow", collisions_overflow), ("obstacles_small", obstacles_small)):
         data = make()
         np.savez_compressed(OUT / f"{name}.npz", **data)
         print(name, {k: v.shape for k, v in data.items()})

@@ -36,6 +36,17 @@ def test_generators_reproduce_golden_inputs():
     assert same(pos, g["pos"]) and same(vel, g["vel"])
     scene, s = load("scene_frames")
     assert bytes(scene) == bytes(W.reference_test_scene(1024))
+    obstacles, o = load("obstacles_small")
+    assert bytes(obstacles) == bytes(W.obstacles_small())
+    pos, vel = W.jittered_block(obstacles, 2048, seed=13)
+    assert same(pos, o["pos"]) and same(vel, o["vel"])
+
+
+def test_oracle_colliders_and_fields(oracle):
+    params, g = load("obstacles_small")
+    for k in (1, 40):
+        pos, vel = oracle.run_substeps(params, g["pos"], g["vel"], 1.0 / 600.0, k, threads=3)
+        assert same(pos, g[f"pos_{k}"]) and same(vel, g[f"vel_{k}"])
 
 
 def test_oracle_scene_frames(oracle):
@@ -86,3 +97,12 @@ def test_gpu_matches_golden(native):
                 done = k
                 pos, vel = solver.state()
                 assert same(pos, g[f"pos_{k}"]) and same(vel, g[f"vel_{k}"]), f"{name} after {k}"
+    params, g = load("obstacles_small")
+    with FluidSolverGpu(params, 2048) as solver:
+        solver.upload(g["pos"], g["vel"])
+        done = 0
+        for k in (1, 40):
+            solver.run(1.0 / 600.0, k - done)
+            done = k
+            pos, vel = solver.state()
+            assert same(pos, g[f"pos_{k}"]) and same(vel, g[f"vel_{k}"]), f"obstacles_small after {k}"

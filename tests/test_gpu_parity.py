@@ -239,11 +239,22 @@ def test_errors_are_status_codes(native):
         with pytest.raises(abi.SphError) as e:
             solver.substep(-1.0)
         assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
-    coll = case.params.copy()
-    coll.collider_count = 1
+    bad = case.params.copy()
+    bad.collider_count = 9
     with pytest.raises(abi.SphError) as e:
-        FluidSolverGpu(coll, 16)
-    assert e.value.status == abi.SPH_ERR_UNSUPPORTED
+        FluidSolverGpu(bad, 16)
+    assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
+    bad = case.params.copy()
+    bad.collider_count = 1
+    bad.colliders[0].type = 6
+    with pytest.raises(abi.SphError) as e:
+        FluidSolverGpu(bad, 16)
+    assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
+    bad = case.params.copy()
+    bad.field_count = 9
+    with pytest.raises(abi.SphError) as e:
+        FluidSolverGpu(bad, 16)
+    assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
 
 
 @pytest.mark.parametrize("tuning", [

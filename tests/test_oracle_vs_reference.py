@@ -76,6 +76,21 @@ def test_collisions_and_overflow_match_reference(oracle, reference):
     assert same_bits(op, rp) and same_bits(ov, rv)
 
 
+def test_colliders_and_fields_match_reference(oracle, reference):
+    """Every collider shape and force-field kind in the 16k dam break's path
+    (fluid_sph.cpp:287-300, collider_shapes.h, force_field.h), 100 substeps."""
+    case = W.obstacle_course()
+    pos, vel = case.initial_state()
+    ref = reference()
+    ref.set_state(pos, vel)
+    for _ in range(100):
+        ref.substep(case.params, case.dt, threads=4)
+    op, ov = oracle.run_substeps(case.params, pos, vel, case.dt, 100, threads=4)
+    rp, rv = ref.state()
+    assert same_bits(op, rp)
+    assert same_bits(ov, rv)
+
+
 @pytest.mark.parametrize("dt", [0.0, 1 / 1200, 1 / 600, 1 / 240, 1 / 60, 1.0])
 def test_substep_rule_matches_reference(oracle, reference, dt):
     for case in (W.dam_break_16k(), ):
