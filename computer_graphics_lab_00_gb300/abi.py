@@ -11,6 +11,8 @@ import ctypes
 import os
 from pathlib import Path
 
+import numpy as np
+
 PACKAGE_DIR = Path(__file__).resolve().parent
 NATIVE_DIR = PACKAGE_DIR / "_native"
 LIBRARY_NAME = "libsph_gb300.so"
@@ -155,6 +157,13 @@ assert ctypes.sizeof(SphForceField) == 48
 assert ctypes.sizeof(SphParams) == 1856
 
 
+# physics::SurfaceVertex / sph_surface_vertex: xyz position, packed unit normal.
+SURFACE_VERTEX = np.dtype([("position", np.float32, 3), ("normal", np.uint32)])
+assert SURFACE_VERTEX.itemsize == 16
+SPH_MC_TABLE_WIDTH = 16
+SPH_SURFACE_MAX_RESOLUTION = 640
+
+
 class SphError(RuntimeError):
     """A non-zero status from the native library."""
 
@@ -223,6 +232,14 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_grid_build": (c_int, [c_void_p]),
         "sph_grid_build_static": (c_int, [P(SphParams), c_void_p, c_u32, c_void_p, c_void_p, c_void_p, c_void_p]),
         "sph_stats_compute": (c_int, [c_void_p, P(SphStats)]),
+        "sph_surface_table": (c_int, [c_void_p]),
+        "sph_surface_field": (c_int, [c_void_p, c_u32]),
+        "sph_surface_field_download": (c_int, [c_void_p, c_void_p]),
+        "sph_surface_march": (c_int, [c_void_p, ctypes.c_float, c_u32, P(c_u32)]),
+        "sph_surface_vertices_download": (c_int, [c_void_p, c_void_p, c_u32]),
+        "sph_surface_device": (c_int, [c_void_p, P(c_void_p), P(c_void_p)]),
+        "sph_march_field": (c_int, [c_void_p, c_u32, c_void_p, c_void_p, ctypes.c_float, c_void_p, c_u32, P(c_u32),
+                                    c_int]),
         "sph_stream": (c_int, [c_void_p, P(c_void_p)]),
         "sph_device_state": (c_int, [c_void_p, P(c_void_p), P(c_void_p)]),
         "sph_run": (c_int, [c_void_p, c_f32, c_u32]),

@@ -28,7 +28,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", f"-I{INCLUDE}"]
 
 # Sources whose float arithmetic must round like the reference's CPU solver.
-EXACT_SOURCES = {"sph_grid.cu", "sph_forces.cu", "sph_engine.cu", "sph_capi.cu", "sph_static_grid.cu"}
+EXACT_SOURCES = {"sph_grid.cu", "sph_forces.cu", "sph_engine.cu", "sph_capi.cu", "sph_static_grid.cu",
+                 "sph_surface.cu"}
 
 
 def nvcc() -> str:

@@ -259,6 +259,125 @@ int sph_grid_build(sph_ctx* ctx) {
     return ctx->engine.build_grid();
 }
 
+int sph_surface_table(int8_t out[256 * 16]) {
+    if (out == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    std::memcpy(out, sph::surface::case_table(), 256 * SPH_MC_TABLE_WIDTH);
+    return SPH_OK;
+}
+
+int sph_surface_field(sph_ctx* ctx, uint32_t resolution) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.surface_field(0, resolution);
+}
+
+int sph_surface_field_download(sph_ctx* ctx, float* field) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.surface_field_download(field);
+}
+
+int sph_surface_march(sph_ctx* ctx, float iso, uint32_t capacity, uint32_t* written) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.surface_march(iso, capacity, written);
+}
+
+int sph_surface_vertices_download(sph_ctx* ctx, sph_surface_vertex* out, uint32_t count) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.surface_vertices_download(out, count);
+}
+
+int sph_surface_device(sph_ctx* ctx, const float** field, const sph_surface_vertex** vertices) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (field != nullptr) {
+        *field = ctx->engine.surface_field_device();
+    }
+    if (vertices != nullptr) {
+        *vertices = ctx->engine.surface_vertices_device();
+    }
+    return SPH_OK;
+}
+
+int sph_march_field(const float* field, uint32_t resolution, const float origin[3], const float cell[3], float iso,
+                    sph_surface_vertex* out, uint32_t capacity, uint32_t* written, int device) {
+    if (field == nullptr || origin == nullptr || cell == nullptr || written == nullptr || resolution == 0 ||
+        resolution > SPH_SURFACE_MAX_RESOLUTION || (out == nullptr && capacity > 0)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *written = 0;
+    if (capacity < 3) {
+        return SPH_OK;
+    }
+    int devices = 0;
+    if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0) {
+        cudaGetLastError();
+        return SPH_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= devices || cudaSetDevice(device) != cudaSuccess) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    const size_t samples = resolution + 1ull;
+    const size_t field_bytes = samples * samples * samples * sizeof(float);
+    const uint32_t tiles = sph::surface::march_tiles(resolution);
+    float* d_field = nullptr;
+    sph_surface_vertex* d_out = nullptr;
+    uint8_t* d_codes = nullptr;
+    uint32_t* d_tiles = nullptr;
+    cudaStream_t stream = nullptr;
+    uint32_t result[2] = {0, 0};
+    cudaError_t err = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaMalloc(&d_field, field_bytes);
+    if (err == cudaSuccess) err = cudaMalloc(&d_out, static_cast<size_t>(capacity) * sizeof(sph_surface_vertex));
+    if (err == cudaSuccess) err = cudaMalloc(&d_codes, static_cast<size_t>(resolution) * resolution * resolution);
+    if (err == cudaSuccess) err = cudaMalloc(&d_tiles, (2 * static_cast<size_t>(tiles) + 2) * sizeof(uint32_t));
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_field, field, field_bytes, cudaMemcpyHostToDevice, stream);
+    if (err == cudaSuccess) {
+        sph::surface::MarchGeom g{};
+        for (int a = 0; a < 3; ++a) {
+            g.origin[a] = origin[a];
+            g.cell[a] = cell[a];
+        }
+        g.iso = iso;
+        g.resolution = resolution;
+        sph::surface::MarchScratch scratch{d_codes, d_tiles, d_tiles + tiles, d_tiles + 2 * static_cast<size_t>(tiles) + 1};
+        err = sph::surface::launch_march(d_field, g, capacity, scratch, d_out, stream);
+        if (err == cudaSuccess) err = cudaMemcpyAsync(&result[0], scratch.offsets + tiles, sizeof(uint32_t),
+                                                      cudaMemcpyDeviceToHost, stream);
+        if (err == cudaSuccess) err = cudaMemcpyAsync(&result[1], scratch.limit, sizeof(uint32_t),
+                                                      cudaMemcpyDeviceToHost, stream);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+        if (err == cudaSuccess) {
+            *written = std::min(result[0], result[1]);
+            err = cudaMemcpy(out, d_out, static_cast<size_t>(*written) * sizeof(sph_surface_vertex),
+                             cudaMemcpyDeviceToHost);
+        }
+    }
+    if (stream != nullptr) {
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+    }
+    cudaFree(d_field);
+    cudaFree(d_out);
+    cudaFree(d_codes);
+    cudaFree(d_tiles);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        *written = 0;
+        return err == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA;
+    }
+    return SPH_OK;
+}
+
 int sph_stats_compute(sph_ctx* ctx, sph_stats* out) {
     if (ctx == nullptr || out == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;

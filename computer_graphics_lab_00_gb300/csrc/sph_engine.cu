@@ -179,7 +179,8 @@ void Engine::release() {
             e = nullptr;
         }
     }
-    void* buffers[] = {d_tanks_,       d_colliders_,  d_fields_,    field_accel_, pos_,          vel_,         prev_,        tank_of_,   stank_,
+    void* buffers[] = {surface_field_, surface_vertices_, surface_codes_, surface_tiles_,
+                       d_tanks_,       d_colliders_,  d_fields_,    field_accel_, pos_,          vel_,         prev_,        tank_of_,   stank_,
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
@@ -1246,6 +1247,136 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
         }
     }
     grid_valid_ = true;
+    return SPH_OK;
+}
+
+// ---- fluid surface ----------------------------------------------------------------
+
+int Engine::grow(void** buffer, size_t* have, size_t need) {
+    if (*buffer != nullptr && *have >= need) {
+        return SPH_OK;
+    }
+    if (*buffer != nullptr) {
+        SPH_CUDA(cudaStreamSynchronize(stream_));
+        SPH_CUDA(cudaFree(*buffer));
+        device_bytes_ -= *have;
+        *buffer = nullptr;
+        *have = 0;
+    }
+    SPH_CUDA(cudaMalloc(buffer, std::max<size_t>(need, 16)));
+    *have = std::max<size_t>(need, 16);
+    device_bytes_ += *have;
+    return SPH_OK;
+}
+
+int Engine::surface_field(uint32_t tank, uint32_t resolution) {
+    if (tank >= tanks_.size() || resolution == 0 || resolution > SPH_SURFACE_MAX_RESOLUTION) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    const uint64_t samples = resolution + 1ull;
+    int status = grow(reinterpret_cast<void**>(&surface_field_), &surface_field_bytes_,
+                      samples * samples * samples * sizeof(float));
+    if (status != SPH_OK) {
+        return status;
+    }
+    const sph_params& p = params_[tank];
+    surface::FieldGeom g{};
+    for (int a = 0; a < 3; ++a) {
+        // buildFluidField (marching_cubes.cpp:375-378): cell = (max - min) / resolution.
+        g.origin[a] = p.container_min[a];
+        g.cell[a] = (p.container_max[a] - p.container_min[a]) / static_cast<float>(resolution);
+    }
+    g.radius = p.smoothing_radius;
+    g.radius_sq = g.radius * g.radius;
+    g.mask = p.lattice[3] - 1U;
+    g.resolution = resolution;
+    surface_resolution_ = resolution;
+    surface_tank_ = tank;
+    surface_written_ = 0;
+    if (tanks_[tank].particle_count == 0 || total_count_ == 0) {
+        SPH_CUDA(cudaMemsetAsync(surface_field_, 0, samples * samples * samples * sizeof(float), stream_));
+        return SPH_OK;
+    }
+    // The grid of the current positions (the solver's own grid is from
+    // before the last integration, marching_cubes.cpp:370-371).
+    status = build_grid();
+    if (status != SPH_OK) {
+        return status;
+    }
+    SPH_CUDA(surface::launch_field(spos_, bucket_ + tanks_[tank].bucket_base, g, surface_field_, stream_));
+    return SPH_OK;
+}
+
+int Engine::surface_march(float iso, uint32_t capacity, uint32_t* written) {
+    if (written == nullptr || surface_resolution_ == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *written = 0;
+    surface_written_ = 0;
+    if (capacity < 3) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    const uint32_t r = surface_resolution_;
+    const uint32_t tiles = surface::march_tiles(r);
+    int status = grow(reinterpret_cast<void**>(&surface_vertices_), &surface_vertices_bytes_,
+                      static_cast<size_t>(capacity) * sizeof(sph_surface_vertex));
+    if (status == SPH_OK) {
+        status = grow(reinterpret_cast<void**>(&surface_codes_), &surface_codes_bytes_,
+                      static_cast<size_t>(r) * r * r);
+    }
+    if (status == SPH_OK) {
+        status = grow(reinterpret_cast<void**>(&surface_tiles_), &surface_tiles_bytes_,
+                      (2 * static_cast<size_t>(tiles) + 2) * sizeof(uint32_t));
+    }
+    if (status != SPH_OK) {
+        return status;
+    }
+    const sph_params& p = params_[surface_tank_];
+    surface::MarchGeom g{};
+    for (int a = 0; a < 3; ++a) {
+        g.origin[a] = p.container_min[a];
+        g.cell[a] = (p.container_max[a] - p.container_min[a]) / static_cast<float>(r);
+    }
+    g.iso = iso;
+    g.resolution = r;
+    surface::MarchScratch scratch{surface_codes_, surface_tiles_, surface_tiles_ + tiles,
+                                  surface_tiles_ + 2 * static_cast<size_t>(tiles) + 1};
+    SPH_CUDA(surface::launch_march(surface_field_, g, capacity, scratch, surface_vertices_, stream_));
+    uint32_t total_and_limit[2] = {0, 0};
+    SPH_CUDA(cudaMemcpyAsync(&total_and_limit[0], scratch.offsets + tiles, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                             stream_));
+    SPH_CUDA(cudaMemcpyAsync(&total_and_limit[1], scratch.limit, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    surface_written_ = std::min(total_and_limit[0], total_and_limit[1]);
+    *written = surface_written_;
+    return SPH_OK;
+}
+
+int Engine::surface_field_download(float* out) {
+    if (out == nullptr || surface_resolution_ == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    const size_t samples = surface_resolution_ + 1ull;
+    SPH_CUDA(cudaMemcpyAsync(out, surface_field_, samples * samples * samples * sizeof(float), cudaMemcpyDeviceToHost,
+                             stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+int Engine::surface_vertices_download(sph_surface_vertex* out, uint32_t count) {
+    if ((out == nullptr && count > 0) || count > surface_written_) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (count == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    SPH_CUDA(cudaMemcpyAsync(out, surface_vertices_, static_cast<size_t>(count) * sizeof(sph_surface_vertex),
+                             cudaMemcpyDeviceToHost, stream_));
+    SPH_CUDA(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }
 

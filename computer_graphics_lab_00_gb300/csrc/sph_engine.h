@@ -17,6 +17,7 @@
 #include "../../include/sph_c.h"
 #include "sph_kernels.h"
 #include "sph_mlp.cuh"
+#include "sph_surface.h"
 
 namespace sph {
 
@@ -89,6 +90,15 @@ public:
     int selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
     const NeighbourTuning& tuning() const { return tuning_; }
     uint32_t radix_bits() const { return radix_bits_; }
+    // Fluid surface of one tank (physics::buildFluidField / marchFluidField):
+    // the field rebuilds the grid from the current positions; the march cuts
+    // the last field into the engine's vertex buffer.
+    int surface_field(uint32_t tank, uint32_t resolution);
+    int surface_march(float iso, uint32_t capacity, uint32_t* written);
+    int surface_field_download(float* out);
+    int surface_vertices_download(sph_surface_vertex* out, uint32_t count);
+    const float* surface_field_device() const { return surface_field_; }
+    const sph_surface_vertex* surface_vertices_device() const { return surface_vertices_; }
     // Runs substeps without the graph, timing each phase with CUDA events on
     // the context stream: keys, sort, bounds+gather, density, integrate.
     static constexpr uint32_t kProfilePhases = 5;
@@ -180,6 +190,19 @@ private:
     mlp::ModelView learned_graph_model_{};
     uint32_t learned_launches_ = 0;
     cudaEvent_t events_[kProfilePhases + 1] = {};
+    // Surface buffers (grown on demand, byte sizes alongside).
+    int grow(void** buffer, size_t* have, size_t need);
+    float* surface_field_ = nullptr;
+    size_t surface_field_bytes_ = 0;
+    uint32_t surface_resolution_ = 0;
+    uint32_t surface_tank_ = 0;
+    sph_surface_vertex* surface_vertices_ = nullptr;
+    size_t surface_vertices_bytes_ = 0;
+    uint32_t surface_written_ = 0;
+    uint8_t* surface_codes_ = nullptr;
+    size_t surface_codes_bytes_ = 0;
+    uint32_t* surface_tiles_ = nullptr;  // tile sums, then offsets (tiles + 1), then the limit
+    size_t surface_tiles_bytes_ = 0;
     std::string last_error_;
 };
 

@@ -1,0 +1,520 @@
+// sph_surface.cu — the fluid surface on the device: the scalar field of
+// physics::buildFluidField and the marching cubes of physics::marchFluidField
+// (src/physics/marching_cubes.cpp:300-483, src/asset/vertex_pack.h:20-51).
+//
+// Every float expression follows the reference operation by operation; this
+// translation unit is compiled with --fmad=false. Vertices come out in the
+// reference's serial order (cell index, then the case's table order): a count
+// pass writes each cell's case code and its block's vertex total, a scan of
+// the block totals gives each block its first slot, and the emit pass scans
+// its block again to place every cell. A cell whose vertices would pass the
+// capacity is dropped together with every later cell, as in the reference.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/sph_c.h"
+#include "sph_device.cuh"
+#include "sph_surface.h"
+
+namespace sph {
+namespace surface {
+
+// ---- the case table -----------------------------------------------------------------
+//
+// Built from the rule the reference documents for its MC_TABLE
+// (marching_cubes.cpp:18-24): the contour on a cell face depends only on
+// that face's four corner signs, an ambiguous face (two diagonal corners
+// inside) wraps each inside corner on its own, and triangles face from the
+// inside corners towards the outside ones. Each contour loop is traced from
+// its lowest-numbered edge, first across the lower-numbered of that edge's
+// two faces, turned outward, and fanned from its first edge; loops are
+// emitted in order of their lowest edge. Corner and edge numbering are the
+// reference's (MC_CORNERS, MC_EDGES).
+
+namespace {
+
+constexpr int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+constexpr int kEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+// Cell faces as corner cycles: z = 0, z = 1, y = 0, y = 1, x = 0, x = 1.
+constexpr int kFace[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {3, 2, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}};
+
+struct Tables {
+    int8_t entry[256][SPH_MC_TABLE_WIDTH];
+    uint8_t count[256];
+};
+
+Tables generate() {
+    Tables t{};
+    // face_edge[f][k]: the edge between corners k and k+1 of face f.
+    int face_edge[6][4];
+    for (int f = 0; f < 6; ++f) {
+        for (int k = 0; k < 4; ++k) {
+            int a = kFace[f][k];
+            int b = kFace[f][(k + 1) & 3];
+            for (int e = 0; e < 12; ++e) {
+                if ((kEdge[e][0] == a && kEdge[e][1] == b) || (kEdge[e][0] == b && kEdge[e][1] == a)) {
+                    face_edge[f][k] = e;
+                }
+            }
+        }
+    }
+    // The two faces of every edge, lower face first.
+    int edge_face[12][2];
+    int seen_faces[12] = {};
+    for (int f = 0; f < 6; ++f) {
+        for (int k = 0; k < 4; ++k) {
+            int e = face_edge[f][k];
+            edge_face[e][seen_faces[e]++] = f;
+        }
+    }
+    for (int code = 0; code < 256; ++code) {
+        auto in = [code](int corner) { return ((code >> corner) & 1) != 0; };
+        uint32_t active = 0;
+        for (int e = 0; e < 12; ++e) {
+            if (in(kEdge[e][0]) != in(kEdge[e][1])) {
+                active |= 1u << e;
+            }
+        }
+        // Across face f from active edge e: walk the face's edge cycle from e
+        // towards e's inside corner to the next active edge.
+        auto across = [&](int f, int e) {
+            int k = 0;
+            while (face_edge[f][k] != e) {
+                ++k;
+            }
+            const int step = in(kFace[f][(k + 1) & 3]) ? 1 : 3;
+            do {
+                k = (k + step) & 3;
+            } while ((active >> face_edge[f][k] & 1u) == 0);
+            return face_edge[f][k];
+        };
+        uint32_t done = 0;
+        int n = 0;
+        for (int first = 0; first < 12; ++first) {
+            if ((active >> first & 1u) == 0 || (done >> first & 1u) != 0) {
+                continue;
+            }
+            int loop[12];
+            int len = 0;
+            int face = edge_face[first][0];
+            int e = first;
+            do {
+                loop[len++] = e;
+                done |= 1u << e;
+                int next = across(face, e);
+                face = edge_face[next][0] == face ? edge_face[next][1] : edge_face[next][0];
+                e = next;
+            } while (e != first);
+            // Orientation: the loop's area vector (over edge midpoints, in
+            // half units) against the summed inside-to-outside edge directions.
+            long area[3] = {0, 0, 0};
+            long outward[3] = {0, 0, 0};
+            for (int i = 0; i < len; ++i) {
+                int a = loop[i];
+                int b = loop[(i + 1) % len];
+                long ma[3], mb[3];
+                for (int d = 0; d < 3; ++d) {
+                    ma[d] = kCorner[kEdge[a][0]][d] + kCorner[kEdge[a][1]][d];
+                    mb[d] = kCorner[kEdge[b][0]][d] + kCorner[kEdge[b][1]][d];
+                }
+                area[0] += ma[1] * mb[2] - ma[2] * mb[1];
+                area[1] += ma[2] * mb[0] - ma[0] * mb[2];
+                area[2] += ma[0] * mb[1] - ma[1] * mb[0];
+                int inner = in(kEdge[a][0]) ? kEdge[a][0] : kEdge[a][1];
+                int outer = inner == kEdge[a][0] ? kEdge[a][1] : kEdge[a][0];
+                for (int d = 0; d < 3; ++d) {
+                    outward[d] += kCorner[outer][d] - kCorner[inner][d];
+                }
+            }
+            if (area[0] * outward[0] + area[1] * outward[1] + area[2] * outward[2] < 0) {
+                std::reverse(loop, loop + len);
+            }
+            for (int i = 1; i + 1 < len; ++i) {
+                t.entry[code][n++] = static_cast<int8_t>(loop[0]);
+                t.entry[code][n++] = static_cast<int8_t>(loop[i]);
+                t.entry[code][n++] = static_cast<int8_t>(loop[i + 1]);
+            }
+        }
+        t.count[code] = static_cast<uint8_t>(n);
+        for (int i = n; i < static_cast<int>(SPH_MC_TABLE_WIDTH); ++i) {
+            t.entry[code][i] = -1;
+        }
+    }
+    return t;
+}
+
+const Tables& tables() {
+    static const Tables t = generate();
+    return t;
+}
+
+__constant__ int8_t c_entry[256][SPH_MC_TABLE_WIDTH];
+__constant__ uint8_t c_count[256];
+__constant__ int8_t c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                      {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+__constant__ int8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                     {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+constexpr uint32_t kBlock = 256;
+constexpr uint32_t kPerThread = 8;
+constexpr uint32_t kTile = kBlock * kPerThread;  // cells per count/emit block
+
+// ---- field ------------------------------------------------------------------------
+
+// sampleField (marching_cubes.cpp:312-347) at every interior sample; border
+// samples are 0 (buildFluidField, :380-391).
+__global__ void __launch_bounds__(kBlock) field_kernel(const float4* __restrict__ spos,
+                                                       const uint2* __restrict__ bucket, FieldGeom g,
+                                                       float* __restrict__ field) {
+    const uint32_t samples = g.resolution + 1;
+    const uint32_t total = samples * samples * samples;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) {
+        return;
+    }
+    const uint32_t x = i % samples;
+    const uint32_t y = (i / samples) % samples;
+    const uint32_t z = i / (samples * samples);
+    if (x == 0 || y == 0 || z == 0 || x == g.resolution || y == g.resolution || z == g.resolution) {
+        field[i] = 0.0f;
+        return;
+    }
+    // origin + vec3{x, y, z} * cell.
+    const float px = __fadd_rn(g.origin[0], __fmul_rn(static_cast<float>(x), g.cell[0]));
+    const float py = __fadd_rn(g.origin[1], __fmul_rn(static_cast<float>(y), g.cell[1]));
+    const float pz = __fadd_rn(g.origin[2], __fmul_rn(static_cast<float>(z), g.cell[2]));
+    const int cx = cell_coord(px, g.radius);
+    const int cy = cell_coord(py, g.radius);
+    const int cz = cell_coord(pz, g.radius);
+    // The 27 buckets in (z, y, x) order; a bucket reached twice (two cells
+    // that hash alike) is summed once.
+    uint32_t b[27];
+    uint32_t repeat = 0;
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        const int dx = k % 3 - 1;
+        const int dy = (k / 3) % 3 - 1;
+        const int dz = k / 9 - 1;
+        b[k] = spatial_hash(static_cast<uint32_t>(cx + dx), static_cast<uint32_t>(cy + dy),
+                            static_cast<uint32_t>(cz + dz), g.mask);
+#pragma unroll
+        for (int j = 0; j < k; ++j) {
+            repeat |= (b[k] == b[j] ? 1u : 0u) << k;
+        }
+    }
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        if ((repeat >> k & 1u) != 0) {
+            continue;
+        }
+        const uint2 range = __ldg(&bucket[b[k]]);
+        const uint32_t count = min(range.y - range.x, kCellCapacity);
+        for (uint32_t s = 0; s < count; ++s) {
+            const float4 p = __ldg(&spos[range.x + s]);
+            const float ex = __fsub_rn(p.x, px);
+            const float ey = __fsub_rn(p.y, py);
+            const float ez = __fsub_rn(p.z, pz);
+            const float d2 = dot3(ex, ey, ez);
+            if (d2 >= g.radius_sq) {
+                continue;
+            }
+            const float d = __fsub_rn(1.0f, __fdiv_rn(d2, g.radius_sq));
+            sum = __fadd_rn(sum, __fmul_rn(__fmul_rn(d, d), d));
+        }
+    }
+    field[i] = sum;
+}
+
+// ---- marching cubes -----------------------------------------------------------------
+
+// fieldAt (marching_cubes.cpp:350-359): 0 outside the sample grid.
+__device__ __forceinline__ float field_at(const float* __restrict__ field, int samples, int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0 || x >= samples || y >= samples || z >= samples) {
+        return 0.0f;
+    }
+    return __ldg(&field[(static_cast<size_t>(z) * samples + y) * samples + x]);
+}
+
+__device__ __forceinline__ uint32_t cell_code(const float* __restrict__ field, const MarchGeom& g, uint32_t cell) {
+    const int r = static_cast<int>(g.resolution);
+    const int s = r + 1;
+    const int bx = static_cast<int>(cell % g.resolution);
+    const int by = static_cast<int>((cell / g.resolution) % g.resolution);
+    const int bz = static_cast<int>(cell / (g.resolution * g.resolution));
+    uint32_t code = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        float v = field_at(field, s, bx + c_corner[c][0], by + c_corner[c][1], bz + c_corner[c][2]);
+        code |= (v >= g.iso ? 1u : 0u) << c;
+    }
+    return code;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[kBlock / 32];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
+    uint32_t inclusive = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t up = __shfl_up_sync(0xFFFFFFFFu, inclusive, d);
+        if (lane >= static_cast<uint32_t>(d)) {
+            inclusive += up;
+        }
+    }
+    if (lane == 31) {
+        warp_sums[warp] = inclusive;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < kBlock / 32 ? warp_sums[lane] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t up = __shfl_up_sync(0xFFFFFFFFu, wi, d);
+            if (lane >= static_cast<uint32_t>(d)) {
+                wi += up;
+            }
+        }
+        if (lane < kBlock / 32) {
+            warp_sums[lane] = wi - w;  // exclusive prefix of this warp
+        }
+        if (lane == kBlock / 32 - 1) {
+            *total = wi;
+        }
+    }
+    __syncthreads();
+    uint32_t out = warp_sums[warp] + inclusive - v;
+    __syncthreads();
+    return out;
+}
+
+// Case code of every cell and the vertex total of every tile of kTile cells.
+__global__ void __launch_bounds__(kBlock) count_kernel(const float* __restrict__ field, MarchGeom g,
+                                                       uint8_t* __restrict__ codes, uint32_t* __restrict__ tile_sums) {
+    const uint32_t cells = g.resolution * g.resolution * g.resolution;
+    const uint32_t first = blockIdx.x * kTile + threadIdx.x * kPerThread;
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kPerThread; ++k) {
+        const uint32_t cell = first + k;
+        if (cell < cells) {
+            const uint32_t code = cell_code(field, g, cell);
+            codes[cell] = static_cast<uint8_t>(code);
+            sum += c_count[code];
+        }
+    }
+    __shared__ uint32_t total;
+    block_exclusive_scan(sum, &total);
+    if (threadIdx.x == 0) {
+        tile_sums[blockIdx.x] = total;
+    }
+}
+
+// Exclusive scan of the tile totals in one block; offsets[tiles] = the grand total.
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const uint32_t* __restrict__ tile_sums, uint32_t tiles,
+                                                         uint32_t* __restrict__ offsets) {
+    __shared__ uint32_t part[1024];
+    const uint32_t per = (tiles + blockDim.x - 1) / blockDim.x;
+    const uint32_t begin = threadIdx.x * per;
+    const uint32_t end = min(begin + per, tiles);
+    uint32_t sum = 0;
+    for (uint32_t t = begin; t < end; ++t) {
+        sum += tile_sums[t];
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    // Hillis-Steele over the 1024 partial sums.
+    for (uint32_t d = 1; d < blockDim.x; d <<= 1) {
+        uint32_t add = threadIdx.x >= d ? part[threadIdx.x - d] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += add;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (uint32_t t = begin; t < end; ++t) {
+        offsets[t] = run;
+        run += tile_sums[t];
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        offsets[tiles] = part[threadIdx.x];
+    }
+}
+
+// vertex_pack.h:20-28: lround(clamp(x, -1, 1) * 32767) in 16 bits.
+__device__ __forceinline__ uint32_t quantize_snorm16(float x) {
+    const float c = x < -1.0f ? -1.0f : (1.0f < x ? 1.0f : x);
+    const int32_t q = static_cast<int32_t>(lroundf(__fmul_rn(c, 32767.0f)));
+    return static_cast<uint32_t>(q) & 0xFFFFu;
+}
+
+// packUnitVector (vertex_pack.h:38-51): octahedral map into two snorm16.
+__device__ __forceinline__ uint32_t pack_unit_vector(float x, float y, float z) {
+    const float sum = __fadd_rn(__fadd_rn(fabsf(x), fabsf(y)), fabsf(z));
+    if (sum <= 0.0f) {
+        return 0u;
+    }
+    x = __fdiv_rn(x, sum);
+    y = __fdiv_rn(y, sum);
+    z = __fdiv_rn(z, sum);
+    float px = x;
+    float py = y;
+    if (z < 0.0f) {
+        px = __fmul_rn(__fsub_rn(1.0f, fabsf(y)), x >= 0.0f ? 1.0f : -1.0f);
+        py = __fmul_rn(__fsub_rn(1.0f, fabsf(x)), y >= 0.0f ? 1.0f : -1.0f);
+    }
+    return quantize_snorm16(px) | (quantize_snorm16(py) << 16u);
+}
+
+// Central difference at sample c divided by the cell size (marching_cubes.cpp:451-460).
+__device__ __forceinline__ float3 gradient(const float* __restrict__ field, int s, int cx, int cy, int cz,
+                                           const MarchGeom& g) {
+    const float gx = __fsub_rn(field_at(field, s, cx + 1, cy, cz), field_at(field, s, cx - 1, cy, cz));
+    const float gy = __fsub_rn(field_at(field, s, cx, cy + 1, cz), field_at(field, s, cx, cy - 1, cz));
+    const float gz = __fsub_rn(field_at(field, s, cx, cy, cz + 1), field_at(field, s, cx, cy, cz - 1));
+    return make_float3(__fdiv_rn(gx, g.cell[0]), __fdiv_rn(gy, g.cell[1]), __fdiv_rn(gz, g.cell[2]));
+}
+
+// Places every cell's vertices at its serial slot (marching_cubes.cpp:397-481).
+__global__ void __launch_bounds__(kBlock) emit_kernel(const float* __restrict__ field, MarchGeom g,
+                                                      const uint8_t* __restrict__ codes,
+                                                      const uint32_t* __restrict__ offsets, uint32_t capacity,
+                                                      uint32_t* __restrict__ limit,
+                                                      sph_surface_vertex* __restrict__ out) {
+    const uint32_t cells = g.resolution * g.resolution * g.resolution;
+    const uint32_t first = blockIdx.x * kTile + threadIdx.x * kPerThread;
+    uint8_t code[kPerThread];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kPerThread; ++k) {
+        const uint32_t cell = first + k;
+        code[k] = cell < cells ? codes[cell] : 0;
+        sum += c_count[code[k]];
+    }
+    __shared__ uint32_t total;
+    uint32_t slot = offsets[blockIdx.x] + block_exclusive_scan(sum, &total);
+    const int s = static_cast<int>(g.resolution) + 1;
+    for (uint32_t k = 0; k < kPerThread; ++k) {
+        const uint32_t n = c_count[code[k]];
+        if (n == 0) {
+            continue;
+        }
+        const uint32_t cell = first + k;
+        if (slot + n > capacity) {
+            atomicMin(limit, slot);
+            return;  // this thread's later cells lie further still
+        }
+        const int base[3] = {static_cast<int>(cell % g.resolution),
+                             static_cast<int>((cell / g.resolution) % g.resolution),
+                             static_cast<int>(cell / (g.resolution * g.resolution))};
+        for (uint32_t v = 0; v < n; ++v) {
+            const int edge = c_entry[code[k]][v];
+            const int a = c_edge[edge][0];
+            const int b = c_edge[edge][1];
+            int ca[3], cb[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                ca[d] = base[d] + c_corner[a][d];
+                cb[d] = base[d] + c_corner[b][d];
+            }
+            const float va = field_at(field, s, ca[0], ca[1], ca[2]);
+            const float vb = field_at(field, s, cb[0], cb[1], cb[2]);
+            const float diff = __fsub_rn(vb, va);
+            float t = fabsf(diff) > 1.0e-8f ? __fdiv_rn(__fsub_rn(g.iso, va), diff) : 0.5f;
+            t = t < 0.0f ? 0.0f : (1.0f < t ? 1.0f : t);
+            float p[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float pa = __fadd_rn(g.origin[d], __fmul_rn(static_cast<float>(ca[d]), g.cell[d]));
+                const float pb = __fadd_rn(g.origin[d], __fmul_rn(static_cast<float>(cb[d]), g.cell[d]));
+                p[d] = __fadd_rn(pa, __fmul_rn(__fsub_rn(pb, pa), t));
+            }
+            const float3 ga = gradient(field, s, ca[0], ca[1], ca[2], g);
+            const float3 gb = gradient(field, s, cb[0], cb[1], cb[2], g);
+            // Outward normal: minus the interpolated gradient.
+            float nx = -__fadd_rn(ga.x, __fmul_rn(__fsub_rn(gb.x, ga.x), t));
+            float ny = -__fadd_rn(ga.y, __fmul_rn(__fsub_rn(gb.y, ga.y), t));
+            float nz = -__fadd_rn(ga.z, __fmul_rn(__fsub_rn(gb.z, ga.z), t));
+            if (!(__fsqrt_rn(dot3(nx, ny, nz)) > 1.0e-12f)) {
+                nx = 0.0f;
+                ny = 1.0f;
+                nz = 0.0f;
+            }
+            // glm::normalize: v * (1 / sqrt(dot(v, v))).
+            const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(nx, ny, nz)));
+            sph_surface_vertex vert;
+            vert.position[0] = p[0];
+            vert.position[1] = p[1];
+            vert.position[2] = p[2];
+            vert.normal = pack_unit_vector(__fmul_rn(nx, inv), __fmul_rn(ny, inv), __fmul_rn(nz, inv));
+            out[slot + v] = vert;
+        }
+        slot += n;
+    }
+}
+
+std::mutex g_upload_guard;
+uint64_t g_uploaded = 0;  // bit d: device d has the tables
+
+}  // namespace
+
+const int8_t* case_table() { return &tables().entry[0][0]; }
+
+cudaError_t ensure_tables() {
+    int device = 0;
+    cudaError_t err = cudaGetDevice(&device);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    std::lock_guard<std::mutex> lock(g_upload_guard);
+    if (device < 64 && (g_uploaded >> device & 1u) != 0) {
+        return cudaSuccess;
+    }
+    const Tables& t = tables();
+    if ((err = cudaMemcpyToSymbol(c_entry, t.entry, sizeof(t.entry))) != cudaSuccess ||
+        (err = cudaMemcpyToSymbol(c_count, t.count, sizeof(t.count))) != cudaSuccess) {
+        return err;
+    }
+    if (device < 64) {
+        g_uploaded |= 1ull << device;
+    }
+    return cudaSuccess;
+}
+
+uint32_t march_tiles(uint32_t resolution) {
+    const uint64_t cells = static_cast<uint64_t>(resolution) * resolution * resolution;
+    return static_cast<uint32_t>((cells + kTile - 1) / kTile);
+}
+
+cudaError_t launch_field(const float4* spos, const uint2* bucket, const FieldGeom& g, float* field,
+                         cudaStream_t stream) {
+    const uint32_t samples = g.resolution + 1;
+    const uint32_t total = samples * samples * samples;
+    field_kernel<<<(total + kBlock - 1) / kBlock, kBlock, 0, stream>>>(spos, bucket, g, field);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_march(const float* field, const MarchGeom& g, uint32_t capacity, MarchScratch s,
+                         sph_surface_vertex* out, cudaStream_t stream) {
+    cudaError_t err = ensure_tables();
+    if (err != cudaSuccess) {
+        return err;
+    }
+    const uint32_t tiles = march_tiles(g.resolution);
+    if ((err = cudaMemsetAsync(s.limit, 0xFF, sizeof(uint32_t), stream)) != cudaSuccess) {
+        return err;
+    }
+    count_kernel<<<tiles, kBlock, 0, stream>>>(field, g, s.codes, s.tile_sums);
+    tile_scan_kernel<<<1, 1024, 0, stream>>>(s.tile_sums, tiles, s.offsets);
+    emit_kernel<<<tiles, kBlock, 0, stream>>>(field, g, s.codes, s.offsets, capacity, s.limit, out);
+    return cudaGetLastError();
+}
+
+}  // namespace surface
+}  // namespace sph

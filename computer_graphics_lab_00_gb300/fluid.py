@@ -49,6 +49,28 @@ def cell_count_uncapped(particles: int) -> int:
     return int(load().sph_cell_count_uncapped(particles))
 
 
+def surface_table() -> np.ndarray:
+    """The marching-cubes case table the device uses (256 x 16, -1 ends a case)."""
+    out = np.zeros((256, abi.SPH_MC_TABLE_WIDTH), np.int8)
+    check(load().sph_surface_table(out.ctypes.data), "sph_surface_table")
+    return out
+
+
+def march_field(field, resolution: int, origin, cell, iso: float, capacity: int, device: int = 0) -> np.ndarray:
+    """physics::marchFluidField (marching_cubes.cpp:397-481) of a host field on
+    the GPU; returns the vertices (structured array, abi.SURFACE_VERTEX)."""
+    f = np.ascontiguousarray(field, dtype=np.float32)
+    if f.size != (resolution + 1) ** 3:
+        raise ValueError("field must hold (resolution + 1)^3 samples")
+    o = np.ascontiguousarray(origin, dtype=np.float32)
+    c = np.ascontiguousarray(cell, dtype=np.float32)
+    out = np.zeros(max(capacity, 1), abi.SURFACE_VERTEX)
+    written = ctypes.c_uint32()
+    check(load().sph_march_field(f.ctypes.data, resolution, o.ctypes.data, c.ctypes.data, ctypes.c_float(iso),
+                                 out.ctypes.data, capacity, ctypes.byref(written), device), "sph_march_field")
+    return out[: written.value].copy()
+
+
 class FluidSolverGpu:
     """One fluid on one GPU; the device twin of physics::FluidSolver."""
 
@@ -176,6 +198,38 @@ class FluidSolverGpu:
 
     def build_grid(self) -> None:
         self._check(self._lib.sph_grid_build(self._ctx), "sph_grid_build")
+
+    # -- fluid surface (physics::buildFluidField / marchFluidField) ----------------
+    def surface_field(self, resolution: int) -> None:
+        """Samples the field of the current particles on the device."""
+        self._surface_resolution = resolution
+        self._check(self._lib.sph_surface_field(self._ctx, resolution), "sph_surface_field")
+
+    def field(self) -> np.ndarray:
+        """The last field, (resolution+1)^3 floats, x fastest."""
+        r = getattr(self, "_surface_resolution", 0)
+        out = np.empty((r + 1) ** 3, np.float32)
+        self._check(self._lib.sph_surface_field_download(self._ctx, out.ctypes.data), "sph_surface_field_download")
+        return out
+
+    def surface_march(self, iso: float, capacity: int) -> int:
+        """Cuts the last field on the device; returns the vertex count."""
+        written = ctypes.c_uint32()
+        self._check(self._lib.sph_surface_march(self._ctx, ctypes.c_float(iso), capacity, ctypes.byref(written)),
+                    "sph_surface_march")
+        return int(written.value)
+
+    def surface_vertices(self, count: int) -> np.ndarray:
+        out = np.zeros(count, abi.SURFACE_VERTEX)
+        self._check(self._lib.sph_surface_vertices_download(self._ctx, out.ctypes.data if count else None, count),
+                    "sph_surface_vertices_download")
+        return out
+
+    def surface(self, resolution: int, iso: float = 0.5, capacity: int = 196608) -> np.ndarray:
+        """Field and marching cubes in one call, as the reference's CPU
+        surface path does per frame (src/gfx/fluid.cpp:787-801)."""
+        self.surface_field(resolution)
+        return self.surface_vertices(self.surface_march(iso, capacity))
 
     def stats(self) -> SphStats:
         out = SphStats()

@@ -241,6 +241,58 @@ int sph_grid_build_static(const sph_params* params,
 /* Reduces statistics of the current state (FP64 on the device). */
 int sph_stats_compute(sph_ctx* ctx, sph_stats* out);
 
+/* ---- fluid surface: scalar field + marching cubes ----------------------
+ * physics::buildFluidField / physics::marchFluidField
+ * (src/physics/marching_cubes.h:39-57, marching_cubes.cpp:312-483) on the
+ * device. The field holds (resolution+1)^3 samples, x fastest; its border
+ * samples are 0. Vertices come out as triangles in the reference's serial
+ * (cell index) order. */
+
+/* Triangle-table width and the largest vertex count one cell emits
+ * (MC_TABLE_WIDTH, MC_MAX_TRIANGLES * 3 in marching_cubes.h:19-20). */
+#define SPH_MC_TABLE_WIDTH 16u
+#define SPH_MC_MAX_CELL_VERTICES 15u
+/* Largest resolution the device path accepts (samples = resolution + 1 per
+ * axis); 15 vertices for each of 640^3 cells still fit a 32-bit count. */
+#define SPH_SURFACE_MAX_RESOLUTION 640u
+
+/* physics::SurfaceVertex (marching_cubes.h:29-34): position and an
+ * octahedral-packed unit normal (asset::packUnitVector). */
+typedef struct sph_surface_vertex {
+    float position[3];
+    uint32_t normal;
+} sph_surface_vertex;
+
+/* The marching-cubes case table (256 x SPH_MC_TABLE_WIDTH edge indices, -1
+ * ends a case) the device uses; it is generated from the face-contour rule
+ * the reference documents for MC_TABLE (marching_cubes.cpp:18-24). */
+int sph_surface_table(int8_t out[256 * 16]);
+/* buildFluidField on the context's particles and constants: rebuilds the
+ * grid from the current positions (afterwards sph_grid_download returns that
+ * grid), then samples the field into a context-owned device buffer. */
+int sph_surface_field(sph_ctx* ctx, uint32_t resolution);
+/* Copies the last field to the host ((resolution+1)^3 floats). */
+int sph_surface_field_download(sph_ctx* ctx, float* field);
+/* marchFluidField on the context's last field with origin = container_min and
+ * cell = (container_max - container_min) / resolution, into a context-owned
+ * buffer of `capacity` vertices; *written is the vertex count (<= capacity;
+ * 0 if capacity < 3). */
+int sph_surface_march(sph_ctx* ctx, float iso, uint32_t capacity, uint32_t* written);
+/* Copies the first `count` vertices of the last march to the host. */
+int sph_surface_vertices_download(sph_ctx* ctx, sph_surface_vertex* out, uint32_t count);
+/* Device pointers of the context's field and vertex buffers (NULL until made). */
+int sph_surface_device(sph_ctx* ctx, const float** field, const sph_surface_vertex** vertices);
+/* marchFluidField on any host field, on `device`: host in, host out. */
+int sph_march_field(const float* field,
+                    uint32_t resolution,
+                    const float origin[3],
+                    const float cell[3],
+                    float iso,
+                    sph_surface_vertex* out,
+                    uint32_t capacity,
+                    uint32_t* written,
+                    int device);
+
 /* ---- device-resident access (for callers that keep data in HBM) ------- */
 
 /* The context's cudaStream_t, as an opaque pointer. */

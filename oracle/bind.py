@@ -57,6 +57,20 @@ def _as_state(pos: np.ndarray, vel: np.ndarray | None):
     return pos, vel
 
 
+def _march(fn, field, resolution, origin, cell, iso, capacity):
+    from computer_graphics_lab_00_gb300.abi import SURFACE_VERTEX
+
+    field = np.ascontiguousarray(field, dtype=np.float32)
+    o = np.asarray(origin, np.float32)
+    c = np.asarray(cell, np.float32)
+    out = np.zeros(max(capacity, 1), SURFACE_VERTEX)
+    written = ctypes.c_uint32()
+    rc = fn(_fp(field), resolution, _fp(o), _fp(c), ctypes.c_float(iso), out.ctypes.data, capacity,
+            ctypes.byref(written))
+    assert rc == 0
+    return out[: written.value].copy()
+
+
 class Oracle:
     """The restated CPU solver. Every call copies its inputs."""
 
@@ -82,12 +96,33 @@ class Oracle:
             lib.oracle_pair_counts.argtypes = [P(SphParams), f32p, ctypes.c_uint32, u64p, u64p, ctypes.c_uint32]
             lib.oracle_stats.argtypes = [P(SphParams), f32p, f32p, ctypes.c_uint32, P(SphStats)]
             lib.oracle_hardware_threads.restype = ctypes.c_uint32
+            lib.oracle_mc_table.argtypes = [ctypes.c_void_p]
+            lib.oracle_surface_field.argtypes = [P(SphParams), f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                 f32p]
+            lib.oracle_march_field.argtypes = [f32p, ctypes.c_uint32, f32p, f32p, ctypes.c_float, ctypes.c_void_p,
+                                               ctypes.c_uint32, P(ctypes.c_uint32)]
             Oracle._lib = lib
         self.lib = Oracle._lib
 
     @property
     def hardware_threads(self) -> int:
         return int(self.lib.oracle_hardware_threads())
+
+    def mc_table(self) -> np.ndarray:
+        out = np.zeros((256, 16), np.int8)
+        self.lib.oracle_mc_table(out.ctypes.data)
+        return out
+
+    def surface_field(self, params: SphParams, pos, resolution: int, threads: int = 1) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        samples = resolution + 1
+        field = np.zeros(samples ** 3, np.float32)
+        rc = self.lib.oracle_surface_field(ctypes.byref(params), _fp(pos), pos.shape[0], resolution, threads, _fp(field))
+        assert rc == 0
+        return field
+
+    def march_field(self, field, resolution: int, origin, cell, iso: float, capacity: int):
+        return _march(self.lib.oracle_march_field, field, resolution, origin, cell, iso, capacity)
 
     def spatial_hash(self, cx: int, cy: int, cz: int, cells: int) -> int:
         return int(self.lib.oracle_spatial_hash(cx, cy, cz, cells))
@@ -193,6 +228,11 @@ class Reference:
             lib.ref_fluid_substeps.restype = ctypes.c_uint32
             lib.ref_fluid_substeps.argtypes = [P(SphParams), ctypes.c_float]
             lib.ref_derive_params.argtypes = [P(SphFluidSettings), f32p, ctypes.c_uint32, ctypes.c_uint32, P(SphParams)]
+            lib.ref_mc_table.argtypes = [ctypes.c_void_p]
+            lib.ref_surface_field.argtypes = [P(SphParams), f32p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                              f32p]
+            lib.ref_march_field.argtypes = [f32p, ctypes.c_uint32, f32p, f32p, ctypes.c_float, ctypes.c_void_p,
+                                            ctypes.c_uint32, P(ctypes.c_uint32)]
             Reference._lib = lib
         self.lib = Reference._lib
         self.handle = ctypes.c_void_p(self.lib.ref_solver_create())
@@ -244,6 +284,21 @@ class Reference:
 
     def fluid_substeps(self, params: SphParams, dt: float) -> int:
         return int(self.lib.ref_fluid_substeps(ctypes.byref(params), ctypes.c_float(dt)))
+
+    def mc_table(self) -> np.ndarray:
+        out = np.zeros((256, 16), np.int8)
+        self.lib.ref_mc_table(out.ctypes.data)
+        return out
+
+    def surface_field(self, params: SphParams, pos, resolution: int, threads: int = 1) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        field = np.zeros((resolution + 1) ** 3, np.float32)
+        self.lib.ref_surface_field(ctypes.byref(params), _fp(pos), pos.shape[0], resolution, threads, _fp(field))
+        return field
+
+    def march_field(self, field, resolution: int, origin, cell, iso: float, capacity: int):
+        """marchFluidField without a job system: vertices in cell order."""
+        return _march(self.lib.ref_march_field, field, resolution, origin, cell, iso, capacity)
 
     def derive_params(self, settings: SphFluidSettings, world, count: int, cells: int) -> SphParams:
         w = np.asarray(world, dtype=np.float32)

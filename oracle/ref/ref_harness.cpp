@@ -27,6 +27,7 @@
 #undef private
 
 #include "core/job_system.h"
+#include "physics/marching_cubes.h"
 #include "sph_c.h"
 
 namespace scene {
@@ -193,6 +194,44 @@ int ref_grid_build(const sph_params* params,
             }
         }
     }
+    return SPH_OK;
+}
+
+void ref_mc_table(int8_t* out) {
+    for (uint32_t code = 0; code < 256; ++code) {
+        for (uint32_t i = 0; i < physics::MC_TABLE_WIDTH; ++i) {
+            out[code * physics::MC_TABLE_WIDTH + i] = physics::MC_TABLE[code][i];
+        }
+    }
+}
+
+int ref_surface_field(const sph_params* params, const float* positions, uint32_t count, uint32_t resolution,
+                      uint32_t threads, float* field) {
+    std::vector<glm::vec4> particles;
+    copyIn(particles, positions, count);
+    std::vector<float> out;
+    physics::FluidGrid grid;
+    physics::buildFluidField(particles, toReference(*params), resolution, out, grid, jobsFor(threads));
+    std::memcpy(field, out.data(), out.size() * sizeof(float));
+    return SPH_OK;
+}
+
+// Serial (no job system), so that vertices come out in cell order.
+int ref_march_field(const float* field, uint32_t resolution, const float origin[3], const float cell[3], float iso,
+                    sph_surface_vertex* out, uint32_t capacity, uint32_t* written) {
+    uint32_t samples = resolution + 1;
+    std::vector<float> values(field, field + static_cast<size_t>(samples) * samples * samples);
+    std::vector<physics::SurfaceVertex> vertices(std::max<uint32_t>(capacity, 1));
+    uint32_t n = physics::marchFluidField(values, resolution, glm::vec3{origin[0], origin[1], origin[2]},
+                                          glm::vec3{cell[0], cell[1], cell[2]}, iso, vertices.data(), capacity,
+                                          nullptr);
+    for (uint32_t i = 0; i < n; ++i) {
+        out[i].position[0] = vertices[i].position.x;
+        out[i].position[1] = vertices[i].position.y;
+        out[i].position[2] = vertices[i].position.z;
+        out[i].normal = vertices[i].normal;
+    }
+    *written = n;
     return SPH_OK;
 }
 

@@ -38,6 +38,9 @@ template <typename T> struct vec<3, T> {
     constexpr vec() : x(0), y(0), z(0) {}
     constexpr explicit vec(T s) : x(s), y(s), z(s) {}
     constexpr vec(T a, T b, T c) : x(a), y(b), z(c) {}
+    // glm's vec(X, Y, Z): each component converted on its own.
+    template <typename A, typename B, typename C>
+    constexpr vec(A a, B b, C c) : x(static_cast<T>(a)), y(static_cast<T>(b)), z(static_cast<T>(c)) {}
     template <typename U> constexpr explicit vec(const vec<3, U>& v)
         : x(static_cast<T>(v.x)), y(static_cast<T>(v.y)), z(static_cast<T>(v.z)) {}
     template <typename U> constexpr explicit vec(const vec<4, U>& v)
@@ -97,12 +100,17 @@ GLM_SHIM_BINOP(*)
 GLM_SHIM_BINOP(/)
 #undef GLM_SHIM_BINOP
 
+template <typename T> constexpr vec<2, T> operator-(T s, const vec<2, T>& a) { return vec<2, T>(s - a.x, s - a.y); }
+template <typename T> constexpr vec<2, T> operator*(const vec<2, T>& a, const vec<2, T>& b) {
+    return vec<2, T>(a.x * b.x, a.y * b.y);
+}
 template <typename T> constexpr vec<3, T> operator-(const vec<3, T>& a) { return vec<3, T>(-a.x, -a.y, -a.z); }
 template <typename T> constexpr vec<4, T> operator-(const vec<4, T>& a) { return vec<4, T>(-a.x, -a.y, -a.z, -a.w); }
 
 // ---- common ----------------------------------------------------------------
 inline vec3 floor(const vec3& v) { return vec3(std::floor(v.x), std::floor(v.y), std::floor(v.z)); }
 inline vec3 abs(const vec3& v) { return vec3(std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)); }
+inline vec2 abs(const vec2& v) { return vec2(std::fabs(v.x), std::fabs(v.y)); }
 template <typename T> constexpr T shim_min(T a, T b) { return b < a ? b : a; }
 template <typename T> constexpr T shim_max(T a, T b) { return a < b ? b : a; }
 template <typename T> constexpr vec<3, T> max(const vec<3, T>& a, const vec<3, T>& b) {

@@ -573,6 +573,196 @@ void integratePass(const sph_params& params,
     });
 }
 
+// ---- fluid surface (marching_cubes.cpp:18-24, :300-483; vertex_pack.h:38-51) ----
+
+// The triangle table, derived from the rule the reference states for its
+// MC_TABLE: a face's contour depends only on its four corner signs (an
+// ambiguous face wraps each inside corner separately), each contour loop is
+// traced from its lowest edge through the lower-numbered face first, turned
+// to face outward, and fanned from its first edge; loops come out in order of
+// their lowest edge.
+struct McTable {
+    int8_t entry[256][SPH_MC_TABLE_WIDTH];
+};
+
+const int MC_CORNER[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+const int MC_EDGE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+const int MC_FACE[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {3, 2, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}};
+
+int edgeBetween(int a, int b) {
+    for (int e = 0; e < 12; ++e) {
+        if ((MC_EDGE[e][0] == a && MC_EDGE[e][1] == b) || (MC_EDGE[e][0] == b && MC_EDGE[e][1] == a)) {
+            return e;
+        }
+    }
+    return -1;
+}
+
+McTable makeMcTable() {
+    McTable table{};
+    int faceEdge[6][4];
+    for (int f = 0; f < 6; ++f) {
+        for (int k = 0; k < 4; ++k) {
+            faceEdge[f][k] = edgeBetween(MC_FACE[f][k], MC_FACE[f][(k + 1) % 4]);
+        }
+    }
+    for (int code = 0; code < 256; ++code) {
+        auto inside = [&](int c) { return ((code >> c) & 1) != 0; };
+        bool active[12];
+        for (int e = 0; e < 12; ++e) {
+            active[e] = inside(MC_EDGE[e][0]) != inside(MC_EDGE[e][1]);
+        }
+        // Partner of edge e on face f: the next active edge walking from e
+        // towards e's inside end.
+        auto partner = [&](int f, int e) {
+            int k = 0;
+            while (faceEdge[f][k] != e) {
+                ++k;
+            }
+            int step = inside(MC_FACE[f][(k + 1) % 4]) ? 1 : 3;
+            int j = k;
+            do {
+                j = (j + step) % 4;
+            } while (!active[faceEdge[f][j]]);
+            return faceEdge[f][j];
+        };
+        auto facesOf = [&](int e, int* out) {
+            int n = 0;
+            for (int f = 0; f < 6; ++f) {
+                for (int k = 0; k < 4; ++k) {
+                    if (faceEdge[f][k] == e) {
+                        out[n++] = f;
+                    }
+                }
+            }
+        };
+        bool seen[12] = {};
+        int written = 0;
+        for (int e0 = 0; e0 < 12; ++e0) {
+            if (!active[e0] || seen[e0]) {
+                continue;
+            }
+            int loop[12];
+            int length = 0;
+            loop[length++] = e0;
+            seen[e0] = true;
+            int faces[2];
+            facesOf(e0, faces);
+            int face = std::min(faces[0], faces[1]);
+            int e = partner(face, e0);
+            while (e != e0) {
+                loop[length++] = e;
+                seen[e] = true;
+                facesOf(e, faces);
+                face = faces[0] == face ? faces[1] : faces[0];
+                e = partner(face, e);
+            }
+            // Outward: the loop's area vector (edge midpoints) against the sum
+            // of the inside-to-outside directions of its edges.
+            double area[3] = {0, 0, 0};
+            double out[3] = {0, 0, 0};
+            for (int i = 0; i < length; ++i) {
+                int a = loop[i];
+                int b = loop[(i + 1) % length];
+                double ma[3], mb[3];
+                for (int d = 0; d < 3; ++d) {
+                    ma[d] = 0.5 * (MC_CORNER[MC_EDGE[a][0]][d] + MC_CORNER[MC_EDGE[a][1]][d]);
+                    mb[d] = 0.5 * (MC_CORNER[MC_EDGE[b][0]][d] + MC_CORNER[MC_EDGE[b][1]][d]);
+                }
+                area[0] += ma[1] * mb[2] - ma[2] * mb[1];
+                area[1] += ma[2] * mb[0] - ma[0] * mb[2];
+                area[2] += ma[0] * mb[1] - ma[1] * mb[0];
+                int from = inside(MC_EDGE[a][0]) ? MC_EDGE[a][0] : MC_EDGE[a][1];
+                int to = from == MC_EDGE[a][0] ? MC_EDGE[a][1] : MC_EDGE[a][0];
+                for (int d = 0; d < 3; ++d) {
+                    out[d] += MC_CORNER[to][d] - MC_CORNER[from][d];
+                }
+            }
+            if (area[0] * out[0] + area[1] * out[1] + area[2] * out[2] < 0.0) {
+                std::reverse(loop, loop + length);
+            }
+            for (int i = 1; i + 1 < length; ++i) {
+                table.entry[code][written++] = static_cast<int8_t>(loop[0]);
+                table.entry[code][written++] = static_cast<int8_t>(loop[i]);
+                table.entry[code][written++] = static_cast<int8_t>(loop[i + 1]);
+            }
+        }
+        for (int i = written; i < static_cast<int>(SPH_MC_TABLE_WIDTH); ++i) {
+            table.entry[code][i] = -1;
+        }
+    }
+    return table;
+}
+
+const McTable& mcTable() {
+    static const McTable table = makeMcTable();
+    return table;
+}
+
+// marching_cubes.cpp:312-347 (sampleField): 27 buckets in (z, y, x) order,
+// a bucket already visited (two neighbour cells that hash alike) skipped.
+float sampleField(const float* positions, const Grid& grid, uint32_t cells, V3 point, float radius) {
+    float radiusSq = radius * radius;
+    float total = 0.0F;
+    Cell base = spatialCell(point, radius);
+    uint32_t visited[27];
+    uint32_t visitedCount = 0;
+    for (int z = -1; z <= 1; ++z) {
+        for (int y = -1; y <= 1; ++y) {
+            for (int x = -1; x <= 1; ++x) {
+                uint32_t bucket = spatialHash({base.x + x, base.y + y, base.z + z}, cells);
+                if (std::find(visited, visited + visitedCount, bucket) != visited + visitedCount) {
+                    continue;
+                }
+                visited[visitedCount++] = bucket;
+                uint32_t n = grid.bucketCount(bucket);
+                for (uint32_t k = 0; k < n; ++k) {
+                    V3 delta = sub(xyz(positions + 4 * static_cast<size_t>(grid.particleAt(bucket, k))), point);
+                    float distanceSq = dot(delta, delta);
+                    if (distanceSq >= radiusSq) {
+                        continue;
+                    }
+                    float d = 1.0F - distanceSq / radiusSq;
+                    total += d * d * d;
+                }
+            }
+        }
+    }
+    return total;
+}
+
+// marching_cubes.cpp:350-359 (fieldAt): 0 outside the sample grid.
+inline float fieldAt(const float* field, uint32_t samples, int x, int y, int z) {
+    int s = static_cast<int>(samples);
+    if (x < 0 || y < 0 || z < 0 || x >= s || y >= s || z >= s) {
+        return 0.0F;
+    }
+    return field[(static_cast<size_t>(z) * samples + static_cast<size_t>(y)) * samples + static_cast<size_t>(x)];
+}
+
+// vertex_pack.h:20-28, :38-51 (packSnorm2x16, packUnitVector).
+inline uint32_t quantizeSnorm16(float x) {
+    auto q = static_cast<int32_t>(std::lround(std::clamp(x, -1.0F, 1.0F) * 32767.0F));
+    return static_cast<uint32_t>(q) & 0xFFFFU;
+}
+
+inline float signNotZero(float v) { return v >= 0.0F ? 1.0F : -1.0F; }
+
+uint32_t packUnitVector(V3 n) {
+    float sum = std::fabs(n.x) + std::fabs(n.y) + std::fabs(n.z);
+    if (sum <= 0.0F) {
+        return quantizeSnorm16(0.0F) | (quantizeSnorm16(0.0F) << 16U);
+    }
+    n = divide(n, sum);
+    float px = n.x;
+    float py = n.y;
+    if (n.z < 0.0F) {
+        px = (1.0F - std::fabs(n.y)) * signNotZero(n.x);
+        py = (1.0F - std::fabs(n.x)) * signNotZero(n.y);
+    }
+    return quantizeSnorm16(px) | (quantizeSnorm16(py) << 16U);
+}
+
 } // namespace
 
 extern "C" {
@@ -843,6 +1033,130 @@ int oracle_stats(const sph_params* params, const float* positions, const float* 
     out->max_density = maxRho;
     out->kinetic_energy = kinetic;
     out->nonfinite = nonfinite;
+    return SPH_OK;
+}
+
+void oracle_mc_table(int8_t* out) {
+    std::memcpy(out, mcTable().entry, sizeof(McTable::entry));
+}
+
+// marching_cubes.cpp:363-395 (buildFluidField).
+int oracle_surface_field(const sph_params* params, const float* positions, uint32_t count, uint32_t resolution,
+                         uint32_t threads, float* field) {
+    if (!validParams(params) || resolution == 0 || field == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    uint32_t samples = resolution + 1;
+    size_t total = static_cast<size_t>(samples) * samples * samples;
+    std::fill(field, field + total, 0.0F);
+    if (count == 0) {
+        return SPH_OK;
+    }
+    Grid grid;
+    buildGrid(grid, *params, positions, count, threads);
+    V3 origin{params->container_min[0], params->container_min[1], params->container_min[2]};
+    V3 span = sub({params->container_max[0], params->container_max[1], params->container_max[2]}, origin);
+    V3 cell = divide(span, static_cast<float>(resolution));
+    float radius = params->smoothing_radius;
+    uint32_t cells = params->lattice[3];
+    forRange(threads, static_cast<uint32_t>(total), [&](uint32_t begin, uint32_t end) {
+        for (uint32_t i = begin; i < end; ++i) {
+            uint32_t x = i % samples;
+            uint32_t y = (i / samples) % samples;
+            uint32_t z = i / (samples * samples);
+            if (x == 0 || y == 0 || z == 0 || x == resolution || y == resolution || z == resolution) {
+                continue;
+            }
+            V3 point = add(origin, V3{static_cast<float>(x) * cell.x, static_cast<float>(y) * cell.y,
+                                      static_cast<float>(z) * cell.z});
+            field[i] = sampleField(positions, grid, cells, point, radius);
+        }
+    });
+    return SPH_OK;
+}
+
+// marching_cubes.cpp:397-481 (marchFluidField), in serial cell order.
+int oracle_march_field(const float* field, uint32_t resolution, const float origin[3], const float cell[3], float iso,
+                       sph_surface_vertex* out, uint32_t capacity, uint32_t* written) {
+    if (field == nullptr || written == nullptr || resolution == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *written = 0;
+    if (capacity < 3) {
+        return SPH_OK;
+    }
+    const McTable& table = mcTable();
+    uint32_t samples = resolution + 1;
+    V3 o{origin[0], origin[1], origin[2]};
+    V3 c{cell[0], cell[1], cell[2]};
+    uint32_t slot = 0;
+    uint32_t cells = resolution * resolution * resolution;
+    for (uint32_t i = 0; i < cells; ++i) {
+        int base[3] = {static_cast<int>(i % resolution), static_cast<int>((i / resolution) % resolution),
+                       static_cast<int>(i / (resolution * resolution))};
+        float values[8];
+        uint32_t code = 0;
+        for (int k = 0; k < 8; ++k) {
+            values[k] = fieldAt(field, samples, base[0] + MC_CORNER[k][0], base[1] + MC_CORNER[k][1],
+                                base[2] + MC_CORNER[k][2]);
+            if (values[k] >= iso) {
+                code |= 1U << k;
+            }
+        }
+        const int8_t* entry = table.entry[code];
+        if (entry[0] < 0) {
+            continue;
+        }
+        uint32_t vertices = 0;
+        while (vertices < SPH_MC_TABLE_WIDTH && entry[vertices] >= 0) {
+            ++vertices;
+        }
+        if (slot + vertices > capacity) {
+            break;  // every later cell's slot lies past this one's
+        }
+        for (uint32_t v = 0; v < vertices; ++v) {
+            int edge = entry[v];
+            int a = MC_EDGE[edge][0];
+            int b = MC_EDGE[edge][1];
+            float va = values[a];
+            float vb = values[b];
+            float t = std::fabs(vb - va) > 1.0e-8F ? (iso - va) / (vb - va) : 0.5F;
+            t = clampf(t, 0.0F, 1.0F);
+            int ca[3], cb[3];
+            for (int d = 0; d < 3; ++d) {
+                ca[d] = base[d] + MC_CORNER[a][d];
+                cb[d] = base[d] + MC_CORNER[b][d];
+            }
+            V3 pa = add(o, V3{static_cast<float>(ca[0]) * c.x, static_cast<float>(ca[1]) * c.y,
+                              static_cast<float>(ca[2]) * c.z});
+            V3 pb = add(o, V3{static_cast<float>(cb[0]) * c.x, static_cast<float>(cb[1]) * c.y,
+                              static_cast<float>(cb[2]) * c.z});
+            V3 d = sub(pb, pa);
+            V3 point = add(pa, V3{d.x * t, d.y * t, d.z * t});
+            auto gradient = [&](const int* p) {
+                V3 g{fieldAt(field, samples, p[0] + 1, p[1], p[2]) - fieldAt(field, samples, p[0] - 1, p[1], p[2]),
+                     fieldAt(field, samples, p[0], p[1] + 1, p[2]) - fieldAt(field, samples, p[0], p[1] - 1, p[2]),
+                     fieldAt(field, samples, p[0], p[1], p[2] + 1) - fieldAt(field, samples, p[0], p[1], p[2] - 1)};
+                return V3{g.x / c.x, g.y / c.y, g.z / c.z};
+            };
+            V3 ga = gradient(ca);
+            V3 gb = gradient(cb);
+            V3 dg = sub(gb, ga);
+            V3 n = add(ga, V3{dg.x * t, dg.y * t, dg.z * t});
+            n = {-n.x, -n.y, -n.z};
+            if (!(length(n) > 1.0e-12F)) {
+                n = {0.0F, 1.0F, 0.0F};
+            }
+            float inv = 1.0F / std::sqrt(dot(n, n));
+            n = {n.x * inv, n.y * inv, n.z * inv};
+            out[slot + v].position[0] = point.x;
+            out[slot + v].position[1] = point.y;
+            out[slot + v].position[2] = point.z;
+            out[slot + v].normal = packUnitVector(n);
+        }
+        slot += vertices;
+    }
+    *written = slot;
     return SPH_OK;
 }
 

@@ -16,6 +16,8 @@
  *   src/physics/fluid_sph.cpp:311-321      FluidSolver::step
  *   src/physics/force_field.h:31-70        forceFieldsAcceleration
  *   src/physics/collider_shapes.h:27-134   closestOnColliderLocal (shape colliders)
+ *   src/physics/marching_cubes.cpp:300-483 buildFluidField / marchFluidField (serial order)
+ *   src/asset/vertex_pack.h:20-51         packUnitVector
  *   src/core/job_system.cpp:80-117         parallelFor chunking (granularity 256)
  * and is pinned against the unmodified reference sources compiled here
  * (oracle/ref, output in oracle/_ref) by tests/test_oracle_vs_reference.py.
@@ -77,6 +79,12 @@ int oracle_stats(const sph_params* params, const float* positions, const float* 
 
 /* Worker threads the host offers. */
 uint32_t oracle_hardware_threads(void);
+
+void oracle_mc_table(int8_t* out);
+int oracle_surface_field(const sph_params* params, const float* positions, uint32_t count, uint32_t resolution,
+                         uint32_t threads, float* field);
+int oracle_march_field(const float* field, uint32_t resolution, const float origin[3], const float cell[3], float iso,
+                       sph_surface_vertex* out, uint32_t capacity, uint32_t* written);
 
 #ifdef __cplusplus
 }

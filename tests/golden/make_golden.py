@@ -96,11 +96,33 @@ def obstacles_small() -> dict:
             "vel_40": vel40}
 
 
+def surface_small() -> dict:
+    """The reference's marching-cubes table, and buildFluidField /
+    marchFluidField (serial) on dam_break_small after 20 substeps, resolution
+    24, iso 0.5: all vertices, and the prefix a 600-vertex capacity keeps."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(0.6, 0.6, 0.6), lattice=(16, 16, 8),
+                           cell_count=4096)
+    pos, vel = W.jittered_block(params, 2048, seed=11)
+    ref = Reference()
+    ref.set_state(pos, vel)
+    for _ in range(20):
+        ref.substep(params, 1.0 / 600.0)
+    pos20, _ = ref.state()
+    field = ref.surface_field(params, pos20, 24)
+    origin = np.array(params.container_min[:3], np.float32)
+    cell = ((np.array(params.container_max[:3], np.float32) - origin) / np.float32(24)).astype(np.float32)
+    full = ref.march_field(field, 24, origin, cell, 0.5, 200000)
+    short = ref.march_field(field, 24, origin, cell, 0.5, 600)
+    return {"params": params_bytes(params), "mc_table": ref.mc_table(), "pos": pos20, "field_24": field,
+            "vertices_24": full.view(np.uint8).reshape(-1, 16), "vertices_24_cap600": short.view(np.uint8).reshape(-1, 16)}
+
+
 def main() -> None:
     if build_reference() is None:
         raise SystemExit("the reference tree is needed to regenerate the golden vectors")
     for name, make in (("scene_frames", scene_frames), ("dam_break_small", dam_break_small),
-                       ("collisions_overflow", collisions_overflow), ("obstacles_small", obstacles_small)):
+                       ("collisions_overflow", collisions_overflow), ("obstacles_small", obstacles_small),
+                       ("surface_small", surface_small)):
         data = make()
         np.savez_compressed(OUT / f"{name}.npz", **data)
         print(name, {k: v.shape for k, v in data.items()})
