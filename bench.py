@@ -58,6 +58,8 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=None, help="steps of the end-to-end leg (default: --steps)")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--surface", action=argparse.BooleanOptionalAction, default=True,
+                   help="time the fluid surface (field + marching cubes) beside the step")
     p.add_argument("--batched-steps", type=int, default=20,
                    help="substeps of the 256-tank leg (0 skips it)")
     p.add_argument("--learned-steps", type=int, default=20,
@@ -229,6 +231,60 @@ def batched_leg(steps: int, flush, device: int, world: int = 1) -> dict:
         "rank0_tanks": len(shard.tanks), "rank0_particles": shard.particles,
     }
     shard.close()
+    return out
+
+
+def surface_leg(device: int, reps: int = 10) -> list:
+    """The fluid surface (buildFluidField + marchFluidField) per frame: the
+    reference's published CPU case (8,192 particles at 40^3 and 64^3 samples,
+    iso 0.5) and the 1M dam break at 128^3 and 256^3. GPU time is wall time of
+    the C-ABI calls (field launch, march with its count read-back) after a
+    synchronize. Its CPU baseline is the oracle port (field on all host
+    cores, march serial as the reference's vertex order needs)."""
+    import torch
+
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+    from oracle.bind import Oracle
+
+    oracle = Oracle()
+    threads = oracle.hardware_threads
+    scene = W.reference_test_scene(8192, W.cell_count_for(8192))
+    big = W.dam_break_1m()
+    cases = [("reference_scene_8192", scene, 8192, None, 40), ("reference_scene_8192", scene, 8192, None, 64),
+             ("dam_break_1m", big.params, big.count, big, 128), ("dam_break_1m", big.params, big.count, big, 256)]
+    out = []
+    for name, params, n, case, resolution in cases:
+        with FluidSolverGpu(params, n, device=device) as solver:
+            if case is None:
+                solver.emit(params, n)
+                for _ in range(60):
+                    solver.step(params, 1.0 / 60.0)
+            else:
+                solver.upload(*case.initial_state())
+                solver.run(case.dt, 2)
+            solver.synchronize()
+            solver.surface(resolution)  # warm-up (allocations, table upload)
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                solver.surface_field(resolution)
+                written = solver.surface_march(0.5, 4_000_000)
+            solver.synchronize()
+            gpu_ms = (time.perf_counter() - t0) / reps * 1e3
+            pos = solver.particles()
+        origin = np.array(params.container_min[:3], np.float32)
+        cell = ((np.array(params.container_max[:3], np.float32) - origin) / np.float32(resolution)).astype(np.float32)
+        t0 = time.perf_counter()
+        field = oracle.surface_field(params, pos, resolution, threads=threads)
+        t1 = time.perf_counter()
+        verts = oracle.march_field(field, resolution, origin, cell, 0.5, 4_000_000)
+        t2 = time.perf_counter()
+        del verts
+        out.append({"workload": name, "particles": n, "resolution": resolution, "iso": 0.5, "vertices": written,
+                    "gpu_ms_per_frame": gpu_ms,
+                    "cpu_baseline": {"kind": "port", "ms_per_frame": (t2 - t0) * 1e3, "field_ms": (t1 - t0) * 1e3,
+                                     "march_ms": (t2 - t1) * 1e3, "cores_field": threads, "cores_march": 1}})
     return out
 
 
@@ -482,6 +538,8 @@ def run_gb300(args) -> None:
         out["batched"] = batched
     if args.learned_steps > 0 and world == 1 and WEIGHTS.exists():
         out["learned"] = learned_leg(args.learned_steps, flush, local, step_ms)
+    if world == 1 and args.surface:
+        out["surface"] = surface_leg(local)
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, args.cpu_seconds)
     solver.close()
