@@ -128,6 +128,7 @@ class SphTuning(ctypes.Structure):
         ("block_size", ctypes.c_uint32),
         ("queue_depth", ctypes.c_uint32),
         ("schedule", ctypes.c_uint32),
+        ("sort", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

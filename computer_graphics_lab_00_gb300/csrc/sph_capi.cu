@@ -40,6 +40,7 @@ void to_api(const sph::TuneChoice& c, sph_tuning* out) {
     out->block_size = c.tuning.block;
     out->queue_depth = c.tuning.queue;
     out->schedule = c.schedule ? 1u : 0u;
+    out->sort = c.onesweep ? 1u : 0u;
 }
 
 int autotune(sph::Engine& engine, float dt, uint32_t substeps, sph_tuning* best, float* best_ms) {
@@ -430,6 +431,7 @@ int sph_get_tuning(const sph_ctx* ctx, sph_tuning* out) {
     out->block_size = t.block;
     out->queue_depth = t.queue;
     out->schedule = ctx->engine.schedule_on() ? 1u : 0u;
+    out->sort = ctx->engine.onesweep_on() ? 1u : 0u;
     return SPH_OK;
 }
 
@@ -441,7 +443,7 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning) {
     t.variant = tuning->neighbour_kernel;
     t.block = tuning->block_size;
     t.queue = tuning->queue_depth;
-    if (tuning->schedule > 1) {
+    if (tuning->schedule > 1 || tuning->sort > 1) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     int status = ctx->engine.set_tuning(t);
@@ -449,6 +451,10 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning) {
         return status;
     }
     status = ctx->engine.set_schedule(tuning->schedule != 0);
+    if (status != SPH_OK) {
+        return status;
+    }
+    status = ctx->engine.set_onesweep(tuning->sort != 0);
     if (status != SPH_OK) {
         return status;
     }
@@ -642,12 +648,13 @@ int sph_batch_get_tuning(const sph_batch* batch, sph_tuning* out) {
     c.tuning = batch->engine.tuning();
     c.radix_bits = batch->engine.radix_bits();
     c.schedule = batch->engine.schedule_on();
+    c.onesweep = batch->engine.onesweep_on();
     to_api(c, out);
     return SPH_OK;
 }
 
 int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
-    if (batch == nullptr || tuning == nullptr || tuning->schedule > 1) {
+    if (batch == nullptr || tuning == nullptr || tuning->schedule > 1 || tuning->sort > 1) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     sph::NeighbourTuning t = batch->engine.tuning();
@@ -657,6 +664,9 @@ int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
     int status = batch->engine.set_tuning(t);
     if (status == SPH_OK) {
         status = batch->engine.set_schedule(tuning->schedule != 0);
+    }
+    if (status == SPH_OK) {
+        status = batch->engine.set_onesweep(tuning->sort != 0);
     }
     if (status == SPH_OK) {
         status = batch->engine.set_radix_bits(tuning->radix_bits);

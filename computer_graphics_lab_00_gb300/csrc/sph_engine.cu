@@ -179,7 +179,7 @@ void Engine::release() {
             e = nullptr;
         }
     }
-    void* buffers[] = {surface_field_, surface_vertices_, surface_codes_, surface_tiles_,
+    void* buffers[] = {surface_field_, surface_vertices_, surface_codes_, surface_tiles_, sweep_,
                        d_tanks_,       d_colliders_,  d_fields_,    field_accel_, pos_,          vel_,         prev_,        tank_of_,   stank_,
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
@@ -253,6 +253,7 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         (status = alloc(&grid_.vals_a, n)) != SPH_OK || (status = alloc(&grid_.keys_b, n)) != SPH_OK ||
         (status = alloc(&grid_.vals_b, n)) != SPH_OK ||
         (status = alloc(&grid_.hist, static_cast<size_t>(radix_tiles(n)) * kRadixMaxBins)) != SPH_OK ||
+        (status = alloc(&sweep_, onesweep_scratch_words(n, kSweepMaxPasses))) != SPH_OK ||
         (status = alloc(&bucket_, total_buckets_)) != SPH_OK || (status = alloc(&spos_, n)) != SPH_OK ||
         (status = alloc(&spos2_, n)) != SPH_OK || (status = alloc(&svel_, n)) != SPH_OK ||
         (status = alloc(&counters_, 1)) != SPH_OK ||
@@ -508,8 +509,14 @@ int Engine::emit(uint32_t tank, uint32_t count) {
 int Engine::enqueue_grid(uint32_t* launches) {
     uint32_t n = total_count_;
     SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
-    SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
-    SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, launches));
+    if (onesweep_) {
+        const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
+        SPH_CUDA(launch_keys_onesweep(pos_, tank_of_, d_tanks_, n, grid_.keys, passes, sweep_, stream_));
+        SPH_CUDA(launch_onesweep_sort(grid_, n, passes, sweep_, stream_, launches));
+    } else {
+        SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
+        SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, launches));
+    }
     int status = enqueue_bounds(launches);
     if (status != SPH_OK) {
         return status;
@@ -760,6 +767,7 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
     const NeighbourTuning original = tuning_;
     const uint32_t original_bits = radix_bits_;
     const bool original_schedule = use_schedule_;
+    const bool original_onesweep = onesweep_;
     auto measure = [&](const TuneChoice& c, float* ms) -> int {
         int st = set_tuning(c.tuning);
         if (st == SPH_OK) {
@@ -767,6 +775,9 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
         }
         if (st == SPH_OK) {
             st = set_radix_bits(c.radix_bits);
+        }
+        if (st == SPH_OK) {
+            st = set_onesweep(c.onesweep);
         }
         if (st == SPH_OK) {
             st = snapshot(false);
@@ -801,6 +812,7 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
                 c.tuning.queue = 32;
                 c.schedule = schedule;
                 c.radix_bits = original_bits;
+                c.onesweep = original_onesweep;
                 stage1.push_back(c);
             }
         }
@@ -818,12 +830,16 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
             tried->push_back(c);
         }
     }
-    for (uint32_t bits : {5u, 6u, 7u, 8u}) {
-        if (status != SPH_OK || bits == winner.radix_bits) {
+    // Stage 2: the grid sort (one-sweep, or three kernels per pass at 5-8 bits).
+    const TuneChoice stage1_winner = winner;
+    for (uint32_t bits : {0u, 5u, 6u, 7u, 8u}) {
+        TuneChoice c = stage1_winner;
+        c.onesweep = bits == 0;
+        c.radix_bits = bits == 0 ? stage1_winner.radix_bits : bits;
+        if (status != SPH_OK || (c.onesweep == stage1_winner.onesweep &&
+                                 (c.onesweep || c.radix_bits == stage1_winner.radix_bits))) {
             continue;
         }
-        TuneChoice c = winner;
-        c.radix_bits = bits;
         status = measure(c, &c.ms);
         if (status == SPH_OK && c.ms < winner.ms) {
             winner = c;
@@ -844,11 +860,15 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
         if (status == SPH_OK) {
             status = set_radix_bits(winner.radix_bits);
         }
+        if (status == SPH_OK) {
+            status = set_onesweep(winner.onesweep);
+        }
         *best = winner;
     } else {
         set_tuning(original);
         set_schedule(original_schedule);
         set_radix_bits(original_bits);
+        set_onesweep(original_onesweep);
     }
     cudaEventDestroy(start);
     cudaEventDestroy(stop);
@@ -1168,6 +1188,22 @@ int Engine::set_tuning(const NeighbourTuning& tuning) {
     return SPH_OK;
 }
 
+int Engine::set_onesweep(bool on) {
+    onesweep_ = on;
+    if (graph_ != nullptr) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    if (learned_graph_ != nullptr) {
+        cudaGraphExecDestroy(learned_graph_);
+        learned_graph_ = nullptr;
+    }
+    grid_.sorted_keys = nullptr;
+    grid_.sorted_ids = nullptr;
+    grid_valid_ = false;
+    return SPH_OK;
+}
+
 int Engine::set_schedule(bool on) {
     use_schedule_ = on;
     if (graph_ != nullptr) {
@@ -1218,9 +1254,18 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
     for (uint32_t s = 0; s < substeps; ++s) {
         SPH_CUDA(cudaEventRecord(events_[0], stream_));
         SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
-        SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
+        const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
+        if (onesweep_) {
+            SPH_CUDA(launch_keys_onesweep(pos_, tank_of_, d_tanks_, n, grid_.keys, passes, sweep_, stream_));
+        } else {
+            SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
+        }
         SPH_CUDA(cudaEventRecord(events_[1], stream_));
-        SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, nullptr));
+        if (onesweep_) {
+            SPH_CUDA(launch_onesweep_sort(grid_, n, passes, sweep_, stream_, nullptr));
+        } else {
+            SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, nullptr));
+        }
         SPH_CUDA(cudaEventRecord(events_[2], stream_));
         status = enqueue_bounds(nullptr);
         if (status != SPH_OK) {

@@ -33,6 +33,7 @@ struct TuneChoice {
     NeighbourTuning tuning{};
     uint32_t radix_bits = 6;
     bool schedule = false;
+    bool onesweep = true;
     float ms = 0.0F;
 };
 
@@ -87,6 +88,10 @@ public:
     int set_tuning(const NeighbourTuning& tuning);
     int set_schedule(bool on);
     bool schedule_on() const { return use_schedule_; }
+    // Grid sort: one kernel per 8-bit digit pass, or three kernels per
+    // radix_bits-wide pass.
+    int set_onesweep(bool on);
+    bool onesweep_on() const { return onesweep_; }
     int selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
     const NeighbourTuning& tuning() const { return tuning_; }
     uint32_t radix_bits() const { return radix_bits_; }
@@ -147,6 +152,8 @@ private:
     NeighbourTuning tuning_{};
     Schedule schedule_{};
     bool use_schedule_ = false;
+    bool onesweep_ = true;
+    unsigned long long* sweep_ = nullptr;  // per-pass tile digit counts and histograms of the one-kernel passes
     float const_dt_ = -1.0f;
     bool consts_dirty_ = true;
 

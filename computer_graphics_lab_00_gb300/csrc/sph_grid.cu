@@ -275,7 +275,246 @@ __global__ void __launch_bounds__(256) schedule_scatter_kernel(uint32_t n, Sched
     }
 }
 
+// ---- one kernel per digit pass -----------------------------------------------------
+//
+// Each pass knows, before it starts, how many keys of every digit each tile
+// holds (tile_counts, tiles x bins): the key kernel counts the first pass's
+// tiles, and every pass counts the next pass's tiles while it scatters. A
+// tile's offset for digit d is then the digit's base (exclusive scan of the
+// pass histogram) plus the sum of d's counts over the earlier tiles, which
+// each block adds up on its own: no block waits on another.
+
+struct SweepLayout {
+    uint32_t* tile_counts;  // passes x tiles x bins
+    uint32_t* hist;         // passes x bins
+};
+
+__host__ __device__ inline SweepLayout sweep_layout(unsigned long long* base, uint32_t tiles, uint32_t passes) {
+    SweepLayout l;
+    l.tile_counts = reinterpret_cast<uint32_t*>(base);
+    l.hist = l.tile_counts + static_cast<size_t>(passes) * tiles * kSweepBins;
+    return l;
+}
+
+// keys_kernel for one tile of kSweepTile particles (1024 threads, four
+// particles each, their loads issued together), plus the first pass's tile
+// counts and every pass's digit histogram.
+constexpr uint32_t kKeysThreads = 1024;
+constexpr uint32_t kKeysItems = kSweepTile / kKeysThreads;
+
+__global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* __restrict__ pos,
+                                                                 const uint16_t* __restrict__ tank_of,
+                                                                 const TankConst* __restrict__ tanks, uint32_t n,
+                                                                 uint32_t* __restrict__ keys, uint32_t passes,
+                                                                 uint32_t* __restrict__ tile_counts,
+                                                                 uint32_t* __restrict__ hist) {
+    __shared__ uint32_t counts[kSweepMaxPasses][kSweepBins];
+    for (uint32_t k = threadIdx.x; k < kSweepMaxPasses * kSweepBins; k += blockDim.x) {
+        (&counts[0][0])[k] = 0;
+    }
+    const uint32_t first = blockIdx.x * kSweepTile;
+    float4 p[kKeysItems];
+    const TankConst* t[kKeysItems];
+#pragma unroll
+    for (uint32_t r = 0; r < kKeysItems; ++r) {
+        const uint32_t i = first + r * kKeysThreads + threadIdx.x;
+        p[r] = i < n ? pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        t[r] = tanks + (tank_of != nullptr && i < n ? tank_of[i] : 0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t r = 0; r < kKeysItems; ++r) {
+        const uint32_t i = first + r * kKeysThreads + threadIdx.x;
+        if (i < n) {
+            const float h = __ldg(&t[r]->h);
+            uint32_t cx = static_cast<uint32_t>(cell_coord(p[r].x, h));
+            uint32_t cy = static_cast<uint32_t>(cell_coord(p[r].y, h));
+            uint32_t cz = static_cast<uint32_t>(cell_coord(p[r].z, h));
+            uint32_t key = __ldg(&t[r]->bucket_base) + spatial_hash(cx, cy, cz, __ldg(&t[r]->cell_mask));
+            keys[i] = key;
+            for (uint32_t pass = 0; pass < passes; ++pass) {
+                atomicAdd(&counts[pass][(key >> (pass * kSweepBits)) & (kSweepBins - 1)], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d < kSweepBins; d += blockDim.x) {
+        tile_counts[static_cast<size_t>(blockIdx.x) * kSweepBins + d] = counts[0][d];
+    }
+    for (uint32_t k = threadIdx.x; k < passes * kSweepBins; k += blockDim.x) {
+        uint32_t c = (&counts[0][0])[k];
+        if (c != 0) {
+            atomicAdd(&hist[k], c);
+        }
+    }
+}
+
+// One stable digit pass over tile blockIdx.x.
+__global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
+    const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out,
+    uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift, const uint32_t* __restrict__ hist,
+    const uint32_t* __restrict__ tile_counts, uint32_t* __restrict__ next_counts, uint32_t next_shift) {
+    static_assert(kSweepThreads == kSweepBins, "one thread per digit");
+    constexpr uint32_t kWarps = kSweepThreads / 32;
+    __shared__ uint32_t warp_counts[kWarps][kSweepBins];
+    __shared__ uint32_t digit_offset[kSweepBins];
+    __shared__ uint32_t scan_warp[kWarps];
+    for (uint32_t k = threadIdx.x; k < kWarps * kSweepBins; k += blockDim.x) {
+        (&warp_counts[0][0])[k] = 0;
+    }
+    const uint32_t tile = blockIdx.x;
+    const uint32_t d = threadIdx.x;
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    // Every digit's keys in all earlier tiles: the block reads the earlier
+    // tiles' count rows four at a time (a row is 64 uint4, thread k reads
+    // column k % 64 of row j + k / 64), eight rows' loads in flight per thread,
+    // then the four partial sums of each digit meet in shared memory.
+    __shared__ uint4 partial[4][kSweepBins / 4];
+    {
+        const uint32_t column = threadIdx.x & 63u;
+        const uint32_t lane_row = threadIdx.x >> 6;
+        const uint4* rows = reinterpret_cast<const uint4*>(tile_counts);
+        uint4 acc = make_uint4(0, 0, 0, 0);
+#pragma unroll 8
+        for (uint32_t j = lane_row; j < tile; j += 4) {
+            uint4 c = __ldg(&rows[static_cast<size_t>(j) * (kSweepBins / 4) + column]);
+            acc.x += c.x;
+            acc.y += c.y;
+            acc.z += c.z;
+            acc.w += c.w;
+        }
+        partial[lane_row][column] = acc;
+    }
+    // Digit base: exclusive scan of the pass histogram.
+    const uint32_t h = __ldg(&hist[d]);
+    uint32_t inc = h;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) {
+            inc += u;
+        }
+    }
+    if (lane == 31) {
+        scan_warp[warp] = inc;
+    }
+    __syncthreads();
+    const uint32_t below = lanemask_lt();
+    const uint32_t base = tile * kSweepTile + warp * (kSweepItems * 32);
+    uint32_t key[kSweepItems];
+    uint32_t val[kSweepItems];
+    uint32_t rank[kSweepItems];
+#pragma unroll
+    for (uint32_t r = 0; r < kSweepItems; ++r) {
+        uint32_t idx = base + r * 32 + lane;
+        bool valid = idx < n;
+        key[r] = valid ? keys_in[idx] : 0;
+        val[r] = valid ? (vals_in != nullptr ? vals_in[idx] : idx) : 0;
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < kSweepItems; ++r) {
+        bool valid = base + r * 32 + lane < n;
+        uint32_t digit = valid ? (key[r] >> shift) & (kSweepBins - 1) : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        uint32_t prior = valid ? warp_counts[warp][digit] : 0;
+        rank[r] = valid ? prior + static_cast<uint32_t>(__popc(peers & below)) : 0xFFFFFFFFu;
+        __syncwarp();
+        if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) {
+            warp_counts[warp][digit] = prior + static_cast<uint32_t>(__popc(peers));
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    uint32_t running = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kWarps; ++w) {
+        uint32_t c = warp_counts[w][d];
+        warp_counts[w][d] = running;
+        running += c;
+    }
+    uint32_t warp_base = 0;
+    for (uint32_t w = 0; w < warp; ++w) {
+        warp_base += scan_warp[w];
+    }
+    const uint32_t* flat = reinterpret_cast<const uint32_t*>(&partial[0][0]);
+    const uint32_t before = flat[d] + flat[kSweepBins + d] + flat[2 * kSweepBins + d] + flat[3 * kSweepBins + d];
+    digit_offset[d] = warp_base + inc - h + before;
+    __syncthreads();
+#pragma unroll
+    for (uint32_t r = 0; r < kSweepItems; ++r) {
+        if (rank[r] != 0xFFFFFFFFu) {
+            uint32_t digit = (key[r] >> shift) & (kSweepBins - 1);
+            uint32_t dst = digit_offset[digit] + warp_counts[warp][digit] + rank[r];
+            keys_out[dst] = key[r];
+            vals_out[dst] = val[r];
+            if (next_counts != nullptr) {
+                atomicAdd(&next_counts[static_cast<size_t>(dst / kSweepTile) * kSweepBins +
+                                       ((key[r] >> next_shift) & (kSweepBins - 1))],
+                          1u);
+            }
+        }
+    }
+}
+
 }  // namespace
+
+size_t onesweep_scratch_words(uint32_t n, uint32_t passes) {
+    const size_t tiles = sweep_tiles(n == 0 ? 1 : n);
+    const size_t words32 = static_cast<size_t>(passes) * tiles * kSweepBins + static_cast<size_t>(passes) * kSweepBins;
+    return (words32 + 1) / 2;
+}
+
+cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    cudaError_t err = cudaMemsetAsync(sweep, 0, onesweep_scratch_words(n, passes) * sizeof(unsigned long long), stream);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    const uint32_t tiles = sweep_tiles(n);
+    SweepLayout l = sweep_layout(sweep, tiles, passes);
+    keys_hist_kernel<<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes, l.tile_counts, l.hist);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_onesweep_sort(GridScratch& s, uint32_t n, uint32_t passes, unsigned long long* sweep,
+                                 cudaStream_t stream, uint32_t* launches) {
+    if (n == 0) {
+        s.sorted_keys = s.keys_a;
+        s.sorted_ids = s.vals_a;
+        return cudaSuccess;
+    }
+    const uint32_t tiles = sweep_tiles(n);
+    SweepLayout l = sweep_layout(sweep, tiles, passes);
+    const uint32_t* kin = s.keys;
+    const uint32_t* vin = nullptr;
+    uint32_t* kout = s.keys_a;
+    uint32_t* vout = s.vals_a;
+    for (uint32_t p = 0; p < passes; ++p) {
+        uint32_t* next = p + 1 < passes ? l.tile_counts + static_cast<size_t>(p + 1) * tiles * kSweepBins : nullptr;
+        sweep_scatter_kernel<<<tiles, kSweepThreads, 0, stream>>>(
+            kin, vin, kout, vout, n, p * kSweepBits, l.hist + static_cast<size_t>(p) * kSweepBins,
+            l.tile_counts + static_cast<size_t>(p) * tiles * kSweepBins, next, (p + 1) * kSweepBits);
+        if (launches != nullptr) {
+            *launches += 1;
+        }
+        kin = kout;
+        vin = vout;
+        if (kout == s.keys_a) {
+            kout = s.keys_b;
+            vout = s.vals_b;
+        } else {
+            kout = s.keys_a;
+            vout = s.vals_a;
+        }
+    }
+    s.sorted_keys = kin;
+    s.sorted_ids = vin;
+    return cudaGetLastError();
+}
 
 RadixPlan plan_radix(uint32_t key_bits, uint32_t digit_bits) {
     RadixPlan plan;

@@ -55,6 +55,29 @@ cudaError_t launch_keys(const float4* pos, const uint16_t* tank_of, const TankCo
 cudaError_t launch_radix_sort(GridScratch& scratch, uint32_t n, const RadixPlan& plan, cudaStream_t stream,
                               uint32_t* launches);
 
+// One kernel per 8-bit digit pass. Every pass knows each tile's digit counts
+// before it runs (the key kernel counts the first pass's tiles, each pass
+// counts the next pass's while it scatters), so a block finds its offsets by
+// adding up the counts of the earlier tiles: no block waits on another.
+// Scratch: onesweep_scratch_words(n, passes) 64-bit words at `sweep`, zeroed
+// by launch_keys_onesweep before every sort.
+constexpr uint32_t kSweepBits = 8;
+constexpr uint32_t kSweepBins = 1u << kSweepBits;
+constexpr uint32_t kSweepMaxPasses = 4;
+constexpr uint32_t kSweepThreads = 256;                      // threads of a pass block (one per digit)
+constexpr uint32_t kSweepItems = 16;                         // keys per thread in a tile
+constexpr uint32_t kSweepTile = kSweepThreads * kSweepItems;  // 4096 keys per tile
+inline uint32_t sweep_tiles(uint32_t n) { return (n + kSweepTile - 1) / kSweepTile; }
+inline uint32_t onesweep_passes(uint32_t key_bits) { return key_bits == 0 ? 1 : (key_bits + kSweepBits - 1) / kSweepBits; }
+size_t onesweep_scratch_words(uint32_t n, uint32_t passes);
+// Keys (as launch_keys) plus the first pass's tile counts and every pass's
+// digit histogram; zeroes the scratch first.
+cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream);
+// The digit passes over keys made by launch_keys_onesweep.
+cudaError_t launch_onesweep_sort(GridScratch& scratch, uint32_t n, uint32_t passes, unsigned long long* sweep,
+                                 cudaStream_t stream, uint32_t* launches);
+
 // Processing order of the neighbour passes. When tile_of is null the passes
 // run in sorted (bucket) order; otherwise bounds_gather bins every particle
 // into a Morton-ordered tile of 4 x 4 x 4 cells (tile_bits bits per axis,

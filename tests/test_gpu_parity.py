@@ -258,19 +258,22 @@ def test_errors_are_status_codes(native):
 
 
 @pytest.mark.parametrize("tuning", [
-    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=7, schedule=0),
-    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=7, schedule=1),
-    dict(neighbour_kernel=1, block_size=64, queue_depth=8, radix_bits=8, schedule=1),
-    dict(neighbour_kernel=1, block_size=128, queue_depth=16, radix_bits=7, schedule=0),
-    dict(neighbour_kernel=1, block_size=256, queue_depth=24, radix_bits=5, schedule=1),
-    dict(neighbour_kernel=1, block_size=128, queue_depth=32, radix_bits=3, schedule=0),
-    dict(neighbour_kernel=2, block_size=64, queue_depth=16, radix_bits=7, schedule=1),
-    dict(neighbour_kernel=2, block_size=128, queue_depth=16, radix_bits=8, schedule=0),
-    dict(neighbour_kernel=3, block_size=128, queue_depth=16, radix_bits=7, schedule=1),
-    dict(neighbour_kernel=3, block_size=256, queue_depth=16, radix_bits=6, schedule=0),
-    dict(neighbour_kernel=4, block_size=64, queue_depth=16, radix_bits=7, schedule=0),
-    dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=1),
-    dict(neighbour_kernel=4, block_size=256, queue_depth=16, radix_bits=8, schedule=1),
+    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=7, schedule=0, sort=0),
+    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=7, schedule=1, sort=0),
+    dict(neighbour_kernel=1, block_size=64, queue_depth=8, radix_bits=8, schedule=1, sort=0),
+    dict(neighbour_kernel=1, block_size=128, queue_depth=16, radix_bits=7, schedule=0, sort=0),
+    dict(neighbour_kernel=1, block_size=256, queue_depth=24, radix_bits=5, schedule=1, sort=0),
+    dict(neighbour_kernel=1, block_size=128, queue_depth=32, radix_bits=3, schedule=0, sort=0),
+    dict(neighbour_kernel=2, block_size=64, queue_depth=16, radix_bits=7, schedule=1, sort=0),
+    dict(neighbour_kernel=2, block_size=128, queue_depth=16, radix_bits=8, schedule=0, sort=0),
+    dict(neighbour_kernel=3, block_size=128, queue_depth=16, radix_bits=7, schedule=1, sort=0),
+    dict(neighbour_kernel=3, block_size=256, queue_depth=16, radix_bits=6, schedule=0, sort=0),
+    dict(neighbour_kernel=4, block_size=64, queue_depth=16, radix_bits=7, schedule=0, sort=0),
+    dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=1, sort=0),
+    dict(neighbour_kernel=4, block_size=256, queue_depth=16, radix_bits=8, schedule=1, sort=0),
+    dict(neighbour_kernel=4, block_size=256, queue_depth=32, radix_bits=6, schedule=0, sort=1),
+    dict(neighbour_kernel=3, block_size=128, queue_depth=16, radix_bits=6, schedule=1, sort=1),
+    dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=6, schedule=0, sort=1),
 ])
 def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     """Every launch shape the autotuner may pick gives the oracle's bits."""
@@ -287,11 +290,25 @@ def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     assert_bit_exact(gv, ov, f"velocities {tuning}")
 
 
+@pytest.mark.parametrize("sort,bits", [(1, 6), (0, 5), (0, 8)])
+def test_grid_sorts_agree_at_one_million(native, oracle, sort, bits):
+    """The one-sweep sort (3 look-back passes over 21-bit keys at 1M) and the
+    three-kernel passes give the oracle's grid bit for bit."""
+    case = W.dam_break_1m()
+    pos, vel = case.initial_state()
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.set_tuning(sort=sort, radix_bits=bits)
+        solver.upload(pos, vel)
+        solver.build_grid()
+        got = solver.grid()
+    assert_grid_equal(got, oracle.grid_build(case.params, pos, threads=oracle.hardware_threads))
+
+
 def test_bad_tuning_is_rejected(native):
     case = W.dam_break_16k()
     with FluidSolverGpu(case.params, 16) as solver:
         for bad in (dict(block_size=100), dict(queue_depth=12), dict(neighbour_kernel=7), dict(radix_bits=0),
-                    dict(radix_bits=9), dict(schedule=2)):
+                    dict(radix_bits=9), dict(schedule=2), dict(sort=2)):
             with pytest.raises(abi.SphError) as e:
                 solver.set_tuning(**bad)
             assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
