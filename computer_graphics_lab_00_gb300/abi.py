@@ -165,6 +165,20 @@ SPH_MC_TABLE_WIDTH = 16
 SPH_SURFACE_MAX_RESOLUTION = 640
 
 
+# gfx::GpuInstance and the TLAS record (sph_instance / sph_tlas_instance).
+INSTANCE = np.dtype([("model", np.float32, 16), ("previous_model", np.float32, 16), ("normal_matrix", np.float32, 16),
+                     ("mesh_index", np.uint32), ("bucket", np.uint32), ("bucket_base", np.uint32),
+                     ("joint_offset", np.uint32), ("skinned_vertex_offset", np.uint32),
+                     ("previous_skinned_vertex_offset", np.uint32), ("skinned_meshlet_offset", np.uint32),
+                     ("visibility_base", np.uint32)])
+TLAS_INSTANCE = np.dtype([("transform", np.float32, 12), ("custom_index_mask", np.uint32),
+                          ("sbt_offset_flags", np.uint32), ("blas", np.uint64)])
+assert INSTANCE.itemsize == 224 and TLAS_INSTANCE.itemsize == 64
+SPH_INSTANCES_RESET_HISTORY = 1
+SPH_INSTANCES_WRITE_TLAS = 2
+SPH_INSTANCES_SURFACE_TLAS = 4
+
+
 class SphError(RuntimeError):
     """A non-zero status from the native library."""
 
@@ -233,6 +247,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_grid_build": (c_int, [c_void_p]),
         "sph_grid_build_static": (c_int, [P(SphParams), c_void_p, c_u32, c_void_p, c_void_p, c_void_p, c_void_p]),
         "sph_stats_compute": (c_int, [c_void_p, P(SphStats)]),
+        "sph_write_instances": (c_int, [c_void_p, c_void_p, c_u32, c_u32, c_void_p, c_u32, ctypes.c_uint64, c_u32,
+                                        c_u32]),
         "sph_surface_table": (c_int, [c_void_p]),
         "sph_surface_field": (c_int, [c_void_p, c_u32]),
         "sph_surface_field_download": (c_int, [c_void_p, c_void_p]),

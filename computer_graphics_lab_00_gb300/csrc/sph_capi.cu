@@ -225,6 +225,15 @@ int sph_substep(sph_ctx* ctx, float dt) {
     return ctx->engine.run(dt, 1);
 }
 
+int sph_write_instances(sph_ctx* ctx, void* instances, uint32_t instance_base, uint32_t sphere_mesh, void* tlas,
+                        uint32_t tlas_base, uint64_t blas, uint32_t fluid_index, uint32_t flags) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.write_instances(static_cast<sph_instance*>(instances), instance_base, sphere_mesh,
+                                       static_cast<sph_tlas_instance*>(tlas), tlas_base, blas, fluid_index, flags);
+}
+
 int sph_keep_rendered(sph_ctx* ctx) {
     if (ctx == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;

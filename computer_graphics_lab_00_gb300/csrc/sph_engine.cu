@@ -484,6 +484,22 @@ int Engine::keep_rendered() {
     return SPH_OK;
 }
 
+int Engine::write_instances(sph_instance* instances, uint32_t instance_base, uint32_t sphere_mesh,
+                            sph_tlas_instance* tlas, uint32_t tlas_base, uint64_t blas, uint32_t fluid_index,
+                            uint32_t flags) {
+    if (instances == nullptr || ((flags & SPH_INSTANCES_WRITE_TLAS) != 0 && tlas == nullptr) ||
+        reinterpret_cast<uintptr_t>(instances) % 16 != 0 || reinterpret_cast<uintptr_t>(tlas) % 16 != 0 ||
+        (flags & ~(SPH_INSTANCES_RESET_HISTORY | SPH_INSTANCES_WRITE_TLAS | SPH_INSTANCES_SURFACE_TLAS)) != 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    const uint32_t n = tanks_[0].particle_count;
+    SPH_CUDA(launch_instances(pos_, prev_, n, params_[0].container_min[3], instances, instance_base, sphere_mesh,
+                              (flags & SPH_INSTANCES_WRITE_TLAS) != 0 ? tlas : nullptr, tlas_base, blas, fluid_index,
+                              flags, stream_));
+    return keep_rendered();
+}
+
 int Engine::emit(uint32_t tank, uint32_t count) {
     if (tank >= tanks_.size()) {
         return SPH_ERR_INVALID_ARGUMENT;

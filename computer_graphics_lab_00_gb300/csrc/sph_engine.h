@@ -17,6 +17,7 @@
 #include "../../include/sph_c.h"
 #include "sph_kernels.h"
 #include "sph_mlp.cuh"
+#include "sph_instances.h"
 #include "sph_surface.h"
 
 namespace sph {
@@ -50,6 +51,10 @@ public:
     int download(uint32_t tank, float* pos, float* vel);
     int download_previous(uint32_t tank, float* pos);
     int keep_rendered();
+    // Draw instances of tank 0's particles into caller device buffers, then keep_rendered.
+    int write_instances(sph_instance* instances, uint32_t instance_base, uint32_t sphere_mesh,
+                        sph_tlas_instance* tlas, uint32_t tlas_base, uint64_t blas, uint32_t fluid_index,
+                        uint32_t flags);
     int emit(uint32_t tank, uint32_t count);
 
     // Enqueues `substeps` substeps of length dt for every active tank.

@@ -158,6 +158,14 @@ class FluidSolverGpu:
         self._check(self._lib.sph_download_previous(self._ctx, _ptr(pos)), "sph_download_previous")
         return pos
 
+    def write_instances(self, instances_ptr: int, instance_base: int = 0, sphere_mesh: int = 0,
+                        tlas_ptr: int | None = None, tlas_base: int = 0, blas: int = 0, fluid_index: int = 0,
+                        flags: int = 0) -> None:
+        """Draw instances into device buffers (fluid_instances.comp), then keep_rendered."""
+        self._check(self._lib.sph_write_instances(self._ctx, ctypes.c_void_p(instances_ptr), instance_base, sphere_mesh,
+                                                  None if tlas_ptr is None else ctypes.c_void_p(tlas_ptr), tlas_base,
+                                                  blas, fluid_index, flags), "sph_write_instances")
+
     def keep_rendered(self) -> None:
         self._check(self._lib.sph_keep_rendered(self._ctx), "sph_keep_rendered")
 

@@ -244,6 +244,54 @@ int sph_grid_build_static(const sph_params* params,
 /* Reduces statistics of the current state (FP64 on the device). */
 int sph_stats_compute(sph_ctx* ctx, sph_stats* out);
 
+/* ---- draw instances ------------------------------------------------------
+ * The instance writer of the reference's renderer (shaders/fluid_instances.comp,
+ * CPU twin src/gfx/fluid.cpp:402-466) into caller-owned device buffers: one
+ * gfx::GpuInstance per particle (a sphere scaled by the particle radius at
+ * its position, the previous frame's position for motion vectors) and,
+ * optionally, one VkAccelerationStructureInstanceKHR-layout record each. */
+
+/* gfx::GpuInstance (src/gfx/geometry.h:98-118), 224 bytes. */
+typedef struct sph_instance {
+    float model[16];          /* column-major */
+    float previous_model[16];
+    float normal_matrix[16];
+    uint32_t mesh_index;
+    uint32_t bucket;
+    uint32_t bucket_base;
+    uint32_t joint_offset;                   /* NO_JOINTS */
+    uint32_t skinned_vertex_offset;          /* NO_SKINNED_VERTICES */
+    uint32_t previous_skinned_vertex_offset; /* NO_SKINNED_VERTICES */
+    uint32_t skinned_meshlet_offset;
+    uint32_t visibility_base;
+} sph_instance;
+
+/* VkAccelerationStructureInstanceKHR layout, 64 bytes: a row-major 3x4
+ * transform, custom index (24 bits) | mask << 24, SBT offset | flags << 24,
+ * acceleration-structure address. */
+typedef struct sph_tlas_instance {
+    float transform[12];
+    uint32_t custom_index_mask;
+    uint32_t sbt_offset_flags;
+    uint64_t blas;
+} sph_tlas_instance;
+
+#define SPH_INSTANCES_RESET_HISTORY 1u /* previous position := current (fresh emit) */
+#define SPH_INSTANCES_WRITE_TLAS 2u    /* also write one TLAS record per particle */
+#define SPH_INSTANCES_SURFACE_TLAS 4u  /* surface mode: record 0 is the surface, the rest inactive */
+#define SPH_NO_JOINTS 0xFFFFFFFFu
+#define SPH_FLUID_SURFACE_CUSTOM_INDEX 0x800000u
+#define SPH_FLUID_SURFACE_RAY_MASK 0x01u
+
+/* Writes instances[instance_base + i] (and tlas[tlas_base + i]) for every
+ * particle, then keeps the current positions as the previous ones
+ * (FluidSolver::keepRendered). `instances` and `tlas` are 16-byte aligned
+ * device pointers (tlas may be NULL without SPH_INSTANCES_WRITE_TLAS); `blas` is the sphere's
+ * (or, in surface mode, the surface's) acceleration-structure address and
+ * fluid_index goes into the surface record's custom index. */
+int sph_write_instances(sph_ctx* ctx, void* instances, uint32_t instance_base, uint32_t sphere_mesh, void* tlas,
+                        uint32_t tlas_base, uint64_t blas, uint32_t fluid_index, uint32_t flags);
+
 /* ---- fluid surface: scalar field + marching cubes ----------------------
  * physics::buildFluidField / physics::marchFluidField
  * (src/physics/marching_cubes.h:39-57, marching_cubes.cpp:312-483) on the
