@@ -1254,19 +1254,25 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
         if (kCount) {
             candidates += r.y - r.x;
         }
-        for (uint32_t q = r.x; q < r.y; ++q) {
-            float4 other = __ldg(&spos[q]);
+        const float4* cand = spos + r.x;
+        const uint32_t count = r.y - r.x;
+        // Branch-free candidate loop: every lane runs the same instructions
+        // for every candidate, so a warp issues each of them once.
+        for (uint32_t s = 0; s < count; ++s) {
+            float4 other = __ldg(&cand[s]);
             float r2 = dot3(__fsub_rn(self.x, other.x), __fsub_rn(self.y, other.y), __fsub_rn(self.z, other.z));
-            if (r2 < h2) {
-                // poly6 (fluid_sph.cpp:24-31) times mass, added in candidate order.
-                float d = __fsub_rn(h2, r2);
-                density = __fadd_rn(density, __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d)));
-                if (kCount) {
-                    ++in_range;
-                }
+            // mass * poly6 (fluid_sph.cpp:24-31, :214) in candidate order; out
+            // of range the reference adds mass * 0 = +0, which leaves the
+            // (non-negative) sum's bits as they are.
+            float d = __fsub_rn(h2, r2);
+            float term = __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d));
+            density = __fadd_rn(density, r2 >= h2 ? 0.0f : term);
+            if (kCount) {
+                in_range += r2 < h2 ? 1u : 0u;
             }
-            bool keep = q != p && !(r2 >= r2_far || r2 <= r2_near);
-            word |= static_cast<uint32_t>(keep) << (q - r.x);
+            // Integrate skips distance >= h or <= 1e-6 (fluid_sph.cpp:245-248);
+            // the particle itself (r2 = 0) fails the second test.
+            word |= static_cast<uint32_t>(!(r2 >= r2_far || r2 <= r2_near)) << s;
         }
         masks[static_cast<size_t>(b) * n + p] = word;
     }
