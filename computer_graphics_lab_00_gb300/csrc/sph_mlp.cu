@@ -148,15 +148,16 @@ __device__ __forceinline__ float erf_as(float x) {
 // GELU of the forward pass (erf form through erf_as).
 __device__ __forceinline__ float gelu_fast(float z) { return 0.5f * z * (1.0f + erf_as(z * 0.70710678118654752f)); }
 
-constexpr uint32_t kForwardThreads = 256;
+constexpr uint32_t kForwardThreads = 512;
+constexpr uint32_t kGroups = kForwardThreads / 128;  // threads sharing one row's epilogue
 
 // One CTA of 256 threads owns 128 TMEM columns and runs 128-particle tiles:
 // X (normalised features, BF16) -> [MMA W1] -> +b1, GELU -> H1 (BF16) ->
 // [MMA W2] -> +b2, GELU -> H2 -> [MMA W3] -> +b3 -> scaled output. Row r of a
 // tile is TMEM lane r; warp w reads the lane quarter w % 4 and, for the hidden
-// layers, the column half w / 4, so two threads share each row's epilogue.
+// layers, the column group w / 4, so kGroups threads share each row's epilogue.
 // One thread issues the MMAs; an mbarrier reports their completion.
-__global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelView model,
+__global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelView model,
                                                                          const float* __restrict__ features,
                                                                          uint32_t n, float* __restrict__ out,
                                                                          ForwardSaves saves, int save,
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelVi
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5;
     const uint32_t quarter = warp & 3u;
-    const uint32_t half = warp >> 2;
+    const uint32_t group = warp >> 2;
     const uint32_t local_row = quarter * 32u + (tid & 31u);
 
     // Weights into the canonical K-major layout (16-byte chunks).
@@ -225,8 +226,8 @@ __global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelVi
         // Normalised features -> BF16 tile; each thread converts 16 of its row's 32.
         const float4* frow = reinterpret_cast<const float4*>(features + static_cast<size_t>(row) * kIn);
 #pragma unroll
-        for (uint32_t j = 0; j < 2; ++j) {
-            uint32_t chunk = half * 2u + j;
+        for (uint32_t j = 0; j < (kIn / 8) / kGroups; ++j) {
+            uint32_t chunk = group * ((kIn / 8) / kGroups) + j;
             float v[8];
             float4 a = valid ? frow[2 * chunk] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             float4 b = valid ? frow[2 * chunk + 1] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -266,8 +267,8 @@ __global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelVi
         parity ^= 1u;
         tc_fence_after();
 #pragma unroll 1
-        for (uint32_t j = 0; j < 4; ++j) {
-            uint32_t c = half * 4u + j;
+        for (uint32_t j = 0; j < (kHidden / 16) / kGroups; ++j) {
+            uint32_t c = group * ((kHidden / 16) / kGroups) + j;
             float v[16];
             tmem_load16(tmem + lane_base + c * 16u, v);
 #pragma unroll
@@ -309,8 +310,8 @@ __global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelVi
         parity ^= 1u;
         tc_fence_after();
 #pragma unroll 1
-        for (uint32_t j = 0; j < 4; ++j) {
-            uint32_t c = half * 4u + j;
+        for (uint32_t j = 0; j < (kHidden / 16) / kGroups; ++j) {
+            uint32_t c = group * ((kHidden / 16) / kGroups) + j;
             float v[16];
             tmem_load16(tmem + lane_base + c * 16u, v);
 #pragma unroll
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(kForwardThreads, 1) mlp_forward_kernel(ModelVi
         }
         parity ^= 1u;
         tc_fence_after();
-        if (half == 0) {
+        if (group == 0) {
             float v[16];
             tmem_load16(tmem + lane_base, v);
             if (valid) {
