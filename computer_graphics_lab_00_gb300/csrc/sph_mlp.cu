@@ -157,10 +157,11 @@ constexpr uint32_t kGroups = kForwardThreads / 128;  // threads sharing one row'
 // tile is TMEM lane r; warp w reads the lane quarter w % 4 and, for the hidden
 // layers, the column group w / 4, so kGroups threads share each row's epilogue.
 // One thread issues the MMAs; an mbarrier reports their completion.
+template <bool kSave>
 __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelView model,
                                                                          const float* __restrict__ features,
                                                                          uint32_t n, float* __restrict__ out,
-                                                                         ForwardSaves saves, int save,
+                                                                         ForwardSaves saves,
                                                                          unsigned int* __restrict__ error_flag) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmemBar);
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
                 v[k] = valid ? (raw[k] - model.in_mean[f]) * model.in_inv_std[f] : 0.0f;
             }
             store_chunk(smem + kSmemX, tile_offset(local_row, chunk, kIn), v);
-            if (save && valid) {
+            if (kSave && valid) {
 #pragma unroll
                 for (uint32_t k = 0; k < 8; ++k) {
                     saves.x[static_cast<size_t>(row) * kIn + chunk * 8 + k] = __float2bfloat16_rn(v[k]);
@@ -274,14 +275,14 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
 #pragma unroll
             for (uint32_t k = 0; k < 16; ++k) {
                 float z = v[k] + b1[c * 16 + k];
-                if (save && valid) {
+                if (kSave && valid) {
                     saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
                 }
                 v[k] = gelu_fast(z);
             }
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c, kHidden), v);
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
-            if (save && valid) {
+            if (kSave && valid) {
 #pragma unroll
                 for (uint32_t k = 0; k < 16; ++k) {
                     saves.h1[static_cast<size_t>(row) * kHidden + c * 16 + k] = __float2bfloat16_rn(v[k]);
@@ -317,14 +318,14 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
 #pragma unroll
             for (uint32_t k = 0; k < 16; ++k) {
                 float z = v[k] + b2[c * 16 + k];
-                if (save && valid) {
+                if (kSave && valid) {
                     saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
                 }
                 v[k] = gelu_fast(z);
             }
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c, kHidden), v);
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
-            if (save && valid) {
+            if (kSave && valid) {
 #pragma unroll
                 for (uint32_t k = 0; k < 16; ++k) {
                     saves.h2[static_cast<size_t>(row) * kHidden + c * 16 + k] = __float2bfloat16_rn(v[k]);
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
                 float y0 = v[0] + b3[0];
                 float y1 = v[1] + b3[1];
                 float y2 = v[2] + b3[2];
-                if (save) {
+                if (kSave) {
                     reinterpret_cast<float4*>(saves.y)[row] = make_float4(y0, y1, y2, 0.0f);
                 }
                 if (out != nullptr) {
@@ -596,8 +597,13 @@ cudaError_t launch_forward(const ModelView& model, const float* features, uint32
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(sms) * 2u);
     ForwardSaves none{};
-    mlp_forward_kernel<<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel, saves ? *saves : none,
-                                                          saves ? 1 : 0, error_flag);
+    if (saves != nullptr) {
+        mlp_forward_kernel<true><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel, *saves,
+                                                                                error_flag);
+    } else {
+        mlp_forward_kernel<false><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel, none,
+                                                                                 error_flag);
+    }
     return cudaGetLastError();
 }
 
@@ -608,8 +614,12 @@ void launch_erf_selftest(uint32_t count, unsigned int* out, cudaStream_t stream)
 cudaError_t prepare_forward() {
     static bool configured = false;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(mlp_forward_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(kSmemBytes));
+        if (e == cudaSuccess) {
+            e = cudaFuncSetAttribute(mlp_forward_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kSmemBytes));
+        }
         if (e != cudaSuccess) {
             return e;
         }
