@@ -1258,6 +1258,7 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
         const uint32_t count = r.y - r.x;
         // Branch-free candidate loop: every lane runs the same instructions
         // for every candidate, so a warp issues each of them once.
+#pragma unroll 4
         for (uint32_t s = 0; s < count; ++s) {
             float4 other = __ldg(&cand[s]);
             float r2 = dot3(__fsub_rn(self.x, other.x), __fsub_rn(self.y, other.y), __fsub_rn(self.z, other.z));
@@ -1312,11 +1313,12 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
     if (order != nullptr && p < n) {
         p = order[p];
     }
-    if (p >= n) {
-        return;
-    }
-    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
-    if (__ldg(&t->active) == 0) {
+    bool valid = p < n;
+    const TankConst* t = tanks + (valid && stank != nullptr ? stank[p] : 0);
+    valid = valid && __ldg(&t->active) != 0;
+    // The lanes with a particle; they walk the 27 buckets in step.
+    const uint32_t live = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!valid) {
         return;
     }
     PairConst k;
@@ -1338,24 +1340,25 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
     uint32_t listed = 0;
     for (uint32_t b = 0; b < 27u; ++b) {
         uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + p]);
-        if (word == 0) {
-            continue;
-        }
-        uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
-        while (word != 0) {
-            uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
-            word &= word - 1;
-            if (listed == static_cast<uint32_t>(kList)) {
-                // Drain a full list, in order, before taking more.
-                for (uint32_t e = 0; e < listed; ++e) {
-                    uint32_t q = list[e][threadIdx.x];
-                    add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
-                                       __ldg(&svel[q]), fx, fy, fz);
-                }
-                listed = 0;
+        // When any lane's list cannot take this bucket's pairs, every lane
+        // drains its list (in order) at once, so the force code runs with
+        // all lanes busy rather than once per lane that filled up.
+        if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
+            for (uint32_t e = 0; e < listed; ++e) {
+                uint32_t q = list[e][threadIdx.x];
+                add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                                   __ldg(&svel[q]), fx, fy, fz);
             }
-            list[listed][threadIdx.x] = start + slot;
-            ++listed;
+            listed = 0;
+        }
+        if (word != 0) {
+            uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
+            while (word != 0) {
+                uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
+                word &= word - 1;
+                list[listed][threadIdx.x] = start + slot;
+                ++listed;
+            }
         }
     }
     for (uint32_t e = 0; e < listed; ++e) {
@@ -1402,6 +1405,7 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
                                                           float* __restrict__ features_out, int id_order) {
     __shared__ uint32_t list[kList][kBlock];
     uint32_t p = blockIdx.x * kBlock + threadIdx.x;
+    const uint32_t live = __ballot_sync(0xFFFFFFFFu, p < n);
     if (p >= n) {
         return;
     }
@@ -1466,21 +1470,21 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
     uint32_t listed = 0;
     for (uint32_t b = 0; b < 27u; ++b) {
         uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + p]);
-        if (word == 0) {
-            continue;
-        }
-        uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
-        while (word != 0) {
-            uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
-            word &= word - 1;
-            if (listed == static_cast<uint32_t>(kList)) {
-                for (uint32_t e = 0; e < listed; ++e) {
-                    visit(list[e][threadIdx.x]);
-                }
-                listed = 0;
+        // Every lane drains together when any lane's list is about to overflow.
+        if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
+            for (uint32_t e = 0; e < listed; ++e) {
+                visit(list[e][threadIdx.x]);
             }
-            list[listed][threadIdx.x] = start + slot;
-            ++listed;
+            listed = 0;
+        }
+        if (word != 0) {
+            uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
+            while (word != 0) {
+                uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
+                word &= word - 1;
+                list[listed][threadIdx.x] = start + slot;
+                ++listed;
+            }
         }
     }
     for (uint32_t e = 0; e < listed; ++e) {
