@@ -64,6 +64,8 @@ def parse_args():
                    help="substeps of the 256-tank leg (0 skips it)")
     p.add_argument("--learned-steps", type=int, default=20,
                    help="coarse steps of the learned 5x-dt leg at 1M (0 skips it)")
+    p.add_argument("--sustained-steps", type=int, default=1000,
+                   help="substeps of the whole-run leg of the 1M dam break (0 skips it)")
     return p.parse_args()
 
 
@@ -286,6 +288,44 @@ def surface_leg(device: int, reps: int = 10) -> list:
                     "cpu_baseline": {"kind": "port", "ms_per_frame": (t2 - t0) * 1e3, "field_ms": (t1 - t0) * 1e3,
                                      "march_ms": (t2 - t1) * 1e3, "cores_field": threads, "cores_march": 1}})
     return out
+
+
+def sustained_leg(steps: int, flush, device: int) -> dict:
+    """The 1M dam break run for `steps` substeps from its initial state (the
+    configuration's full length), each substep timed with CUDA events after an
+    L2 flush. The dam collapses and compresses as it runs, so later substeps
+    see more pairs per particle than the first ones: this is the figure a
+    whole run gets."""
+    import torch
+
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+
+    case = W.dam_break_1m()
+    n = case.count
+    with FluidSolverGpu(case.params, n, device=device) as solver:
+        solver.upload(*case.initial_state())
+        stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                starts[k].record(stream)
+            solver.run(case.dt, 1)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+        stats = solver.stats()
+    mean = sum(ms) / steps
+    tenth = max(1, steps // 10)
+    return {
+        "workload": case.name, "substeps": steps, "ms_per_step": mean, "value": n * case.dt / (mean / 1e3),
+        "unit": UNIT, "ms_per_step_by_tenth": [sum(ms[i:i + tenth]) / len(ms[i:i + tenth])
+                                               for i in range(0, steps, tenth)],
+        "final_pairs_per_particle": stats.pairs_in_range / n, "final_mean_compression": stats.mean_compression,
+        "l2": "flushed before every substep",
+    }
 
 
 def learned_leg(steps: int, flush, device: int, plain_ms: float) -> dict:
@@ -534,6 +574,8 @@ def run_gb300(args) -> None:
         "clocks": clocks,
         "wall_s_timed": wall,
     }
+    if world == 1 and args.sustained_steps > 0:
+        out["sustained"] = sustained_leg(args.sustained_steps, flush, local)
     if batched is not None:
         out["batched"] = batched
     if args.learned_steps > 0 and world == 1 and WEIGHTS.exists():
