@@ -1308,6 +1308,8 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
                                                                 const uint32_t* __restrict__ masks,
                                                                 float4* __restrict__ pos_out,
                                                                 float4* __restrict__ vel_out) {
+    // One bucket may hand over 32 pairs at once, after the warp has drained.
+    static_assert(kList >= 32, "a pair list must hold a whole bucket");
     __shared__ uint32_t list[kList][kBlock];
     uint32_t p = blockIdx.x * kBlock + threadIdx.x;
     if (order != nullptr && p < n) {
@@ -1403,6 +1405,7 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
                                                           const uint32_t* __restrict__ masks,
                                                           float4* __restrict__ force_out,
                                                           float* __restrict__ features_out, int id_order) {
+    static_assert(kList >= 32, "a pair list must hold a whole bucket");
     __shared__ uint32_t list[kList][kBlock];
     uint32_t p = blockIdx.x * kBlock + threadIdx.x;
     const uint32_t live = __ballot_sync(0xFFFFFFFFu, p < n);
@@ -1689,10 +1692,7 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
                                                                             stank, n, tuning.order, tuning.masks, pos, vel);
             break;
         case 256:
-            if (tuning.queue <= 24) {
-                integrate_mask_kernel<256, 24><<<(n + 255) / 256, 256, 0, stream>>>(
-                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
-            } else if (tuning.queue == 32) {
+            if (tuning.queue <= 32) {
                 integrate_mask_kernel<256, 32><<<(n + 255) / 256, 256, 0, stream>>>(
                     spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
             } else {

@@ -346,9 +346,10 @@ def test_pair_list_overflow_falls_back_bit_exact(native, oracle):
     pos[:, :3] = (0.4 + rng.uniform(0.0, 0.12, size=(n, 3))).astype(np.float32)
     pos[:, 3] = 1000.0
     vel = np.zeros((n, 4), np.float32)
-    for variant, schedule in ((2, 0), (3, 1), (4, 0), (4, 1)):
+    for variant, schedule, block, queue in ((2, 0, 256, 32), (3, 1, 256, 32), (4, 0, 256, 32), (4, 1, 256, 32),
+                                            (4, 0, 256, 24), (4, 0, 256, 16), (4, 0, 128, 32), (4, 0, 64, 32)):
         with FluidSolverGpu(params, n) as solver:
-            solver.set_tuning(neighbour_kernel=variant, schedule=schedule)
+            solver.set_tuning(neighbour_kernel=variant, schedule=schedule, block_size=block, queue_depth=queue)
             solver.upload(pos, vel)
             solver.run(1.0 / 600.0, 2)
             gp, gv = solver.state()
