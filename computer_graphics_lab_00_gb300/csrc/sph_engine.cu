@@ -184,7 +184,7 @@ void Engine::release() {
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
-                       schedule_.tile_of, schedule_.order, schedule_.tile_hist, snap_pos_[0], snap_vel_[0],
+                       rank_,          order_,        snap_pos_[0], snap_vel_[0],
                        snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_};
     for (void* b : buffers) {
         if (b != nullptr) {
@@ -264,10 +264,7 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         (status = alloc(&tuning_.masks, static_cast<size_t>(n) * 27)) != SPH_OK) {
         return status;
     }
-    schedule_.tile_bits = tanks_.size() == 1 ? 5u : 3u;
-    schedule_.bins = static_cast<uint32_t>(tanks_.size()) << (3 * schedule_.tile_bits);
-    if ((status = alloc(&schedule_.tile_of, n)) != SPH_OK || (status = alloc(&schedule_.order, n)) != SPH_OK ||
-        (status = alloc(&schedule_.tile_hist, schedule_.bins)) != SPH_OK) {
+    if ((status = alloc(&rank_, n)) != SPH_OK || (status = alloc(&order_, n)) != SPH_OK) {
         return status;
     }
     if (tanks_.size() > 1) {
@@ -440,6 +437,7 @@ int Engine::upload(uint32_t tank, const float* pos, const float* vel, uint32_t c
         consts_dirty_ = true;
     }
     grid_valid_ = false;
+    since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
     return SPH_OK;
 }
 
@@ -519,11 +517,50 @@ int Engine::emit(uint32_t tank, uint32_t count) {
     }
     SPH_CUDA(launch_emit(d_tanks_ + tank, tanks_[tank].particle_base, count, pos_, vel_, prev_, stream_));
     grid_valid_ = false;
+    since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
+    return SPH_OK;
+}
+
+// Morton processing order: rank_ is refreshed from the current positions
+// every kScheduleRefresh grid builds (particles move a fraction of a cell per
+// substep, so an order a few substeps old keeps its locality) and whenever the
+// particle count changed since the last refresh. Never called while a graph
+// is being captured: the graphs only hold the per-substep order scatter.
+int Engine::prepare_schedule(uint32_t* launches) {
+    if (!use_schedule_ || total_count_ == 0) {
+        return SPH_OK;
+    }
+    if (rank_count_ == total_count_ && since_refresh_ + 1 < kScheduleRefresh) {
+        ++since_refresh_;
+        return SPH_OK;
+    }
+    // Bits per axis: enough for the widest tank's cells, within 32 key bits.
+    uint32_t cells = 1;
+    for (const TankConst& t : tanks_) {
+        for (int a = 0; a < 3; ++a) {
+            float extent = (t.high[a] - t.low[a]) / t.h;
+            uint32_t c = std::isfinite(extent) && extent > 0.0F ? static_cast<uint32_t>(std::min(extent, 4096.0F)) + 1U
+                                                               : 1U;
+            cells = std::max(cells, c);
+        }
+    }
+    const uint32_t tank_bits = bit_width(static_cast<uint32_t>(tanks_.size()) - 1U);
+    const uint32_t axis_bits = std::max(1U, std::min({bit_width(cells - 1U), 10U, (32U - tank_bits) / 3U}));
+    SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, 3U * axis_bits + tank_bits, grid_,
+                                sweep_, rank_, stream_, launches));
+    rank_count_ = total_count_;
+    since_refresh_ = 0;
     return SPH_OK;
 }
 
 int Engine::enqueue_grid(uint32_t* launches) {
     uint32_t n = total_count_;
+    if (!capturing_) {
+        int status = prepare_schedule(nullptr);
+        if (status != SPH_OK) {
+            return status;
+        }
+    }
     SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
     if (onesweep_) {
         const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
@@ -545,18 +582,19 @@ int Engine::enqueue_grid(uint32_t* launches) {
 
 int Engine::enqueue_bounds(uint32_t* launches) {
     uint32_t n = total_count_;
-    Schedule schedule = schedule_;
-    if (!use_schedule_) {
-        schedule.tile_of = nullptr;
-    } else {
-        SPH_CUDA(cudaMemsetAsync(schedule.tile_hist, 0, sizeof(uint32_t) * schedule.bins, stream_));
+    Schedule schedule{};
+    if (use_schedule_) {
+        if (rank_count_ != n) {
+            return SPH_ERR_INVALID_ARGUMENT;  // prepare_schedule did not run for this particle count
+        }
+        schedule.rank = rank_;
+        schedule.order = order_;
     }
     SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_, svel_,
-                                  stank_, d_tanks_, schedule, stream_));
-    SPH_CUDA(launch_schedule(n, schedule, stream_));
-    tuning_.order = use_schedule_ ? schedule_.order : nullptr;
+                                  stank_, schedule, stream_));
+    tuning_.order = use_schedule_ ? order_ : nullptr;
     if (launches != nullptr) {
-        *launches += use_schedule_ ? 3 : 1;
+        *launches += 1;
     }
     return SPH_OK;
 }
@@ -587,10 +625,16 @@ int Engine::ensure_graph() {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    int status = prepare_schedule(nullptr);
+    if (status != SPH_OK) {
+        return status;
+    }
     cudaGraph_t graph = nullptr;
     SPH_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     uint32_t launches = 0;
-    int status = enqueue_substep(&launches);
+    capturing_ = true;
+    status = enqueue_substep(&launches);
+    capturing_ = false;
     cudaError_t end = cudaStreamEndCapture(stream_, &graph);
     if (status != SPH_OK) {
         if (graph != nullptr) {
@@ -629,6 +673,9 @@ int Engine::run(float dt, uint32_t substeps) {
         return status;
     }
     for (uint32_t s = 0; s < substeps; ++s) {
+        if ((status = prepare_schedule(nullptr)) != SPH_OK) {
+            return status;
+        }
         SPH_CUDA(cudaGraphLaunch(graph_, stream_));
     }
     grid_valid_ = true;
@@ -668,6 +715,9 @@ int Engine::run_per_tank(const std::vector<float>& dt, const std::vector<uint32_
         }
         SPH_CUDA(cudaMemcpyAsync(d_tanks_, tanks_.data(), tanks_.size() * sizeof(TankConst), cudaMemcpyHostToDevice,
                                  stream_));
+        if ((status = prepare_schedule(nullptr)) != SPH_OK) {
+            return status;
+        }
         SPH_CUDA(cudaGraphLaunch(graph_, stream_));
     }
     for (size_t t = 0; t < tanks_.size(); ++t) {
@@ -733,6 +783,7 @@ int Engine::snapshot(bool save, uint32_t slot) {
         SPH_CUDA(cudaMemcpyAsync(pos_, snap_pos_[slot], bytes, cudaMemcpyDeviceToDevice, stream_));
         SPH_CUDA(cudaMemcpyAsync(vel_, snap_vel_[slot], bytes, cudaMemcpyDeviceToDevice, stream_));
         grid_valid_ = false;
+        since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
     }
     return SPH_OK;
 }
@@ -764,6 +815,7 @@ int Engine::restore_tanks(uint32_t slot, const std::vector<uint8_t>& which) {
         SPH_CUDA(cudaMemcpyAsync(vel_ + first, snap_vel_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
     }
     grid_valid_ = false;
+    since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
     return SPH_OK;
 }
 
@@ -804,15 +856,17 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
         if (st != SPH_OK) {
             return st;
         }
+        // At least one Morton order remake per timed run, so its cost counts.
+        const uint32_t timed = std::max(substeps, kScheduleRefresh);
         SPH_CUDA(cudaEventRecord(start, stream_));
-        st = run(dt, substeps);
+        st = run(dt, timed);
         if (st != SPH_OK) {
             return st;
         }
         SPH_CUDA(cudaEventRecord(stop, stream_));
         SPH_CUDA(cudaEventSynchronize(stop));
         SPH_CUDA(cudaEventElapsedTime(ms, start, stop));
-        *ms /= static_cast<float>(substeps);
+        *ms /= static_cast<float>(timed);
         return SPH_OK;
     };
     // Stage 1: neighbour kernel, block size and processing order; stage 2:
@@ -920,8 +974,8 @@ int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launc
         return status;
     }
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
-    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.masks, sforce_,
-                             sfeatures_, false, stream_));
+    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.order,
+                             tuning_.masks, sforce_, sfeatures_, false, stream_));
     if (model != nullptr) {
         SPH_CUDA(mlp::launch_forward(*model, sfeatures_, n, reinterpret_cast<float*>(scorrection_), nullptr,
                                      &counters_->error_flags, stream_));
@@ -959,10 +1013,15 @@ int Engine::run_learned(float dt, uint32_t substeps, const mlp::ModelView* model
             learned_graph_ = nullptr;
         }
         SPH_CUDA(cudaMemsetAsync(&counters_->error_flags, 0, sizeof(unsigned int), stream_));
+        if ((status = prepare_schedule(nullptr)) != SPH_OK) {
+            return status;
+        }
         cudaGraph_t graph = nullptr;
         SPH_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         uint32_t launches = 0;
+        capturing_ = true;
         status = enqueue_learned_substep(model, &launches);
+        capturing_ = false;
         cudaError_t end = cudaStreamEndCapture(stream_, &graph);
         if (status != SPH_OK) {
             if (graph != nullptr) {
@@ -987,6 +1046,9 @@ int Engine::run_learned(float dt, uint32_t substeps, const mlp::ModelView* model
         learned_launches_ = launches;
     }
     for (uint32_t s = 0; s < substeps; ++s) {
+        if ((status = prepare_schedule(nullptr)) != SPH_OK) {
+            return status;
+        }
         SPH_CUDA(cudaGraphLaunch(learned_graph_, stream_));
     }
     grid_valid_ = true;
@@ -1028,8 +1090,8 @@ int Engine::learned_features(float dt, float* features) {
     NeighbourTuning masked = tuning_;
     masked.variant = 4;
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
-    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.masks, sforce_,
-                             features, true, stream_));
+    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.order,
+                             tuning_.masks, sforce_, features, true, stream_));
     grid_valid_ = true;
     return SPH_OK;
 }
@@ -1222,6 +1284,7 @@ int Engine::set_onesweep(bool on) {
 
 int Engine::set_schedule(bool on) {
     use_schedule_ = on;
+    rank_count_ = 0xFFFFFFFFu;
     if (graph_ != nullptr) {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
@@ -1269,6 +1332,9 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
     uint32_t n = total_count_;
     for (uint32_t s = 0; s < substeps; ++s) {
         SPH_CUDA(cudaEventRecord(events_[0], stream_));
+        if ((status = prepare_schedule(nullptr)) != SPH_OK) {  // counted with the keys
+            return status;
+        }
         SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
         const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
         if (onesweep_) {

@@ -141,6 +141,8 @@ private:
     int enqueue_fields(uint32_t* launches);
     int enqueue_colliders(uint32_t* launches);
     int ensure_graph();
+    int prepare_schedule(uint32_t* launches);
+    static constexpr uint32_t kScheduleRefresh = 8;  // grid builds between Morton order refreshes
     void release();
     template <typename T> int alloc(T** ptr, size_t count);
 
@@ -155,8 +157,12 @@ private:
     uint32_t radix_bits_ = 6;
     RadixPlan plan_{};
     NeighbourTuning tuning_{};
-    Schedule schedule_{};
-    bool use_schedule_ = false;
+    bool use_schedule_ = true;
+    bool capturing_ = false;               // a graph capture is open on stream_
+    uint32_t* rank_ = nullptr;             // Morton slot of each particle id (a permutation)
+    uint32_t* order_ = nullptr;            // sorted positions in processing order
+    uint32_t rank_count_ = 0xFFFFFFFFu;    // particle count rank_ was made for
+    uint32_t since_refresh_ = 0;           // grid builds since rank_ was made
     bool onesweep_ = true;
     unsigned long long* sweep_ = nullptr;  // per-pass tile digit counts and histograms of the one-kernel passes
     float const_dt_ = -1.0f;

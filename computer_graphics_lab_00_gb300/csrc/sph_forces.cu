@@ -982,7 +982,8 @@ __global__ void __launch_bounds__(128) density_list_kernel(const float4* __restr
                                                            uint16_t* __restrict__ pair_list,
                                                            uint16_t* __restrict__ pair_count, uint32_t cap,
                                                            StepCounters* __restrict__ counters) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;  // processing slot: indexes the masks
+    uint32_t p = slot;
     if (order != nullptr && p < n) {
         p = order[p];
     }
@@ -1213,8 +1214,9 @@ __global__ void __launch_bounds__(kBlock) integrate_list_kernel(const float4* __
 // Density keeps the nested bucket loops (all lanes of a warp step through the
 // 27 buckets together) and, per bucket, ORs into one 32-bit word the slots
 // integrate will use (j != i and !(sqrt(r2) >= h || sqrt(r2) <= 1e-6), via the
-// exact r2 thresholds). The word is stored bucket-major, masks[b * n + p], so
-// each store of a warp is one contiguous 128-byte line. Integrate reads its 27
+// exact r2 thresholds). The word is stored bucket-major by processing slot,
+// masks[b * n + slot], so each store of a warp is one contiguous 128-byte line
+// whatever the processing order. Integrate reads its 27
 // words (again one line per warp and bucket), expands the set bits into a
 // list of sorted positions in shared memory in stream order, and runs the
 // pair forces over that list with all lanes busy.
@@ -1225,7 +1227,8 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
                                                            const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
                                                            uint32_t* __restrict__ masks,
                                                            StepCounters* __restrict__ counters) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;  // processing slot: indexes the masks
+    uint32_t p = slot;
     if (order != nullptr && p < n) {
         p = order[p];
     }
@@ -1275,7 +1278,7 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
             // the particle itself (r2 = 0) fails the second test.
             word |= static_cast<uint32_t>(!(r2 >= r2_far || r2 <= r2_near)) << s;
         }
-        masks[static_cast<size_t>(b) * n + p] = word;
+        masks[static_cast<size_t>(b) * n + slot] = word;
     }
     if (kCount) {
         unsigned long long c = candidates;
@@ -1311,7 +1314,8 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
     // One bucket may hand over 32 pairs at once, after the warp has drained.
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
     __shared__ uint32_t list[kList][kBlock];
-    uint32_t p = blockIdx.x * kBlock + threadIdx.x;
+    const uint32_t slot = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t p = slot;
     if (order != nullptr && p < n) {
         p = order[p];
     }
@@ -1341,7 +1345,7 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
     float fz = 0.0f;
     uint32_t listed = 0;
     for (uint32_t b = 0; b < 27u; ++b) {
-        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + p]);
+        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + slot]);
         // When any lane's list cannot take this bucket's pairs, every lane
         // drains its list (in order) at once, so the force code runs with
         // all lanes busy rather than once per lane that filled up.
@@ -1402,12 +1406,17 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
                                                           const uint2* __restrict__ bucket,
                                                           const TankConst* __restrict__ tanks,
                                                           const uint16_t* __restrict__ stank, uint32_t n,
+                                                          const uint32_t* __restrict__ order,
                                                           const uint32_t* __restrict__ masks,
                                                           float4* __restrict__ force_out,
                                                           float* __restrict__ features_out, int id_order) {
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
     __shared__ uint32_t list[kList][kBlock];
-    uint32_t p = blockIdx.x * kBlock + threadIdx.x;
+    const uint32_t slot = blockIdx.x * kBlock + threadIdx.x;
+    uint32_t p = slot;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
     const uint32_t live = __ballot_sync(0xFFFFFFFFu, p < n);
     if (p >= n) {
         return;
@@ -1472,7 +1481,7 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
     };
     uint32_t listed = 0;
     for (uint32_t b = 0; b < 27u; ++b) {
-        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + p]);
+        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + slot]);
         // Every lane drains together when any lane's list is about to overflow.
         if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
             for (uint32_t e = 0; e < listed; ++e) {
@@ -1813,13 +1822,14 @@ cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_
 }
 
 cudaError_t launch_features(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
-                            const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* masks,
-                            float4* force, float* features, bool id_order, cudaStream_t stream) {
+                            const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* order,
+                            const uint32_t* masks, float4* force, float* features, bool id_order,
+                            cudaStream_t stream) {
     if (n == 0) {
         return cudaSuccess;
     }
     features_kernel<128, 48><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
-                                                                  masks, force, features, id_order ? 1 : 0);
+                                                                  order, masks, force, features, id_order ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -210,68 +210,35 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
                                                             const float4* __restrict__ vel,
                                                             const uint16_t* __restrict__ tank_of,
                                                             float4* __restrict__ spos, float4* __restrict__ svel,
-                                                            uint16_t* __restrict__ stank,
-                                                            const TankConst* __restrict__ tanks, Schedule schedule) {
+                                                            uint16_t* __restrict__ stank, Schedule schedule) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool valid = p < n;
-    uint32_t i = 0;
-    uint32_t tank = 0;
-    float4 position = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (valid) {
-        uint32_t key = sorted_keys[p];
-        if (p == 0 || sorted_keys[p - 1] != key) {
-            bucket_words[2 * static_cast<size_t>(key)] = p;
-        }
-        if (p + 1 == n || sorted_keys[p + 1] != key) {
-            bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
-        }
-        i = sorted_ids[p];
-        position = pos[i];
-        spos[p] = position;
-        svel[p] = vel[i];
-        if (tank_of != nullptr) {
-            tank = tank_of[i];
-            stank[p] = static_cast<uint16_t>(tank);
-        }
-    }
-    if (schedule.tile_of == nullptr) {
+    if (p >= n) {
         return;
     }
-    // Processing order: cells grouped into 4 x 4 x 4 tiles, tiles in Morton
-    // order, so the particles a block works on sit next to each other.
-    uint32_t bin = 0xFFFFFFFFu;
-    if (valid) {
-        float h = __ldg(&tanks[tank].h);
-        uint32_t axis_mask = (1u << schedule.tile_bits) - 1u;
-        uint32_t tx = (static_cast<uint32_t>(cell_coord(position.x, h)) >> 2) & axis_mask;
-        uint32_t ty = (static_cast<uint32_t>(cell_coord(position.y, h)) >> 2) & axis_mask;
-        uint32_t tz = (static_cast<uint32_t>(cell_coord(position.z, h)) >> 2) & axis_mask;
-        bin = (tank << (3 * schedule.tile_bits)) + (spread3(tx) | (spread3(ty) << 1) | (spread3(tz) << 2));
-        schedule.tile_of[p] = bin;
+    uint32_t key = sorted_keys[p];
+    if (p == 0 || sorted_keys[p - 1] != key) {
+        bucket_words[2 * static_cast<size_t>(key)] = p;
     }
-    uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
-    if (valid && (threadIdx.x & 31) == static_cast<uint32_t>(__ffs(peers) - 1)) {
-        atomicAdd(&schedule.tile_hist[bin], static_cast<uint32_t>(__popc(peers)));
+    if (p + 1 == n || sorted_keys[p + 1] != key) {
+        bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
+    }
+    uint32_t i = sorted_ids[p];
+    spos[p] = pos[i];
+    svel[p] = vel[i];
+    if (tank_of != nullptr) {
+        stank[p] = tank_of[i];
+    }
+    if (schedule.rank != nullptr) {
+        schedule.order[schedule.rank[i]] = p;
     }
 }
 
-// Scatters sorted positions into the processing order: lanes with the same
-// tile take one contiguous range (one atomic per group), keeping a cell's
-// particles adjacent.
-__global__ void __launch_bounds__(256) schedule_scatter_kernel(uint32_t n, Schedule schedule) {
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool valid = p < n;
-    uint32_t bin = valid ? schedule.tile_of[p] : 0xFFFFFFFFu;
-    uint32_t peers = __match_any_sync(0xFFFFFFFFu, bin);
-    uint32_t leader = static_cast<uint32_t>(__ffs(peers) - 1);
-    uint32_t lane = threadIdx.x & 31;
-    uint32_t base = 0;
-    if (valid && lane == leader) {
-        base = atomicAdd(&schedule.tile_hist[bin], static_cast<uint32_t>(__popc(peers)));
-    }
-    base = __shfl_sync(0xFFFFFFFFu, base, static_cast<int>(leader));
-    if (valid) {
-        schedule.order[base + static_cast<uint32_t>(__popc(peers & lanemask_lt()))] = p;
+// Processing slot of every particle id: the inverse of the Morton-sorted ids.
+__global__ void __launch_bounds__(256) rank_kernel(const uint32_t* __restrict__ sorted_ids, uint32_t n,
+                                                   uint32_t* __restrict__ rank) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        rank[sorted_ids[t]] = t;
     }
 }
 
@@ -302,35 +269,67 @@ __host__ __device__ inline SweepLayout sweep_layout(unsigned long long* base, ui
 constexpr uint32_t kKeysThreads = 1024;
 constexpr uint32_t kKeysItems = kSweepTile / kKeysThreads;
 
+// Morton code of a particle's cell for the processing order: the grid's own
+// cell (so a cell's particles stay together), offset from the cell of the
+// tank's low corner and clamped to `bits` bits per axis, the tank index
+// above them.
+__device__ __forceinline__ uint32_t morton_key(float4 p, const TankConst* t, uint32_t tank, uint32_t bits) {
+    const float h = __ldg(&t->h);
+    const int limit = static_cast<int>((1u << bits) - 1u);
+    const int cx = min(max(cell_coord(p.x, h) - cell_coord(__ldg(&t->low[0]), h), 0), limit);
+    const int cy = min(max(cell_coord(p.y, h) - cell_coord(__ldg(&t->low[1]), h), 0), limit);
+    const int cz = min(max(cell_coord(p.z, h) - cell_coord(__ldg(&t->low[2]), h), 0), limit);
+    return (tank << (3 * bits)) | spread3(static_cast<uint32_t>(cx)) | (spread3(static_cast<uint32_t>(cy)) << 1) |
+           (spread3(static_cast<uint32_t>(cz)) << 2);
+}
+
+// kMorton false: the spatial-hash bucket keys of the grid (spread evenly over
+// the digits); true: Morton keys of the processing order, whose high digits
+// bunch up, so the lanes of a warp with the same digit add their counts with
+// one atomic.
+template <bool kMorton>
 __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* __restrict__ pos,
                                                                  const uint16_t* __restrict__ tank_of,
                                                                  const TankConst* __restrict__ tanks, uint32_t n,
                                                                  uint32_t* __restrict__ keys, uint32_t passes,
                                                                  uint32_t* __restrict__ tile_counts,
-                                                                 uint32_t* __restrict__ hist) {
+                                                                 uint32_t* __restrict__ hist, uint32_t morton_bits) {
     __shared__ uint32_t counts[kSweepMaxPasses][kSweepBins];
     for (uint32_t k = threadIdx.x; k < kSweepMaxPasses * kSweepBins; k += blockDim.x) {
         (&counts[0][0])[k] = 0;
     }
     const uint32_t first = blockIdx.x * kSweepTile;
     float4 p[kKeysItems];
-    const TankConst* t[kKeysItems];
+    uint32_t tank[kKeysItems];
 #pragma unroll
     for (uint32_t r = 0; r < kKeysItems; ++r) {
         const uint32_t i = first + r * kKeysThreads + threadIdx.x;
         p[r] = i < n ? pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        t[r] = tanks + (tank_of != nullptr && i < n ? tank_of[i] : 0);
+        tank[r] = tank_of != nullptr && i < n ? tank_of[i] : 0;
     }
     __syncthreads();
 #pragma unroll
     for (uint32_t r = 0; r < kKeysItems; ++r) {
         const uint32_t i = first + r * kKeysThreads + threadIdx.x;
-        if (i < n) {
-            const float h = __ldg(&t[r]->h);
+        const TankConst* t = tanks + tank[r];
+        if (kMorton) {
+            const uint32_t key = morton_key(p[r], t, tank[r], morton_bits);
+            if (i < n) {
+                keys[i] = key;
+            }
+            for (uint32_t pass = 0; pass < passes; ++pass) {
+                const uint32_t digit = i < n ? (key >> (pass * kSweepBits)) & (kSweepBins - 1) : 0xFFFFFFFFu;
+                const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+                if (i < n && (threadIdx.x & 31) == static_cast<uint32_t>(__ffs(peers) - 1)) {
+                    atomicAdd(&counts[pass][digit], static_cast<uint32_t>(__popc(peers)));
+                }
+            }
+        } else if (i < n) {
+            const float h = __ldg(&t->h);
             uint32_t cx = static_cast<uint32_t>(cell_coord(p[r].x, h));
             uint32_t cy = static_cast<uint32_t>(cell_coord(p[r].y, h));
             uint32_t cz = static_cast<uint32_t>(cell_coord(p[r].z, h));
-            uint32_t key = __ldg(&t[r]->bucket_base) + spatial_hash(cx, cy, cz, __ldg(&t[r]->cell_mask));
+            const uint32_t key = __ldg(&t->bucket_base) + spatial_hash(cx, cy, cz, __ldg(&t->cell_mask));
             keys[i] = key;
             for (uint32_t pass = 0; pass < passes; ++pass) {
                 atomicAdd(&counts[pass][(key >> (pass * kSweepBits)) & (kSweepBins - 1)], 1u);
@@ -349,7 +348,10 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
     }
 }
 
-// One stable digit pass over tile blockIdx.x.
+// One stable digit pass over tile blockIdx.x. kAggregate: the lanes of a warp
+// that add to the same next-pass tile count add once (keys whose digits bunch
+// up); otherwise every key adds its own 1 (keys spread evenly).
+template <bool kAggregate>
 __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift, const uint32_t* __restrict__ hist,
@@ -443,15 +445,23 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
     __syncthreads();
 #pragma unroll
     for (uint32_t r = 0; r < kSweepItems; ++r) {
-        if (rank[r] != 0xFFFFFFFFu) {
+        const bool valid = rank[r] != 0xFFFFFFFFu;
+        uint32_t slot = 0xFFFFFFFFu;  // next-pass count this key adds to
+        if (valid) {
             uint32_t digit = (key[r] >> shift) & (kSweepBins - 1);
             uint32_t dst = digit_offset[digit] + warp_counts[warp][digit] + rank[r];
             keys_out[dst] = key[r];
             vals_out[dst] = val[r];
-            if (next_counts != nullptr) {
-                atomicAdd(&next_counts[static_cast<size_t>(dst / kSweepTile) * kSweepBins +
-                                       ((key[r] >> next_shift) & (kSweepBins - 1))],
-                          1u);
+            slot = (dst / kSweepTile) * kSweepBins + ((key[r] >> next_shift) & (kSweepBins - 1));
+        }
+        if (next_counts != nullptr) {
+            if (kAggregate) {
+                const uint32_t peers = __match_any_sync(0xFFFFFFFFu, slot);
+                if (valid && lane == static_cast<uint32_t>(__ffs(peers) - 1)) {
+                    atomicAdd(&next_counts[slot], static_cast<uint32_t>(__popc(peers)));
+                }
+            } else if (valid) {
+                atomicAdd(&next_counts[slot], 1u);
             }
         }
     }
@@ -465,23 +475,66 @@ size_t onesweep_scratch_words(uint32_t n, uint32_t passes) {
     return (words32 + 1) / 2;
 }
 
-cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
-                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream) {
-    if (n == 0) {
-        return cudaSuccess;
-    }
+namespace {
+
+cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                            uint32_t* keys, uint32_t passes, unsigned long long* sweep, uint32_t morton_bits,
+                            cudaStream_t stream) {
     cudaError_t err = cudaMemsetAsync(sweep, 0, onesweep_scratch_words(n, passes) * sizeof(unsigned long long), stream);
     if (err != cudaSuccess) {
         return err;
     }
     const uint32_t tiles = sweep_tiles(n);
     SweepLayout l = sweep_layout(sweep, tiles, passes);
-    keys_hist_kernel<<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes, l.tile_counts, l.hist);
+    if (morton_bits != 0) {
+        keys_hist_kernel<true><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes, l.tile_counts,
+                                                                   l.hist, morton_bits);
+    } else {
+        keys_hist_kernel<false><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes,
+                                                                    l.tile_counts, l.hist, 0);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    return keys_and_counts(pos, tank_of, tanks, n, keys, passes, sweep, 0, stream);
+}
+
+cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                               uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
+                               unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    if (morton_bits == 0 || morton_bits > 10 || key_bits > 32) {
+        return cudaErrorInvalidValue;
+    }
+    const uint32_t passes = onesweep_passes(key_bits);
+    if (passes > kSweepMaxPasses) {
+        return cudaErrorInvalidValue;
+    }
+    cudaError_t err = keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, stream);
+    if (err == cudaSuccess) {
+        err = launch_onesweep_sort(scratch, n, passes, sweep, stream, launches, true);
+    }
+    if (err != cudaSuccess) {
+        return err;
+    }
+    rank_kernel<<<(n + 255) / 256, 256, 0, stream>>>(scratch.sorted_ids, n, rank);
+    if (launches != nullptr) {
+        *launches += 2;
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_onesweep_sort(GridScratch& s, uint32_t n, uint32_t passes, unsigned long long* sweep,
-                                 cudaStream_t stream, uint32_t* launches) {
+                                 cudaStream_t stream, uint32_t* launches, bool aggregate) {
     if (n == 0) {
         s.sorted_keys = s.keys_a;
         s.sorted_ids = s.vals_a;
@@ -495,9 +548,15 @@ cudaError_t launch_onesweep_sort(GridScratch& s, uint32_t n, uint32_t passes, un
     uint32_t* vout = s.vals_a;
     for (uint32_t p = 0; p < passes; ++p) {
         uint32_t* next = p + 1 < passes ? l.tile_counts + static_cast<size_t>(p + 1) * tiles * kSweepBins : nullptr;
-        sweep_scatter_kernel<<<tiles, kSweepThreads, 0, stream>>>(
-            kin, vin, kout, vout, n, p * kSweepBits, l.hist + static_cast<size_t>(p) * kSweepBins,
-            l.tile_counts + static_cast<size_t>(p) * tiles * kSweepBins, next, (p + 1) * kSweepBits);
+        const uint32_t* counts = l.tile_counts + static_cast<size_t>(p) * tiles * kSweepBins;
+        const uint32_t* hist = l.hist + static_cast<size_t>(p) * kSweepBins;
+        if (aggregate) {
+            sweep_scatter_kernel<true><<<tiles, kSweepThreads, 0, stream>>>(kin, vin, kout, vout, n, p * kSweepBits,
+                                                                            hist, counts, next, (p + 1) * kSweepBits);
+        } else {
+            sweep_scatter_kernel<false><<<tiles, kSweepThreads, 0, stream>>>(kin, vin, kout, vout, n, p * kSweepBits,
+                                                                             hist, counts, next, (p + 1) * kSweepBits);
+        }
         if (launches != nullptr) {
             *launches += 1;
         }
@@ -586,23 +645,13 @@ cudaError_t launch_radix_sort(GridScratch& s, uint32_t n, const RadixPlan& plan,
 
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
-                                 float4* svel, uint16_t* stank, const TankConst* tanks, const Schedule& schedule,
-                                 cudaStream_t stream) {
+                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream) {
     if (n == 0) {
         return cudaSuccess;
     }
     bounds_gather_kernel<<<(n + 255) / 256, 256, 0, stream>>>(sorted_keys, sorted_ids, n,
                                                               reinterpret_cast<uint32_t*>(bucket), pos, vel, tank_of,
-                                                              spos, svel, stank, tanks, schedule);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_schedule(uint32_t n, const Schedule& schedule, cudaStream_t stream) {
-    if (n == 0 || schedule.tile_of == nullptr) {
-        return cudaSuccess;
-    }
-    scan_exclusive_block<<<1, 1024, 0, stream>>>(schedule.tile_hist, schedule.bins);
-    schedule_scatter_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, schedule);
+                                                              spos, svel, stank, schedule);
     return cudaGetLastError();
 }
 

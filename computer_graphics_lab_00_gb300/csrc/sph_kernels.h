@@ -74,31 +74,38 @@ size_t onesweep_scratch_words(uint32_t n, uint32_t passes);
 // digit histogram; zeroes the scratch first.
 cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                                  uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream);
-// The digit passes over keys made by launch_keys_onesweep.
+// The digit passes over keys made by launch_keys_onesweep. aggregate: one
+// atomic per group of lanes adding to the same count (keys whose digits bunch
+// up, as Morton codes of a compact body do).
 cudaError_t launch_onesweep_sort(GridScratch& scratch, uint32_t n, uint32_t passes, unsigned long long* sweep,
-                                 cudaStream_t stream, uint32_t* launches);
+                                 cudaStream_t stream, uint32_t* launches, bool aggregate = false);
 
-// Processing order of the neighbour passes. When tile_of is null the passes
-// run in sorted (bucket) order; otherwise bounds_gather bins every particle
-// into a Morton-ordered tile of 4 x 4 x 4 cells (tile_bits bits per axis,
-// per tank) and launch_schedule turns the bins into `order`.
+// Processing order of the neighbour passes. When rank is null the passes run
+// in sorted (bucket) order. Otherwise rank is a permutation over particle ids
+// (the slot of each id in a Morton order of the cells, made by
+// launch_morton_rank every few substeps) and bounds_gather writes, for the
+// particle at sorted position p with id i, order[rank[i]] = p. The results do
+// not depend on the order: every particle's sums run over the same pairs in
+// the same sequence whichever thread computes them.
 struct Schedule {
-    uint32_t* tile_of = nullptr;    // n: bin of each sorted position
-    uint32_t* tile_hist = nullptr;  // bins: counts, then running offsets
-    uint32_t* order = nullptr;      // n: sorted positions in processing order
-    uint32_t tile_bits = 5;
-    uint32_t bins = 0;
+    const uint32_t* rank = nullptr;  // n: processing slot of each particle id
+    uint32_t* order = nullptr;       // n: sorted positions in processing order
 };
 
+// Morton keys of the particles' cells (morton_bits bits per axis, counted
+// from each tank's low corner and clamped, the tank index above them), sorted
+// with the one-kernel passes in the sort buffers of `scratch` (a copy: the
+// caller's grid pointers stay as they were), then rank[id] = slot.
+cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                               uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
+                               unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches);
+
 // Bucket table (start, end) from sorted keys (table pre-zeroed), the
-// cell-ordered copies of position, velocity and tank id, and (optionally) the
-// tile histogram of the processing order (tile_hist pre-zeroed).
+// cell-ordered copies of position, velocity and tank id, and (with a
+// schedule) the processing order.
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
-                                 float4* svel, uint16_t* stank, const TankConst* tanks, const Schedule& schedule,
-                                 cudaStream_t stream);
-// Scan of the tile histogram and scatter into schedule.order.
-cudaError_t launch_schedule(uint32_t n, const Schedule& schedule, cudaStream_t stream);
+                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream);
 
 // Shape of the neighbour passes. variant 0: one thread per particle with
 // nested bucket loops; 1: flat candidate stream (density) and the queued pair
@@ -156,8 +163,9 @@ cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_
 // (force[p], sorted order) and the 32 correction features (row p, or row
 // sorted_ids[p] when id_order). Needs the variant-4 pair masks of density.
 cudaError_t launch_features(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
-                            const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* masks,
-                            float4* force, float* features, bool id_order, cudaStream_t stream);
+                            const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* order,
+                            const uint32_t* masks, float4* force, float* features, bool id_order,
+                            cudaStream_t stream);
 // Second half: acceleration = plain + correction[p] (null: none), then the
 // plain step's velocity update, clamp, walls and id-order write.
 cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,

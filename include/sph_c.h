@@ -131,7 +131,7 @@ typedef struct sph_tuning {
                                   4: density stores per-bucket pair masks, integrate expands them */
     uint32_t block_size;       /* threads per block of integrate (32..512, multiple of 32; 64/128/256 for 2-4) */
     uint32_t queue_depth;      /* in-range pairs buffered per thread: 8, 16, 24 or 32 */
-    uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 Morton order of 4x4x4-cell tiles */
+    uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 (default) Morton order of the cells, remade every 8 grid builds */
     uint32_t sort;             /* grid sort: 0 three kernels per digit pass (radix_bits wide);
                                   1 one kernel per 8-bit pass, tile offsets from tile digit counts
                                     made by the previous pass (radix_bits unused) */

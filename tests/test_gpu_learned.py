@@ -21,9 +21,11 @@ def small():
     return T.learned_tanks(tanks=4, particles=4096, seed=2)
 
 
-def test_zero_correction_is_the_plain_step(native, oracle, small):
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_zero_correction_is_the_plain_step(native, oracle, small, schedule):
     a = T.load_tanks(small)
     b = T.load_tanks(small)
+    a.set_tuning(schedule=schedule)
     a.run_learned(T.COARSE_DT, 3, None)
     b.run(T.COARSE_DT, 3)
     for t in range(small.counts.__len__()):
@@ -55,6 +57,23 @@ def test_features_are_finite_and_plausible(native, small):
     assert 5 < np.median(pairs) < 60
     assert (f[:, 26:] >= 0).all() and (f[:, 26:] <= 4).all()
     s.close()
+
+
+def test_features_do_not_depend_on_the_processing_order(native, small):
+    """Sorted and Morton processing orders give the same feature bits."""
+    import torch
+
+    got = []
+    for schedule in (0, 1):
+        s = T.load_tanks(small)
+        s.set_tuning(schedule=schedule)
+        s.run(T.FINE_DT, 20)
+        f = torch.empty((s.total_particles, 32), dtype=torch.float32, device="cuda")
+        s.learned_features(T.COARSE_DT, f.data_ptr())
+        s.synchronize()
+        got.append(f.cpu().numpy())
+        s.close()
+    assert same(got[0], got[1])
 
 
 def test_pipeline_end_to_end(native, small, tmp_path):

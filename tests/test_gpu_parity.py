@@ -290,6 +290,33 @@ def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     assert_bit_exact(gv, ov, f"velocities {tuning}")
 
 
+def test_morton_order_across_remakes_and_count_changes(native, oracle):
+    """The Morton processing order is remade every 16 grid builds, after an
+    upload and after a change of particle count; the bits stay the oracle's
+    throughout, through graph runs and the direct grid build."""
+    n = 8192
+    dt = 1.0 / 600.0
+    params, pos, vel = small_block(n, (16, 16, 32), box=(0.5, 0.8, 0.8), cells=W.cell_count_for(n))
+    threads = oracle.hardware_threads
+    with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(schedule=1)
+        solver.upload(pos, vel)
+        solver.run(dt, 15)
+        solver.build_grid()
+        solver.run(dt, 22)
+        gp, gv = solver.state()
+        op, ov = oracle.run_substeps(params, pos, vel, dt, 37, threads=threads)
+        assert_bit_exact(gp, op, "positions after 37 substeps")
+        assert_bit_exact(gv, ov, "velocities after 37 substeps")
+        m = 5000
+        solver.upload(op[:m], ov[:m])
+        solver.run(dt, 18)
+        gp, gv = solver.state()
+        op, ov = oracle.run_substeps(params, op[:m], ov[:m], dt, 18, threads=threads)
+        assert_bit_exact(gp, op, "positions after the count change")
+        assert_bit_exact(gv, ov, "velocities after the count change")
+
+
 @pytest.mark.parametrize("sort,bits", [(1, 6), (0, 5), (0, 8)])
 def test_grid_sorts_agree_at_one_million(native, oracle, sort, bits):
     """The one-sweep sort (3 look-back passes over 21-bit keys at 1M) and the
