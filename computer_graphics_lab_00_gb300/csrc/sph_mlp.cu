@@ -131,22 +131,37 @@ __device__ __forceinline__ void store_chunk(uint8_t* base, uint32_t offset, cons
     *reinterpret_cast<uint4*>(base + offset) = q;
 }
 
-// erf by Abramowitz & Stegun 7.1.26 (Handbook of Mathematical Functions,
-// 1964): 1 - (a1 t + ... + a5 t^5) exp(-x^2), t = 1 / (1 + p |x|), absolute
-// error at most 1.5e-7 — far below the BF16 rounding the activations get
-// next (plus a few ulp of __expf). Checked against erff by
-// sph_mlp_selftest_erf.
-__device__ __forceinline__ float erf_as(float x) {
-    float ax = fabsf(x);
-    float t = __frcp_rn(fmaf(0.3275911f, ax, 1.0f));
-    float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f), -0.284496736f),
-                          0.254829592f);
-    float y = 1.0f - poly * __expf(-ax * ax);
-    return copysignf(y, x);
+// Abramowitz & Stegun 7.1.28 (Handbook of Mathematical Functions, 1964, after
+// Hastings): for x >= 0, erf(x) = 1 - r with r = (1 + a1 x + ... + a6 x^6)^-16
+// and |error| <= 3e-7. One approximate reciprocal (an exact 1 for x past ~13,
+// where the 16th power overflows to infinity) and no exponential, so the
+// epilogue issues one special-function op per activation. Evaluated in FP32 the
+// error against erff stays under 2e-6 (the 16th power scales the rounding of
+// the polynomial); the activations are rounded to BF16 (relative step 2^-8)
+// right after. Checked by sph_mlp_selftest_erf.
+__device__ __forceinline__ float erfc_power(float ax) {
+    float s = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(4.30638e-5f, ax, 2.765672e-4f), ax, 1.520143e-4f), ax, 9.2705272e-3f), ax,
+                             4.22820123e-2f),
+                        ax, 7.05230784e-2f),
+                   ax, 1.0f);
+    s = s * s;
+    s = s * s;
+    s = s * s;
+    s = s * s;
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+    return r;
 }
 
-// GELU of the forward pass (erf form through erf_as).
-__device__ __forceinline__ float gelu_fast(float z) { return 0.5f * z * (1.0f + erf_as(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float erf_as(float x) { return copysignf(1.0f - erfc_power(fabsf(x)), x); }
+
+// GELU of the forward pass, erf form: with r as above at |z| / sqrt(2),
+// 1 + erf(z / sqrt(2)) is 2 - r for z >= 0 and r for z < 0, so the negative
+// side keeps its relative accuracy (no 1 - (1 - r) cancellation).
+__device__ __forceinline__ float gelu_fast(float z) {
+    const float m = 0.5f * z * erfc_power(fabsf(z) * 0.70710678118654752f);
+    return z >= 0.0f ? z - m : m;
+}
 
 constexpr uint32_t kForwardThreads = 512;
 constexpr uint32_t kGroups = kForwardThreads / 128;  // threads sharing one row's epilogue

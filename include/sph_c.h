@@ -463,7 +463,7 @@ int sph_mlp_stream(sph_mlp* mlp, void** stream);
  * fluid path); the update rule is adamStep (src/gfx/neural_math.cpp:1177-1208). */
 int sph_mlp_apply_gradients(sph_mlp* mlp, const float* grads, float learning_rate);
 /* Diagnostic: largest |erf(x) - erff(x)| of the forward pass's erf
- * (Abramowitz & Stegun 7.1.26) over `count` points on [-6, 6]. */
+ * (Abramowitz & Stegun 7.1.28) over `count` points on [-6, 6]. */
 int sph_mlp_selftest_erf(sph_mlp* mlp, uint32_t count, float* max_abs_error);
 
 /* Learned coarse substeps (no counterpart in the reference): the plain SPH

@@ -124,11 +124,13 @@ def test_training_fits_a_smooth_target(native, torch_cuda):
 
 
 def test_forward_erf_is_within_its_published_bound(native):
-    """The forward pass evaluates GELU's erf by Abramowitz & Stegun 7.1.26
-    (absolute error 1.5e-7) with the fast exponential (__expf, a few ulp);
-    against erff the sum must stay below 1e-6, four orders under the BF16
-    rounding the activation gets next."""
+    """The forward pass evaluates GELU's erf by Abramowitz & Stegun 7.1.28
+    (absolute error 3e-7) with one approximate reciprocal; in FP32 the 16th
+    power scales the polynomial's rounding, and a float32 evaluation of the
+    same steps stays under 1.8e-6 against the exact erf. Against erff the
+    GPU must stay below 2.5e-6, three orders under the BF16 rounding the
+    activation gets next."""
     from computer_graphics_lab_00_gb300.learned import MlpGpu
 
     with MlpGpu() as mlp:
-        assert mlp.selftest_erf() < 1e-6
+        assert mlp.selftest_erf() < 2.5e-6
