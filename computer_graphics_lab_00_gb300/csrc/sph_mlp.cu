@@ -115,7 +115,17 @@ constexpr uint32_t kSmemW3 = kSmemW2 + kHidden * kHidden * 2;    // +32 KB
 constexpr uint32_t kSmemX = kSmemW3 + kOutPad * kHidden * 2;     // +4 KB
 constexpr uint32_t kSmemH = kSmemX + kTile * kIn * 2;            // +8 KB
 constexpr uint32_t kSmemBar = kSmemH + kTile * kHidden * 2;      // +32 KB
-constexpr uint32_t kSmemBytes = kSmemBar + 64;
+// Small FP32 vectors, staged once per CTA: b1, b2, input mean, input 1/std,
+// b3 and the output scale (each padded to whole float4s).
+constexpr uint32_t kVecB1 = 0;
+constexpr uint32_t kVecB2 = kVecB1 + kHidden;
+constexpr uint32_t kVecMean = kVecB2 + kHidden;
+constexpr uint32_t kVecInvStd = kVecMean + kIn;
+constexpr uint32_t kVecB3 = kVecInvStd + kIn;
+constexpr uint32_t kVecScale = kVecB3 + 4;
+constexpr uint32_t kVecFloats = kVecScale + 4;
+constexpr uint32_t kSmemVec = kSmemBar + 64;
+constexpr uint32_t kSmemBytes = kSmemVec + kVecFloats * 4;
 constexpr uint32_t kTmemCols = 128;
 
 __device__ __forceinline__ void store_chunk(uint8_t* base, uint32_t offset, const float* v8) {
@@ -206,6 +216,24 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
         *reinterpret_cast<uint4*>(smem + kSmemW3 + tile_offset(row, chunk, kHidden)) =
             *reinterpret_cast<const uint4*>(model.w3 + row * kHidden + chunk * 8);
     }
+    float* vec = reinterpret_cast<float*>(smem + kSmemVec);
+    for (uint32_t i = tid; i < kVecFloats; i += blockDim.x) {
+        float v = 0.0f;
+        if (i < kVecB2) {
+            v = model.params[kB1 + i];
+        } else if (i < kVecMean) {
+            v = model.params[kB2 + (i - kVecB2)];
+        } else if (i < kVecInvStd) {
+            v = model.in_mean[i - kVecMean];
+        } else if (i < kVecB3) {
+            v = model.in_inv_std[i - kVecInvStd];
+        } else if (i < kVecScale) {
+            v = i - kVecB3 < static_cast<uint32_t>(kOut) ? model.params[kB3 + (i - kVecB3)] : 0.0f;
+        } else {
+            v = i - kVecScale < static_cast<uint32_t>(kOut) ? model.out_scale[i - kVecScale] : 0.0f;
+        }
+        vec[i] = v;
+    }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(kTmemCols)
@@ -222,9 +250,12 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const uint32_t lane_base = (quarter * 32u) << 16;
-    const float* b1 = model.params + kB1;
-    const float* b2 = model.params + kB2;
-    const float* b3 = model.params + kB3;
+    const float* b1 = vec + kVecB1;
+    const float* b2 = vec + kVecB2;
+    const float* b3 = vec + kVecB3;
+    const float* in_mean = vec + kVecMean;
+    const float* in_inv_std = vec + kVecInvStd;
+    const float* out_scale = vec + kVecScale;
     const uint32_t sX = smem_u32(smem + kSmemX);
     const uint32_t sH = smem_u32(smem + kSmemH);
     const uint32_t sW1 = smem_u32(smem + kSmemW1);
@@ -236,22 +267,38 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     bool failed = false;
     const uint32_t tiles = (n + kTile - 1) / kTile;
 
+    // Each thread converts one 8-feature chunk of its row; the next tile's
+    // chunk is loaded while this tile runs its three layers.
+    static_assert((kIn / 8) / kGroups == 1, "one 8-feature chunk per thread");
+    const uint32_t chunk = group;
+    auto fetch = [&](uint32_t t, float4& a, float4& b) {
+        const uint32_t r = t * kTile + local_row;
+        if (t < tiles && r < n) {
+            const float4* frow = reinterpret_cast<const float4*>(features + static_cast<size_t>(r) * kIn);
+            a = __ldg(&frow[2 * chunk]);
+            b = __ldg(&frow[2 * chunk + 1]);
+        } else {
+            a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            b = a;
+        }
+    };
+    float4 next_a;
+    float4 next_b;
+    fetch(blockIdx.x, next_a, next_b);
+
     for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const uint32_t row = tile * kTile + local_row;
         const bool valid = row < n;
-        // Normalised features -> BF16 tile; each thread converts 16 of its row's 32.
-        const float4* frow = reinterpret_cast<const float4*>(features + static_cast<size_t>(row) * kIn);
-#pragma unroll
-        for (uint32_t j = 0; j < (kIn / 8) / kGroups; ++j) {
-            uint32_t chunk = group * ((kIn / 8) / kGroups) + j;
+        const float4 a = next_a;
+        const float4 b = next_b;
+        fetch(tile + gridDim.x, next_a, next_b);
+        {
             float v[8];
-            float4 a = valid ? frow[2 * chunk] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            float4 b = valid ? frow[2 * chunk + 1] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             const float raw[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
             for (uint32_t k = 0; k < 8; ++k) {
                 uint32_t f = chunk * 8 + k;
-                v[k] = valid ? (raw[k] - model.in_mean[f]) * model.in_inv_std[f] : 0.0f;
+                v[k] = valid ? (raw[k] - in_mean[f]) * in_inv_std[f] : 0.0f;
             }
             store_chunk(smem + kSmemX, tile_offset(local_row, chunk, kIn), v);
             if (kSave && valid) {
@@ -287,9 +334,18 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
             uint32_t c = group * ((kHidden / 16) / kGroups) + j;
             float v[16];
             tmem_load16(tmem + lane_base + c * 16u, v);
+            float bias[16];
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                const float4 b4 = reinterpret_cast<const float4*>(b1 + c * 16)[q];
+                bias[4 * q] = b4.x;
+                bias[4 * q + 1] = b4.y;
+                bias[4 * q + 2] = b4.z;
+                bias[4 * q + 3] = b4.w;
+            }
 #pragma unroll
             for (uint32_t k = 0; k < 16; ++k) {
-                float z = v[k] + b1[c * 16 + k];
+                float z = v[k] + bias[k];
                 if (kSave && valid) {
                     saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
                 }
@@ -330,9 +386,18 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
             uint32_t c = group * ((kHidden / 16) / kGroups) + j;
             float v[16];
             tmem_load16(tmem + lane_base + c * 16u, v);
+            float bias[16];
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                const float4 b4 = reinterpret_cast<const float4*>(b2 + c * 16)[q];
+                bias[4 * q] = b4.x;
+                bias[4 * q + 1] = b4.y;
+                bias[4 * q + 2] = b4.z;
+                bias[4 * q + 3] = b4.w;
+            }
 #pragma unroll
             for (uint32_t k = 0; k < 16; ++k) {
-                float z = v[k] + b2[c * 16 + k];
+                float z = v[k] + bias[k];
                 if (kSave && valid) {
                     saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
                 }
@@ -380,7 +445,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
                 }
                 if (out != nullptr) {
                     reinterpret_cast<float4*>(out)[row] =
-                        make_float4(y0 * model.out_scale[0], y1 * model.out_scale[1], y2 * model.out_scale[2], 0.0f);
+                        make_float4(y0 * out_scale[0], y1 * out_scale[1], y2 * out_scale[2], 0.0f);
                 }
             }
         }
