@@ -1102,11 +1102,19 @@ __device__ __forceinline__ float div_by(float x, float y, float r) {
     return __fmaf_rn(e, r, q);
 }
 
+// Intermediates of one pair that the learned step's features reuse.
+struct PairParts {
+    float ex, ey, ez;  // x_i - x_j
+    float distance;
+    float dvx, dvy, dvz;  // v_j - v_i
+};
+
 // Pair force with the two shared reciprocals (1/distance, 1/rho_j); the same
-// operations and order as add_pair_force.
+// operations and order as add_pair_force. `parts` receives the offset,
+// distance and velocity difference it computed on the way.
 __device__ __forceinline__ void add_pair_force_rcp(const PairConst& k, const float4& self, float vx, float vy, float vz,
                                                    float pressure, const float4& other, const float4& ov, float& fx,
-                                                   float& fy, float& fz) {
+                                                   float& fy, float& fz, PairParts& parts) {
     float ex = __fsub_rn(self.x, other.x);
     float ey = __fsub_rn(self.y, other.y);
     float ez = __fsub_rn(self.z, other.z);
@@ -1123,9 +1131,26 @@ __device__ __forceinline__ void add_pair_force_rcp(const PairConst& k, const flo
     fy = __fadd_rn(fy, __fmul_rn(ps, __fmul_rn(gs, div_by(ey, distance, inv_distance))));
     fz = __fadd_rn(fz, __fmul_rn(ps, __fmul_rn(gs, div_by(ez, distance, inv_distance))));
     float lap = __fmul_rn(k.c_visc, d);
-    fx = __fadd_rn(fx, __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.x, vx)), other_density, inv_density), lap));
-    fy = __fadd_rn(fy, __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.y, vy)), other_density, inv_density), lap));
-    fz = __fadd_rn(fz, __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.z, vz)), other_density, inv_density), lap));
+    const float dvx = __fsub_rn(ov.x, vx);
+    const float dvy = __fsub_rn(ov.y, vy);
+    const float dvz = __fsub_rn(ov.z, vz);
+    fx = __fadd_rn(fx, __fmul_rn(div_by(__fmul_rn(k.visc_mass, dvx), other_density, inv_density), lap));
+    fy = __fadd_rn(fy, __fmul_rn(div_by(__fmul_rn(k.visc_mass, dvy), other_density, inv_density), lap));
+    fz = __fadd_rn(fz, __fmul_rn(div_by(__fmul_rn(k.visc_mass, dvz), other_density, inv_density), lap));
+    parts.ex = ex;
+    parts.ey = ey;
+    parts.ez = ez;
+    parts.distance = distance;
+    parts.dvx = dvx;
+    parts.dvy = dvy;
+    parts.dvz = dvz;
+}
+
+__device__ __forceinline__ void add_pair_force_rcp(const PairConst& k, const float4& self, float vx, float vy, float vz,
+                                                   float pressure, const float4& other, const float4& ov, float& fx,
+                                                   float& fy, float& fz) {
+    PairParts unused;
+    add_pair_force_rcp(k, self, vx, vy, vz, pressure, other, ov, fx, fy, fz, unused);
 }
 
 template <int kBlock, bool kRcp>
@@ -1450,33 +1475,42 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
         f[q] = 0.0f;
     }
     uint32_t pairs = 0;
+    // The feature sums reuse the pair force's offset, distance and velocity
+    // difference (u = -e / h, |u| = distance / h) and leave the constant
+    // factors (D / h, 1 / (k rho0), 1 / rho0) to the end; the features are
+    // MLP inputs, rounded to BF16, so their sums use FMA.
+    const float neg_inv_h = -inv_h;
     auto visit = [&](uint32_t q) {
         float4 other = __ldg(&spos2[q]);
         float4 ov = __ldg(&svel[q]);
-        add_pair_force_rcp(k, self, sv.x, sv.y, sv.z, sv.w, other, ov, fx, fy, fz);
-        float ux = (other.x - self.x) * inv_h;
-        float uy = (other.y - self.y) * inv_h;
-        float uz = (other.z - self.z) * inv_h;
-        float r = sqrtf(ux * ux + uy * uy + uz * uz);
-        float w = (1.0f - r) * (1.0f - r);
+        PairParts e;
+        add_pair_force_rcp(k, self, sv.x, sv.y, sv.z, sv.w, other, ov, fx, fy, fz, e);
+        const float ux = e.ex * neg_inv_h;
+        const float uy = e.ey * neg_inv_h;
+        const float uz = e.ez * neg_inv_h;
+        const float om = 1.0f - e.distance * inv_h;
+        const float w = om * om;
+        const float wx = w * ux;
+        const float wy = w * uy;
+        const float wz = w * uz;
         f[9] += w;
-        f[10] += w * ux;
-        f[11] += w * uy;
-        f[12] += w * uz;
-        f[13] += w * (ov.x - sv.x) * vscale;
-        f[14] += w * (ov.y - sv.y) * vscale;
-        f[15] += w * (ov.z - sv.z) * vscale;
-        f[16] += w * ux * ux;
-        f[17] += w * uy * uy;
-        f[18] += w * uz * uz;
-        f[19] += w * ux * uy;
-        f[20] += w * ux * uz;
-        f[21] += w * uy * uz;
-        float dp = (ov.w - sv.w) * inv_prho;
-        f[22] += w * dp * ux;
-        f[23] += w * dp * uy;
-        f[24] += w * dp * uz;
-        f[25] += w * (other.w - self.w) / rho0;
+        f[10] += wx;
+        f[11] += wy;
+        f[12] += wz;
+        f[13] = fmaf(w, e.dvx, f[13]);
+        f[14] = fmaf(w, e.dvy, f[14]);
+        f[15] = fmaf(w, e.dvz, f[15]);
+        f[16] = fmaf(wx, ux, f[16]);
+        f[17] = fmaf(wy, uy, f[17]);
+        f[18] = fmaf(wz, uz, f[18]);
+        f[19] = fmaf(wx, uy, f[19]);
+        f[20] = fmaf(wx, uz, f[20]);
+        f[21] = fmaf(wy, uz, f[21]);
+        const float wdp = w * (ov.w - sv.w);
+        f[22] = fmaf(wdp, ux, f[22]);
+        f[23] = fmaf(wdp, uy, f[23]);
+        f[24] = fmaf(wdp, uz, f[24]);
+        f[25] = fmaf(w, other.w - self.w, f[25]);
         ++pairs;
     };
     uint32_t listed = 0;
@@ -1502,6 +1536,15 @@ __global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restri
     for (uint32_t e = 0; e < listed; ++e) {
         visit(list[e][threadIdx.x]);
     }
+#pragma unroll
+    for (int q = 13; q < 16; ++q) {
+        f[q] *= vscale;
+    }
+#pragma unroll
+    for (int q = 22; q < 25; ++q) {
+        f[q] *= inv_prho;
+    }
+    f[25] /= rho0;
     const float density = max_like_std(self.w, 1e-6f);
     f[0] = (self.w - rho0) / rho0;
     f[1] = sv.w * inv_prho;
