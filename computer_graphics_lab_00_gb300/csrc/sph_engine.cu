@@ -437,7 +437,6 @@ int Engine::upload(uint32_t tank, const float* pos, const float* vel, uint32_t c
         consts_dirty_ = true;
     }
     grid_valid_ = false;
-    since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
     return SPH_OK;
 }
 
@@ -517,14 +516,16 @@ int Engine::emit(uint32_t tank, uint32_t count) {
     }
     SPH_CUDA(launch_emit(d_tanks_ + tank, tanks_[tank].particle_base, count, pos_, vel_, prev_, stream_));
     grid_valid_ = false;
-    since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
+    since_refresh_ = kScheduleRefresh;  // a new lattice: remake the order at the next build
     return SPH_OK;
 }
 
 // Morton processing order: rank_ is refreshed from the current positions
 // every kScheduleRefresh grid builds (particles move a fraction of a cell per
-// substep, so an order a few substeps old keeps its locality) and whenever the
-// particle count changed since the last refresh. Never called while a graph
+// substep, so an order a few substeps old keeps its locality), after an emit
+// and whenever the particle count changed since the last refresh. An upload or
+// a restore of the same count keeps the order (still a permutation of the
+// ids; the usual refresh renews its locality). Never called while a graph
 // is being captured: the graphs only hold the per-substep order scatter.
 int Engine::prepare_schedule(uint32_t* launches) {
     if (!use_schedule_ || total_count_ == 0) {
@@ -783,7 +784,6 @@ int Engine::snapshot(bool save, uint32_t slot) {
         SPH_CUDA(cudaMemcpyAsync(pos_, snap_pos_[slot], bytes, cudaMemcpyDeviceToDevice, stream_));
         SPH_CUDA(cudaMemcpyAsync(vel_, snap_vel_[slot], bytes, cudaMemcpyDeviceToDevice, stream_));
         grid_valid_ = false;
-        since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
     }
     return SPH_OK;
 }
@@ -815,7 +815,6 @@ int Engine::restore_tanks(uint32_t slot, const std::vector<uint8_t>& which) {
         SPH_CUDA(cudaMemcpyAsync(vel_ + first, snap_vel_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
     }
     grid_valid_ = false;
-    since_refresh_ = kScheduleRefresh;  // new positions: refresh the order at the next build
     return SPH_OK;
 }
 

@@ -291,9 +291,10 @@ def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
 
 
 def test_morton_order_across_remakes_and_count_changes(native, oracle):
-    """The Morton processing order is remade every 16 grid builds, after an
-    upload and after a change of particle count; the bits stay the oracle's
-    throughout, through graph runs and the direct grid build."""
+    """The Morton processing order is remade every 8 grid builds and after a
+    change of particle count, and kept across an upload of the same count (a
+    stale order); the bits stay the oracle's throughout, through graph runs
+    and the direct grid build."""
     n = 8192
     dt = 1.0 / 600.0
     params, pos, vel = small_block(n, (16, 16, 32), box=(0.5, 0.8, 0.8), cells=W.cell_count_for(n))
@@ -308,6 +309,14 @@ def test_morton_order_across_remakes_and_count_changes(native, oracle):
         op, ov = oracle.run_substeps(params, pos, vel, dt, 37, threads=threads)
         assert_bit_exact(gp, op, "positions after 37 substeps")
         assert_bit_exact(gv, ov, "velocities after 37 substeps")
+        # Same count, unrelated positions: the order is stale, not wrong.
+        solver.upload(pos[::-1].copy(), vel[::-1].copy())
+        solver.run(dt, 3)
+        gp, gv = solver.state()
+        op, ov = oracle.run_substeps(params, pos[::-1].copy(), vel[::-1].copy(), dt, 3, threads=threads)
+        assert_bit_exact(gp, op, "positions after a same-count upload")
+        assert_bit_exact(gv, ov, "velocities after a same-count upload")
+        op, ov = oracle.run_substeps(params, pos, vel, dt, 37, threads=threads)
         m = 5000
         solver.upload(op[:m], ov[:m])
         solver.run(dt, 18)
