@@ -1326,8 +1326,11 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
     reinterpret_cast<float*>(svel)[4 * static_cast<size_t>(p) + 3] = pressure;
 }
 
-template <int kBlock, int kList>
-__global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __restrict__ spos2,
+// kMinBlocks: resident blocks per SM the register budget must allow (128
+// threads x 9 blocks = 36 warps at 56 registers, against 32 warps at the
+// 57 registers the kernel takes unbounded, whose allocation rounds to 64).
+template <int kBlock, int kList, int kMinBlocks = 1>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(const float4* __restrict__ spos2,
                                                                 const float4* __restrict__ svel,
                                                                 const uint32_t* __restrict__ sorted_ids,
                                                                 const uint2* __restrict__ bucket,
@@ -1424,8 +1427,8 @@ __global__ void __launch_bounds__(kBlock) integrate_mask_kernel(const float4* __
 //   26-28  min(max((x_i - wall_low) / h, 0), 4)   29-31  same for the high walls
 constexpr int kFeatures = 32;
 
-template <int kBlock, int kList>
-__global__ void __launch_bounds__(kBlock) features_kernel(const float4* __restrict__ spos2,
+template <int kBlock, int kList, int kMinBlocks = 1>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const float4* __restrict__ spos2,
                                                           const float4* __restrict__ svel,
                                                           const uint32_t* __restrict__ sorted_ids,
                                                           const uint2* __restrict__ bucket,
@@ -1744,17 +1747,12 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
                                                                             stank, n, tuning.order, tuning.masks, pos, vel);
             break;
         case 256:
-            if (tuning.queue <= 32) {
-                integrate_mask_kernel<256, 32><<<(n + 255) / 256, 256, 0, stream>>>(
-                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
-            } else {
-                integrate_mask_kernel<256, 40><<<(n + 255) / 256, 256, 0, stream>>>(
-                    spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
-            }
+            integrate_mask_kernel<256, 32><<<(n + 255) / 256, 256, 0, stream>>>(
+                spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
             break;
         default:
-            integrate_mask_kernel<128, 48><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks,
-                                                                                stank, n, tuning.order, tuning.masks, pos, vel);
+            integrate_mask_kernel<128, 32, 9><<<(n + 127) / 128, 128, 0, stream>>>(
+                spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
             break;
         }
         return cudaGetLastError();
@@ -1871,8 +1869,9 @@ cudaError_t launch_features(const float4* spos2, const float4* svel, const uint3
     if (n == 0) {
         return cudaSuccess;
     }
-    features_kernel<128, 48><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
-                                                                  order, masks, force, features, id_order ? 1 : 0);
+    // Seven blocks per SM (72 registers) rather than six at the 80 it takes unbounded.
+    features_kernel<128, 48, 7><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
+                                                                     order, masks, force, features, id_order ? 1 : 0);
     return cudaGetLastError();
 }
 

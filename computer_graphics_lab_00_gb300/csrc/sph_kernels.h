@@ -119,7 +119,7 @@ cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* so
 // per-particle pair lists of variants 2-3 (device buffers the engine owns).
 struct NeighbourTuning {
     uint32_t variant = 4;
-    uint32_t block = 256;
+    uint32_t block = 128;
     uint32_t queue = 32;
     uint16_t* pair_list = nullptr;
     uint16_t* pair_count = nullptr;
