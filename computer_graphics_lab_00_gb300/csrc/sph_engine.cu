@@ -179,7 +179,7 @@ void Engine::release() {
             e = nullptr;
         }
     }
-    void* buffers[] = {surface_field_, surface_vertices_, surface_codes_, surface_tiles_, sweep_,
+    void* buffers[] = {surface_field_, surface_runs_, surface_vertices_, surface_codes_, surface_tiles_, sweep_,
                        d_tanks_,       d_colliders_,  d_fields_,    field_accel_, pos_,          vel_,         prev_,        tank_of_,   stank_,
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
@@ -1403,6 +1403,9 @@ int Engine::surface_field(uint32_t tank, uint32_t resolution) {
     const uint64_t samples = resolution + 1ull;
     int status = grow(reinterpret_cast<void**>(&surface_field_), &surface_field_bytes_,
                       samples * samples * samples * sizeof(float));
+    if (status == SPH_OK) {
+        status = grow(&surface_runs_, &surface_runs_bytes_, sizeof(surface::FieldRuns));
+    }
     if (status != SPH_OK) {
         return status;
     }
@@ -1430,7 +1433,8 @@ int Engine::surface_field(uint32_t tank, uint32_t resolution) {
     if (status != SPH_OK) {
         return status;
     }
-    SPH_CUDA(surface::launch_field(spos_, bucket_ + tanks_[tank].bucket_base, g, surface_field_, stream_));
+    SPH_CUDA(surface::launch_field(spos_, bucket_ + tanks_[tank].bucket_base, g,
+                                   static_cast<surface::FieldRuns*>(surface_runs_), surface_field_, stream_));
     return SPH_OK;
 }
 

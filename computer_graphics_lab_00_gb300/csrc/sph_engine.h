@@ -212,6 +212,8 @@ private:
     int grow(void** buffer, size_t* have, size_t need);
     float* surface_field_ = nullptr;
     size_t surface_field_bytes_ = 0;
+    void* surface_runs_ = nullptr;  // surface::FieldRuns
+    size_t surface_runs_bytes_ = 0;
     uint32_t surface_resolution_ = 0;
     uint32_t surface_tank_ = 0;
     sph_surface_vertex* surface_vertices_ = nullptr;

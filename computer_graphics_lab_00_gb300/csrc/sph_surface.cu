@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -167,67 +168,177 @@ constexpr uint32_t kTile = kBlock * kPerThread;  // cells per count/emit block
 
 // sampleField (marching_cubes.cpp:312-347) at every interior sample; border
 // samples are 0 (buildFluidField, :380-391).
-__global__ void __launch_bounds__(kBlock) field_kernel(const float4* __restrict__ spos,
-                                                       const uint2* __restrict__ bucket, FieldGeom g,
-                                                       float* __restrict__ field) {
-    const uint32_t samples = g.resolution + 1;
-    const uint32_t total = samples * samples * samples;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) {
-        return;
+//
+// Every sample of one grid cell (cell size = the kernel radius) visits the
+// same 27 buckets, so the samples are grouped by cell: along each axis the
+// sample -> cell map is monotone, so a cell's samples form a box of per-axis
+// runs, and one warp takes a box. Its lanes walk the buckets in step (one
+// broadcast load per candidate, no divergent trip counts), kPer samples per
+// lane. Each sample still sums its candidates in the reference's order.
+
+// Per-axis runs of interior samples [1, resolution) with the same cell.
+__global__ void __launch_bounds__(1024) field_runs_kernel(FieldGeom g, FieldRuns* __restrict__ runs) {
+    __shared__ int32_t cells[SPH_SURFACE_MAX_RESOLUTION + 1];
+    const uint32_t a = blockIdx.x;
+    const uint32_t r = g.resolution;
+    const float origin = a == 0 ? g.origin[0] : (a == 1 ? g.origin[1] : g.origin[2]);
+    const float cell = a == 0 ? g.cell[0] : (a == 1 ? g.cell[1] : g.cell[2]);
+    for (uint32_t x = 1 + threadIdx.x; x < r; x += blockDim.x) {
+        // origin + float(x) * cell, as the sample position.
+        cells[x] = cell_coord(__fadd_rn(origin, __fmul_rn(static_cast<float>(x), cell)), g.radius);
     }
-    const uint32_t x = i % samples;
-    const uint32_t y = (i / samples) % samples;
-    const uint32_t z = i / (samples * samples);
-    if (x == 0 || y == 0 || z == 0 || x == g.resolution || y == g.resolution || z == g.resolution) {
-        field[i] = 0.0f;
-        return;
-    }
-    // origin + vec3{x, y, z} * cell.
-    const float px = __fadd_rn(g.origin[0], __fmul_rn(static_cast<float>(x), g.cell[0]));
-    const float py = __fadd_rn(g.origin[1], __fmul_rn(static_cast<float>(y), g.cell[1]));
-    const float pz = __fadd_rn(g.origin[2], __fmul_rn(static_cast<float>(z), g.cell[2]));
-    const int cx = cell_coord(px, g.radius);
-    const int cy = cell_coord(py, g.radius);
-    const int cz = cell_coord(pz, g.radius);
-    // The 27 buckets in (z, y, x) order; a bucket reached twice (two cells
-    // that hash alike) is summed once.
-    uint32_t b[27];
-    uint32_t repeat = 0;
-#pragma unroll
-    for (int k = 0; k < 27; ++k) {
-        const int dx = k % 3 - 1;
-        const int dy = (k / 3) % 3 - 1;
-        const int dz = k / 9 - 1;
-        b[k] = spatial_hash(static_cast<uint32_t>(cx + dx), static_cast<uint32_t>(cy + dy),
-                            static_cast<uint32_t>(cz + dz), g.mask);
-#pragma unroll
-        for (int j = 0; j < k; ++j) {
-            repeat |= (b[k] == b[j] ? 1u : 0u) << k;
-        }
-    }
-    float sum = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 27; ++k) {
-        if ((repeat >> k & 1u) != 0) {
-            continue;
-        }
-        const uint2 range = __ldg(&bucket[b[k]]);
-        const uint32_t count = min(range.y - range.x, kCellCapacity);
-        for (uint32_t s = 0; s < count; ++s) {
-            const float4 p = __ldg(&spos[range.x + s]);
-            const float ex = __fsub_rn(p.x, px);
-            const float ey = __fsub_rn(p.y, py);
-            const float ez = __fsub_rn(p.z, pz);
-            const float d2 = dot3(ex, ey, ez);
-            if (d2 >= g.radius_sq) {
-                continue;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t n = 0;
+        for (uint32_t x = 1; x < r; ++x) {
+            if (x == 1 || cells[x] != cells[x - 1]) {
+                if (n > 0) {
+                    runs->run[a][n - 1].end = x;
+                }
+                runs->run[a][n] = AxisRun{x, x, cells[x], 0u};
+                ++n;
             }
-            const float d = __fsub_rn(1.0f, __fdiv_rn(d2, g.radius_sq));
-            sum = __fadd_rn(sum, __fmul_rn(__fmul_rn(d, d), d));
+        }
+        if (n > 0) {
+            runs->run[a][n - 1].end = r;
+        }
+        runs->count[a] = n;
+    }
+}
+
+// kGroup lanes (8, 16 or 32) share one box; a warp holds 32 / kGroup boxes.
+// Lane j of a group hashes neighbours j, j + kGroup, ... and the group reads
+// them back by shuffle.
+template <int kGroup, int kPer>
+__global__ void __launch_bounds__(kBlock) field_cells_kernel(const float4* __restrict__ spos,
+                                                             const uint2* __restrict__ bucket, FieldGeom g,
+                                                             const FieldRuns* __restrict__ runs,
+                                                             float* __restrict__ field) {
+    static_assert(kGroup == 8 || kGroup == 16 || kGroup == 32, "group of 8, 16 or 32 lanes");
+    constexpr uint32_t kAll = 0xFFFFFFFFu;
+    constexpr int kSlots = (27 + kGroup - 1) / kGroup;  // neighbours per lane
+    constexpr uint32_t kGroupsPerWarp = 32u / kGroup;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t glane = lane % kGroup;
+    const uint32_t gbase = lane - glane;
+    const uint32_t nx = runs->count[0];
+    const uint32_t ny = runs->count[1];
+    const uint32_t nz = runs->count[2];
+    const uint32_t boxes = nx * ny * nz;
+    const uint32_t samples = g.resolution + 1;
+    const uint32_t warps = gridDim.x * (kBlock / 32u);
+    const uint32_t warp_id = blockIdx.x * (kBlock / 32u) + (threadIdx.x >> 5);
+    const uint32_t rounds = (boxes + warps * kGroupsPerWarp - 1) / (warps * kGroupsPerWarp);
+    for (uint32_t round = 0; round < rounds; ++round) {
+        // Every lane stays in the loop (the shuffles need the whole warp); a
+        // group past the last box works on box 0 and writes nothing.
+        const uint32_t w = (round * warps + warp_id) * kGroupsPerWarp + lane / kGroup;
+        const bool live = w < boxes;
+        const uint32_t box = live ? w : 0u;
+        const AxisRun rx = runs->run[0][box % nx];
+        const AxisRun ry = runs->run[1][(box / nx) % ny];
+        const AxisRun rz = runs->run[2][box / (nx * ny)];
+        // The 27 buckets in (z, y, x) order; a bucket reached twice (two
+        // cells that hash alike) is summed once, at its first offset.
+        uint32_t h[kSlots];
+        uint2 range[kSlots];
+#pragma unroll
+        for (int t = 0; t < kSlots; ++t) {
+            const uint32_t k = glane + static_cast<uint32_t>(t) * kGroup;
+            h[t] = 0xFFFFFFFFu;
+            if (k < 27u) {
+                const int dx = static_cast<int>(k % 3u) - 1;
+                const int dy = static_cast<int>((k / 3u) % 3u) - 1;
+                const int dz = static_cast<int>(k / 9u) - 1;
+                h[t] = spatial_hash(static_cast<uint32_t>(rx.cell + dx), static_cast<uint32_t>(ry.cell + dy),
+                                    static_cast<uint32_t>(rz.cell + dz), g.mask);
+            }
+            range[t] = k < 27u ? __ldg(&bucket[h[t]]) : make_uint2(0u, 0u);
+        }
+        uint32_t skip = 0;  // bit k: neighbour k repeats an earlier bucket
+#pragma unroll
+        for (int t = 0; t < kSlots; ++t) {
+            const uint32_t k = glane + static_cast<uint32_t>(t) * kGroup;
+            bool repeat = false;
+#pragma unroll
+            for (uint32_t j = 0; j < 27u; ++j) {
+                const uint32_t bj = __shfl_sync(kAll, h[j / kGroup], static_cast<int>(gbase + j % kGroup));
+                repeat = repeat || (j < k && bj == h[t]);
+            }
+            const uint32_t votes = __ballot_sync(kAll, k < 27u && repeat);
+            skip |= ((votes >> gbase) & (kGroup == 32 ? kAll : ((1u << kGroup) - 1u))) << (t * kGroup);
+        }
+        const uint32_t bw = rx.end - rx.begin;
+        const uint32_t bh = ry.end - ry.begin;
+        const uint32_t n_box = bw * bh * (rz.end - rz.begin);
+        // Passes over the box; a group with fewer samples idles through the
+        // extra passes of a bigger box in its warp.
+        const uint32_t my_passes = (n_box + kGroup * kPer - 1) / (kGroup * kPer);
+        uint32_t passes = my_passes;
+#pragma unroll
+        for (uint32_t o = kGroup; o < 32u; o <<= 1) {
+            passes = max(passes, __shfl_xor_sync(kAll, passes, static_cast<int>(o)));
+        }
+        for (uint32_t pass = 0; pass < passes; ++pass) {
+            const uint32_t first = pass * kGroup * kPer;
+            float px[kPer];
+            float py[kPer];
+            float pz[kPer];
+            float sum[kPer];
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const uint32_t i = min(first + static_cast<uint32_t>(q) * kGroup + glane, n_box - 1u);
+                const uint32_t x = rx.begin + i % bw;
+                const uint32_t y = ry.begin + (i / bw) % bh;
+                const uint32_t z = rz.begin + i / (bw * bh);
+                // origin + vec3{x, y, z} * cell.
+                px[q] = __fadd_rn(g.origin[0], __fmul_rn(static_cast<float>(x), g.cell[0]));
+                py[q] = __fadd_rn(g.origin[1], __fmul_rn(static_cast<float>(y), g.cell[1]));
+                pz[q] = __fadd_rn(g.origin[2], __fmul_rn(static_cast<float>(z), g.cell[2]));
+                sum[q] = 0.0f;
+            }
+            for (uint32_t k = 0; k < 27u; ++k) {
+                const int src = static_cast<int>(gbase + k % kGroup);
+                uint2 held = range[0];  // this lane's slot k / kGroup, without a dynamic index
+#pragma unroll
+                for (int t = 1; t < kSlots; ++t) {
+                    if (k >= static_cast<uint32_t>(t) * kGroup) {
+                        held = range[t];
+                    }
+                }
+                const uint32_t start = __shfl_sync(kAll, held.x, src);
+                const uint32_t end = __shfl_sync(kAll, held.y, src);
+                if ((skip >> k & 1u) != 0 || pass >= my_passes) {
+                    continue;
+                }
+                const uint32_t count = min(end - start, kCellCapacity);
+                for (uint32_t s = 0; s < count; ++s) {
+                    const float4 p = __ldg(&spos[start + s]);
+#pragma unroll
+                    for (int q = 0; q < kPer; ++q) {
+                        const float ex = __fsub_rn(p.x, px[q]);
+                        const float ey = __fsub_rn(p.y, py[q]);
+                        const float ez = __fsub_rn(p.z, pz[q]);
+                        const float d2 = dot3(ex, ey, ez);
+                        if (!(d2 >= g.radius_sq)) {
+                            const float d = __fsub_rn(1.0f, __fdiv_rn(d2, g.radius_sq));
+                            sum[q] = __fadd_rn(sum[q], __fmul_rn(__fmul_rn(d, d), d));
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const uint32_t i = first + static_cast<uint32_t>(q) * kGroup + glane;
+                if (live && i < n_box) {
+                    const uint32_t x = rx.begin + i % bw;
+                    const uint32_t y = ry.begin + (i / bw) % bh;
+                    const uint32_t z = rz.begin + i / (bw * bh);
+                    field[(static_cast<size_t>(z) * samples + y) * samples + x] = sum[q];
+                }
+            }
         }
     }
-    field[i] = sum;
 }
 
 // ---- marching cubes -----------------------------------------------------------------
@@ -492,11 +603,43 @@ uint32_t march_tiles(uint32_t resolution) {
     return static_cast<uint32_t>((cells + kTile - 1) / kTile);
 }
 
-cudaError_t launch_field(const float4* spos, const uint2* bucket, const FieldGeom& g, float* field,
+cudaError_t launch_field(const float4* spos, const uint2* bucket, const FieldGeom& g, FieldRuns* runs, float* field,
                          cudaStream_t stream) {
-    const uint32_t samples = g.resolution + 1;
-    const uint32_t total = samples * samples * samples;
-    field_kernel<<<(total + kBlock - 1) / kBlock, kBlock, 0, stream>>>(spos, bucket, g, field);
+    const size_t samples = g.resolution + 1ull;
+    cudaError_t err = cudaMemsetAsync(field, 0, samples * samples * samples * sizeof(float), stream);
+    if (err != cudaSuccess) {
+        return err;
+    }
+    field_runs_kernel<<<3, 1024, 0, stream>>>(g, runs);
+    // Lane groups and samples per lane from the box sizes: a cell holds at
+    // most floor(radius / cell) + 1 samples along an axis, radius / cell on
+    // average.
+    float most = 1.0f;
+    float mean = 1.0f;
+    for (int a = 0; a < 3; ++a) {
+        const float per = g.cell[a] > 0.0f ? g.radius / g.cell[a] : 0.0f;
+        const float cap = static_cast<float>(g.resolution);
+        most *= std::min(std::floor(per) + 1.0f, cap);
+        mean *= std::min(std::max(per, 1.0f), cap);
+    }
+    int device = 0;
+    int sms = 0;
+    if ((err = cudaGetDevice(&device)) != cudaSuccess ||
+        (err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) {
+        return err;
+    }
+    const uint32_t blocks = static_cast<uint32_t>(sms) * 8u;  // grid-stride over the cell boxes
+    if (most <= 8.0f) {
+        field_cells_kernel<8, 1><<<blocks, kBlock, 0, stream>>>(spos, bucket, g, runs, field);
+    } else if (most <= 16.0f || mean <= 12.0f) {
+        field_cells_kernel<16, 1><<<blocks, kBlock, 0, stream>>>(spos, bucket, g, runs, field);
+    } else if (most <= 32.0f) {
+        field_cells_kernel<32, 1><<<blocks, kBlock, 0, stream>>>(spos, bucket, g, runs, field);
+    } else if (most <= 64.0f) {
+        field_cells_kernel<32, 2><<<blocks, kBlock, 0, stream>>>(spos, bucket, g, runs, field);
+    } else {
+        field_cells_kernel<32, 4><<<blocks, kBlock, 0, stream>>>(spos, bucket, g, runs, field);
+    }
     return cudaGetLastError();
 }
 

@@ -21,6 +21,21 @@ struct FieldGeom {
     uint32_t resolution;
 };
 
+// The interior samples along one axis that fall in one grid cell (the
+// mapping sample -> cell is monotone per axis): x in [begin, end).
+struct AxisRun {
+    uint32_t begin;
+    uint32_t end;
+    int32_t cell;
+    uint32_t pad;
+};
+
+// Device scratch of one field: the runs of the three axes.
+struct FieldRuns {
+    uint32_t count[4];
+    AxisRun run[3][SPH_SURFACE_MAX_RESOLUTION];
+};
+
 // Arguments of marchFluidField.
 struct MarchGeom {
     float origin[3];
@@ -44,7 +59,9 @@ const int8_t* case_table();
 cudaError_t ensure_tables();
 uint32_t march_tiles(uint32_t resolution);
 
-cudaError_t launch_field(const float4* spos, const uint2* bucket, const FieldGeom& g, float* field,
+// Zeroes the field, splits each axis into per-cell runs, then samples every
+// grid cell's box of interior samples with one warp.
+cudaError_t launch_field(const float4* spos, const uint2* bucket, const FieldGeom& g, FieldRuns* runs, float* field,
                          cudaStream_t stream);
 // After it: vertex count = min(offsets[tiles], *limit).
 cudaError_t launch_march(const float* field, const MarchGeom& g, uint32_t capacity, MarchScratch s,
