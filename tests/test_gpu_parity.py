@@ -203,6 +203,30 @@ def test_1m_grid_and_two_substeps_bit_exact(native, oracle):
     assert_bit_exact(gv, ov, "1M velocities")
 
 
+def test_1m_compressed_state_bit_exact(native, oracle):
+    """The 1M dam break 300 substeps in (collapsing and compressed, so many
+    particles pass integrate's 32-entry lists and drain mid-walk, and the
+    Morton order is several substeps stale): two more substeps from the GPU's
+    own state equal the oracle's from the same state, and the pair counts
+    agree."""
+    case = W.dam_break_1m()
+    pos, vel = case.initial_state()
+    threads = oracle.hardware_threads
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        solver.run(case.dt, 300)
+        sp, sv = solver.state()
+        st = solver.stats()
+        assert st.pairs_in_range > 30 * case.count  # denser than the lattice (29.3 per particle)
+        p, q = oracle.pair_counts(case.params, sp, threads=threads)
+        assert (st.candidates, st.pairs_in_range) == (p, q)
+        solver.run(case.dt, 2)
+        gp, gv = solver.state()
+    op, ov = oracle.run_substeps(case.params, sp, sv, case.dt, 2, threads=threads)
+    assert_bit_exact(gp, op, "1M positions from the compressed state")
+    assert_bit_exact(gv, ov, "1M velocities from the compressed state")
+
+
 def test_gpu_runs_are_deterministic(native):
     case = W.dam_break_16k()
     pos, vel = case.initial_state()
