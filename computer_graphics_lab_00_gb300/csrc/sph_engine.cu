@@ -184,7 +184,8 @@ void Engine::release() {
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
                        bucket_,        spos_,         spos2_,       svel_,        counters_,  stats_acc_,
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
-                       rank_,          order_,        snap_pos_[0], snap_vel_[0],
+                       rank_,          order_,        compact_ids_, compact_sorted_, compact_ranges_,
+                       snap_pos_[0], snap_vel_[0],
                        snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_};
     for (void* b : buffers) {
         if (b != nullptr) {
@@ -287,6 +288,7 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         attach_shapes(t);
     }
     consts_dirty_ = true;
+    shapes_dirty_ = true;
     return update_shape_flags();
 }
 
@@ -325,6 +327,7 @@ int Engine::set_params(uint32_t tank, const sph_params& params) {
     params_[tank] = params;
     attach_shapes(tank);
     consts_dirty_ = true;
+    shapes_dirty_ = true;
     return update_shape_flags();
 }
 
@@ -382,15 +385,25 @@ int Engine::enqueue_colliders(uint32_t* launches) {
 
 int Engine::refresh_constants(float dt) {
     if (!consts_dirty_ && dt == const_dt_) {
+        if (active_dirty_) {
+            // A new active mask alone: patch the flags of the device table.
+            active_host_.resize(tanks_.size());
+            for (size_t t = 0; t < tanks_.size(); ++t) {
+                active_host_[t] = static_cast<uint8_t>(tanks_[t].active);
+            }
+            SPH_CUDA(launch_set_active(d_tanks_, active_host_.data(), static_cast<uint32_t>(tanks_.size()), stream_));
+            active_dirty_ = false;
+        }
         return SPH_OK;
     }
+    active_dirty_ = false;  // the whole table goes up below
     for (TankConst& t : tanks_) {
         t.dt = dt;
         t.max_speed = dt > 0.0F ? 0.4F * t.h / dt : 0.0F;
     }
     SPH_CUDA(cudaMemcpyAsync(d_tanks_, tanks_.data(), tanks_.size() * sizeof(TankConst), cudaMemcpyHostToDevice,
                              stream_));
-    if (consts_dirty_) {
+    if (shapes_dirty_) {
         SPH_CUDA(cudaMemcpyAsync(d_colliders_, colliders_host_.data(), colliders_host_.size() * sizeof(sph_collider),
                                  cudaMemcpyHostToDevice, stream_));
         SPH_CUDA(cudaMemcpyAsync(d_fields_, fields_host_.data(), fields_host_.size() * sizeof(sph_force_field),
@@ -398,6 +411,7 @@ int Engine::refresh_constants(float dt) {
     }
     const_dt_ = dt;
     consts_dirty_ = false;
+    shapes_dirty_ = false;
     return SPH_OK;
 }
 
@@ -669,6 +683,17 @@ int Engine::run(float dt, uint32_t substeps) {
     if (status != SPH_OK) {
         return status;
     }
+    // A batch with most particles in tanks that sit out: build the grid over
+    // the active tanks' particles only.
+    if (tanks_.size() > 1 && onesweep_) {
+        uint32_t active = 0;
+        for (const TankConst& t : tanks_) {
+            active += t.active != 0 ? t.particle_count : 0U;
+        }
+        if (2ull * active <= total_count_) {
+            return run_compact(substeps, active);
+        }
+    }
     status = ensure_graph();
     if (status != SPH_OK) {
         return status;
@@ -680,6 +705,70 @@ int Engine::run(float dt, uint32_t substeps) {
         SPH_CUDA(cudaGraphLaunch(graph_, stream_));
     }
     grid_valid_ = true;
+    return SPH_OK;
+}
+
+// The substep over a compacted particle set: the active tanks' ids in one
+// list, keys, sort, bounds and the neighbour passes over that list only, the
+// results written back through the ids. Every active particle sees exactly
+// the pairs and order of a full build (tanks never share buckets), so the
+// bits are the same; direct launches (the set changes between calls).
+int Engine::run_compact(uint32_t substeps, uint32_t active_particles) {
+    int status = SPH_OK;
+    if (compact_ids_ == nullptr) {
+        if ((status = alloc(&compact_ids_, total_capacity_)) != SPH_OK ||
+            (status = alloc(&compact_sorted_, total_capacity_)) != SPH_OK ||
+            (status = alloc(&compact_ranges_, 3 * tanks_.size())) != SPH_OK) {
+            return status;
+        }
+    }
+    compact_ranges_host_.clear();
+    uint32_t compact = 0;
+    for (const TankConst& t : tanks_) {
+        if (t.active != 0 && t.particle_count > 0) {
+            compact_ranges_host_.insert(compact_ranges_host_.end(), {t.particle_base, compact, t.particle_count});
+            compact += t.particle_count;
+        }
+    }
+    const uint32_t ranges = static_cast<uint32_t>(compact_ranges_host_.size() / 3);
+    grid_valid_ = false;  // the grid buffers now hold the compacted build
+    if (active_particles == 0 || ranges == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaMemcpyAsync(compact_ranges_, compact_ranges_host_.data(), compact_ranges_host_.size() * sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, stream_));
+    SPH_CUDA(launch_compact_ids(compact_ranges_, ranges, compact_ids_, stream_));
+    const uint32_t n = active_particles;
+    const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
+    NeighbourTuning tuning = tuning_;
+    tuning.order = nullptr;
+    for (uint32_t s = 0; s < substeps; ++s) {
+        // Only the active tanks' buckets are read, so only they need clearing
+        // (one memset per tank while that is the smaller job).
+        if (ranges <= 32) {
+            for (const TankConst& t : tanks_) {
+                if (t.active != 0 && t.particle_count > 0) {
+                    SPH_CUDA(
+                        cudaMemsetAsync(bucket_ + t.bucket_base, 0, sizeof(uint2) * (t.cell_mask + 1U), stream_));
+                }
+            }
+        } else {
+            SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
+        }
+        SPH_CUDA(launch_keys_onesweep(pos_, tank_of_, d_tanks_, n, grid_.keys, passes, sweep_, stream_, compact_ids_));
+        SPH_CUDA(launch_onesweep_sort(grid_, n, passes, sweep_, stream_, nullptr));
+        SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_,
+                                      svel_, stank_, Schedule{}, stream_, compact_ids_, compact_sorted_));
+        if ((status = enqueue_fields(nullptr)) != SPH_OK) {
+            return status;
+        }
+        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning));
+        SPH_CUDA(launch_integrate(spos2_, svel_, compact_sorted_, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
+                                  tuning));
+        if ((status = enqueue_colliders(nullptr)) != SPH_OK) {
+            return status;
+        }
+    }
     return SPH_OK;
 }
 
@@ -805,14 +894,37 @@ int Engine::restore_tanks(uint32_t slot, const std::vector<uint8_t>& which) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     SPH_CUDA(cudaSetDevice(device_));
+    // Neighbouring selected tanks whose particles are adjacent share one copy.
+    size_t first = 0;
+    size_t count = 0;
+    auto flush = [&]() -> int {
+        if (count > 0) {
+            size_t bytes = sizeof(float4) * count;
+            SPH_CUDA(cudaMemcpyAsync(pos_ + first, snap_pos_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
+            SPH_CUDA(cudaMemcpyAsync(vel_ + first, snap_vel_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
+        }
+        count = 0;
+        return SPH_OK;
+    };
     for (size_t t = 0; t < tanks_.size(); ++t) {
-        if (which[t] == 0) {
+        if (which[t] == 0 || tanks_[t].particle_count == 0) {
             continue;
         }
-        size_t first = tanks_[t].particle_base;
-        size_t bytes = sizeof(float4) * tanks_[t].particle_count;
-        SPH_CUDA(cudaMemcpyAsync(pos_ + first, snap_pos_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
-        SPH_CUDA(cudaMemcpyAsync(vel_ + first, snap_vel_[slot] + first, bytes, cudaMemcpyDeviceToDevice, stream_));
+        const size_t base = tanks_[t].particle_base;
+        if (count > 0 && base != first + count) {
+            int status = flush();
+            if (status != SPH_OK) {
+                return status;
+            }
+        }
+        if (count == 0) {
+            first = base;
+        }
+        count += tanks_[t].particle_count;
+    }
+    int status = flush();
+    if (status != SPH_OK) {
+        return status;
     }
     grid_valid_ = false;
     return SPH_OK;
@@ -1088,6 +1200,7 @@ int Engine::learned_features(float dt, float* features) {
     uint32_t n = total_count_;
     NeighbourTuning masked = tuning_;
     masked.variant = 4;
+    masked.all_tanks = true;  // features of every tank, active or not
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
     SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.order,
                              tuning_.masks, sforce_, features, true, stream_));
@@ -1224,7 +1337,7 @@ int Engine::set_active(const std::vector<uint8_t>& active) {
     for (size_t t = 0; t < tanks_.size(); ++t) {
         tanks_[t].active = active[t] != 0 ? 1U : 0U;
     }
-    consts_dirty_ = true;
+    active_dirty_ = true;  // only the flags go up (refresh_constants)
     return SPH_OK;
 }
 

@@ -142,6 +142,7 @@ private:
     int enqueue_colliders(uint32_t* launches);
     int ensure_graph();
     int prepare_schedule(uint32_t* launches);
+    int run_compact(uint32_t substeps, uint32_t active_particles);
     static constexpr uint32_t kScheduleRefresh = 8;  // grid builds between Morton order refreshes
     void release();
     template <typename T> int alloc(T** ptr, size_t count);
@@ -163,10 +164,17 @@ private:
     uint32_t* order_ = nullptr;            // sorted positions in processing order
     uint32_t rank_count_ = 0xFFFFFFFFu;    // particle count rank_ was made for
     uint32_t since_refresh_ = 0;           // grid builds since rank_ was made
+    uint32_t* compact_ids_ = nullptr;      // ids of the active tanks' particles (a batch run with most tanks idle)
+    uint32_t* compact_sorted_ = nullptr;   // their ids in sorted order, for the write-back
+    uint32_t* compact_ranges_ = nullptr;   // (global base, compact base, count) per active tank
+    std::vector<uint32_t> compact_ranges_host_;
     bool onesweep_ = true;
     unsigned long long* sweep_ = nullptr;  // per-pass tile digit counts and histograms of the one-kernel passes
     float const_dt_ = -1.0f;
-    bool consts_dirty_ = true;
+    bool consts_dirty_ = true;   // tank table to upload (constants, counts, active flags)
+    bool shapes_dirty_ = true;   // collider and force-field tables to upload
+    bool active_dirty_ = false;  // only the tanks' active flags changed
+    std::vector<uint8_t> active_host_;
 
     TankConst* d_tanks_ = nullptr;
     sph_collider* d_colliders_ = nullptr;        // SPH_MAX_COLLIDERS per tank

@@ -1251,7 +1251,7 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
                                                            const TankConst* __restrict__ tanks,
                                                            const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
                                                            uint32_t* __restrict__ masks,
-                                                           StepCounters* __restrict__ counters) {
+                                                           StepCounters* __restrict__ counters, int all_tanks) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;  // processing slot: indexes the masks
     uint32_t p = slot;
     if (order != nullptr && p < n) {
@@ -1261,6 +1261,11 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
         return;
     }
     const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    // A tank that sits this substep out is not integrated, and tanks never
+    // share pairs, so its densities are not needed (pair counting visits all).
+    if (!kCount && all_tanks == 0 && __ldg(&t->active) == 0) {
+        return;
+    }
     const float h = __ldg(&t->h);
     const float h2 = __ldg(&t->h2);
     const float c6 = __ldg(&t->c_poly6);
@@ -1445,11 +1450,15 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const floa
     if (order != nullptr && p < n) {
         p = order[p];
     }
-    const uint32_t live = __ballot_sync(0xFFFFFFFFu, p < n);
-    if (p >= n) {
+    // Features of a tank that sits this substep out are not used (its finish
+    // is skipped), so its particles leave the walk.
+    bool valid = p < n;
+    const TankConst* t = tanks + (valid && stank != nullptr ? stank[p] : 0);
+    valid = valid && (id_order != 0 || __ldg(&t->active) != 0);
+    const uint32_t live = __ballot_sync(0xFFFFFFFFu, valid);
+    if (!valid) {
         return;
     }
-    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
     PairConst k;
     k.h = __ldg(&t->h);
     k.c_spiky = __ldg(&t->c_spiky);
@@ -1699,10 +1708,11 @@ cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, cons
         uint32_t blocks = (n + 127) / 128;
         if (counters != nullptr) {
             density_mask_kernel<true><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
-                                                                  tuning.order, tuning.masks, counters);
+                                                                  tuning.order, tuning.masks, counters, 1);
         } else {
             density_mask_kernel<false><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
-                                                                   tuning.order, tuning.masks, nullptr);
+                                                                   tuning.order, tuning.masks, nullptr,
+                                                                   tuning.all_tanks ? 1 : 0);
         }
         return cudaGetLastError();
     }

@@ -17,6 +17,8 @@
 // so the sort is stable without any per-element atomics in global memory.
 #include "sph_kernels.h"
 
+#include <cstring>
+
 namespace sph {
 
 namespace {
@@ -210,7 +212,9 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
                                                             const float4* __restrict__ vel,
                                                             const uint16_t* __restrict__ tank_of,
                                                             float4* __restrict__ spos, float4* __restrict__ svel,
-                                                            uint16_t* __restrict__ stank, Schedule schedule) {
+                                                            uint16_t* __restrict__ stank, Schedule schedule,
+                                                            const uint32_t* __restrict__ ids,
+                                                            uint32_t* __restrict__ global_sorted) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) {
         return;
@@ -223,6 +227,11 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
         bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
     }
     uint32_t i = sorted_ids[p];
+    if (ids != nullptr) {
+        // A compacted particle set: sorted entries are positions in `ids`.
+        i = ids[i];
+        global_sorted[p] = i;
+    }
     spos[p] = pos[i];
     svel[p] = vel[i];
     if (tank_of != nullptr) {
@@ -293,7 +302,8 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
                                                                  const TankConst* __restrict__ tanks, uint32_t n,
                                                                  uint32_t* __restrict__ keys, uint32_t passes,
                                                                  uint32_t* __restrict__ tile_counts,
-                                                                 uint32_t* __restrict__ hist, uint32_t morton_bits) {
+                                                                 uint32_t* __restrict__ hist, uint32_t morton_bits,
+                                                                 const uint32_t* __restrict__ ids) {
     __shared__ uint32_t counts[kSweepMaxPasses][kSweepBins];
     for (uint32_t k = threadIdx.x; k < kSweepMaxPasses * kSweepBins; k += blockDim.x) {
         (&counts[0][0])[k] = 0;
@@ -304,8 +314,9 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
 #pragma unroll
     for (uint32_t r = 0; r < kKeysItems; ++r) {
         const uint32_t i = first + r * kKeysThreads + threadIdx.x;
-        p[r] = i < n ? pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        tank[r] = tank_of != nullptr && i < n ? tank_of[i] : 0;
+        const uint32_t g = i < n && ids != nullptr ? ids[i] : i;
+        p[r] = i < n ? pos[g] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        tank[r] = tank_of != nullptr && i < n ? tank_of[g] : 0;
     }
     __syncthreads();
 #pragma unroll
@@ -479,7 +490,7 @@ namespace {
 
 cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                             uint32_t* keys, uint32_t passes, unsigned long long* sweep, uint32_t morton_bits,
-                            cudaStream_t stream) {
+                            const uint32_t* ids, cudaStream_t stream) {
     cudaError_t err = cudaMemsetAsync(sweep, 0, onesweep_scratch_words(n, passes) * sizeof(unsigned long long), stream);
     if (err != cudaSuccess) {
         return err;
@@ -488,10 +499,10 @@ cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const Ta
     SweepLayout l = sweep_layout(sweep, tiles, passes);
     if (morton_bits != 0) {
         keys_hist_kernel<true><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes, l.tile_counts,
-                                                                   l.hist, morton_bits);
+                                                                   l.hist, morton_bits, ids);
     } else {
         keys_hist_kernel<false><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes,
-                                                                    l.tile_counts, l.hist, 0);
+                                                                    l.tile_counts, l.hist, 0, ids);
     }
     return cudaGetLastError();
 }
@@ -499,11 +510,12 @@ cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const Ta
 }  // namespace
 
 cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
-                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream) {
+                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream,
+                                 const uint32_t* ids) {
     if (n == 0) {
         return cudaSuccess;
     }
-    return keys_and_counts(pos, tank_of, tanks, n, keys, passes, sweep, 0, stream);
+    return keys_and_counts(pos, tank_of, tanks, n, keys, passes, sweep, 0, ids, stream);
 }
 
 cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
@@ -519,7 +531,8 @@ cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const
     if (passes > kSweepMaxPasses) {
         return cudaErrorInvalidValue;
     }
-    cudaError_t err = keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, stream);
+    cudaError_t err =
+        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, nullptr, stream);
     if (err == cudaSuccess) {
         err = launch_onesweep_sort(scratch, n, passes, sweep, stream, launches, true);
     }
@@ -530,6 +543,62 @@ cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const
     if (launches != nullptr) {
         *launches += 2;
     }
+    return cudaGetLastError();
+}
+
+namespace {
+
+// ids[compact_base + j] = global_base + j for each range (one block per range).
+__global__ void __launch_bounds__(256) compact_ids_kernel(const uint32_t* __restrict__ ranges, uint32_t* __restrict__ ids) {
+    const uint32_t global_base = ranges[3 * blockIdx.x];
+    const uint32_t compact_base = ranges[3 * blockIdx.x + 1];
+    const uint32_t count = ranges[3 * blockIdx.x + 2];
+    for (uint32_t j = threadIdx.x; j < count; j += blockDim.x) {
+        ids[compact_base + j] = global_base + j;
+    }
+}
+
+}  // namespace
+
+namespace {
+
+// A chunk of active flags travels as the launch's argument: nothing to copy
+// (and nothing for the host to wait on) before the launch.
+constexpr uint32_t kFlagChunk = 2048;
+struct FlagChunk {
+    uint32_t first;
+    uint32_t count;
+    uint8_t flag[kFlagChunk];
+};
+
+__global__ void __launch_bounds__(256) set_active_kernel(TankConst* __restrict__ tanks, const FlagChunk chunk) {
+    for (uint32_t j = threadIdx.x; j < chunk.count; j += blockDim.x) {
+        tanks[chunk.first + j].active = chunk.flag[j] != 0 ? 1u : 0u;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_set_active(TankConst* tanks, const uint8_t* active, uint32_t count, cudaStream_t stream) {
+    for (uint32_t first = 0; first < count; first += kFlagChunk) {
+        FlagChunk chunk;
+        chunk.first = first;
+        chunk.count = count - first < kFlagChunk ? count - first : kFlagChunk;
+        std::memcpy(chunk.flag, active + first, chunk.count);
+        set_active_kernel<<<1, 256, 0, stream>>>(tanks, chunk);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) {
+            return err;
+        }
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_compact_ids(const uint32_t* ranges, uint32_t range_count, uint32_t* ids, cudaStream_t stream) {
+    if (range_count == 0) {
+        return cudaSuccess;
+    }
+    compact_ids_kernel<<<range_count, 256, 0, stream>>>(ranges, ids);
     return cudaGetLastError();
 }
 
@@ -645,13 +714,14 @@ cudaError_t launch_radix_sort(GridScratch& s, uint32_t n, const RadixPlan& plan,
 
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
-                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream) {
+                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream,
+                                 const uint32_t* ids, uint32_t* global_sorted) {
     if (n == 0) {
         return cudaSuccess;
     }
     bounds_gather_kernel<<<(n + 255) / 256, 256, 0, stream>>>(sorted_keys, sorted_ids, n,
                                                               reinterpret_cast<uint32_t*>(bucket), pos, vel, tank_of,
-                                                              spos, svel, stank, schedule);
+                                                              spos, svel, stank, schedule, ids, global_sorted);
     return cudaGetLastError();
 }
 

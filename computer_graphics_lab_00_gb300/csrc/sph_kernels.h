@@ -72,8 +72,15 @@ inline uint32_t onesweep_passes(uint32_t key_bits) { return key_bits == 0 ? 1 : 
 size_t onesweep_scratch_words(uint32_t n, uint32_t passes);
 // Keys (as launch_keys) plus the first pass's tile counts and every pass's
 // digit histogram; zeroes the scratch first.
+// ids (optional): the particles keyed are pos[ids[v]] for v < n (a compacted set).
 cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
-                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream);
+                                 uint32_t* keys, uint32_t passes, unsigned long long* sweep, cudaStream_t stream,
+                                 const uint32_t* ids = nullptr);
+// tanks[t].active = active[t] != 0 for every tank (`active` in host memory,
+// passed by launch argument).
+cudaError_t launch_set_active(TankConst* tanks, const uint8_t* active, uint32_t count, cudaStream_t stream);
+// Fills ids from (global_base, compact_base, count) triples, one per range.
+cudaError_t launch_compact_ids(const uint32_t* ranges, uint32_t range_count, uint32_t* ids, cudaStream_t stream);
 // The digit passes over keys made by launch_keys_onesweep. aggregate: one
 // atomic per group of lanes adding to the same count (keys whose digits bunch
 // up, as Morton codes of a compact body do).
@@ -103,9 +110,12 @@ cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const
 // Bucket table (start, end) from sorted keys (table pre-zeroed), the
 // cell-ordered copies of position, velocity and tank id, and (with a
 // schedule) the processing order.
+// With `ids` the sorted entries index a compacted set: the particle is
+// ids[entry], and global_sorted[p] receives its id for the write-back.
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
-                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream);
+                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream,
+                                 const uint32_t* ids = nullptr, uint32_t* global_sorted = nullptr);
 
 // Shape of the neighbour passes. variant 0: one thread per particle with
 // nested bucket loops; 1: flat candidate stream (density) and the queued pair
@@ -126,6 +136,7 @@ struct NeighbourTuning {
     uint32_t list_cap = 64;
     uint32_t* masks = nullptr;  // 27 words per particle, bucket-major (variant 4)
     const uint32_t* order = nullptr;  // processing order (null: sorted order)
+    bool all_tanks = false;           // density of inactive tanks too (variant 4 skips them otherwise)
 };
 
 // Density and pressure (fluid_sph.cpp:200-222). Writes spos2 = (xyz, rho)

@@ -72,6 +72,48 @@ def test_per_tank_step_lengths_and_frozen_tanks(native, oracle, tanks):
             assert same(gp, op) and same(gv, ov), f"tank {t}"
 
 
+def test_few_active_tanks_build_a_compacted_grid(native, oracle, tanks):
+    """With at most half the particles active, run() builds the grid over the
+    active tanks alone (a compacted id list). The active tanks match the
+    oracle, idle tanks keep their bits, and a full run afterwards (every tank
+    active again) continues bit-exactly."""
+    n = len(tanks.counts)
+    states = [tanks.initial_state(t) for t in range(n)]
+    with load(tanks) as solver:
+        active = [0] * n
+        active[0] = 1
+        active[3] = 1
+        assert tanks.counts[0] + tanks.counts[3] <= sum(tanks.counts) // 2
+        solver.set_active(active)
+        solver.run(tanks.dt, 4)
+        solver.set_active([1] * n)
+        solver.run(tanks.dt, 2)
+        for t in range(n):
+            gp, gv = solver.download(t)
+            runs = 6 if active[t] else 2
+            op, ov = oracle.run_substeps(tanks.params[t], *states[t], tanks.dt, runs)
+            assert same(gp, op) and same(gv, ov), f"tank {t}"
+
+
+def test_restore_selected_tanks_from_a_snapshot(native, tanks):
+    """restore_tanks copies back exactly the selected tanks (adjacent ones in
+    one copy) and leaves the others as they ran."""
+    n = len(tanks.counts)
+    with load(tanks) as solver:
+        solver.run(tanks.dt, 2)
+        saved = [solver.download(t) for t in range(n)]
+        solver.snapshot(1, save=True)
+        solver.run(tanks.dt, 3)
+        moved = [solver.download(t) for t in range(n)]
+        which = [1, 1, 0, 1, 0, 1][:n]
+        solver.restore_tanks(1, which)
+        for t in range(n):
+            gp, gv = solver.download(t)
+            want = saved[t] if which[t] else moved[t]
+            assert same(gp, want[0]) and same(gv, want[1]), f"tank {t}"
+            assert which[t] or not same(gp, saved[t][0])
+
+
 def test_batch_step_matches_fluid_solver_step(native, oracle, tanks):
     with load(tanks) as solver:
         for _ in range(3):
