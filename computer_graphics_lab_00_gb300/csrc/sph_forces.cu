@@ -13,6 +13,8 @@
 // rounding of each operation.
 #include "sph_kernels.h"
 
+#include <type_traits>
+
 namespace sph {
 
 namespace {
@@ -1281,34 +1283,52 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
     float density = 0.0f;
     uint32_t candidates = 0;
     uint32_t in_range = 0;
-    for (uint32_t b = 0; b < 27u; ++b) {
-        uint2 r = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base);
-        uint32_t word = 0;
-        if (kCount) {
-            candidates += r.y - r.x;
-        }
-        const float4* cand = spos + r.x;
-        const uint32_t count = r.y - r.x;
-        // Branch-free candidate loop: every lane runs the same instructions
-        // for every candidate, so a warp issues each of them once.
-#pragma unroll 4
-        for (uint32_t s = 0; s < count; ++s) {
-            float4 other = __ldg(&cand[s]);
-            float r2 = dot3(__fsub_rn(self.x, other.x), __fsub_rn(self.y, other.y), __fsub_rn(self.z, other.z));
-            // mass * poly6 (fluid_sph.cpp:24-31, :214) in candidate order; out
-            // of range the reference adds mass * 0 = +0, which leaves the
-            // (non-negative) sum's bits as they are.
-            float d = __fsub_rn(h2, r2);
-            float term = __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d));
-            density = __fadd_rn(density, r2 >= h2 ? 0.0f : term);
+    // kMax: out-of-range terms are dropped by max.NaN(term, +0), valid while
+    // mass * c_poly6 > 0 (then out of range, where d <= 0, the term is negative
+    // or +0); otherwise by the reference's compare and select.
+    auto walk = [&](auto max_form) {
+        constexpr bool kMax = decltype(max_form)::value;
+        for (uint32_t b = 0; b < 27u; ++b) {
+            uint2 r = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base);
+            uint32_t word = 0;
             if (kCount) {
-                in_range += r2 < h2 ? 1u : 0u;
+                candidates += r.y - r.x;
             }
-            // Integrate skips distance >= h or <= 1e-6 (fluid_sph.cpp:245-248);
-            // the particle itself (r2 = 0) fails the second test.
-            word |= static_cast<uint32_t>(!(r2 >= r2_far || r2 <= r2_near)) << s;
+            const float4* cand = spos + r.x;
+            const uint32_t count = r.y - r.x;
+            // Branch-free candidate loop: every lane runs the same instructions
+            // for every candidate, so a warp issues each of them once.
+#pragma unroll 2
+            for (uint32_t s = 0; s < count; ++s) {
+                float4 other = __ldg(&cand[s]);
+                float r2 = dot3(__fsub_rn(self.x, other.x), __fsub_rn(self.y, other.y), __fsub_rn(self.z, other.z));
+                // mass * poly6 (fluid_sph.cpp:24-31, :214) in candidate order;
+                // out of range the reference adds mass * 0 = +0, which leaves
+                // the (non-negative) sum's bits as they are, and a NaN distance
+                // makes the sum NaN (max.NaN keeps it).
+                float d = __fsub_rn(h2, r2);
+                float term = __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d));
+                float kept;
+                if (kMax) {
+                    asm("max.NaN.f32 %0, %1, %2;" : "=f"(kept) : "f"(term), "f"(0.0f));
+                } else {
+                    kept = r2 >= h2 ? 0.0f : term;
+                }
+                density = __fadd_rn(density, kept);
+                if (kCount) {
+                    in_range += r2 < h2 ? 1u : 0u;
+                }
+                // Integrate skips distance >= h or <= 1e-6 (fluid_sph.cpp:245-248);
+                // the particle itself (r2 = 0) fails the second test.
+                word |= static_cast<uint32_t>(!(r2 >= r2_far || r2 <= r2_near)) << s;
+            }
+            masks[static_cast<size_t>(b) * n + slot] = word;
         }
-        masks[static_cast<size_t>(b) * n + slot] = word;
+    };
+    if (mass > 0.0f && c6 > 0.0f) {
+        walk(std::true_type{});
+    } else {
+        walk(std::false_type{});
     }
     if (kCount) {
         unsigned long long c = candidates;

@@ -227,6 +227,23 @@ def test_1m_compressed_state_bit_exact(native, oracle):
     assert_bit_exact(gv, ov, "1M velocities from the compressed state")
 
 
+@pytest.mark.parametrize("mass", [0.0, -0.3])
+def test_nonpositive_mass_matches_oracle(native, oracle, mass):
+    """Density drops out-of-range terms with a NaN-keeping max while mass and
+    the poly6 constant are positive, and with the reference's select
+    otherwise; a zero or negative particle mass takes the second form."""
+    n = 4096
+    params, pos, vel = small_block(n, (16, 16, 16), box=(0.5, 0.5, 0.5), cells=W.cell_count_for(n))
+    params.gravity[3] = mass
+    with FluidSolverGpu(params, n) as solver:
+        solver.upload(pos, vel)
+        solver.run(1.0 / 600.0, 2)
+        gp, gv = solver.state()
+    op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 2)
+    assert_bit_exact(gp, op, f"positions, mass {mass}")
+    assert_bit_exact(gv, ov, f"velocities, mass {mass}")
+
+
 def test_gpu_runs_are_deterministic(native):
     case = W.dam_break_16k()
     pos, vel = case.initial_state()
