@@ -1319,9 +1319,12 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
                     in_range += r2 < h2 ? 1u : 0u;
                 }
                 // Integrate skips distance >= h or <= 1e-6 (fluid_sph.cpp:245-248);
-                // the particle itself (r2 = 0) fails the second test.
-                word |= static_cast<uint32_t>(!(r2 >= r2_far || r2 <= r2_near)) << s;
+                // the particle itself (r2 = 0) fails the second test. Slot s's
+                // bit is shifted in s-th (no per-candidate shift count).
+                word = (word << 1) | static_cast<uint32_t>(!(r2 >= r2_far || r2 <= r2_near));
             }
+            // Reverse into place: bit s for slot s (count <= 32 slots).
+            word = count == 0 ? 0u : (__brev(word) >> (32u - count));
             masks[static_cast<size_t>(b) * n + slot] = word;
         }
     };
