@@ -129,9 +129,11 @@ typedef struct sph_tuning {
                                   2: density records in-range pairs, integrate runs them;
                                   3: as 2, divisions through a shared correctly rounded reciprocal;
                                   4: density stores per-bucket pair masks, integrate expands them */
-    uint32_t block_size;       /* threads per block of integrate (32..512, multiple of 32; 64/128/256 for 2-4) */
+    uint32_t block_size;       /* threads per block of integrate (32..512, multiple of 32; 64/128/256 for 2-4;
+                                  default 128) */
     uint32_t queue_depth;      /* in-range pairs buffered per thread: 8, 16, 24 or 32 */
-    uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 (default) Morton order of the cells, remade every 8 grid builds */
+    uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 (default) Morton order of
+                                  the cells, remade every 8 grid builds */
     uint32_t sort;             /* grid sort: 0 three kernels per digit pass (radix_bits wide);
                                   1 one kernel per 8-bit pass, tile offsets from tile digit counts
                                     made by the previous pass (radix_bits unused) */
@@ -402,7 +404,9 @@ int sph_batch_download(sph_batch* batch, uint32_t tank, float* positions, float*
 int sph_batch_emit(sph_batch* batch, uint32_t tank);
 /* Tanks with active[t] == 0 keep their state through later substeps. */
 int sph_batch_set_active(sph_batch* batch, const uint8_t* active);
-/* `substeps` substeps of `dt` for every active tank. */
+/* `substeps` substeps of `dt` for every active tank. While the active tanks
+ * hold at most half the particles, the grid is built over their particles
+ * alone (same bits, less work). */
 int sph_batch_run(sph_batch* batch, float dt, uint32_t substeps);
 /* Tank t runs substeps[t] substeps of dt[t]; tanks done early sit out. */
 int sph_batch_run_per_tank(sph_batch* batch, const float* dt, const uint32_t* substeps);
