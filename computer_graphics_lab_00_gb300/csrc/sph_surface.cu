@@ -492,81 +492,114 @@ __device__ __forceinline__ float3 gradient(const float* __restrict__ field, int 
     return make_float3(__fdiv_rn(gx, g.cell[0]), __fdiv_rn(gy, g.cell[1]), __fdiv_rn(gz, g.cell[2]));
 }
 
+// One vertex of a cell (marching_cubes.cpp:418-478): the interpolated point on
+// table entry v's edge and the packed outward normal.
+__device__ __forceinline__ sph_surface_vertex cell_vertex(const float* __restrict__ field, const MarchGeom& g,
+                                                          uint32_t cell, uint32_t code, uint32_t v) {
+    const int s = static_cast<int>(g.resolution) + 1;
+    const int base[3] = {static_cast<int>(cell % g.resolution), static_cast<int>((cell / g.resolution) % g.resolution),
+                         static_cast<int>(cell / (g.resolution * g.resolution))};
+    const int edge = c_entry[code][v];
+    const int a = c_edge[edge][0];
+    const int b = c_edge[edge][1];
+    int ca[3], cb[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        ca[d] = base[d] + c_corner[a][d];
+        cb[d] = base[d] + c_corner[b][d];
+    }
+    const float va = field_at(field, s, ca[0], ca[1], ca[2]);
+    const float vb = field_at(field, s, cb[0], cb[1], cb[2]);
+    const float diff = __fsub_rn(vb, va);
+    float t = fabsf(diff) > 1.0e-8f ? __fdiv_rn(__fsub_rn(g.iso, va), diff) : 0.5f;
+    t = t < 0.0f ? 0.0f : (1.0f < t ? 1.0f : t);
+    float p[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float pa = __fadd_rn(g.origin[d], __fmul_rn(static_cast<float>(ca[d]), g.cell[d]));
+        const float pb = __fadd_rn(g.origin[d], __fmul_rn(static_cast<float>(cb[d]), g.cell[d]));
+        p[d] = __fadd_rn(pa, __fmul_rn(__fsub_rn(pb, pa), t));
+    }
+    const float3 ga = gradient(field, s, ca[0], ca[1], ca[2], g);
+    const float3 gb = gradient(field, s, cb[0], cb[1], cb[2], g);
+    // Outward normal: minus the interpolated gradient.
+    float nx = -__fadd_rn(ga.x, __fmul_rn(__fsub_rn(gb.x, ga.x), t));
+    float ny = -__fadd_rn(ga.y, __fmul_rn(__fsub_rn(gb.y, ga.y), t));
+    float nz = -__fadd_rn(ga.z, __fmul_rn(__fsub_rn(gb.z, ga.z), t));
+    if (!(__fsqrt_rn(dot3(nx, ny, nz)) > 1.0e-12f)) {
+        nx = 0.0f;
+        ny = 1.0f;
+        nz = 0.0f;
+    }
+    // glm::normalize: v * (1 / sqrt(dot(v, v))).
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(nx, ny, nz)));
+    sph_surface_vertex vert;
+    vert.position[0] = p[0];
+    vert.position[1] = p[1];
+    vert.position[2] = p[2];
+    vert.normal = pack_unit_vector(__fmul_rn(nx, inv), __fmul_rn(ny, inv), __fmul_rn(nz, inv));
+    return vert;
+}
+
 // Places every cell's vertices at its serial slot (marching_cubes.cpp:397-481).
+// Few cells cut the surface, so the block first lays out its tile (codes and
+// each thread's first vertex in shared memory) and then deals the tile's
+// vertices out round-robin: a thread finds a vertex's cell by binary search
+// over the threads' first vertices and a walk over that thread's cells.
 __global__ void __launch_bounds__(kBlock) emit_kernel(const float* __restrict__ field, MarchGeom g,
                                                       const uint8_t* __restrict__ codes,
                                                       const uint32_t* __restrict__ offsets, uint32_t capacity,
                                                       uint32_t* __restrict__ limit,
                                                       sph_surface_vertex* __restrict__ out) {
+    __shared__ uint8_t s_code[kTile];
+    __shared__ uint32_t s_first[kBlock + 1];
+    __shared__ uint32_t total;
     const uint32_t cells = g.resolution * g.resolution * g.resolution;
-    const uint32_t first = blockIdx.x * kTile + threadIdx.x * kPerThread;
-    uint8_t code[kPerThread];
+    const uint32_t tile_first = blockIdx.x * kTile;
     uint32_t sum = 0;
 #pragma unroll
     for (uint32_t k = 0; k < kPerThread; ++k) {
-        const uint32_t cell = first + k;
-        code[k] = cell < cells ? codes[cell] : 0;
-        sum += c_count[code[k]];
+        const uint32_t cell = tile_first + threadIdx.x * kPerThread + k;
+        const uint32_t code = cell < cells ? codes[cell] : 0u;
+        s_code[threadIdx.x * kPerThread + k] = static_cast<uint8_t>(code);
+        sum += c_count[code];
     }
-    __shared__ uint32_t total;
-    uint32_t slot = offsets[blockIdx.x] + block_exclusive_scan(sum, &total);
-    const int s = static_cast<int>(g.resolution) + 1;
-    for (uint32_t k = 0; k < kPerThread; ++k) {
-        const uint32_t n = c_count[code[k]];
-        if (n == 0) {
+    s_first[threadIdx.x] = block_exclusive_scan(sum, &total);
+    if (threadIdx.x == 0) {
+        s_first[kBlock] = total;
+    }
+    __syncthreads();
+    const uint32_t block_slot = offsets[blockIdx.x];
+    const uint32_t vertices = s_first[kBlock];
+    for (uint32_t v = threadIdx.x; v < vertices; v += kBlock) {
+        // The thread whose vertices hold v: the last t with s_first[t] <= v
+        // (threads without vertices share their successor's first vertex).
+        uint32_t lo = 0;
+        uint32_t hi = kBlock;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_first[mid] <= v) {
+                lo = mid;
+            } else {
+                hi = mid;
+            }
+        }
+        uint32_t rem = v - s_first[lo];
+        uint32_t local = s_first[lo];
+        uint32_t k = lo * kPerThread;
+        uint32_t n = c_count[s_code[k]];
+        while (rem >= n) {
+            rem -= n;
+            local += n;
+            n = c_count[s_code[++k]];
+        }
+        const uint32_t slot = block_slot + local;  // the cell's first vertex
+        if (slot + n > capacity) {
+            // The cell and every later one are dropped, as in the reference.
+            atomicMin(limit, slot);
             continue;
         }
-        const uint32_t cell = first + k;
-        if (slot + n > capacity) {
-            atomicMin(limit, slot);
-            return;  // this thread's later cells lie further still
-        }
-        const int base[3] = {static_cast<int>(cell % g.resolution),
-                             static_cast<int>((cell / g.resolution) % g.resolution),
-                             static_cast<int>(cell / (g.resolution * g.resolution))};
-        for (uint32_t v = 0; v < n; ++v) {
-            const int edge = c_entry[code[k]][v];
-            const int a = c_edge[edge][0];
-            const int b = c_edge[edge][1];
-            int ca[3], cb[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                ca[d] = base[d] + c_corner[a][d];
-                cb[d] = base[d] + c_corner[b][d];
-            }
-            const float va = field_at(field, s, ca[0], ca[1], ca[2]);
-            const float vb = field_at(field, s, cb[0], cb[1], cb[2]);
-            const float diff = __fsub_rn(vb, va);
-            float t = fabsf(diff) > 1.0e-8f ? __fdiv_rn(__fsub_rn(g.iso, va), diff) : 0.5f;
-            t = t < 0.0f ? 0.0f : (1.0f < t ? 1.0f : t);
-            float p[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const float pa = __fadd_rn(g.origin[d], __fmul_rn(static_cast<float>(ca[d]), g.cell[d]));
-                const float pb = __fadd_rn(g.origin[d], __fmul_rn(static_cast<float>(cb[d]), g.cell[d]));
-                p[d] = __fadd_rn(pa, __fmul_rn(__fsub_rn(pb, pa), t));
-            }
-            const float3 ga = gradient(field, s, ca[0], ca[1], ca[2], g);
-            const float3 gb = gradient(field, s, cb[0], cb[1], cb[2], g);
-            // Outward normal: minus the interpolated gradient.
-            float nx = -__fadd_rn(ga.x, __fmul_rn(__fsub_rn(gb.x, ga.x), t));
-            float ny = -__fadd_rn(ga.y, __fmul_rn(__fsub_rn(gb.y, ga.y), t));
-            float nz = -__fadd_rn(ga.z, __fmul_rn(__fsub_rn(gb.z, ga.z), t));
-            if (!(__fsqrt_rn(dot3(nx, ny, nz)) > 1.0e-12f)) {
-                nx = 0.0f;
-                ny = 1.0f;
-                nz = 0.0f;
-            }
-            // glm::normalize: v * (1 / sqrt(dot(v, v))).
-            const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3(nx, ny, nz)));
-            sph_surface_vertex vert;
-            vert.position[0] = p[0];
-            vert.position[1] = p[1];
-            vert.position[2] = p[2];
-            vert.normal = pack_unit_vector(__fmul_rn(nx, inv), __fmul_rn(ny, inv), __fmul_rn(nz, inv));
-            out[slot + v] = vert;
-        }
-        slot += n;
+        out[slot + rem] = cell_vertex(field, g, tile_first + k, s_code[k], rem);
     }
 }
 
