@@ -1342,7 +1342,7 @@ int Engine::set_active(const std::vector<uint8_t>& active) {
 }
 
 int Engine::selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t* mismatches) {
-    if (mismatches == nullptr || mode < 0 || mode > 5) {
+    if (mismatches == nullptr || mode < 0 || mode > 6) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     SPH_CUDA(cudaSetDevice(device_));

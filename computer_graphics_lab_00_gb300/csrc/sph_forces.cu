@@ -1091,18 +1091,6 @@ __global__ void __launch_bounds__(128) density_list_kernel(const float4* __restr
     reinterpret_cast<float*>(svel)[4 * static_cast<size_t>(p) + 3] = pressure;
 }
 
-// Correctly rounded x / y given r = RN(1/y): q = RN(x r) is within one ulp of
-// x / y, the residual x - q y is exact in one FMA, and one more FMA rounds
-// q + (x - q y) r to the correctly rounded quotient (Markstein's division
-// theorem; P. Markstein, IBM J. Res. Dev. 34(1), 1990). Holds for the
-// magnitudes of this solver (no overflow or subnormal intermediates). A zero
-// dividend yields +0 where IEEE division gives the dividend's signed zero; the
-// force sums it feeds start at +0 and so never change bits because of it.
-__device__ __forceinline__ float div_by(float x, float y, float r) {
-    float q = __fmul_rn(x, r);
-    float e = __fmaf_rn(-q, y, x);
-    return __fmaf_rn(e, r, q);
-}
 
 // Intermediates of one pair that the learned step's features reuse.
 struct PairParts {
@@ -1642,7 +1630,13 @@ __global__ void division_selftest_kernel(uint64_t seed, uint64_t count, int mode
     for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
         float x;
         float y;
-        if (mode == 0) {
+        if (mode == 6) {
+            // Consecutive floats x from the one with the seed's high 32 bits,
+            // y the float with its low 32 bits: the quotients x / y in [0, 1)
+            // of the surface field's d2 / radius^2.
+            x = __uint_as_float(static_cast<uint32_t>(seed >> 32) + static_cast<uint32_t>(i));
+            y = __uint_as_float(static_cast<uint32_t>(seed));
+        } else if (mode == 0) {
             // Every divisor mantissa in [1, 2) against dividends from a mixer.
             uint32_t ym = static_cast<uint32_t>(i & 0x7FFFFFu);
             uint64_t z = (i >> 23) * 0x9E3779B97F4A7C15ULL + seed;
@@ -1665,7 +1659,7 @@ __global__ void division_selftest_kernel(uint64_t seed, uint64_t count, int mode
         }
         float want;
         float got;
-        if (mode <= 1) {
+        if (mode <= 1 || mode == 6) {
             want = __fdiv_rn(x, y);
             got = div_by(x, y, __frcp_rn(y));
         } else {

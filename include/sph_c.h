@@ -367,7 +367,9 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning);
 /* Diagnostic: counts, over `count` generated (x, y), the quotients where
  * division through a correctly rounded reciprocal (the integrate pass of
  * neighbour_kernel 3) differs from IEEE x / y. mode 0: every divisor mantissa
- * in [1, 2); mode 1: random signs, mantissas and exponents 2^-60..2^60. */
+ * in [1, 2); mode 1: random signs, mantissas and exponents 2^-60..2^60; mode 6:
+ * y = the float with the seed's low 32 bits and x `count` consecutive floats
+ * from the one with its high 32 bits (an exhaustive sweep of one divisor). */
 int sph_selftest_division(sph_ctx* ctx, uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
 /* Number of kernel launches one substep enqueues. */
 int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches);

@@ -412,6 +412,37 @@ def test_reciprocal_division_matches_ieee(native, mode, count):
         assert bad.value == 0
 
 
+def _sweep_mismatches(native, x_from, x_to, y):
+    """Dividends x in [x_from, x_to) (every float), divisor y: how many
+    quotients through the reciprocal differ from IEEE division."""
+    import ctypes
+
+    lo = int(np.array([x_from], np.float32).view(np.uint32)[0])
+    hi = int(np.array([x_to], np.float32).view(np.uint32)[0])
+    yb = int(np.array([y], np.float32).view(np.uint32)[0])
+    bad = ctypes.c_uint64()
+    with FluidSolverGpu(W.dam_break_16k().params, 16) as solver:
+        assert native.sph_selftest_division(solver._ctx, (lo << 32) | yb, hi - lo, 6, ctypes.byref(bad)) == 0
+    return bad.value
+
+
+@pytest.mark.parametrize("divisor", [0.04 * 0.04, 0.1 * 0.1, 1.0, 998.3, 3.7e-5])
+def test_reciprocal_division_floor(native, divisor):
+    """Exhaustive over one divisor: division through the correctly rounded
+    reciprocal equals IEEE division for every dividend from 2^-100 up to the
+    divisor, the floor the exact passes rely on (their dividends stay far
+    above it)."""
+    y = np.float32(divisor)
+    assert _sweep_mismatches(native, np.float32(2.0 ** -100), y, y) == 0
+
+
+def test_reciprocal_division_below_the_floor_can_differ(native):
+    """Below about 2^-105 the FMA residual underflows and some quotients are
+    one ulp off IEEE division: the reason for the floor."""
+    y = np.float32(0.04) * np.float32(0.04)
+    assert _sweep_mismatches(native, np.float32(0.0), np.float32(2.0 ** -100), y) > 0
+
+
 def test_pair_list_overflow_falls_back_bit_exact(native, oracle):
     """Particles with more in-range pairs than a list holds (64) are scanned
     directly by integrate; a compressed clump forces that path."""
