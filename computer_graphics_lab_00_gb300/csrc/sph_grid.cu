@@ -367,30 +367,33 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift, const uint32_t* __restrict__ hist,
     const uint32_t* __restrict__ tile_counts, uint32_t* __restrict__ next_counts, uint32_t next_shift) {
-    static_assert(kSweepThreads == kSweepBins, "one thread per digit");
+    static_assert(kSweepThreads % kSweepBins == 0 && kSweepThreads >= kSweepBins,
+                  "the first kSweepBins threads each own one digit");
     constexpr uint32_t kWarps = kSweepThreads / 32;
+    constexpr uint32_t kRowLanes = kSweepThreads / (kSweepBins / 4);  // count rows read side by side
     __shared__ uint32_t warp_counts[kWarps][kSweepBins];
     __shared__ uint32_t digit_offset[kSweepBins];
-    __shared__ uint32_t scan_warp[kWarps];
+    __shared__ uint32_t scan_warp[kSweepBins / 32];
     for (uint32_t k = threadIdx.x; k < kWarps * kSweepBins; k += blockDim.x) {
         (&warp_counts[0][0])[k] = 0;
     }
     const uint32_t tile = blockIdx.x;
-    const uint32_t d = threadIdx.x;
+    const uint32_t d = threadIdx.x;  // the digit this thread owns (threads below kSweepBins)
+    const bool owns_digit = d < kSweepBins;
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t lane = threadIdx.x & 31;
     // Every digit's keys in all earlier tiles: the block reads the earlier
-    // tiles' count rows four at a time (a row is 64 uint4, thread k reads
+    // tiles' count rows kRowLanes at a time (a row is 64 uint4, thread k reads
     // column k % 64 of row j + k / 64), eight rows' loads in flight per thread,
-    // then the four partial sums of each digit meet in shared memory.
-    __shared__ uint4 partial[4][kSweepBins / 4];
+    // then the partial sums of each digit meet in shared memory.
+    __shared__ uint4 partial[kRowLanes][kSweepBins / 4];
     {
         const uint32_t column = threadIdx.x & 63u;
         const uint32_t lane_row = threadIdx.x >> 6;
         const uint4* rows = reinterpret_cast<const uint4*>(tile_counts);
         uint4 acc = make_uint4(0, 0, 0, 0);
 #pragma unroll 8
-        for (uint32_t j = lane_row; j < tile; j += 4) {
+        for (uint32_t j = lane_row; j < tile; j += kRowLanes) {
             uint4 c = __ldg(&rows[static_cast<size_t>(j) * (kSweepBins / 4) + column]);
             acc.x += c.x;
             acc.y += c.y;
@@ -399,18 +402,20 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
         }
         partial[lane_row][column] = acc;
     }
-    // Digit base: exclusive scan of the pass histogram.
-    const uint32_t h = __ldg(&hist[d]);
+    // Digit base: exclusive scan of the pass histogram (digit-owning warps).
+    const uint32_t h = owns_digit ? __ldg(&hist[d]) : 0u;
     uint32_t inc = h;
+    if (owns_digit) {
 #pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-        if (lane >= o) {
-            inc += u;
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) {
+                inc += u;
+            }
         }
-    }
-    if (lane == 31) {
-        scan_warp[warp] = inc;
+        if (lane == 31) {
+            scan_warp[warp] = inc;
+        }
     }
     __syncthreads();
     const uint32_t below = lanemask_lt();
@@ -439,20 +444,26 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
         __syncwarp();
     }
     __syncthreads();
-    uint32_t running = 0;
+    if (owns_digit) {
+        uint32_t running = 0;
 #pragma unroll
-    for (uint32_t w = 0; w < kWarps; ++w) {
-        uint32_t c = warp_counts[w][d];
-        warp_counts[w][d] = running;
-        running += c;
+        for (uint32_t w = 0; w < kWarps; ++w) {
+            uint32_t c = warp_counts[w][d];
+            warp_counts[w][d] = running;
+            running += c;
+        }
+        uint32_t warp_base = 0;
+        for (uint32_t w = 0; w < warp; ++w) {
+            warp_base += scan_warp[w];
+        }
+        const uint32_t* flat = reinterpret_cast<const uint32_t*>(&partial[0][0]);
+        uint32_t before = 0;
+#pragma unroll
+        for (uint32_t l = 0; l < kRowLanes; ++l) {
+            before += flat[l * kSweepBins + d];
+        }
+        digit_offset[d] = warp_base + inc - h + before;
     }
-    uint32_t warp_base = 0;
-    for (uint32_t w = 0; w < warp; ++w) {
-        warp_base += scan_warp[w];
-    }
-    const uint32_t* flat = reinterpret_cast<const uint32_t*>(&partial[0][0]);
-    const uint32_t before = flat[d] + flat[kSweepBins + d] + flat[2 * kSweepBins + d] + flat[3 * kSweepBins + d];
-    digit_offset[d] = warp_base + inc - h + before;
     __syncthreads();
 #pragma unroll
     for (uint32_t r = 0; r < kSweepItems; ++r) {

@@ -64,8 +64,8 @@ cudaError_t launch_radix_sort(GridScratch& scratch, uint32_t n, const RadixPlan&
 constexpr uint32_t kSweepBits = 8;
 constexpr uint32_t kSweepBins = 1u << kSweepBits;
 constexpr uint32_t kSweepMaxPasses = 4;
-constexpr uint32_t kSweepThreads = 256;                      // threads of a pass block (one per digit)
-constexpr uint32_t kSweepItems = 16;                         // keys per thread in a tile
+constexpr uint32_t kSweepThreads = 512;                      // threads of a pass block (the first 256 own a digit each)
+constexpr uint32_t kSweepItems = 8;                          // keys per thread in a tile
 constexpr uint32_t kSweepTile = kSweepThreads * kSweepItems;  // 4096 keys per tile
 inline uint32_t sweep_tiles(uint32_t n) { return (n + kSweepTile - 1) / kSweepTile; }
 inline uint32_t onesweep_passes(uint32_t key_bits) { return key_bits == 0 ? 1 : (key_bits + kSweepBits - 1) / kSweepBits; }
