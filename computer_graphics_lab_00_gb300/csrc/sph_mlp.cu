@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -691,21 +692,43 @@ void launch_erf_selftest(uint32_t count, unsigned int* out, cudaStream_t stream)
     erf_selftest_kernel<<<152 * 4, 256, 0, stream>>>(count, out);
 }
 
+namespace {
+
+// Kernel attributes are per device: which devices have had them set.
+std::mutex g_attribute_guard;
+uint64_t g_forward_ready = 0;
+uint64_t g_backward_ready = 0;
+
+// Runs `set` once per device (devices past 63 every time), under the guard.
+template <typename Set>
+cudaError_t once_per_device(uint64_t* ready, Set set) {
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    std::lock_guard<std::mutex> lock(g_attribute_guard);
+    if (device < 64 && (*ready >> device & 1u) != 0) {
+        return cudaSuccess;
+    }
+    if ((e = set()) == cudaSuccess && device < 64) {
+        *ready |= 1ull << device;
+    }
+    return e;
+}
+
+}  // namespace
+
 cudaError_t prepare_forward() {
-    static bool configured = false;
-    if (!configured) {
+    return once_per_device(&g_forward_ready, [] {
         cudaError_t e = cudaFuncSetAttribute(mlp_forward_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(kSmemBytes));
         if (e == cudaSuccess) {
             e = cudaFuncSetAttribute(mlp_forward_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(kSmemBytes));
         }
-        if (e != cudaSuccess) {
-            return e;
-        }
-        configured = true;
-    }
-    return cudaSuccess;
+        return e;
+    });
 }
 
 size_t backward_scratch_floats(uint32_t n) {
@@ -727,14 +750,12 @@ cudaError_t launch_backward(const ModelView& model, const ForwardSaves& saves, c
     float* loss_parts = partial + static_cast<size_t>(chunks) * kHidden * (kHidden + 1);
     uint32_t blocks = (n + 127) / 128;
     size_t smem = (kHidden * kHidden + kOut * kHidden + 128 * kHidden) * sizeof(float);
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(backward_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem));
-        if (e != cudaSuccess) {
-            return e;
-        }
-        configured = true;
+    cudaError_t attr = once_per_device(&g_backward_ready, [smem] {
+        return cudaFuncSetAttribute(backward_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem));
+    });
+    if (attr != cudaSuccess) {
+        return attr;
     }
     backward_rows_kernel<<<blocks, 128, smem, stream>>>(model, saves, targets, n, dz1, dz2, dy, loss_parts);
     loss_sum_kernel<<<1, 32, 0, stream>>>(loss_parts, blocks, loss);
