@@ -16,6 +16,9 @@ Our arm (default) prints one JSON line with
            event-timed duration, against the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle (a restatement of the reference's CPU solver)
            timed on this host's cores on a bounded sample.
+On one GPU it adds the other legs: the whole 1,000-substep run (sustained),
+256 batched tanks, the learned 5x-dt step, the tank with shape colliders and
+force fields (obstacles), the instance writer and the fluid surface.
 `--impl reference` times the reference's CPU solver path (the oracle port,
 all host threads) on the same workload and metric.
 
@@ -66,6 +69,10 @@ def parse_args():
                    help="coarse steps of the learned 5x-dt leg at 1M (0 skips it)")
     p.add_argument("--sustained-steps", type=int, default=1000,
                    help="substeps of the whole-run leg of the 1M dam break (0 skips it)")
+    p.add_argument("--instance-reps", type=int, default=20,
+                   help="timed calls of the instance writer at 1M (0 skips it)")
+    p.add_argument("--obstacle-steps", type=int, default=50,
+                   help="substeps of the 1M colliders-and-fields leg, and of the plain tank beside it (0 skips it)")
     return p.parse_args()
 
 
@@ -328,6 +335,130 @@ def sustained_leg(steps: int, flush, device: int) -> dict:
     }
 
 
+def obstacles_leg(steps: int, flush, device: int, cpu: bool) -> dict:
+    """The 1M dam break with five shape colliders and three force fields
+    (workloads.obstacle_course_1m) beside the same tank without them: the
+    first `steps` substeps of each from the initial state, each timed with
+    CUDA events after an L2 flush. Its CPU baseline is the oracle with the
+    same shapes, two substeps on all host cores."""
+    import torch
+
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+
+    def timed(case) -> float:
+        with FluidSolverGpu(case.params, case.count, device=device) as solver:
+            solver.upload(*case.initial_state())
+            solver.run(case.dt, 3)
+            solver.synchronize()
+            stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
+            total = 0.0
+            for _ in range(steps):
+                start = torch.cuda.Event(enable_timing=True)
+                end = torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                    start.record(stream)
+                solver.run(case.dt, 1)
+                end.record(stream)
+                end.synchronize()
+                total += start.elapsed_time(end)
+        return total / steps
+
+    shapes = W.obstacle_course_1m()
+    plain_ms = timed(W.dam_break_1m())
+    ms = timed(shapes)
+    n = shapes.count
+    out = {
+        "workload": shapes.name, "colliders": int(shapes.params.collider_count),
+        "force_fields": int(shapes.params.field_count), "substeps": steps, "ms_per_step": ms,
+        "value": n * shapes.dt / (ms / 1e3), "unit": UNIT, "plain_ms_per_step": plain_ms,
+        "shape_overhead_ms": ms - plain_ms, "l2": "flushed before every substep",
+    }
+    if cpu:
+        from oracle.bind import Oracle
+
+        oracle = Oracle()
+        pos, vel = shapes.initial_state()
+        start = time.perf_counter()
+        oracle.run_substeps(shapes.params, pos, vel, shapes.dt, 2, threads=oracle.hardware_threads)
+        wall = time.perf_counter() - start
+        out["cpu_baseline"] = {"kind": "port", "cores": oracle.hardware_threads, "ms_per_step": 1e3 * wall / 2,
+                               "value": n * shapes.dt * 2 / wall, "unit": UNIT,
+                               "sample": "2 whole-tank substeps with the same colliders and fields"}
+    return out
+
+
+def instances_leg(reps: int, flush, device: int, cpu: bool) -> dict:
+    """The instance writer (sph_write_instances: one 224-byte draw instance
+    and one 64-byte TLAS record per particle, then keepRendered) for the 1M
+    dam break, timed with CUDA events after an L2 flush, against the measured
+    HBM copy bandwidth: it reads 32 bytes a particle (position, previous
+    position) and writes 288, plus keepRendered's 16 + 16. Its CPU baseline is
+    the oracle's restatement of the reference's CPU writer on all host
+    cores."""
+    import numpy as np
+    import torch
+
+    from computer_graphics_lab_00_gb300 import abi
+    from computer_graphics_lab_00_gb300 import workloads as W
+    from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
+
+    case = W.dam_break_1m()
+    n = case.count
+    per_particle = 32 + abi.INSTANCE.itemsize + abi.TLAS_INSTANCE.itemsize + 32
+    with FluidSolverGpu(case.params, n, device=device) as solver:
+        solver.upload(*case.initial_state())
+        solver.run(case.dt, 1)
+        inst = torch.empty(n * abi.INSTANCE.itemsize, dtype=torch.uint8, device=f"cuda:{device}")
+        tlas = torch.empty(n * abi.TLAS_INSTANCE.itemsize, dtype=torch.uint8, device=f"cuda:{device}")
+        stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", device))
+
+        def write():
+            solver.write_instances(inst.data_ptr(), 0, 0, tlas.data_ptr(), 0, 0x1000, 0, abi.SPH_INSTANCES_WRITE_TLAS)
+
+        for _ in range(3):
+            write()
+        solver.synchronize()
+        total = 0.0
+        for _ in range(reps):
+            start = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                start.record(stream)
+            write()
+            end.record(stream)
+            end.synchronize()
+            total += start.elapsed_time(end)
+        pos = solver.particles()
+        prev = solver.previous_particles()
+    ms = total / reps
+    peak, peak_kind = measured_hbm_peak()
+    achieved = per_particle * n / (ms / 1e3) / 1e9
+    out = {
+        "workload": case.name, "particles": n, "reps": reps, "ms_per_call": ms,
+        "bytes_per_particle": per_particle,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "l2": "flushed before every call",
+    }
+    if cpu:
+        from oracle.bind import Oracle
+
+        oracle = Oracle()
+        host_inst = np.zeros(n, abi.INSTANCE)
+        host_tlas = np.zeros(n, abi.TLAS_INSTANCE)
+        radius = float(case.params.container_min[3])
+        start = time.perf_counter()
+        oracle.write_instances(pos, prev, radius, host_inst, 0, 0, host_tlas, 0, 0x1000, 0,
+                               abi.SPH_INSTANCES_WRITE_TLAS, threads=oracle.hardware_threads)
+        wall = time.perf_counter() - start
+        out["cpu_baseline"] = {"kind": "port", "cores": oracle.hardware_threads, "ms_per_call": 1e3 * wall,
+                               "sample": "one call over the whole 1M tank"}
+    return out
+
+
 def learned_leg(steps: int, flush, device: int, plain_ms: float) -> dict:
     """The learned 5x-dt form on the same 1,048,576-particle tank: coarse
     steps of 1/240 s (plain force + tensor-core MLP correction), timed like
@@ -580,6 +711,10 @@ def run_gb300(args) -> None:
         out["batched"] = batched
     if args.learned_steps > 0 and world == 1 and WEIGHTS.exists():
         out["learned"] = learned_leg(args.learned_steps, flush, local, step_ms)
+    if world == 1 and args.obstacle_steps > 0:
+        out["obstacles"] = obstacles_leg(args.obstacle_steps, flush, local, not args.no_cpu_baseline)
+    if world == 1 and args.instance_reps > 0:
+        out["instances"] = instances_leg(args.instance_reps, flush, local, not args.no_cpu_baseline)
     if world == 1 and args.surface:
         out["surface"] = surface_leg(local)
     if world == 1 and not args.no_cpu_baseline:

@@ -309,6 +309,26 @@ def obstacle_course(seed: int = 0, count: int = 16384) -> Case:
     return Case("obstacle_course_16k", p, case.count, case.dt, case.steps, seed, case.notes)
 
 
+def obstacle_course_1m(seed: int = 0) -> Case:
+    """The 1M dam break with the 16k obstacle course scaled into its 4 x 2 x 2
+    m box (positions by the box, sizes and field radii by 2): a tilted plane,
+    a rotated box, a sphere, an upright cylinder, a lying capsule, a bounded
+    wind, an unbounded vortex and a bounded point attractor. Falloffs are 1,
+    where the reference's powf is exact."""
+    case = dam_break_1m(seed)
+    p = case.params
+    add_collider(p, PLANE, pose((2.2, 0.1, 0.7), ((0.0, 0.0, 1.0), 0.35)))
+    add_collider(p, BOX, pose((2.2, 0.24, 1.4), ((0.3, 1.0, 0.2), 0.6)), half_extents=(0.16, 0.2, 0.12))
+    add_collider(p, SPHERE, pose((1.2, 0.2, 0.4)), radius=0.18)
+    add_collider(p, CYLINDER, pose((3.2, 0.3, 1.0)), half_extents=(0.0, 0.3, 0.0), radius=0.14)
+    add_collider(p, CAPSULE, pose((1.8, 0.16, 1.0), ((1.0, 0.0, 0.0), 1.5707964)), half_extents=(0.0, 0.24, 0.0),
+                 radius=0.1)
+    add_force_field(p, WIND, (2.0, 0.6, 1.0), (1.0, 0.0, 0.0), 3.0, radius=1.2, falloff=1.0)
+    add_force_field(p, VORTEX, (2.0, 0.0, 1.0), (0.0, 1.0, 0.0), 4.0, radius=0.0)
+    add_force_field(p, POINT, (2.8, 0.8, 1.0), (0.0, 0.0, 0.0), 5.0, radius=1.0, falloff=1.0)
+    return Case("obstacle_course_1m", p, case.count, case.dt, case.steps, seed, case.notes)
+
+
 def obstacles_small() -> SphParams:
     """2,048 particles (16 x 16 x 8) in a 0.6 m box with one collider of each
     shape and one field of each kind close to the block, so that every

@@ -101,6 +101,9 @@ class Oracle:
                                                  f32p]
             lib.oracle_march_field.argtypes = [f32p, ctypes.c_uint32, f32p, f32p, ctypes.c_float, ctypes.c_void_p,
                                                ctypes.c_uint32, P(ctypes.c_uint32)]
+            lib.oracle_write_instances.argtypes = [f32p, f32p, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p,
+                                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                                                   ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
             Oracle._lib = lib
         self.lib = Oracle._lib
 
@@ -123,6 +126,18 @@ class Oracle:
 
     def march_field(self, field, resolution: int, origin, cell, iso: float, capacity: int):
         return _march(self.lib.oracle_march_field, field, resolution, origin, cell, iso, capacity)
+
+    def write_instances(self, pos, prev, radius: float, instances, instance_base: int = 0, sphere_mesh: int = 0,
+                        tlas=None, tlas_base: int = 0, blas: int = 0, fluid_index: int = 0, flags: int = 0,
+                        threads: int = 1) -> None:
+        """fluid.cpp:402-466 into the given structured arrays (abi.INSTANCE,
+        abi.TLAS_INSTANCE), which must hold the bases plus the count."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        prev = np.ascontiguousarray(prev if prev is not None else pos, dtype=np.float32)
+        rc = self.lib.oracle_write_instances(
+            _fp(pos), _fp(prev), pos.shape[0], ctypes.c_float(radius), instances.ctypes.data, instance_base,
+            sphere_mesh, None if tlas is None else tlas.ctypes.data, tlas_base, blas, fluid_index, flags, threads)
+        assert rc == 0
 
     def spatial_hash(self, cx: int, cy: int, cz: int, cells: int) -> int:
         return int(self.lib.oracle_spatial_hash(cx, cy, cz, cells))

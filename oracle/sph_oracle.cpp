@@ -1160,6 +1160,82 @@ int oracle_march_field(const float* field, uint32_t resolution, const float orig
     return SPH_OK;
 }
 
+// fluid.cpp:402-466. glm::scale(glm::translate(I, p), vec3{r}) has the
+// radius on the diagonal and the position in column 3; the TLAS transform is
+// that matrix's first three rows (row-major), as the reference copies it.
+int oracle_write_instances(const float* pos, const float* prev, uint32_t n, float radius, sph_instance* instances,
+                           uint32_t instance_base, uint32_t sphere_mesh, sph_tlas_instance* tlas, uint32_t tlas_base,
+                           uint64_t blas, uint32_t fluid_index, uint32_t flags, uint32_t threads) {
+    if (n == 0) {
+        return 0;
+    }
+    if (pos == nullptr || instances == nullptr || (prev == nullptr && (flags & SPH_INSTANCES_RESET_HISTORY) == 0) ||
+        ((flags & SPH_INSTANCES_WRITE_TLAS) != 0 && tlas == nullptr)) {
+        return 1;
+    }
+    const bool history = (flags & SPH_INSTANCES_RESET_HISTORY) == 0;
+    const bool write_tlas = (flags & SPH_INSTANCES_WRITE_TLAS) != 0;
+    const bool surface = (flags & SPH_INSTANCES_SURFACE_TLAS) != 0;
+    auto model = [radius](const float* p, float out[16]) {
+        for (int k = 0; k < 16; ++k) {
+            out[k] = 0.0F;
+        }
+        out[0] = radius;
+        out[5] = radius;
+        out[10] = radius;
+        out[12] = p[0];
+        out[13] = p[1];
+        out[14] = p[2];
+        out[15] = 1.0F;
+    };
+    if (write_tlas && surface) {
+        // The surface record first, every other record inactive (all zero).
+        std::memset(tlas + tlas_base, 0, sizeof(sph_tlas_instance) * n);
+        sph_tlas_instance& entry = tlas[tlas_base];
+        entry.transform[0] = 1.0F;
+        entry.transform[5] = 1.0F;
+        entry.transform[10] = 1.0F;
+        entry.custom_index_mask = (SPH_FLUID_SURFACE_CUSTOM_INDEX | fluid_index) | (SPH_FLUID_SURFACE_RAY_MASK << 24U);
+        entry.sbt_offset_flags = 1U << 24U;  // VK_GEOMETRY_INSTANCE_TRIANGLE_FACING_CULL_DISABLE_BIT_KHR
+        entry.blas = blas;
+    }
+    Pool pool(std::max(1U, threads));
+    pool.parallelFor(n, [&](uint32_t begin, uint32_t end) {
+        for (uint32_t i = begin; i < end; ++i) {
+            const float* p = pos + 4 * static_cast<size_t>(i);
+            const float* q = history ? prev + 4 * static_cast<size_t>(i) : p;
+            const uint32_t slot = instance_base + i;
+            sph_instance& out = instances[slot];
+            model(p, out.model);
+            model(q, out.previous_model);
+            for (int k = 0; k < 16; ++k) {
+                out.normal_matrix[k] = (k % 5 == 0) ? 1.0F : 0.0F;
+            }
+            out.mesh_index = sphere_mesh;
+            out.bucket = 0;
+            out.bucket_base = 0;
+            out.joint_offset = SPH_NO_JOINTS;
+            out.skinned_vertex_offset = SPH_NO_JOINTS;
+            out.previous_skinned_vertex_offset = SPH_NO_JOINTS;
+            out.skinned_meshlet_offset = 0;
+            out.visibility_base = 0;
+            if (write_tlas && !surface) {
+                sph_tlas_instance entry{};
+                for (int row = 0; row < 3; ++row) {
+                    for (int column = 0; column < 4; ++column) {
+                        entry.transform[row * 4 + column] = out.model[column * 4 + row];
+                    }
+                }
+                entry.custom_index_mask = (slot & 0xFFFFFFU) | (0xFFU << 24U);
+                entry.sbt_offset_flags = 0;
+                entry.blas = blas;
+                tlas[tlas_base + i] = entry;
+            }
+        }
+    });
+    return 0;
+}
+
 uint32_t oracle_hardware_threads(void) { return std::max(1U, std::thread::hardware_concurrency()); }
 
 } // extern "C"

@@ -78,6 +78,17 @@ int oracle_pair_counts(const sph_params* params,
 int oracle_stats(const sph_params* params, const float* positions, const float* velocities, uint32_t count, sph_stats* out);
 
 /* Worker threads the host offers. */
+/* gfx::FluidSimulator's CPU instance writer (src/gfx/fluid.cpp:402-466):
+ * per particle one instance record (model = scale(translate(I, p), r); the
+ * previous model from `prev` unless SPH_INSTANCES_RESET_HISTORY; identity
+ * normal matrix; `sphere_mesh`; no joints or skinned vertices) and, with
+ * SPH_INSTANCES_WRITE_TLAS, its acceleration-structure record (row-major 3x4
+ * of the model, custom index = slot & 0xFFFFFF, mask 0xFF, `blas`); with
+ * SPH_INSTANCES_SURFACE_TLAS as well, record 0 is the surface and the others
+ * are zero. Positions and previous positions are AoS float4. */
+int oracle_write_instances(const float* pos, const float* prev, uint32_t n, float radius, sph_instance* instances,
+                           uint32_t instance_base, uint32_t sphere_mesh, sph_tlas_instance* tlas, uint32_t tlas_base,
+                           uint64_t blas, uint32_t fluid_index, uint32_t flags, uint32_t threads);
 uint32_t oracle_hardware_threads(void);
 
 void oracle_mc_table(int8_t* out);

@@ -42,6 +42,7 @@ def test_instances_and_tlas_records(native):
         assert not np.array_equal(pos, prev)
         inst = torch.zeros((base + 1024) * abi.INSTANCE.itemsize, dtype=torch.uint8, device="cuda")
         tlas = torch.zeros((tbase + 1024) * abi.TLAS_INSTANCE.itemsize, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()  # the zero fill runs on torch's stream, the writer on the solver's
         solver.write_instances(inst.data_ptr(), base, 7, tlas.data_ptr(), tbase, 0x1234_5678_9ABC, 0,
                                abi.SPH_INSTANCES_WRITE_TLAS)
         solver.synchronize()
@@ -71,3 +72,32 @@ def test_instances_and_tlas_records(native):
         assert t["blas"][0] == 0xABCD and not t[1:].view(np.uint8).any()
         with pytest.raises(abi.SphError):
             solver.write_instances(inst.data_ptr() + 4, 0, 7)
+
+
+@pytest.mark.parametrize("flags", [abi.SPH_INSTANCES_WRITE_TLAS, 0, abi.SPH_INSTANCES_RESET_HISTORY,
+                                   abi.SPH_INSTANCES_WRITE_TLAS | abi.SPH_INSTANCES_SURFACE_TLAS])
+def test_instances_equal_the_oracle(native, oracle, flags):
+    """Device records against the oracle's restatement of the reference's
+    CPU writer (fluid.cpp:402-466), byte for byte, at 1M particles."""
+    case = W.dam_break_1m()
+    n = case.count
+    radius = np.float32(case.params.container_min[3])
+    with FluidSolverGpu(case.params, n) as solver:
+        solver.upload(*case.initial_state())
+        solver.run(case.dt, 2)
+        pos = solver.particles()
+        prev = solver.previous_particles()
+        inst = torch.zeros((n + 3) * abi.INSTANCE.itemsize, dtype=torch.uint8, device="cuda")
+        tlas = torch.zeros((n + 2) * abi.TLAS_INSTANCE.itemsize, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()  # the zero fill runs on torch's stream, the writer on the solver's
+        solver.write_instances(inst.data_ptr(), 3, 5, tlas.data_ptr(), 2, 0x1234_5678_9ABC, 6, flags)
+        solver.synchronize()
+        got = inst.cpu().numpy().view(abi.INSTANCE)
+        got_t = tlas.cpu().numpy().view(abi.TLAS_INSTANCE)
+    want = np.zeros(n + 3, abi.INSTANCE)
+    want_t = np.zeros(n + 2, abi.TLAS_INSTANCE)
+    oracle.write_instances(pos, prev, radius, want, 3, 5, want_t, 2, 0x1234_5678_9ABC, 6, flags,
+                           threads=oracle.hardware_threads)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    assert np.array_equal(got_t.view(np.uint8), want_t.view(np.uint8))
+

@@ -41,6 +41,7 @@ def test_forward_matches_oracle(native, torch_cuda, n):
         mlp.set_normalisation(mean, std, scale)
         d_f = torch.from_numpy(f).cuda()
         d_out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()  # torch's copies and fill finish before the library's stream reads them
         mlp.forward(d_f.data_ptr(), n, d_out.data_ptr())
         got = d_out.cpu().numpy()
     y, _ = M.forward(params, f, mean, std, scale)
@@ -68,6 +69,7 @@ def test_gradients_match_oracle(native, torch_cuda):
         params = mlp.params()
         d_f = torch.from_numpy(f).cuda()  # kept alive while the library reads them
         d_t = torch.from_numpy(t).cuda()
+        torch.cuda.synchronize()
         loss, g = mlp.gradients(d_f.data_ptr(), d_t.data_ptr(), n)
     ref_loss, ref_g = M.loss_and_grad(params, f, t, mean, std, scale)
     assert loss == pytest.approx(ref_loss, rel=5e-3)
@@ -98,6 +100,7 @@ def test_train_step_is_adam_on_the_gradient(native, torch_cuda):
         p0 = mlp.params()
         d_f = torch.from_numpy(f).cuda()
         d_t = torch.from_numpy(t).cuda()
+        torch.cuda.synchronize()
         _, g = mlp.gradients(d_f.data_ptr(), d_t.data_ptr(), n)
         mlp.train_step(d_f.data_ptr(), d_t.data_ptr(), n, lr=1e-3)
         p1 = mlp.params()
@@ -117,6 +120,7 @@ def test_training_fits_a_smooth_target(native, torch_cuda):
         mlp.set_normalisation(np.zeros(M.IN), np.ones(M.IN), np.ones(M.OUT))
         d_f = torch.from_numpy(f).cuda()
         d_t = torch.from_numpy(t).cuda()
+        torch.cuda.synchronize()
         first = mlp.train_step(d_f.data_ptr(), d_t.data_ptr(), n, lr=1e-3)
         for _ in range(300):
             last = mlp.train_step(d_f.data_ptr(), d_t.data_ptr(), n, lr=1e-3)

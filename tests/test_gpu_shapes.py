@@ -71,6 +71,20 @@ def test_obstacle_course_16k_300_substeps(native, oracle):
     assert_same(gv, ov, "velocities")
 
 
+def test_obstacle_course_1m_two_substeps(native, oracle):
+    """The 1M dam break with five colliders and three fields (the bench's
+    obstacle workload): two substeps bit for bit."""
+    case = W.obstacle_course_1m()
+    pos, vel = case.initial_state()
+    with FluidSolverGpu(case.params, case.count) as solver:
+        solver.upload(pos, vel)
+        solver.run(case.dt, 2)
+        gp, gv = solver.state()
+    op, ov = oracle.run_substeps(case.params, pos, vel, case.dt, 2, threads=oracle.hardware_threads)
+    assert_same(gp, op, "positions")
+    assert_same(gv, ov, "velocities")
+
+
 @pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
 def test_every_neighbour_kernel_with_shapes(native, oracle, variant):
     case = W.obstacle_course()

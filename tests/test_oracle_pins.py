@@ -108,3 +108,41 @@ def test_grid_against_brute_force_neighbours(oracle):
     brute = (r2 < h * h).sum(axis=1)
     p, q = oracle.pair_counts(params, pos)
     assert q >= brute.sum()  # duplicates of colliding buckets can only add
+
+
+def test_oracle_instances_match_the_host_construction(oracle):
+    """The oracle's instance writer (fluid.cpp:402-466) against the records
+    built from the reference's formulas: model = scale(translate(I, p), r),
+    identity normal matrix, no joints, and the TLAS row-major transform."""
+    from computer_graphics_lab_00_gb300 import abi
+
+    rng = np.random.default_rng(3)
+    n = 300
+    pos = rng.uniform(-1, 1, (n, 4)).astype(np.float32)
+    prev = rng.uniform(-1, 1, (n, 4)).astype(np.float32)
+    r = np.float32(0.025)
+    inst = np.zeros(n + 4, abi.INSTANCE)
+    tlas = np.zeros(n + 1, abi.TLAS_INSTANCE)
+    oracle.write_instances(pos, prev, r, inst, 4, 9, tlas, 1, 77, 0, abi.SPH_INSTANCES_WRITE_TLAS, threads=3)
+    got = inst[4:]
+    for key, src in (("model", pos), ("previous_model", prev)):
+        m = np.zeros((n, 16), np.float32)
+        m[:, 0] = m[:, 5] = m[:, 10] = r
+        m[:, 12:15] = src[:, :3]
+        m[:, 15] = 1.0
+        assert np.array_equal(got[key], m)
+    assert np.array_equal(got["normal_matrix"], np.tile(np.eye(4, dtype=np.float32).reshape(16), (n, 1)))
+    assert (got["mesh_index"] == 9).all() and (got["joint_offset"] == 0xFFFFFFFF).all()
+    assert (got["skinned_vertex_offset"] == 0xFFFFFFFF).all() and (got["bucket"] == 0).all()
+    assert not inst[:4].view(np.uint8).any()
+    t = tlas[1:]
+    rows = np.zeros((n, 12), np.float32)
+    rows[:, 0] = rows[:, 5] = rows[:, 10] = r
+    rows[:, 3], rows[:, 7], rows[:, 11] = pos[:, 0], pos[:, 1], pos[:, 2]
+    assert np.array_equal(t["transform"], rows)
+    assert np.array_equal(t["custom_index_mask"], (np.arange(n) + 4) | (0xFF << 24))
+    assert (t["blas"] == 77).all()
+    # History reset: the previous model is the current one.
+    oracle.write_instances(pos, None, r, inst, 0, 9, flags=abi.SPH_INSTANCES_RESET_HISTORY)
+    assert np.array_equal(inst["previous_model"][:n], inst["model"][:n])
+

@@ -217,6 +217,7 @@ def test_apply_gradients_matches_train_step(native):
     rng = np.random.default_rng(4)
     f = torch.from_numpy(rng.normal(0, 1, (512, 32)).astype(np.float32)).cuda()
     t = torch.from_numpy(rng.normal(0, 1, (512, 3)).astype(np.float32)).cuda()
+    torch.cuda.synchronize()
     with MlpGpu(seed=9) as a, MlpGpu(seed=9) as b:
         for _ in range(3):
             a.train_step(f.data_ptr(), t.data_ptr(), 512, 1e-3)
