@@ -346,7 +346,11 @@ def obstacles_leg(steps: int, flush, device: int, cpu: bool) -> dict:
     from computer_graphics_lab_00_gb300 import workloads as W
     from computer_graphics_lab_00_gb300.fluid import FluidSolverGpu
 
-    def timed(case) -> float:
+    # The shapes change the physics as well as adding two passes: particles
+    # pressed against the colliders have more neighbours, which the density
+    # and integrate phases pay for; the per-phase split and the final pair
+    # count of each run show which is which.
+    def timed(case) -> tuple[float, dict]:
         with FluidSolverGpu(case.params, case.count, device=device) as solver:
             solver.upload(*case.initial_state())
             solver.run(case.dt, 3)
@@ -363,17 +367,26 @@ def obstacles_leg(steps: int, flush, device: int, cpu: bool) -> dict:
                 end.record(stream)
                 end.synchronize()
                 total += start.elapsed_time(end)
-        return total / steps
+            # Per-phase device times over a few more substeps (one by one).
+            phases = {name: 0.0 for name in FluidSolverGpu.PROFILE_PHASES}
+            for _ in range(5):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                for name, t in solver.profile(case.dt, 1).items():
+                    phases[name] += t / 5
+            phases["pairs_per_particle"] = solver.stats().pairs_in_range / case.count
+        return total / steps, phases
 
     shapes = W.obstacle_course_1m()
-    plain_ms = timed(W.dam_break_1m())
-    ms = timed(shapes)
+    plain_ms, plain_phases = timed(W.dam_break_1m())
+    ms, phases = timed(shapes)
     n = shapes.count
     out = {
         "workload": shapes.name, "colliders": int(shapes.params.collider_count),
         "force_fields": int(shapes.params.field_count), "substeps": steps, "ms_per_step": ms,
         "value": n * shapes.dt / (ms / 1e3), "unit": UNIT, "plain_ms_per_step": plain_ms,
-        "shape_overhead_ms": ms - plain_ms, "l2": "flushed before every substep",
+        "shape_overhead_ms": ms - plain_ms, "phase_ms": phases, "plain_phase_ms": plain_phases,
+        "l2": "flushed before every substep",
     }
     if cpu:
         from oracle.bind import Oracle
@@ -394,7 +407,8 @@ def instances_leg(reps: int, flush, device: int, cpu: bool) -> dict:
     and one 64-byte TLAS record per particle, then keepRendered) for the 1M
     dam break, timed with CUDA events after an L2 flush, against the measured
     HBM copy bandwidth: it reads 32 bytes a particle (position, previous
-    position) and writes 288, plus keepRendered's 16 + 16. Its CPU baseline is
+    position) and writes 288, plus keepRendered's 16 (the writer copies the
+    position over the previous one in the same pass). Its CPU baseline is
     the oracle's restatement of the reference's CPU writer on all host
     cores."""
     import numpy as np
@@ -406,7 +420,7 @@ def instances_leg(reps: int, flush, device: int, cpu: bool) -> dict:
 
     case = W.dam_break_1m()
     n = case.count
-    per_particle = 32 + abi.INSTANCE.itemsize + abi.TLAS_INSTANCE.itemsize + 32
+    per_particle = 32 + abi.INSTANCE.itemsize + abi.TLAS_INSTANCE.itemsize + 16
     with FluidSolverGpu(case.params, n, device=device) as solver:
         solver.upload(*case.initial_state())
         solver.run(case.dt, 1)

@@ -25,7 +25,7 @@ def _ptr(a: np.ndarray | None):
 class BatchSolverGpu:
     """A set of tanks on one GPU."""
 
-    PROFILE_PHASES = ("keys", "sort", "bounds_gather", "density", "integrate")
+    PROFILE_PHASES = ("keys", "sort", "bounds_gather", "density", "integrate", "shapes")
 
     def __init__(self, params: list[SphParams], counts: list[int], device: int = 0):
         if len(params) != len(counts) or not params:

@@ -508,7 +508,12 @@ int Engine::write_instances(sph_instance* instances, uint32_t instance_base, uin
     SPH_CUDA(launch_instances(pos_, prev_, n, params_[0].container_min[3], instances, instance_base, sphere_mesh,
                               (flags & SPH_INSTANCES_WRITE_TLAS) != 0 ? tlas : nullptr, tlas_base, blas, fluid_index,
                               flags, stream_));
-    return keep_rendered();
+    // The kernel has kept particles [0, n); tanks behind the first keep theirs here.
+    if (total_count_ > n) {
+        SPH_CUDA(cudaMemcpyAsync(prev_ + n, pos_ + n, sizeof(float4) * (total_count_ - n), cudaMemcpyDeviceToDevice,
+                                 stream_));
+    }
+    return SPH_OK;
 }
 
 int Engine::emit(uint32_t tank, uint32_t count) {
@@ -1468,21 +1473,28 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
         SPH_CUDA(cudaEventRecord(events_[3], stream_));
         SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning_));
         SPH_CUDA(cudaEventRecord(events_[4], stream_));
-        // Force fields and colliders, when present, count as integrate.
+        // Force fields (before integrate, at the start positions) and
+        // colliders (after it), when present, make up the shapes phase.
         if ((status = enqueue_fields(nullptr)) != SPH_OK) {
             return status;
         }
+        SPH_CUDA(cudaEventRecord(events_[5], stream_));
         SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
                                   tuning_));
+        SPH_CUDA(cudaEventRecord(events_[6], stream_));
         if ((status = enqueue_colliders(nullptr)) != SPH_OK) {
             return status;
         }
-        SPH_CUDA(cudaEventRecord(events_[5], stream_));
-        SPH_CUDA(cudaEventSynchronize(events_[5]));
+        SPH_CUDA(cudaEventRecord(events_[7], stream_));
+        SPH_CUDA(cudaEventSynchronize(events_[7]));
+        float ms[7] = {};
+        for (uint32_t k = 0; k < 7; ++k) {
+            SPH_CUDA(cudaEventElapsedTime(&ms[k], events_[k], events_[k + 1]));
+        }
+        // keys, sort, bounds + gather, density, integrate, shapes.
+        const float phase[kProfilePhases] = {ms[0], ms[1], ms[2], ms[3], ms[5], ms[4] + ms[6]};
         for (uint32_t k = 0; k < kProfilePhases; ++k) {
-            float ms = 0.0F;
-            SPH_CUDA(cudaEventElapsedTime(&ms, events_[k], events_[k + 1]));
-            phase_ms[k] += ms;
+            phase_ms[k] += phase[k];
         }
     }
     grid_valid_ = true;

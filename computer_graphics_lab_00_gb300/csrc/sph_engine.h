@@ -111,7 +111,7 @@ public:
     const sph_surface_vertex* surface_vertices_device() const { return surface_vertices_; }
     // Runs substeps without the graph, timing each phase with CUDA events on
     // the context stream: keys, sort, bounds+gather, density, integrate.
-    static constexpr uint32_t kProfilePhases = 5;
+    static constexpr uint32_t kProfilePhases = 6;
     int profile(float dt, uint32_t substeps, double* phase_ms);
 
     uint32_t tank_count() const { return static_cast<uint32_t>(tanks_.size()); }
@@ -215,7 +215,7 @@ private:
     bool learned_graph_has_model_ = false;
     mlp::ModelView learned_graph_model_{};
     uint32_t learned_launches_ = 0;
-    cudaEvent_t events_[kProfilePhases + 1] = {};
+    cudaEvent_t events_[8] = {};  // phase boundaries of one profiled substep
     // Surface buffers (grown on demand, byte sizes alongside).
     int grow(void** buffer, size_t* have, size_t need);
     float* surface_field_ = nullptr;

@@ -328,7 +328,19 @@ __device__ __forceinline__ float min_like_std(float a, float b) { return b < a ?
 // on about 0.1 % of arguments in (0, 1) it returns the neighbouring float, so
 // a falloff other than 1 agrees with the reference to 1 ulp in the weight;
 // a falloff of 1 or a radius of 0 (no power) is bit-exact.
+//
+// The two common falloffs skip the double-precision power, whose cost
+// dominates a field pass on a part with a low FP64 rate: x^1 is x itself
+// (the double result lies within a few double ulps of the float x and rounds
+// back to it) and x^0 is 1 for every x, so both shortcuts return the same
+// bits as the general path.
 __device__ __forceinline__ float pow_float(float x, float y) {
+    if (y == 1.0f) {
+        return x;
+    }
+    if (y == 0.0f) {
+        return 1.0f;
+    }
     return __double2float_rn(pow(static_cast<double>(x), static_cast<double>(y)));
 }
 

@@ -8,7 +8,9 @@
 
 namespace sph {
 
-cudaError_t launch_instances(const float4* pos, const float4* prev, uint32_t n, float radius, sph_instance* instances,
+// Writes the instances (and TLAS records) of particles [0, n) and then
+// copies pos[0, n) over prev[0, n) (keepRendered for those particles).
+cudaError_t launch_instances(const float4* pos, float4* prev, uint32_t n, float radius, sph_instance* instances,
                              uint32_t instance_base, uint32_t sphere_mesh, sph_tlas_instance* tlas, uint32_t tlas_base,
                              unsigned long long blas, uint32_t fluid_index, uint32_t flags, cudaStream_t stream);
 

@@ -268,7 +268,7 @@ class FluidSolverGpu:
         t = abi.SphTuning(**current)
         self._check(self._lib.sph_set_tuning(self._ctx, ctypes.byref(t)), "sph_set_tuning")
 
-    PROFILE_PHASES = ("keys", "sort", "bounds_gather", "density", "integrate")
+    PROFILE_PHASES = ("keys", "sort", "bounds_gather", "density", "integrate", "shapes")
 
     def profile(self, dt: float, substeps: int) -> dict:
         """Runs substeps phase by phase; returns total device ms per phase."""

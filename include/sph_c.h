@@ -357,9 +357,10 @@ int sph_device_state(sph_ctx* ctx, void** positions, void** velocities);
 int sph_run(sph_ctx* ctx, float dt, uint32_t substeps);
 /* Runs `substeps` substeps without the CUDA graph and adds the device time of
  * each phase, measured with CUDA events on the context stream, to
- * phase_ms[0..4]: keys, radix sort, bounds + gather, density, integrate.
- * Synchronises. Results are identical to sph_run. */
-#define SPH_PROFILE_PHASES 5
+ * phase_ms[0..5]: keys, radix sort, bounds + gather, density, integrate, and
+ * shapes (the force-field and collider passes; 0 without fields and
+ * colliders). Synchronises. Results are identical to sph_run. */
+#define SPH_PROFILE_PHASES 6
 int sph_profile_substeps(sph_ctx* ctx, float dt, uint32_t substeps, double* phase_ms);
 /* Reads / replaces the launch shape (an autotuner's knobs). */
 int sph_get_tuning(const sph_ctx* ctx, sph_tuning* out);

@@ -94,6 +94,7 @@ def test_instances_equal_the_oracle(native, oracle, flags):
         solver.synchronize()
         got = inst.cpu().numpy().view(abi.INSTANCE)
         got_t = tlas.cpu().numpy().view(abi.TLAS_INSTANCE)
+        np.testing.assert_array_equal(solver.previous_particles(), pos)  # keepRendered
     want = np.zeros(n + 3, abi.INSTANCE)
     want_t = np.zeros(n + 2, abi.TLAS_INSTANCE)
     oracle.write_instances(pos, prev, radius, want, 3, 5, want_t, 2, 0x1234_5678_9ABC, 6, flags,
@@ -101,3 +102,33 @@ def test_instances_equal_the_oracle(native, oracle, flags):
     assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
     assert np.array_equal(got_t.view(np.uint8), want_t.view(np.uint8))
 
+
+
+@pytest.mark.parametrize("count", [1, 31, 33, 1000])
+def test_ragged_counts_write_only_their_records(native, oracle, count):
+    """Counts that leave a warp partly empty: the records equal the oracle's,
+    nothing past the last record is written, and keepRendered covers every
+    particle."""
+    params = W.reference_test_scene(count)
+    radius = np.float32(params.container_min[3])
+    with FluidSolverGpu(params, count) as solver:
+        solver.emit(params, count)
+        for _ in range(2):
+            solver.step(params, 1.0 / 60.0)
+        pos = solver.particles()
+        prev = solver.previous_particles()
+        inst = torch.full(((count + 40) * abi.INSTANCE.itemsize,), 0xA5, dtype=torch.uint8, device="cuda")
+        tlas = torch.full(((count + 40) * abi.TLAS_INSTANCE.itemsize,), 0xA5, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        solver.write_instances(inst.data_ptr(), 1, 2, tlas.data_ptr(), 4, 0x77, 0, abi.SPH_INSTANCES_WRITE_TLAS)
+        solver.synchronize()
+        got = inst.cpu().numpy().view(abi.INSTANCE)
+        got_t = tlas.cpu().numpy().view(abi.TLAS_INSTANCE)
+        np.testing.assert_array_equal(solver.previous_particles(), pos)
+    want = np.zeros(count + 40, abi.INSTANCE)
+    want_t = np.zeros(count + 40, abi.TLAS_INSTANCE)
+    want.view(np.uint8)[:] = 0xA5
+    want_t.view(np.uint8)[:] = 0xA5
+    oracle.write_instances(pos, prev, radius, want, 1, 2, want_t, 4, 0x77, 0, abi.SPH_INSTANCES_WRITE_TLAS)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    assert np.array_equal(got_t.view(np.uint8), want_t.view(np.uint8))
