@@ -10,8 +10,8 @@ Our arm (default) prints one JSON line with
            from CUDA events on the solver's stream, L2 flushed before every
            timed substep (a 256 MB write);
   e2e      the same metric through the C ABI with host buffers: every step
-           uploads the state from pinned host memory, runs the substep and
-           downloads the new state;
+           is one sph_step_host call, which uploads the state from pinned
+           host memory, runs the substep and downloads the new state;
   roofline the dominant kernel's algorithmic bytes per launch over its
            event-timed duration, against the measured HBM copy bandwidth;
   cpu_baseline  the CPU oracle (a restatement of the reference's CPU solver)
@@ -632,19 +632,19 @@ def run_gb300(args) -> None:
             phases[name] += ms
     phases = {k: v / prof_steps for k, v in phases.items()}
 
-    # End-to-end leg: host state in pinned memory, copies inside the timed region.
+    # End-to-end leg: host state in pinned memory, copies inside the timed
+    # region. Each step is one sph_step_host call: upload the state (32 B a
+    # particle), one substep, download it (32 B a particle), the velocity
+    # upload overlapping the keys and sort.
     e2e_steps = args.e2e_steps or min(args.steps, 100)
     host_pos = torch.from_numpy(pos0.copy()).pin_memory()
     host_vel = torch.from_numpy(vel0.copy()).pin_memory()
-    solver.upload_from(host_pos.data_ptr(), host_vel.data_ptr(), n)
-    solver.substep(dt)
-    solver.download_to(host_pos.data_ptr(), host_vel.data_ptr())
+    hp, hv = host_pos.data_ptr(), host_vel.data_ptr()
+    solver.step_host(hp, hv, n, dt, 1, hp, hv)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        solver.upload_from(host_pos.data_ptr(), host_vel.data_ptr(), n)
-        solver.substep(dt)
-        solver.download_to(host_pos.data_ptr(), host_vel.data_ptr())
+        solver.step_host(hp, hv, n, dt, 1, hp, hv)
     barrier()
     e2e_wall = time.perf_counter() - t0
 

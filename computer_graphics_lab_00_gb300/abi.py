@@ -238,6 +238,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_emit": (c_int, [c_void_p, c_u32]),
         "sph_upload": (c_int, [c_void_p, c_void_p, c_void_p, c_u32]),
         "sph_download": (c_int, [c_void_p, c_void_p, c_void_p]),
+        "sph_step_host": (c_int, [c_void_p, c_void_p, c_void_p, c_u32, c_f32, c_u32, c_void_p, c_void_p]),
         "sph_step": (c_int, [c_void_p, c_f32]),
         "sph_substep": (c_int, [c_void_p, c_f32]),
         "sph_keep_rendered": (c_int, [c_void_p]),

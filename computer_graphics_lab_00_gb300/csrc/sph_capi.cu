@@ -197,6 +197,14 @@ int sph_upload(sph_ctx* ctx, const float* positions, const float* velocities, ui
     return ctx->engine.upload(0, positions, velocities, count);
 }
 
+int sph_step_host(sph_ctx* ctx, const float* positions, const float* velocities, uint32_t count, float dt,
+                  uint32_t substeps, float* positions_out, float* velocities_out) {
+    if (ctx == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return ctx->engine.step_host(positions, velocities, count, dt, substeps, positions_out, velocities_out);
+}
+
 int sph_download(sph_ctx* ctx, float* positions, float* velocities) {
     if (ctx == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;

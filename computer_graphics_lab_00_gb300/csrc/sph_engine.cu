@@ -179,6 +179,20 @@ void Engine::release() {
             e = nullptr;
         }
     }
+    for (cudaEvent_t& e : copy_events_) {
+        if (e != nullptr) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    }
+    if (copy_stream_ != nullptr) {
+        cudaStreamDestroy(copy_stream_);
+        copy_stream_ = nullptr;
+    }
+    if (flag_host_ != nullptr) {
+        cudaFreeHost(flag_host_);
+        flag_host_ = nullptr;
+    }
     void* buffers[] = {surface_field_, surface_runs_, surface_vertices_, surface_codes_, surface_tiles_, sweep_,
                        d_tanks_,       d_colliders_,  d_fields_,    field_accel_, pos_,          vel_,         prev_,        tank_of_,   stank_,
                        grid_.keys,     grid_.keys_a,  grid_.vals_a, grid_.keys_b, grid_.vals_b, grid_.hist,
@@ -445,10 +459,10 @@ int Engine::upload(uint32_t tank, const float* pos, const float* vel, uint32_t c
     if (nonfinite_host_ != 0) {
         return SPH_ERR_NONFINITE;
     }
-    if (tanks_.size() == 1) {
+    if (tanks_.size() == 1 && (tanks_[0].particle_count != count || total_count_ != count)) {
         tanks_[0].particle_count = count;
         total_count_ = count;
-        consts_dirty_ = true;
+        consts_dirty_ = true;  // the device tank table carries the count
     }
     grid_valid_ = false;
     return SPH_OK;
@@ -471,6 +485,90 @@ int Engine::download(uint32_t tank, float* pos, float* vel) {
     if (vel != nullptr) {
         SPH_CUDA(cudaMemcpy(vel, vel_ + base, bytes, cudaMemcpyDeviceToHost));
     }
+    return SPH_OK;
+}
+
+int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, float dt, uint32_t substeps,
+                      float* pos_out, float* vel_out) {
+    if (tanks_.size() != 1 || (count > 0 && pos_in == nullptr) || !(dt > 0.0F) || !std::isfinite(dt)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (count > capacity_[0]) {
+        return SPH_ERR_CAPACITY;
+    }
+    if (count == 0 || substeps == 0) {  // nothing to overlap
+        int status = upload(0, pos_in, vel_in, count);
+        if (status == SPH_OK) {
+            status = run(dt, substeps);
+        }
+        return status == SPH_OK ? download(0, pos_out, vel_out) : status;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    if (copy_stream_ == nullptr) {
+        SPH_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : copy_events_) {
+            SPH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        SPH_CUDA(cudaMallocHost(&flag_host_, sizeof(uint32_t)));
+    }
+    if (tanks_[0].particle_count != count || total_count_ != count) {
+        tanks_[0].particle_count = count;
+        total_count_ = count;
+        consts_dirty_ = true;  // the device tank table carries the count
+    }
+    int status = refresh_constants(dt);
+    if (status != SPH_OK) {
+        return status;
+    }
+    // Positions first: the keys and the sort read nothing else. The
+    // velocities follow on the copy stream, with upload's keepRendered copy
+    // and the non-finite check of both arrays, while those passes run.
+    const size_t bytes = sizeof(float4) * count;
+    SPH_CUDA(cudaMemcpyAsync(pos_, pos_in, bytes, cudaMemcpyHostToDevice, stream_));
+    SPH_CUDA(cudaEventRecord(copy_events_[0], stream_));
+    SPH_CUDA(cudaStreamWaitEvent(copy_stream_, copy_events_[0], 0));
+    if (vel_in != nullptr) {
+        SPH_CUDA(cudaMemcpyAsync(vel_, vel_in, bytes, cudaMemcpyHostToDevice, copy_stream_));
+    } else {
+        SPH_CUDA(cudaMemsetAsync(vel_, 0, bytes, copy_stream_));
+    }
+    SPH_CUDA(cudaMemcpyAsync(prev_, pos_, bytes, cudaMemcpyDeviceToDevice, copy_stream_));
+    SPH_CUDA(cudaMemsetAsync(bucket_stats_, 0, sizeof(uint32_t), copy_stream_));
+    SPH_CUDA(launch_count_nonfinite(pos_, vel_, count, bucket_stats_, copy_stream_));
+    SPH_CUDA(cudaMemcpyAsync(flag_host_, bucket_stats_, sizeof(uint32_t), cudaMemcpyDeviceToHost, copy_stream_));
+    SPH_CUDA(cudaEventRecord(copy_events_[1], copy_stream_));
+    // The first substep launched directly, its gather waiting for the copy
+    // stream; the rest through the graph, as run() does.
+    gather_wait_ = copy_events_[1];
+    status = enqueue_substep(nullptr);
+    gather_wait_ = nullptr;
+    if (status != SPH_OK) {
+        return status;
+    }
+    if (substeps > 1) {
+        if ((status = ensure_graph()) != SPH_OK) {
+            return status;
+        }
+        for (uint32_t s = 1; s < substeps; ++s) {
+            if ((status = prepare_schedule(nullptr)) != SPH_OK) {
+                return status;
+            }
+            SPH_CUDA(cudaGraphLaunch(graph_, stream_));
+        }
+    }
+    grid_valid_ = true;
+    // The context stream has waited for the copy stream, so the flag is in.
+    SPH_CUDA(cudaStreamSynchronize(stream_));
+    if (*flag_host_ != 0) {
+        return SPH_ERR_NONFINITE;  // the caller's arrays are left as they were
+    }
+    if (pos_out != nullptr) {
+        SPH_CUDA(cudaMemcpyAsync(pos_out, pos_, bytes, cudaMemcpyDeviceToHost, stream_));
+    }
+    if (vel_out != nullptr) {
+        SPH_CUDA(cudaMemcpyAsync(vel_out, vel_, bytes, cudaMemcpyDeviceToHost, stream_));
+    }
+    SPH_CUDA(cudaStreamSynchronize(stream_));
     return SPH_OK;
 }
 
@@ -589,6 +687,9 @@ int Engine::enqueue_grid(uint32_t* launches) {
     } else {
         SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
         SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, launches));
+    }
+    if (gather_wait_ != nullptr) {  // the gather is the first pass that reads velocities
+        SPH_CUDA(cudaStreamWaitEvent(stream_, gather_wait_, 0));
     }
     int status = enqueue_bounds(launches);
     if (status != SPH_OK) {

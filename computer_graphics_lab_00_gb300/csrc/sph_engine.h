@@ -56,6 +56,11 @@ public:
                         sph_tlas_instance* tlas, uint32_t tlas_base, uint64_t blas, uint32_t fluid_index,
                         uint32_t flags);
     int emit(uint32_t tank, uint32_t count);
+    // upload + run + download of a single tank in one call, with the
+    // velocity upload overlapping the first substep's keys and sort; same
+    // results and checks. pos_out / vel_out may alias the inputs or be null.
+    int step_host(const float* pos_in, const float* vel_in, uint32_t count, float dt, uint32_t substeps,
+                  float* pos_out, float* vel_out);
 
     // Enqueues `substeps` substeps of length dt for every active tank.
     int run(float dt, uint32_t substeps);
@@ -204,6 +209,10 @@ private:
     uint32_t launches_per_substep_ = 0;
     bool grid_valid_ = false;
     uint32_t nonfinite_host_ = 0;
+    cudaStream_t copy_stream_ = nullptr;  // step_host: velocity upload and checks beside the keys and sort
+    cudaEvent_t copy_events_[2] = {};     // positions landed; velocities landed and checked
+    cudaEvent_t gather_wait_ = nullptr;   // when set, a direct-launched gather first waits for it
+    uint32_t* flag_host_ = nullptr;       // page-locked non-finite count read back by step_host
     std::vector<uint8_t> user_active_;
     float4* snap_pos_[kSnapshotSlots] = {nullptr, nullptr};
     float4* snap_vel_[kSnapshotSlots] = {nullptr, nullptr};

@@ -189,6 +189,29 @@ class FluidSolverGpu:
                                            None if velocities_ptr is None else ctypes.c_void_p(velocities_ptr)),
                     "sph_download")
 
+    def step_host(self, positions_ptr: int, velocities_ptr: int | None, count: int, dt: float, substeps: int,
+                  positions_out_ptr: int | None, velocities_out_ptr: int | None) -> None:
+        """sph_step_host: upload from, step, and download into raw host
+        addresses in one call (the copies overlap where the passes allow)."""
+        def opt(p):
+            return None if p is None else ctypes.c_void_p(p)
+
+        self._check(self._lib.sph_step_host(self._ctx, ctypes.c_void_p(positions_ptr), opt(velocities_ptr), count,
+                                            ctypes.c_float(dt), substeps, opt(positions_out_ptr),
+                                            opt(velocities_out_ptr)), "sph_step_host")
+
+    def step_host_arrays(self, positions: np.ndarray, velocities: np.ndarray | None, dt: float, substeps: int = 1):
+        """sph_step_host on numpy (N, 4) float32 arrays; returns new arrays."""
+        pos = np.ascontiguousarray(positions, dtype=np.float32)
+        vel = None if velocities is None else np.ascontiguousarray(velocities, dtype=np.float32)
+        if pos.ndim != 2 or pos.shape[1] != 4 or (vel is not None and vel.shape != pos.shape):
+            raise ValueError("positions/velocities must be (N, 4) float32")
+        out_p = np.empty_like(pos)
+        out_v = np.empty_like(pos)
+        self.step_host(pos.ctypes.data, None if vel is None else vel.ctypes.data, pos.shape[0], dt, substeps,
+                       out_p.ctypes.data, out_v.ctypes.data)
+        return out_p, out_v
+
     def synchronize(self) -> None:
         self._check(self._lib.sph_synchronize(self._ctx), "sph_synchronize")
 

@@ -183,6 +183,16 @@ int sph_emit(sph_ctx* ctx, uint32_t count);
 int sph_upload(sph_ctx* ctx, const float* positions, const float* velocities, uint32_t count);
 /* Downloads the current state (host AoS float4). Either pointer may be NULL. */
 int sph_download(sph_ctx* ctx, float* positions, float* velocities);
+/* sph_upload + `substeps` substeps of `dt` + sph_download in one call, for
+ * a caller that keeps the state on the host: the same results and checks,
+ * with the velocity upload overlapping the first substep's grid keys and
+ * sort (page-locked host arrays let the copies run asynchronously).
+ * `velocities` may be NULL (zeros); either output may be NULL or alias its
+ * input. On SPH_ERR_NONFINITE the outputs are left as they were and the
+ * context holds the rejected state, as after a rejected sph_upload.
+ * Synchronises. */
+int sph_step_host(sph_ctx* ctx, const float* positions, const float* velocities, uint32_t count, float dt,
+                  uint32_t substeps, float* positions_out, float* velocities_out);
 /* FluidSolver::step (fluid_sph.cpp:311-321): splits the frame with fluidSubsteps. */
 int sph_step(sph_ctx* ctx, float delta_seconds);
 /* FluidSolver::substep (fluid_sph.cpp:190-309): one grid + density + integrate pass. */

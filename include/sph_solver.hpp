@@ -105,6 +105,19 @@ public:
               "sph_upload", ctx_);
     }
 
+    // For a caller that keeps the state on the host: uploads it, runs
+    // `substeps` substeps of `dt` and writes the result back in place, with
+    // the copies overlapped where the passes allow (sph_step_host).
+    void stepHost(std::vector<Float4>& positions, std::vector<Float4>& velocities, float dt, uint32_t substeps = 1) {
+        if (velocities.size() != positions.size()) {
+            throw std::invalid_argument("stepHost: positions and velocities differ in length");
+        }
+        float* p = positions.empty() ? nullptr : &positions[0].x;
+        float* v = velocities.empty() ? nullptr : &velocities[0].x;
+        check(sph_step_host(ctx_, p, v, static_cast<uint32_t>(positions.size()), dt, substeps, p, v),
+              "sph_step_host", ctx_);
+    }
+
     sph_ctx* handle() { return ctx_; }
 
 private:

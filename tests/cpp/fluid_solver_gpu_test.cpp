@@ -101,6 +101,29 @@ int main() {
             assert(std::memcmp(&a[i], &b[i], sizeof(gb::Float4)) == 0);
         }
     }
+    // stepHost (upload, substeps, download in one call, written back in
+    // place) equals upload + substeps + particles()/velocities().
+    {
+        sph_params p = paramsFor(1024);
+        gb::FluidSolverGpu device(p, 1024);
+        gb::FluidSolverGpu host(p, 1024);
+        device.emit(p, 1024);
+        for (int frame = 0; frame < 10; ++frame) {
+            device.step(p, 1.0F / 60.0F);
+        }
+        std::vector<gb::Float4> pos = device.particles();
+        std::vector<gb::Float4> vel = device.velocities();
+        for (int k = 0; k < 3; ++k) {
+            gb::check(sph_substep(device.handle(), 1.0F / 600.0F), "sph_substep");
+        }
+        host.stepHost(pos, vel, 1.0F / 600.0F, 3);
+        std::vector<gb::Float4> a = device.particles();
+        std::vector<gb::Float4> b = device.velocities();
+        for (size_t i = 0; i < a.size(); ++i) {
+            assert(std::memcmp(&a[i], &pos[i], sizeof(gb::Float4)) == 0);
+            assert(std::memcmp(&b[i], &vel[i], sizeof(gb::Float4)) == 0);
+        }
+    }
     // Parameter derivation (fluid_test.cpp:181-194).
     {
         sph_fluid_settings s{};
