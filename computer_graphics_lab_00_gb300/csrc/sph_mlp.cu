@@ -98,8 +98,7 @@ __device__ __forceinline__ void tmem_load16(uint32_t taddr, float* v) {
     }
 }
 
-// GELU, erf form (Hendrycks & Gimpel 2016).
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// Derivative of GELU, erf form (Hendrycks & Gimpel 2016): Phi(z) + z phi(z).
 __device__ __forceinline__ float gelu_grad(float z) {
     return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
 }
@@ -150,10 +149,11 @@ __device__ __forceinline__ void store_chunk(uint8_t* base, uint32_t offset, cons
 // error against erff stays under 2e-6 (the 16th power scales the rounding of
 // the polynomial); the activations are rounded to BF16 (relative step 2^-8)
 // right after. Checked by sph_mlp_selftest_erf.
+constexpr float kErfA1 = 7.05230784e-2f, kErfA2 = 4.22820123e-2f, kErfA3 = 9.2705272e-3f, kErfA4 = 1.520143e-4f,
+                kErfA5 = 2.765672e-4f, kErfA6 = 4.30638e-5f;
+
 __device__ __forceinline__ float erfc_power(float ax) {
-    float s = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(4.30638e-5f, ax, 2.765672e-4f), ax, 1.520143e-4f), ax, 9.2705272e-3f), ax,
-                             4.22820123e-2f),
-                        ax, 7.05230784e-2f),
+    float s = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(kErfA6, ax, kErfA5), ax, kErfA4), ax, kErfA3), ax, kErfA2), ax, kErfA1),
                    ax, 1.0f);
     s = s * s;
     s = s * s;
@@ -166,12 +166,68 @@ __device__ __forceinline__ float erfc_power(float ax) {
 
 __device__ __forceinline__ float erf_as(float x) { return copysignf(1.0f - erfc_power(fabsf(x)), x); }
 
-// GELU of the forward pass, erf form: with r as above at |z| / sqrt(2),
-// 1 + erf(z / sqrt(2)) is 2 - r for z >= 0 and r for z < 0, so the negative
-// side keeps its relative accuracy (no 1 - (1 - r) cancellation).
-__device__ __forceinline__ float gelu_fast(float z) {
-    const float m = 0.5f * z * erfc_power(fabsf(z) * 0.70710678118654752f);
-    return z >= 0.0f ? z - m : m;
+// GELU of the forward pass, erf form (Hendrycks & Gimpel 2016): with r =
+// erfc_power(|z| / sqrt(2)), 1 + erf(z / sqrt(2)) is 2 - r for z >= 0 and r
+// for z < 0, so with m = (0.5 z) r, GELU(z) = z - m for z >= 0 and m below
+// (the negative side keeps its relative accuracy: no 1 - (1 - r)
+// cancellation).
+//
+// Two activations go at once on the packed FP32 pipe: fma.rn.f32x2 and
+// mul.rn.f32x2 perform, lane by lane, the same rounded operations as scalar
+// fmaf and multiplies, so each lane's value is that of the scalar form while
+// the Horner steps, squarings and scalings take half the issue slots.
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 pack2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpack2(f32x2 r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// z = v + bias and GELU(z) for two columns; z is returned for the training
+// saves.
+__device__ __forceinline__ void bias_gelu2(float v0, float v1, float b0, float b1, float& z0, float& z1, float& g0,
+                                           float& g1) {
+    unpack2(add2(pack2(v0, v1), pack2(b0, b1)), z0, z1);
+    const f32x2 ax = pack2(fabsf(z0) * 0.70710678118654752f, fabsf(z1) * 0.70710678118654752f);
+    f32x2 s = fma2(pack2(kErfA6, kErfA6), ax, pack2(kErfA5, kErfA5));
+    s = fma2(s, ax, pack2(kErfA4, kErfA4));
+    s = fma2(s, ax, pack2(kErfA3, kErfA3));
+    s = fma2(s, ax, pack2(kErfA2, kErfA2));
+    s = fma2(s, ax, pack2(kErfA1, kErfA1));
+    s = fma2(s, ax, pack2(1.0f, 1.0f));
+    s = mul2(s, s);
+    s = mul2(s, s);
+    s = mul2(s, s);
+    s = mul2(s, s);
+    float s0, s1, r0, r1;
+    unpack2(s, s0, s1);
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(s0));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(s1));
+    const f32x2 zz = pack2(z0, z1);
+    float m0, m1;
+    unpack2(mul2(mul2(pack2(0.5f, 0.5f), zz), pack2(r0, r1)), m0, m1);
+    float d0, d1;
+    unpack2(add2(zz, pack2(-m0, -m1)), d0, d1);
+    g0 = z0 >= 0.0f ? d0 : m0;
+    g1 = z1 >= 0.0f ? d1 : m1;
 }
 
 constexpr uint32_t kForwardThreads = 512;
@@ -345,12 +401,13 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
                 bias[4 * q + 3] = b4.w;
             }
 #pragma unroll
-            for (uint32_t k = 0; k < 16; ++k) {
-                float z = v[k] + bias[k];
+            for (uint32_t k = 0; k < 16; k += 2) {
+                float z0, z1;
+                bias_gelu2(v[k], v[k + 1], bias[k], bias[k + 1], z0, z1, v[k], v[k + 1]);
                 if (kSave && valid) {
-                    saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
+                    saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k] = z0;
+                    saves.z1[static_cast<size_t>(row) * kHidden + c * 16 + k + 1] = z1;
                 }
-                v[k] = gelu_fast(z);
             }
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c, kHidden), v);
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
@@ -397,12 +454,13 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
                 bias[4 * q + 3] = b4.w;
             }
 #pragma unroll
-            for (uint32_t k = 0; k < 16; ++k) {
-                float z = v[k] + bias[k];
+            for (uint32_t k = 0; k < 16; k += 2) {
+                float z0, z1;
+                bias_gelu2(v[k], v[k + 1], bias[k], bias[k + 1], z0, z1, v[k], v[k + 1]);
                 if (kSave && valid) {
-                    saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k] = z;
+                    saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k] = z0;
+                    saves.z2[static_cast<size_t>(row) * kHidden + c * 16 + k + 1] = z1;
                 }
-                v[k] = gelu_fast(z);
             }
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c, kHidden), v);
             store_chunk(smem + kSmemH, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
