@@ -557,9 +557,11 @@ int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, 
         }
     }
     grid_valid_ = true;
-    // The context stream has waited for the copy stream, so the flag is in.
-    SPH_CUDA(cudaStreamSynchronize(stream_));
+    // The check lands long before the substeps end: read it then, and queue
+    // the download behind them so that it starts as the last pass ends.
+    SPH_CUDA(cudaEventSynchronize(copy_events_[1]));
     if (*flag_host_ != 0) {
+        SPH_CUDA(cudaStreamSynchronize(stream_));
         return SPH_ERR_NONFINITE;  // the caller's arrays are left as they were
     }
     if (pos_out != nullptr) {
