@@ -350,7 +350,7 @@ def obstacles_leg(steps: int, flush, device: int, cpu: bool) -> dict:
     # pressed against the colliders have more neighbours, which the density
     # and integrate phases pay for; the per-phase split and the final pair
     # count of each run show which is which.
-    def timed(case) -> tuple[float, dict]:
+    def timed(case) -> tuple[float, dict, float]:
         with FluidSolverGpu(case.params, case.count, device=device) as solver:
             solver.upload(*case.initial_state())
             solver.run(case.dt, 3)
@@ -374,18 +374,19 @@ def obstacles_leg(steps: int, flush, device: int, cpu: bool) -> dict:
                     flush.zero_()
                 for name, t in solver.profile(case.dt, 1).items():
                     phases[name] += t / 5
-            phases["pairs_per_particle"] = solver.stats().pairs_in_range / case.count
-        return total / steps, phases
+            pairs = solver.stats().pairs_in_range / case.count
+        return total / steps, phases, pairs
 
     shapes = W.obstacle_course_1m()
-    plain_ms, plain_phases = timed(W.dam_break_1m())
-    ms, phases = timed(shapes)
+    plain_ms, plain_phases, plain_pairs = timed(W.dam_break_1m())
+    ms, phases, pairs = timed(shapes)
     n = shapes.count
     out = {
         "workload": shapes.name, "colliders": int(shapes.params.collider_count),
         "force_fields": int(shapes.params.field_count), "substeps": steps, "ms_per_step": ms,
         "value": n * shapes.dt / (ms / 1e3), "unit": UNIT, "plain_ms_per_step": plain_ms,
         "shape_overhead_ms": ms - plain_ms, "phase_ms": phases, "plain_phase_ms": plain_phases,
+        "final_pairs_per_particle": pairs, "plain_final_pairs_per_particle": plain_pairs,
         "l2": "flushed before every substep",
     }
     if cpu:
