@@ -153,12 +153,29 @@ const Tables& tables() {
     return t;
 }
 
-__constant__ int8_t c_entry[256][SPH_MC_TABLE_WIDTH];
-__constant__ uint8_t c_count[256];
+// The case table and vertex counts sit in global memory and the march kernels
+// stage them in shared memory: the lanes of a warp look up different cases,
+// which constant memory would serve one address at a time.
+__device__ int8_t g_entry[256][SPH_MC_TABLE_WIDTH];
+__device__ uint8_t g_count[256];
 __constant__ int8_t c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
                                       {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-__constant__ int8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
-                                     {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+// Corner c of a cell (the corner table above, as bits) and the corners of
+// edge e: the four bottom edges (0-1, 1-2, 2-3, 3-0), the four top edges
+// (4-5, 5-6, 6-7, 7-4), then the four verticals (0-4, 1-5, 2-6, 3-7).
+__device__ __forceinline__ int corner_offset(int c, int d) {
+    return d == 0 ? ((c ^ (c >> 1)) & 1) : (d == 1 ? ((c >> 1) & 1) : (c >> 2));
+}
+__device__ __forceinline__ void edge_corners(int e, int& a, int& b) {
+    if (e < 8) {
+        a = e;
+        b = (e & 4) | ((e + 1) & 3);
+    } else {
+        a = e - 8;
+        b = e - 4;
+    }
+}
 
 constexpr uint32_t kBlock = 256;
 constexpr uint32_t kPerThread = 8;
@@ -409,6 +426,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
 // Case code of every cell and the vertex total of every tile of kTile cells.
 __global__ void __launch_bounds__(kBlock) count_kernel(const float* __restrict__ field, MarchGeom g,
                                                        uint8_t* __restrict__ codes, uint32_t* __restrict__ tile_sums) {
+    static_assert(kBlock == 256, "one thread stages one case's count");
+    __shared__ uint8_t s_count[256];
+    s_count[threadIdx.x] = g_count[threadIdx.x];
+    __syncthreads();
     const uint32_t cells = g.resolution * g.resolution * g.resolution;
     const uint32_t first = blockIdx.x * kTile + threadIdx.x * kPerThread;
     uint32_t sum = 0;
@@ -418,7 +439,7 @@ __global__ void __launch_bounds__(kBlock) count_kernel(const float* __restrict__
         if (cell < cells) {
             const uint32_t code = cell_code(field, g, cell);
             codes[cell] = static_cast<uint8_t>(code);
-            sum += c_count[code];
+            sum += s_count[code];
         }
     }
     __shared__ uint32_t total;
@@ -495,18 +516,17 @@ __device__ __forceinline__ float3 gradient(const float* __restrict__ field, int 
 // One vertex of a cell (marching_cubes.cpp:418-478): the interpolated point on
 // table entry v's edge and the packed outward normal.
 __device__ __forceinline__ sph_surface_vertex cell_vertex(const float* __restrict__ field, const MarchGeom& g,
-                                                          uint32_t cell, uint32_t code, uint32_t v) {
+                                                          uint32_t cell, const int8_t* entry, uint32_t v) {
     const int s = static_cast<int>(g.resolution) + 1;
     const int base[3] = {static_cast<int>(cell % g.resolution), static_cast<int>((cell / g.resolution) % g.resolution),
                          static_cast<int>(cell / (g.resolution * g.resolution))};
-    const int edge = c_entry[code][v];
-    const int a = c_edge[edge][0];
-    const int b = c_edge[edge][1];
+    int a, b;
+    edge_corners(entry[v], a, b);
     int ca[3], cb[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        ca[d] = base[d] + c_corner[a][d];
-        cb[d] = base[d] + c_corner[b][d];
+        ca[d] = base[d] + corner_offset(a, d);
+        cb[d] = base[d] + corner_offset(b, d);
     }
     const float va = field_at(field, s, ca[0], ca[1], ca[2]);
     const float vb = field_at(field, s, cb[0], cb[1], cb[2]);
@@ -554,6 +574,12 @@ __global__ void __launch_bounds__(kBlock) emit_kernel(const float* __restrict__ 
     __shared__ uint8_t s_code[kTile];
     __shared__ uint32_t s_first[kBlock + 1];
     __shared__ uint32_t total;
+    __shared__ alignas(16) int8_t s_entry[256][SPH_MC_TABLE_WIDTH];
+    __shared__ uint8_t s_count[256];
+    static_assert(kBlock == 256 && SPH_MC_TABLE_WIDTH == 16, "one thread stages one case's row and count");
+    reinterpret_cast<uint4*>(&s_entry[0][0])[threadIdx.x] = reinterpret_cast<const uint4*>(&g_entry[0][0])[threadIdx.x];
+    s_count[threadIdx.x] = g_count[threadIdx.x];
+    __syncthreads();
     const uint32_t cells = g.resolution * g.resolution * g.resolution;
     const uint32_t tile_first = blockIdx.x * kTile;
     uint32_t sum = 0;
@@ -562,7 +588,7 @@ __global__ void __launch_bounds__(kBlock) emit_kernel(const float* __restrict__ 
         const uint32_t cell = tile_first + threadIdx.x * kPerThread + k;
         const uint32_t code = cell < cells ? codes[cell] : 0u;
         s_code[threadIdx.x * kPerThread + k] = static_cast<uint8_t>(code);
-        sum += c_count[code];
+        sum += s_count[code];
     }
     s_first[threadIdx.x] = block_exclusive_scan(sum, &total);
     if (threadIdx.x == 0) {
@@ -587,11 +613,11 @@ __global__ void __launch_bounds__(kBlock) emit_kernel(const float* __restrict__ 
         uint32_t rem = v - s_first[lo];
         uint32_t local = s_first[lo];
         uint32_t k = lo * kPerThread;
-        uint32_t n = c_count[s_code[k]];
+        uint32_t n = s_count[s_code[k]];
         while (rem >= n) {
             rem -= n;
             local += n;
-            n = c_count[s_code[++k]];
+            n = s_count[s_code[++k]];
         }
         const uint32_t slot = block_slot + local;  // the cell's first vertex
         if (slot + n > capacity) {
@@ -599,7 +625,7 @@ __global__ void __launch_bounds__(kBlock) emit_kernel(const float* __restrict__ 
             atomicMin(limit, slot);
             continue;
         }
-        out[slot + rem] = cell_vertex(field, g, tile_first + k, s_code[k], rem);
+        out[slot + rem] = cell_vertex(field, g, tile_first + k, s_entry[s_code[k]], rem);
     }
 }
 
@@ -621,8 +647,8 @@ cudaError_t ensure_tables() {
         return cudaSuccess;
     }
     const Tables& t = tables();
-    if ((err = cudaMemcpyToSymbol(c_entry, t.entry, sizeof(t.entry))) != cudaSuccess ||
-        (err = cudaMemcpyToSymbol(c_count, t.count, sizeof(t.count))) != cudaSuccess) {
+    if ((err = cudaMemcpyToSymbol(g_entry, t.entry, sizeof(t.entry))) != cudaSuccess ||
+        (err = cudaMemcpyToSymbol(g_count, t.count, sizeof(t.count))) != cudaSuccess) {
         return err;
     }
     if (device < 64) {
