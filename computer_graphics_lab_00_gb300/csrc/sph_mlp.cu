@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/sph_c.h"
+#include "sph_f32x2.cuh"
 #include "sph_mlp.cuh"
 
 namespace sph {
@@ -172,34 +173,9 @@ __device__ __forceinline__ float erf_as(float x) { return copysignf(1.0f - erfc_
 // (the negative side keeps its relative accuracy: no 1 - (1 - r)
 // cancellation).
 //
-// Two activations go at once on the packed FP32 pipe: fma.rn.f32x2 and
-// mul.rn.f32x2 perform, lane by lane, the same rounded operations as scalar
-// fmaf and multiplies, so each lane's value is that of the scalar form while
-// the Horner steps, squarings and scalings take half the issue slots.
-using f32x2 = unsigned long long;
-__device__ __forceinline__ f32x2 pack2(float a, float b) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void unpack2(f32x2 r, float& a, float& b) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
-    f32x2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
-    f32x2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
+// Two activations go at once on the packed FP32 pipe (sph_f32x2.cuh): each
+// lane's value is that of the scalar form while the Horner steps, squarings
+// and scalings take half the issue slots.
 
 // z = v + bias and GELU(z) for two columns; z is returned for the training
 // saves.
