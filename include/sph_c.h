@@ -432,6 +432,7 @@ int sph_batch_stream(sph_batch* batch, void** stream);
 int sph_batch_get_tuning(const sph_batch* batch, sph_tuning* out);
 int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning);
 int sph_batch_autotune(sph_batch* batch, float dt, uint32_t substeps_per_trial, sph_tuning* best, float* best_ms);
+/* sph_profile_substeps for the whole batch: SPH_PROFILE_PHASES totals. */
 int sph_batch_profile_substeps(sph_batch* batch, float dt, uint32_t substeps, double* phase_ms);
 int sph_batch_launches_per_substep(const sph_batch* batch, uint32_t* launches);
 int sph_batch_device_bytes(const sph_batch* batch, uint64_t* bytes);
