@@ -1,8 +1,14 @@
 // sph_f32x2.cuh — two FP32 values in one 64-bit register pair for the packed
-// FP32 pipe (add/mul/fma.rn.f32x2). Each lane performs the same rounded
-// operation as the scalar instruction, so packed code gives the scalar bits
-// in half the issue slots. Only the explicit .rn forms are used: no
-// contraction question arises for them.
+// FP32 pipe (add/mul/fma.rn.f32x2), in half the issue slots of scalar code.
+//
+// One packed add, sub or mul rounds each lane as the scalar instruction does
+// (the division self-test's modes 2-4 compare them lane by lane). A chain of
+// them does not have to: ptxas contracts a packed mul whose result feeds a
+// packed add into one packed FMA even under --fmad=false (self-test mode 5,
+// a squared distance, differs from the scalar chain). So the exact passes
+// use scalar arithmetic, and these helpers serve only code whose results are
+// not held to the scalar bits: the MLP epilogue (bias add and GELU, rounded
+// to BF16 and checked against the oracle with a tolerance).
 #pragma once
 
 namespace sph {

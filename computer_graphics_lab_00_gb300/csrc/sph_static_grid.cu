@@ -29,10 +29,16 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 std::array<uint32_t*, kMaxDevices> g_scratch_address{};
 
-// The device address of g_grid_scratch on the current device. Host code must
+// The device address of g_grid_scratch in the current context. Host code must
 // not hand the symbol itself to a kernel: on the host it names a stand-in,
-// not device memory. Looked up once per device.
-cudaError_t scratch_for_current_device(uint32_t** out) {
+// not device memory. The address belongs to the context the library's module
+// was loaded into, so it is looked up again on every call made outside a
+// stream capture (a host-side table lookup once the module is loaded): after
+// a cudaDeviceReset, or with another context current, the next such call
+// picks the new address up. A call made while `stream` is being captured
+// (where a first lookup could load the module) reuses the address that the
+// last uncaptured call on this device found, and fails if there was none.
+cudaError_t scratch_for_current_device(cudaStream_t stream, uint32_t** out) {
     int device = 0;
     cudaError_t status = cudaGetDevice(&device);
     if (status != cudaSuccess) {
@@ -41,14 +47,22 @@ cudaError_t scratch_for_current_device(uint32_t** out) {
     if (device < 0 || device >= kMaxDevices) {
         return cudaErrorInvalidDevice;
     }
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    cudaError_t query = cudaStreamIsCapturing(stream, &capture);
+    bool capturing = query != cudaSuccess || capture != cudaStreamCaptureStatusNone;
+    if (query != cudaSuccess) {
+        cudaGetLastError();  // e.g. the legacy stream while another stream captures
+    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (g_scratch_address[device] == nullptr) {
+    if (!capturing) {
         void* address = nullptr;
         status = cudaGetSymbolAddress(&address, g_grid_scratch);
         if (status != cudaSuccess) {
             return status;
         }
         g_scratch_address[device] = static_cast<uint32_t*>(address);
+    } else if (g_scratch_address[device] == nullptr) {
+        return cudaErrorStreamCaptureUnsupported;
     }
     *out = g_scratch_address[device];
     return cudaSuccess;
@@ -139,12 +153,21 @@ extern "C" int sph_grid_build_static(const sph_params* params,
         cell_particles == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
+    // Positions are read as float4 (16-byte loads); the u32 arrays as words.
+    auto misaligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) % a) != 0; };
+    if (misaligned(positions, 16) || misaligned(cell_of, 4) || misaligned(cell_counts, 4) ||
+        misaligned(cell_particles, 4)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // This library's CUDA runtime is private to it, so an error pending in it
+    // was left by an earlier call of this library; it is not this call's.
+    cudaGetLastError();
     uint32_t* scratch = nullptr;
-    if (scratch_for_current_device(&scratch) != cudaSuccess) {
+    if (scratch_for_current_device(s, &scratch) != cudaSuccess) {
         cudaGetLastError();
         return SPH_ERR_CUDA;
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     auto* counts = static_cast<uint32_t*>(cell_counts);
     if (cudaMemsetAsync(counts, 0, sizeof(uint32_t) * cells, s) != cudaSuccess) {
         cudaGetLastError();
@@ -156,6 +179,9 @@ extern "C" int sph_grid_build_static(const sph_params* params,
     auto* keys = static_cast<uint32_t*>(cell_of);
     static_keys_kernel<<<(count + 255) / 256, 256, 0, s>>>(static_cast<const float4*>(positions), count, h, cells - 1U,
                                                           keys);
+    if (cudaGetLastError() != cudaSuccess) {
+        return SPH_ERR_CUDA;
+    }
     sph::GridScratch grid;
     grid.keys = keys;
     grid.keys_a = scratch;
@@ -171,6 +197,9 @@ extern "C" int sph_grid_build_static(const sph_params* params,
         return SPH_ERR_CUDA;
     }
     static_bounds_kernel<<<(count + 255) / 256, 256, 0, s>>>(grid.sorted_keys, count, start, end);
+    if (cudaGetLastError() != cudaSuccess) {
+        return SPH_ERR_CUDA;
+    }
     static_slots_kernel<<<(count + 255) / 256, 256, 0, s>>>(grid.sorted_keys, grid.sorted_ids, count, start, end,
                                                            counts, static_cast<uint32_t*>(cell_particles));
     if (cudaGetLastError() != cudaSuccess) {

@@ -128,7 +128,9 @@ typedef struct sph_tuning {
     uint32_t neighbour_kernel; /* 0: nested per-candidate loops; 1: flat stream + queued pair pass;
                                   2: density records in-range pairs, integrate runs them;
                                   3: as 2, divisions through a shared correctly rounded reciprocal;
-                                  4: density stores per-bucket pair masks, integrate expands them */
+                                  4: density stores per-bucket pair masks, integrate expands them;
+                                  5: cell-cooperative: the particles of a cell share one candidate list in
+                                     shared memory, lanes take candidates (density) and pairs (integrate) */
     uint32_t block_size;       /* threads per block of integrate (32..512, multiple of 32; 64/128/256 for 2-4;
                                   default 128) */
     uint32_t queue_depth;      /* in-range pairs buffered per thread: 8, 16, 24 or 32 */
@@ -224,22 +226,29 @@ int sph_grid_build(sph_ctx* ctx);
  * own allocator up front), or a latency-critical loop that cannot afford the
  * implicit device synchronisation a cudaMalloc may bring.
  *
- * The caller passes device buffers: `positions` (count AoS float4, id order),
- * and receives `cell_of` (count u32), `cell_counts` (C u32, un-truncated) and
- * `cell_particles` (C * 32 u32: the first 32 ids of each bucket, ascending;
- * slots past a bucket's count are left untouched) — the arrays of
- * FluidGrid::build for C = params->lattice[3]. Work is enqueued on `stream`
- * (a cudaStream_t, NULL for the legacy default stream) and is complete when
- * that stream reaches it.
+ * The caller passes device buffers: `positions` (count AoS float4 (x, y, z,
+ * w), id order, 16-byte aligned), and receives `cell_of` (count u32: the
+ * bucket of each particle), `cell_counts` (C u32: particles per bucket, not
+ * truncated) and `cell_particles` (C * 32 u32: the first 32 ids of each
+ * bucket, ascending; slots past a bucket's count are left untouched), for
+ * C = params->lattice[3] buckets. The u32 arrays must be 4-byte aligned; a
+ * misaligned buffer returns SPH_ERR_INVALID_ARGUMENT. Work is enqueued on
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) and is
+ * complete when that stream reaches it.
  *
  * The sort's scratch is a static device array inside the library, sized for
  * at most SPH_STATIC_MAX_PARTICLES particles and SPH_STATIC_MAX_CELLS buckets
  * (about 1.6 MB, held on every GPU that uses this call until the process
- * exits); larger requests return SPH_ERR_CAPACITY. The first call on a device
- * looks the array's device address up (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture. All calls share
- * the one array, so calls whose work overlaps on the GPU (on different
- * streams, or from different threads) race with each other: serialise them.
+ * exits); larger requests return SPH_ERR_CAPACITY. Every call made outside a
+ * stream capture looks the array's device address up (cudaGetSymbolAddress)
+ * in the current context, so a context reset or a different current context
+ * is picked up; a call on a stream that is being captured reuses the address
+ * found by the last uncaptured call on that device, so make one call on each
+ * device before capturing it (a captured call without one returns
+ * SPH_ERR_CUDA). All calls share the one array, so calls whose work overlaps
+ * on the GPU (on different streams, or from different threads) race with each
+ * other: serialise them. A CUDA failure returns SPH_ERR_CUDA; this call has
+ * no context object, so no error text goes with it.
  */
 #define SPH_STATIC_MAX_PARTICLES 65536u
 #define SPH_STATIC_MAX_CELLS 65536u
@@ -475,6 +484,11 @@ int sph_mlp_set_adam(sph_mlp* mlp, float beta1, float beta2, float epsilon);
 int sph_mlp_train_step(sph_mlp* mlp, const void* features, const void* targets, uint32_t count, float learning_rate,
                        float* loss);
 int sph_mlp_stream(sph_mlp* mlp, void** stream);
+/* Learned steps with this model take each tank's mean correction off along
+ * the axes set in `axes` (bit 0 x, 1 y, 2 z; 0, the default, keeps it), so
+ * the correction exerts no net force on a tank along them. No counterpart in
+ * the reference (it has no learned fluid path). */
+int sph_mlp_set_net_force_free(sph_mlp* mlp, uint32_t axes);
 /* One Adam step with a gradient supplied by the caller (host, SPH_MLP_PARAMS
  * floats), e.g. the average of several GPUs' sph_mlp_gradients in
  * data-parallel training. No counterpart in the reference (it has no learned

@@ -11,6 +11,7 @@ TEST INFRASTRUCTURE ONLY (see oracle/__init__.py).
 from __future__ import annotations
 
 import ctypes
+import os
 import subprocess
 from pathlib import Path
 
@@ -21,7 +22,8 @@ from computer_graphics_lab_00_gb300.abi import SphFluidSettings, SphParams, SphS
 ORACLE_DIR = Path(__file__).resolve().parent
 ORACLE_LIB = ORACLE_DIR / "build" / "libsph_oracle.so"
 REFERENCE_LIB = ORACLE_DIR / "_ref" / "libsph_ref.so"
-REFERENCE_TREE = Path("/root/reference")
+# The reference source tree; SPH_REFERENCE_TREE overrides the default location.
+REFERENCE_TREE = Path(os.environ.get("SPH_REFERENCE_TREE", "/root/reference"))
 
 P = ctypes.POINTER
 f32p = P(ctypes.c_float)
