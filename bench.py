@@ -67,6 +67,10 @@ def parse_args():
                    help="substeps of the 256-tank leg (0 skips it)")
     p.add_argument("--learned-steps", type=int, default=20,
                    help="coarse steps of the learned 5x-dt leg at 1M (0 skips it)")
+    p.add_argument("--learned-eval", action=argparse.BooleanOptionalAction, default=True,
+                   help="config 4: 64 held-out tanks of 32,768 over 2 s, learned and plain coarse vs plain fine")
+    p.add_argument("--fallback-steps", type=int, default=600,
+                   help="config 5: coarse steps of the 1,024 x 8,192 learned-with-fallback leg (0: skip)")
     p.add_argument("--sustained-steps", type=int, default=1000,
                    help="substeps of the whole-run leg of the 1M dam break (0 skips it)")
     p.add_argument("--instance-reps", type=int, default=20,
@@ -505,28 +509,80 @@ def learned_leg(steps: int, flush, device: int, plain_ms: float) -> dict:
         ends[k].record(stream)
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
-    # Accuracy over 0.1 s from the initial state.
+    # Accuracy over 2 s from the initial state (checks every 0.1 s) against
+    # the plain fine run, beside the plain coarse step without the network.
     fine = FluidSolverGpu(case.params, n, device=device)
-    fine.upload(pos, vel)
-    fine.run(T.FINE_DT, 120)
-    solver.upload(pos, vel)
-    solver.run_learned(T.COARSE_DT, 24, mlp)
-    sf = fine.stats()
-    sl = solver.stats()
+    plain = FluidSolverGpu(case.params, n, device=device)
+    for s in (fine, plain, solver):
+        s.upload(pos, vel)
+    err = {"learned": [], "plain": []}
+    drift = {"learned": [], "plain": []}
+    for _ in range(20):
+        fine.run(T.FINE_DT, 120)
+        solver.run_learned(T.COARSE_DT, 24, mlp)
+        plain.run_learned(T.COARSE_DT, 24, None)
+        sf = fine.stats()
+        for name, s in (("learned", solver), ("plain", plain)):
+            st = s.stats()
+            err[name].append(abs(st.mean_compression - sf.mean_compression))
+            drift[name].append(float(np.linalg.norm(np.array(st.centre_of_mass[:]) - np.array(sf.centre_of_mass[:]))))
     value = n * T.COARSE_DT / (ms / 1e3)
     plain_fine_value = n * T.FINE_DT / (plain_ms / 1e3)
     out = {
         "dt": T.COARSE_DT, "steps": steps, "ms_per_step": ms, "value": value, "unit": UNIT,
         "speedup_vs_plain_fine_step": value / plain_fine_value,
         "speedup_vs_plain_1_600": value / (n * case.dt / (plain_ms / 1e3)),
-        "density_error_0p1s": abs(sl.mean_compression - sf.mean_compression),
-        "fine_mean_compression_0p1s": sf.mean_compression,
-        "com_drift_0p1s_m": float(np.linalg.norm(np.array(sl.centre_of_mass[:]) - np.array(sf.centre_of_mass[:]))),
+        "density_error_2s": {k: float(np.mean(v)) for k, v in err.items()},
+        "com_drift_2s_m": {k: float(np.mean(v)) for k, v in drift.items()},
         "weights": str(WEIGHTS.relative_to(ROOT)),
     }
-    for s in (solver, fine, mlp):
+    for s in (solver, fine, plain, mlp):
         s.close()
     return out
+
+
+def learned_eval_leg(device: int) -> dict:
+    """Config 4's evaluation: 64 held-out dam-break/drop tanks of 32,768
+    particles over 2 s; mean density error and centre-of-mass drift of the
+    learned coarse step and of the plain coarse step (1/240 s) against the
+    plain fine run (1/1200 s)."""
+    from computer_graphics_lab_00_gb300 import training as T
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    held = T.learned_tanks(64, 32768, seed=T.HELD_OUT_SEED)
+    with MlpGpu(device=device) as mlp:
+        T.load_model(mlp, WEIGHTS)
+        start = time.perf_counter()
+        cmp = T.compare_with_fine(held, mlp, duration=2.0, every=0.1, device=device)
+        wall = time.perf_counter() - start
+    keep = ("mean_density_error", "final_density_error", "mean_com_drift_m", "final_com_drift_m")
+    return {"tanks": 64, "particles_per_tank": 32768, "seconds": 2.0, "wall_s": wall,
+            **{k: {q: v[q] for q in keep} for k, v in cmp.items()},
+            "ratio_density": cmp["learned"]["mean_density_error"] / cmp["plain"]["mean_density_error"],
+            "ratio_com": cmp["learned"]["mean_com_drift_m"] / cmp["plain"]["mean_com_drift_m"]}
+
+
+def learned_batched_leg(coarse_steps: int, device: int) -> dict:
+    """Config 5: 1,024 tanks of 8,192 particles (uneven blocks), learned
+    coarse steps of 1/240 s with the fine solver as judge and per-tank
+    fallback, against the plain batched form at the fine step (1/1200 s)
+    over the same simulated time on the same GPU."""
+    from computer_graphics_lab_00_gb300 import training as T
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    tankset = T.learned_tanks(1024, 8192, seed=7)
+    with MlpGpu(device=device) as mlp:
+        T.load_model(mlp, WEIGHTS)
+        learned = T.run_with_fallback(tankset, mlp, coarse_steps=coarse_steps, device=device)
+    plain = T.run_plain_fine(tankset, coarse_steps=coarse_steps, device=device)
+    errors = T.fallback_errors(learned, plain)
+    return {"tanks": 1024, "particles_per_tank": 8192, "coarse_steps": coarse_steps,
+            "speedup_vs_plain_fine": learned["sim_s_particles_per_s"] / plain["sim_s_particles_per_s"],
+            "learned_value": learned["sim_s_particles_per_s"], "plain_fine_value": plain["sim_s_particles_per_s"],
+            "unit": UNIT, "learned_wall_s": learned["wall_s"], "plain_fine_wall_s": plain["wall_s"],
+            "vs_plain_fine": errors, "fallback_fraction": learned["fallback_fraction"],
+            "judged_tank_intervals": learned["judged_tank_intervals"], "rejected": learned["rejected_checks"],
+            "drift_fallbacks": learned["drift_fallbacks"], "check_errors_mean": learned["check_errors_mean"]}
 
 
 def run_reference(args) -> None:
@@ -722,10 +778,6 @@ def run_gb300(args) -> None:
     }
     if world == 1 and args.sustained_steps > 0:
         out["sustained"] = sustained_leg(args.sustained_steps, flush, local)
-    if batched is not None:
-        out["batched"] = batched
-    if args.learned_steps > 0 and world == 1 and WEIGHTS.exists():
-        out["learned"] = learned_leg(args.learned_steps, flush, local, step_ms)
     if world == 1 and args.obstacle_steps > 0:
         out["obstacles"] = obstacles_leg(args.obstacle_steps, flush, local, not args.no_cpu_baseline)
     if world == 1 and args.instance_reps > 0:
@@ -735,6 +787,16 @@ def run_gb300(args) -> None:
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, args.cpu_seconds)
     solver.close()
+    # The batched and learned legs go last: they close the JSON line.
+    if batched is not None:
+        out["batched"] = batched
+    if world == 1 and WEIGHTS.exists():
+        if args.learned_steps > 0:
+            out["learned"] = learned_leg(args.learned_steps, flush, local, step_ms)
+        if args.learned_eval:
+            out["learned_eval"] = learned_eval_leg(local)
+        if args.fallback_steps > 0:
+            out["learned_batched"] = learned_batched_leg(args.fallback_steps, local)
     print(json.dumps(out), flush=True)
 
 

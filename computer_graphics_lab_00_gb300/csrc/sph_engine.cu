@@ -200,7 +200,7 @@ void Engine::release() {
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
                        rank_,          order_,        compact_ids_, compact_sorted_, compact_ranges_,
                        snap_pos_[0], snap_vel_[0],
-                       snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_};
+                       snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_, correction_sums_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -1171,6 +1171,7 @@ int Engine::ensure_learned_buffers() {
     int status = SPH_OK;
     if ((status = alloc(&sforce_, total_capacity_)) != SPH_OK ||
         (status = alloc(&scorrection_, total_capacity_)) != SPH_OK ||
+        (status = alloc(&correction_sums_, tanks_.size() * kCorrectionSumWords)) != SPH_OK ||
         (status = alloc(&sfeatures_, static_cast<size_t>(total_capacity_) * 32)) != SPH_OK) {
         return status;
     }
@@ -1198,11 +1199,18 @@ int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launc
     if (model != nullptr) {
         SPH_CUDA(mlp::launch_forward(*model, sfeatures_, n, reinterpret_cast<float*>(scorrection_), nullptr,
                                      &counters_->error_flags, stream_));
+        if (model->free_axes != 0) {
+            // No net force along these axes: each tank's mean correction is removed.
+            SPH_CUDA(launch_correction_sums(scorrection_, d_tanks_, stank_, n, static_cast<uint32_t>(tanks_.size()),
+                                            correction_sums_, stream_));
+        }
     }
+    const bool free = model != nullptr && model->free_axes != 0;
     SPH_CUDA(launch_finish_learned(spos2_, svel_, grid_.sorted_ids, d_tanks_, stank_, n, sforce_,
-                                   model != nullptr ? scorrection_ : nullptr, pos_, vel_, stream_));
+                                   model != nullptr ? scorrection_ : nullptr, free ? correction_sums_ : nullptr,
+                                   free ? model->free_axes : 0u, pos_, vel_, stream_));
     if (launches != nullptr) {
-        *launches += model != nullptr ? 4 : 3;
+        *launches += model != nullptr ? (free ? 5 : 4) : 3;
     }
     return enqueue_colliders(launches);
 }
@@ -1465,7 +1473,7 @@ int Engine::selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t*
 
 int Engine::set_tuning(const NeighbourTuning& tuning) {
     bool queue_ok = tuning.queue == 8 || tuning.queue == 16 || tuning.queue == 24 || tuning.queue == 32;
-    if (tuning.variant > 4 || tuning.block < 32 || tuning.block > 512 || tuning.block % 32 != 0 || !queue_ok ||
+    if (tuning.variant > 5 || tuning.block < 32 || tuning.block > 512 || tuning.block % 32 != 0 || !queue_ok ||
         static_cast<size_t>(tuning.queue) * tuning.block * sizeof(uint32_t) > 48 * 1024) {
         return SPH_ERR_INVALID_ARGUMENT;
     }

@@ -218,6 +218,7 @@ private:
     float4* snap_vel_[kSnapshotSlots] = {nullptr, nullptr};
     float4* sforce_ = nullptr;
     float4* scorrection_ = nullptr;
+    unsigned long long* correction_sums_ = nullptr;  // kCorrectionSumWords per tank
     float* sfeatures_ = nullptr;
     cudaGraphExec_t learned_graph_ = nullptr;
     uint32_t learned_graph_count_ = 0xFFFFFFFFu;

@@ -1436,6 +1436,425 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(cons
                     sorted_ids[p], pos_out, vel_out);
 }
 
+// ---- cell-cooperative variant ------------------------------------------------
+//
+// A warp owns 32 consecutive processing slots. Consecutive slots whose
+// particles lie in the same cell of the same tank form a group: a cell's
+// particles are consecutive in the Morton processing order (in sorted order
+// a bucket shared by two cells can split a cell into several groups, which
+// costs time only). Every particle of a group has the same 27 neighbour
+// buckets, so the group's candidates, the first min(count, 32) entries of
+// each bucket concatenated in the reference's (dz, dy, dx) order
+// (fluid_sph.cpp:205-216, :234-258), are listed once in shared memory and
+// visited by all 32 lanes at once instead of once per particle.
+//
+// Density: lanes take 32 candidates at a time and loop over the group's
+// particles. Each (particle, candidate) poly6 term goes to shared memory and
+// the particle's own lane adds its row in candidate order; an out-of-range
+// term is +0, which leaves the non-negative sum's bits as they are, so the
+// sum is the reference's bit for bit. The same pass records which pairs
+// integrate uses, one 32-bit word per particle and 32 candidates, stored
+// chunk-major by processing slot (masks[c * n + slot]).
+//
+// Integrate: the group's pairs are computed in rounds. Each particle's lane
+// lists its next pairs (in candidate order); all 32 lanes compute the
+// pressure and viscosity terms of the listed pairs into shared memory, one
+// pair per lane; then lanes that own one (particle, axis) add the terms in
+// the reference's order. The forces, and so every result bit, are those of
+// the per-particle kernels.
+
+constexpr uint32_t kCoopWarps = 4;                             // warps per block
+constexpr uint32_t kCoopMaxCandidates = 27u * kCellCapacity;  // 864
+constexpr uint32_t kCoopMaxChunks = kCoopMaxCandidates / 32u;  // 27 mask words per particle at most
+constexpr uint32_t kCoopPairs = 256;                           // pairs listed per integrate round
+constexpr uint32_t kFullMask = 0xFFFFFFFFu;
+static_assert(kCoopMaxChunks <= 27u, "the mask buffer holds 27 words per particle");
+
+// Group starts of a window: lane l starts a group when it holds a particle
+// and lane l - 1 holds none, or one of another cell or tank.
+__device__ __forceinline__ uint32_t coop_group_starts(bool valid, uint32_t tank, uint32_t cx, uint32_t cy,
+                                                      uint32_t cz, uint32_t lane, uint32_t& valid_mask) {
+    const uint32_t pcx = __shfl_up_sync(kFullMask, cx, 1);
+    const uint32_t pcy = __shfl_up_sync(kFullMask, cy, 1);
+    const uint32_t pcz = __shfl_up_sync(kFullMask, cz, 1);
+    const uint32_t ptank = __shfl_up_sync(kFullMask, tank, 1);
+    valid_mask = __ballot_sync(kFullMask, valid);
+    const bool prev_valid = lane > 0 && ((valid_mask >> (lane - 1u)) & 1u) != 0;
+    const bool start = valid && (!prev_valid || pcx != cx || pcy != cy || pcz != cz || ptank != tank);
+    return __ballot_sync(kFullMask, start);
+}
+
+// One past the last lane of the group that starts at lane s: the next group
+// start or the first lane without a particle after s.
+__device__ __forceinline__ uint32_t coop_group_end(uint32_t s, uint32_t later_starts, uint32_t valid_mask) {
+    const uint32_t above = s >= 31u ? 0u : (kFullMask << (s + 1u));
+    const uint32_t stop = (later_starts | ~valid_mask) & above;
+    return stop == 0 ? 32u : static_cast<uint32_t>(__ffs(stop) - 1);
+}
+
+// The group's candidate list: lane b < 27 finds bucket b's range, and the
+// sorted positions of the buckets' first min(count, 32) entries go to cidx in
+// bucket order. Returns their number (at most 864). All lanes take part.
+__device__ __forceinline__ uint32_t coop_candidates(const uint2* __restrict__ bucket, uint32_t cx, uint32_t cy,
+                                                    uint32_t cz, uint32_t cell_mask, uint32_t base, uint32_t lane,
+                                                    uint32_t* cidx) {
+    uint32_t start = 0;
+    uint32_t count = 0;
+    if (lane < 27u) {
+        const uint2 r = neighbour_range(bucket, cx, cy, cz, lane, cell_mask, base);
+        start = r.x;
+        count = r.y - r.x;
+    }
+    uint32_t inclusive = count;
+#pragma unroll
+    for (uint32_t o = 1; o < 32u; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFullMask, inclusive, o);
+        if (lane >= o) {
+            inclusive += v;
+        }
+    }
+    const uint32_t total = __shfl_sync(kFullMask, inclusive, 31);
+    const uint32_t offset = inclusive - count;
+    for (uint32_t k = 0; k < count; ++k) {
+        cidx[offset + k] = start + k;
+    }
+    __syncwarp();
+    return total;
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(kCoopWarps * 32) density_coop_kernel(const float4* __restrict__ spos,
+                                                                       float4* __restrict__ svel,
+                                                                       float4* __restrict__ spos2,
+                                                                       const uint2* __restrict__ bucket,
+                                                                       const TankConst* __restrict__ tanks,
+                                                                       const uint16_t* __restrict__ stank, uint32_t n,
+                                                                       const uint32_t* __restrict__ order,
+                                                                       uint32_t* __restrict__ masks,
+                                                                       StepCounters* __restrict__ counters,
+                                                                       int all_tanks) {
+    __shared__ uint32_t s_cidx[kCoopWarps][kCoopMaxCandidates];
+    __shared__ float4 s_self[kCoopWarps][32];
+    // Row i: the terms of the group's i-th particle against the 32 candidates
+    // of a chunk (36 floats a row: conflict-free 16-byte reads of a column).
+    __shared__ __align__(16) float s_term[kCoopWarps][32][36];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t w = threadIdx.x >> 5;
+    const uint32_t slot = (blockIdx.x * kCoopWarps + w) * 32u + lane;
+    uint32_t p = slot;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    bool valid = p < n;
+    const uint32_t tank = valid && stank != nullptr ? stank[p] : 0u;
+    const TankConst* t = tanks + tank;
+    // A tank that sits this substep out is not integrated, and tanks never
+    // share pairs, so its densities are not needed (pair counting visits all).
+    if (!kCount && all_tanks == 0 && valid && __ldg(&t->active) == 0) {
+        valid = false;
+    }
+    float4 self = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t cx = 0;
+    uint32_t cy = 0;
+    uint32_t cz = 0;
+    if (valid) {
+        self = spos[p];
+        const float h = __ldg(&t->h);
+        cx = static_cast<uint32_t>(cell_coord(self.x, h));
+        cy = static_cast<uint32_t>(cell_coord(self.y, h));
+        cz = static_cast<uint32_t>(cell_coord(self.z, h));
+    }
+    s_self[w][lane] = self;
+    uint32_t valid_mask = 0;
+    uint32_t starts = coop_group_starts(valid, tank, cx, cy, cz, lane, valid_mask);
+    float density = 0.0f;
+    unsigned long long candidates = 0;
+    unsigned long long in_range = 0;
+    const float far = __int_as_float(0x7F800000);  // +inf: a padding lane's candidate
+    while (starts != 0) {
+        const uint32_t s = static_cast<uint32_t>(__ffs(starts) - 1);
+        starts &= starts - 1u;
+        const uint32_t e = coop_group_end(s, starts, valid_mask);
+        const uint32_t m = e - s;
+        const bool mine = lane >= s && lane < e;
+        const TankConst* g = tanks + __shfl_sync(kFullMask, tank, s);
+        const uint32_t gx = __shfl_sync(kFullMask, cx, s);
+        const uint32_t gy = __shfl_sync(kFullMask, cy, s);
+        const uint32_t gz = __shfl_sync(kFullMask, cz, s);
+        const float h2 = __ldg(&g->h2);
+        const float c6 = __ldg(&g->c_poly6);
+        const float mass = __ldg(&g->mass);
+        const float r2_far = __ldg(&g->r2_far);
+        const float r2_near = __ldg(&g->r2_near);
+        const uint32_t count = coop_candidates(bucket, gx, gy, gz, __ldg(&g->cell_mask), __ldg(&g->bucket_base),
+                                               lane, s_cidx[w]);
+        // max.NaN(term, +0) drops out-of-range terms while mass * c_poly6 > 0
+        // (out of range d <= 0, so the term is negative or +0); otherwise the
+        // reference's compare and select.
+        const bool by_max = mass > 0.0f && c6 > 0.0f;
+        const uint32_t chunks = (count + 31u) / 32u;
+        for (uint32_t c = 0; c < chunks; ++c) {
+            const uint32_t q = c * 32u + lane;
+            const uint32_t left = count - c * 32u;
+            const uint32_t live = left >= 32u ? kFullMask : ((1u << left) - 1u);
+            float ox = far;
+            float oy = far;
+            float oz = far;
+            if (q < count) {
+                const float4 o = __ldg(&spos[s_cidx[w][q]]);
+                ox = o.x;
+                oy = o.y;
+                oz = o.z;
+            }
+            uint32_t word = 0;
+            for (uint32_t i = 0; i < m; ++i) {
+                const float4 si = s_self[w][s + i];
+                const float r2 = dot3(__fsub_rn(si.x, ox), __fsub_rn(si.y, oy), __fsub_rn(si.z, oz));
+                // mass * poly6 (fluid_sph.cpp:24-31, :214).
+                const float d = __fsub_rn(h2, r2);
+                const float term = __fmul_rn(mass, __fmul_rn(__fmul_rn(__fmul_rn(c6, d), d), d));
+                float kept;
+                if (by_max) {
+                    asm("max.NaN.f32 %0, %1, %2;" : "=f"(kept) : "f"(term), "f"(0.0f));
+                } else {
+                    kept = r2 >= h2 ? 0.0f : term;
+                }
+                s_term[w][i][lane] = kept;
+                // Integrate skips distance >= h or <= 1e-6 (fluid_sph.cpp:245-248);
+                // the particle itself (r2 = 0) fails the second test.
+                const uint32_t used = __ballot_sync(kFullMask, !(r2 >= r2_far || r2 <= r2_near)) & live;
+                if (lane == s + i) {
+                    word = used;
+                }
+                if (kCount) {
+                    const uint32_t near = __ballot_sync(kFullMask, r2 < h2) & live;
+                    if (lane == 0) {
+                        in_range += static_cast<unsigned long long>(__popc(near));
+                    }
+                }
+            }
+            __syncwarp();
+            if (mine) {
+                const float* row = s_term[w][lane - s];
+#pragma unroll
+                for (uint32_t k = 0; k < 32u; k += 4u) {
+                    const float4 v = *reinterpret_cast<const float4*>(row + k);
+                    density = __fadd_rn(density, v.x);
+                    density = __fadd_rn(density, v.y);
+                    density = __fadd_rn(density, v.z);
+                    density = __fadd_rn(density, v.w);
+                }
+                masks[static_cast<size_t>(c) * n + slot] = word;
+            }
+            __syncwarp();
+        }
+        if (kCount && mine) {
+            candidates += count;
+        }
+    }
+    if (kCount) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            candidates += __shfl_down_sync(kFullMask, candidates, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&counters->candidates, candidates);
+            atomicAdd(&counters->in_range, in_range);
+        }
+    }
+    if (!valid) {
+        return;
+    }
+    density = max_like_std(density, 1e-6f);
+    const float pressure =
+        max_like_std(__fmul_rn(__ldg(&t->stiffness), __fsub_rn(density, __ldg(&t->rest_density))), 0.0f);
+    spos2[p] = make_float4(self.x, self.y, self.z, density);
+    reinterpret_cast<float*>(svel)[4 * static_cast<size_t>(p) + 3] = pressure;
+}
+
+// Pressure and viscosity terms of one in-range pair with the two shared
+// reciprocals: the operations of add_pair_force_rcp, whose sums add pv.xyz
+// then pv.w / vyz in this order per axis.
+__device__ __forceinline__ void pair_terms(const PairConst& k, const float4& self, const float4& sv,
+                                           const float4& other, const float4& ov, float4& pv, float2& vyz) {
+    const float ex = __fsub_rn(self.x, other.x);
+    const float ey = __fsub_rn(self.y, other.y);
+    const float ez = __fsub_rn(self.z, other.z);
+    const float distance = __fsqrt_rn(dot3(ex, ey, ez));
+    const float inv_distance = __frcp_rn(distance);
+    const float other_density = max_like_std(other.w, 1e-6f);
+    const float inv_density = __frcp_rn(other_density);
+    const float ps = div_by(__fmul_rn(k.neg_mass, __fadd_rn(sv.w, ov.w)), __fmul_rn(2.0f, other_density),
+                            __fmul_rn(0.5f, inv_density));
+    const float d = __fsub_rn(k.h, distance);
+    const float gs = __fmul_rn(__fmul_rn(k.c_spiky, d), d);
+    pv.x = __fmul_rn(ps, __fmul_rn(gs, div_by(ex, distance, inv_distance)));
+    pv.y = __fmul_rn(ps, __fmul_rn(gs, div_by(ey, distance, inv_distance)));
+    pv.z = __fmul_rn(ps, __fmul_rn(gs, div_by(ez, distance, inv_distance)));
+    const float lap = __fmul_rn(k.c_visc, d);
+    pv.w = __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.x, sv.x)), other_density, inv_density), lap);
+    vyz.x = __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.y, sv.y)), other_density, inv_density), lap);
+    vyz.y = __fmul_rn(div_by(__fmul_rn(k.visc_mass, __fsub_rn(ov.z, sv.z)), other_density, inv_density), lap);
+}
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kCoopWarps * 32, kMinBlocks) integrate_coop_kernel(
+    const float4* __restrict__ spos2, const float4* __restrict__ svel, const uint32_t* __restrict__ sorted_ids,
+    const uint2* __restrict__ bucket, const TankConst* __restrict__ tanks, const uint16_t* __restrict__ stank,
+    uint32_t n, const uint32_t* __restrict__ order, const uint32_t* __restrict__ masks, float4* __restrict__ pos_out,
+    float4* __restrict__ vel_out) {
+    __shared__ uint32_t s_cidx[kCoopWarps][kCoopMaxCandidates];
+    __shared__ float4 s_selfp[kCoopWarps][32];
+    __shared__ float4 s_selfv[kCoopWarps][32];
+    __shared__ float4 s_pv[kCoopWarps][kCoopPairs];   // pressure xyz, viscosity x
+    __shared__ float2 s_vyz[kCoopWarps][kCoopPairs];  // viscosity y, z
+    __shared__ uint16_t s_pq[kCoopWarps][kCoopPairs];  // candidate of each listed pair
+    __shared__ uint8_t s_pi[kCoopWarps][kCoopPairs];   // its particle, within the group
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t w = threadIdx.x >> 5;
+    const uint32_t slot = (blockIdx.x * kCoopWarps + w) * 32u + lane;
+    uint32_t p = slot;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    bool valid = p < n;
+    const uint32_t tank = valid && stank != nullptr ? stank[p] : 0u;
+    const TankConst* t = tanks + tank;
+    valid = valid && __ldg(&t->active) != 0;
+    float4 self = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 sv = self;
+    uint32_t cx = 0;
+    uint32_t cy = 0;
+    uint32_t cz = 0;
+    if (valid) {
+        self = spos2[p];
+        sv = svel[p];
+        const float h = __ldg(&t->h);
+        cx = static_cast<uint32_t>(cell_coord(self.x, h));
+        cy = static_cast<uint32_t>(cell_coord(self.y, h));
+        cz = static_cast<uint32_t>(cell_coord(self.z, h));
+    }
+    s_selfp[w][lane] = self;
+    s_selfv[w][lane] = sv;
+    uint32_t valid_mask = 0;
+    uint32_t starts = coop_group_starts(valid, tank, cx, cy, cz, lane, valid_mask);
+    float fx = 0.0f;
+    float fy = 0.0f;
+    float fz = 0.0f;
+    while (starts != 0) {
+        const uint32_t s = static_cast<uint32_t>(__ffs(starts) - 1);
+        starts &= starts - 1u;
+        const uint32_t e = coop_group_end(s, starts, valid_mask);
+        const uint32_t m = e - s;
+        const bool mine = lane >= s && lane < e;
+        const TankConst* g = tanks + __shfl_sync(kFullMask, tank, s);
+        PairConst k;
+        k.h = __ldg(&g->h);
+        k.c_spiky = __ldg(&g->c_spiky);
+        k.c_visc = __ldg(&g->c_visc);
+        k.neg_mass = __ldg(&g->neg_mass);
+        k.visc_mass = __ldg(&g->visc_mass);
+        const uint32_t count =
+            coop_candidates(bucket, __shfl_sync(kFullMask, cx, s), __shfl_sync(kFullMask, cy, s),
+                            __shfl_sync(kFullMask, cz, s), __ldg(&g->cell_mask), __ldg(&g->bucket_base), lane, s_cidx[w]);
+        const uint32_t chunks = (count + 31u) / 32u;
+        // This lane's particle: its pairs left to list and its place in the
+        // mask words (chunk c, the bits not yet listed).
+        uint32_t left = 0;
+        uint32_t c = 0;
+        uint32_t word = 0;
+        if (mine) {
+            for (uint32_t j = 0; j < chunks; ++j) {
+                left += static_cast<uint32_t>(__popc(__ldg(&masks[static_cast<size_t>(j) * n + slot])));
+            }
+            if (chunks != 0) {
+                word = __ldg(&masks[slot]);
+            }
+        }
+        // Lanes a, a + 32, a + 64 own the sums of (particle a / 3, axis a % 3).
+        float acc[3] = {0.0f, 0.0f, 0.0f};
+        const uint32_t per_particle = kCoopPairs / m;
+        while (__any_sync(kFullMask, left != 0)) {
+            // List each particle's next pairs, in candidate order.
+            const uint32_t take = min(left, per_particle);
+            uint32_t first = take;
+#pragma unroll
+            for (uint32_t o = 1; o < 32u; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(kFullMask, first, o);
+                if (lane >= o) {
+                    first += v;
+                }
+            }
+            const uint32_t total = __shfl_sync(kFullMask, first, 31);
+            first -= take;
+            for (uint32_t j = 0; j < take; ++j) {
+                while (word == 0) {
+                    ++c;
+                    word = __ldg(&masks[static_cast<size_t>(c) * n + slot]);
+                }
+                const uint32_t bit = static_cast<uint32_t>(__ffs(word) - 1);
+                word &= word - 1u;
+                s_pq[w][first + j] = static_cast<uint16_t>(c * 32u + bit);
+                s_pi[w][first + j] = static_cast<uint8_t>(lane - s);
+            }
+            left -= take;
+            __syncwarp();
+            // Pair terms, one pair per lane.
+            for (uint32_t f = lane; f < total; f += 32u) {
+                const uint32_t i = s + s_pi[w][f];
+                const uint32_t q = s_cidx[w][s_pq[w][f]];
+                float4 pv;
+                float2 vyz;
+                pair_terms(k, s_selfp[w][i], s_selfv[w][i], __ldg(&spos2[q]), __ldg(&svel[q]), pv, vyz);
+                s_pv[w][f] = pv;
+                s_vyz[w][f] = vyz;
+            }
+            __syncwarp();
+            // Sums per (particle, axis): pressure then viscosity term of each
+            // pair, pairs in order (fluid_sph.cpp:249-254).
+#pragma unroll
+            for (uint32_t r = 0; r < 3u; ++r) {
+                const uint32_t a = lane + 32u * r;
+                const uint32_t i = a / 3u;
+                const uint32_t axis = a - 3u * i;
+                const uint32_t src = min(s + i, 31u);
+                const uint32_t from = __shfl_sync(kFullMask, first, src);
+                const uint32_t n_i = __shfl_sync(kFullMask, take, src);
+                if (i < m) {
+                    for (uint32_t f = from; f < from + n_i; ++f) {
+                        const float* pvf = reinterpret_cast<const float*>(&s_pv[w][f]);
+                        const float vis = axis == 0u ? pvf[3] : reinterpret_cast<const float*>(&s_vyz[w][f])[axis - 1u];
+                        acc[r] = __fadd_rn(__fadd_rn(acc[r], pvf[axis]), vis);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        // Hand each particle's three sums to its own lane.
+        float* sums = reinterpret_cast<float*>(s_pv[w]);
+#pragma unroll
+        for (uint32_t r = 0; r < 3u; ++r) {
+            const uint32_t a = lane + 32u * r;
+            if (a < 3u * m) {
+                sums[a] = acc[r];
+            }
+        }
+        __syncwarp();
+        if (mine) {
+            const uint32_t i = lane - s;
+            fx = sums[3u * i];
+            fy = sums[3u * i + 1u];
+            fz = sums[3u * i + 2u];
+        }
+        __syncwarp();
+    }
+    if (!valid) {
+        return;
+    }
+    finish_particle(t, self, max_like_std(self.w, 1e-6f), sv.x, sv.y, sv.z, sv.w, fx, fy, fz, sorted_ids[p], pos_out,
+                    vel_out);
+}
+
 // ---- learned coarse step ------------------------------------------------------
 //
 // The learned step splits integrate in two: `features_kernel` computes the
@@ -1609,6 +2028,63 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const floa
     }
 }
 
+// The correction's net force on each tank, as the sum of its particles'
+// corrections in 2^-24 m/s^2 fixed point: integer sums do not depend on the
+// order of the atomics, so the mean (and the step) is the same on every run.
+// sums holds kCorrectionSumWords per tank: x, y, z and the particle count.
+constexpr float kCorrectionFixed = 16777216.0f;  // 2^24
+constexpr float kCorrectionFixedMax = 1.0e9f;    // |correction| beyond this (or NaN) counts as 0
+__device__ __forceinline__ long long correction_fixed(float v) {
+    return fabsf(v) <= kCorrectionFixedMax ? __float2ll_rn(v * kCorrectionFixed) : 0ll;
+}
+
+__global__ void __launch_bounds__(256) correction_sums_kernel(const float4* __restrict__ correction,
+                                                              const TankConst* __restrict__ tanks,
+                                                              const uint16_t* __restrict__ stank, uint32_t n,
+                                                              unsigned long long* __restrict__ sums) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    const uint32_t t = valid && stank != nullptr ? stank[p] : 0u;
+    const bool counted = valid && __ldg(&tanks[t].active) != 0;
+    long long x = 0;
+    long long y = 0;
+    long long z = 0;
+    if (counted) {
+        const float4 c = correction[p];
+        x = correction_fixed(c.x);
+        y = correction_fixed(c.y);
+        z = correction_fixed(c.z);
+    }
+    // Lanes of one tank add up with shuffles first (tanks are contiguous in
+    // the sorted order, so a warp rarely straddles two).
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t same = __match_any_sync(0xFFFFFFFFu, counted ? t : 0xFFFFFFFFu);
+    const uint32_t leader = static_cast<uint32_t>(__ffs(same) - 1);
+    if (same == 0xFFFFFFFFu) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            x += __shfl_down_sync(0xFFFFFFFFu, x, o);
+            y += __shfl_down_sync(0xFFFFFFFFu, y, o);
+            z += __shfl_down_sync(0xFFFFFFFFu, z, o);
+        }
+        if (lane == 0 && counted) {
+            unsigned long long* s = sums + static_cast<size_t>(t) * kCorrectionSumWords;
+            atomicAdd(&s[0], static_cast<unsigned long long>(x));
+            atomicAdd(&s[1], static_cast<unsigned long long>(y));
+            atomicAdd(&s[2], static_cast<unsigned long long>(z));
+            atomicAdd(&s[3], 32ull);
+        }
+    } else if (counted) {
+        unsigned long long* s = sums + static_cast<size_t>(t) * kCorrectionSumWords;
+        atomicAdd(&s[0], static_cast<unsigned long long>(x));
+        atomicAdd(&s[1], static_cast<unsigned long long>(y));
+        atomicAdd(&s[2], static_cast<unsigned long long>(z));
+        if (lane == leader) {
+            atomicAdd(&s[3], static_cast<unsigned long long>(__popc(same)));
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) finish_learned_kernel(const float4* __restrict__ spos2,
                                                              const float4* __restrict__ svel,
                                                              const uint32_t* __restrict__ sorted_ids,
@@ -1616,20 +2092,37 @@ __global__ void __launch_bounds__(256) finish_learned_kernel(const float4* __res
                                                              const uint16_t* __restrict__ stank, uint32_t n,
                                                              const float4* __restrict__ force,
                                                              const float4* __restrict__ correction,
-                                                             float4* __restrict__ pos_out,
+                                                             const unsigned long long* __restrict__ sums,
+                                                             uint32_t free_axes, float4* __restrict__ pos_out,
                                                              float4* __restrict__ vel_out) {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) {
         return;
     }
-    const TankConst* t = tanks + (stank != nullptr ? stank[p] : 0);
+    const uint32_t tank = stank != nullptr ? stank[p] : 0u;
+    const TankConst* t = tanks + tank;
     if (__ldg(&t->active) == 0) {
         return;
     }
     const float4 self = spos2[p];
     const float4 sv = svel[p];
     const float4 fo = force[p];
-    const float4 da = correction != nullptr ? correction[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 da = correction != nullptr ? correction[p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (correction != nullptr && sums != nullptr) {
+        // No net force along the chosen axes: the tank's mean correction is
+        // taken off every particle.
+        const unsigned long long* s = sums + static_cast<size_t>(tank) * kCorrectionSumWords;
+        const double scale = 1.0 / (static_cast<double>(kCorrectionFixed) * static_cast<double>(__ldg(&s[3])));
+        if (free_axes & 1u) {
+            da.x -= static_cast<float>(static_cast<double>(static_cast<long long>(__ldg(&s[0]))) * scale);
+        }
+        if (free_axes & 2u) {
+            da.y -= static_cast<float>(static_cast<double>(static_cast<long long>(__ldg(&s[1]))) * scale);
+        }
+        if (free_axes & 4u) {
+            da.z -= static_cast<float>(static_cast<double>(static_cast<long long>(__ldg(&s[2]))) * scale);
+        }
+    }
     finish_particle(t, self, max_like_std(self.w, 1e-6f), sv.x, sv.y, sv.z, sv.w, fo.x, fo.y, fo.z, sorted_ids[p],
                     pos_out, vel_out, da);
 }
@@ -1737,6 +2230,17 @@ cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, cons
         }
         return cudaGetLastError();
     }
+    if (tuning.variant == 5) {
+        const uint32_t blocks = (n + kCoopWarps * 32u - 1u) / (kCoopWarps * 32u);
+        if (counters != nullptr) {
+            density_coop_kernel<true><<<blocks, kCoopWarps * 32u, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
+                                                                             tuning.order, tuning.masks, counters, 1);
+        } else {
+            density_coop_kernel<false><<<blocks, kCoopWarps * 32u, 0, stream>>>(
+                spos, svel, spos2, bucket, tanks, stank, n, tuning.order, tuning.masks, nullptr, tuning.all_tanks ? 1 : 0);
+        }
+        return cudaGetLastError();
+    }
     if (tuning.variant == 4) {
         uint32_t blocks = (n + 127) / 128;
         if (counters != nullptr) {
@@ -1781,6 +2285,12 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
     if (tuning.variant == 0) {
         integrate_kernel<<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, pos,
                                                               vel);
+        return cudaGetLastError();
+    }
+    if (tuning.variant == 5) {
+        const uint32_t blocks = (n + kCoopWarps * 32u - 1u) / (kCoopWarps * 32u);
+        integrate_coop_kernel<1><<<blocks, kCoopWarps * 32u, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
+                                                                        tuning.order, tuning.masks, pos, vel);
         return cudaGetLastError();
     }
     if (tuning.variant == 4) {
@@ -1918,14 +2428,25 @@ cudaError_t launch_features(const float4* spos2, const float4* svel, const uint3
     return cudaGetLastError();
 }
 
+cudaError_t launch_correction_sums(const float4* correction, const TankConst* tanks, const uint16_t* stank, uint32_t n,
+                                   uint32_t tank_count, unsigned long long* sums, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * kCorrectionSumWords * tank_count, stream);
+    if (e != cudaSuccess || n == 0) {
+        return e;
+    }
+    correction_sums_kernel<<<(n + 255) / 256, 256, 0, stream>>>(correction, tanks, stank, n, sums);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,
                                   const TankConst* tanks, const uint16_t* stank, uint32_t n, const float4* force,
-                                  const float4* correction, float4* pos, float4* vel, cudaStream_t stream) {
+                                  const float4* correction, const unsigned long long* sums, uint32_t free_axes,
+                                  float4* pos, float4* vel, cudaStream_t stream) {
     if (n == 0) {
         return cudaSuccess;
     }
     finish_learned_kernel<<<(n + 255) / 256, 256, 0, stream>>>(spos2, svel, sorted_ids, tanks, stank, n, force,
-                                                                correction, pos, vel);
+                                                                correction, sums, free_axes, pos, vel);
     return cudaGetLastError();
 }
 

@@ -123,7 +123,10 @@ cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* so
 // integrate runs only those; 3: as 2 with divisions through a shared
 // correctly rounded reciprocal; 4: density stores per-bucket 32-bit masks
 // of the pairs integrate uses (bucket-major, coalesced) and integrate expands
-// them (reciprocal divisions). block: threads per block of integrate
+// them (reciprocal divisions); 5: cell-cooperative (a warp's particles of one
+// cell share a candidate list in shared memory; density stores chunk-major
+// masks over that list, 27 words per particle at most, and integrate
+// computes the listed pairs one per lane). block: threads per block of integrate
 // (64/128/256 for variants 2-3); queue: in-range pairs buffered per thread
 // (variant 1: 8, 16, 24 or 32). pair_list / pair_count / list_cap: the
 // per-particle pair lists of variants 2-3 (device buffers the engine owns).
@@ -177,11 +180,20 @@ cudaError_t launch_features(const float4* spos2, const float4* svel, const uint3
                             const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* order,
                             const uint32_t* masks, float4* force, float* features, bool id_order,
                             cudaStream_t stream);
-// Second half: acceleration = plain + correction[p] (null: none), then the
-// plain step's velocity update, clamp, walls and id-order write.
+// Net correction of each active tank: kCorrectionSumWords unsigned words per
+// tank (x, y, z sums in 2^-24 fixed point, two's complement, and the count),
+// zeroed first. Deterministic: integer sums do not depend on atomic order.
+constexpr uint32_t kCorrectionSumWords = 4;
+cudaError_t launch_correction_sums(const float4* correction, const TankConst* tanks, const uint16_t* stank, uint32_t n,
+                                   uint32_t tank_count, unsigned long long* sums, cudaStream_t stream);
+// Second half: acceleration = plain + correction[p] (null: none), minus the
+// tank's mean correction along the axes in `free_axes` (bit a: axis a) when
+// `sums` (launch_correction_sums) is given, then the plain step's velocity
+// update, clamp, walls and id-order write.
 cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,
                                   const TankConst* tanks, const uint16_t* stank, uint32_t n, const float4* force,
-                                  const float4* correction, float4* pos, float4* vel, cudaStream_t stream);
+                                  const float4* correction, const unsigned long long* sums, uint32_t free_axes,
+                                  float4* pos, float4* vel, cudaStream_t stream);
 // Counts x / y (over `count` generated pairs) where division through a
 // correctly rounded reciprocal differs from IEEE division. mode 0: every
 // divisor mantissa; mode 1: random signs, mantissas, exponents.

@@ -70,9 +70,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
     return done != 0;
 }
 
-// Bounded wait: gives up after ~2^22 polls instead of hanging.
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
-    for (uint32_t i = 0; i < (1u << 22); ++i) {
+// Bounded wait: gives up after `polls` tries (each try_wait may itself
+// suspend the thread for a short, hardware-chosen time) instead of hanging.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t polls) {
+    for (uint32_t i = 0; i < polls; ++i) {
         if (mbar_try_wait(mbar, parity)) {
             return true;
         }
@@ -99,9 +100,20 @@ __device__ __forceinline__ void tmem_load16(uint32_t taddr, float* v) {
     }
 }
 
-// Derivative of GELU, erf form (Hendrycks & Gimpel 2016): Phi(z) + z phi(z).
+// GELU(z) = z Phi(z) = 0.5 z (1 + erf(z / sqrt(2))) (Hendrycks & Gimpel 2016),
+// with erf(z / sqrt(2)) taken as tanh(a z + b z^3), a = sqrt(2 / pi),
+// b = 0.044715 a: the approximation that gives the paper its tanh form. Over
+// [-6, 6] it is within 3.6e-4 of the exact erf (4.7e-4 in GELU), below the
+// BF16 rounding (relative step 2^-8) that the activations get next.
+constexpr float kGeluA = 0.7978845608028654f;   // sqrt(2 / pi)
+constexpr float kGeluB = 0.0356774081363001f;   // 0.044715 sqrt(2 / pi)
+
+// Derivative of that GELU (backward, FP32 with the accurate tanhf):
+// 0.5 (1 + t) + 0.5 z (1 - t^2) (a + 3 b z^2), t = tanh(a z + b z^3).
 __device__ __forceinline__ float gelu_grad(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float z2 = z * z;
+    const float t = tanhf(z * fmaf(kGeluB, z2, kGeluA));
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * fmaf(3.0f * kGeluB, z2, kGeluA);
 }
 
 // Byte offset of (row, 8-element chunk) in a K-major no-swizzle tile whose
@@ -142,68 +154,34 @@ __device__ __forceinline__ void store_chunk(uint8_t* base, uint32_t offset, cons
     *reinterpret_cast<uint4*>(base + offset) = q;
 }
 
-// Abramowitz & Stegun 7.1.28 (Handbook of Mathematical Functions, 1964, after
-// Hastings): for x >= 0, erf(x) = 1 - r with r = (1 + a1 x + ... + a6 x^6)^-16
-// and |error| <= 3e-7. One approximate reciprocal (an exact 1 for x past ~13,
-// where the 16th power overflows to infinity) and no exponential, so the
-// epilogue issues one special-function op per activation. Evaluated in FP32 the
-// error against erff stays under 2e-6 (the 16th power scales the rounding of
-// the polynomial); the activations are rounded to BF16 (relative step 2^-8)
-// right after. Checked by sph_mlp_selftest_erf.
-constexpr float kErfA1 = 7.05230784e-2f, kErfA2 = 4.22820123e-2f, kErfA3 = 9.2705272e-3f, kErfA4 = 1.520143e-4f,
-                kErfA5 = 2.765672e-4f, kErfA6 = 4.30638e-5f;
-
-__device__ __forceinline__ float erfc_power(float ax) {
-    float s = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(kErfA6, ax, kErfA5), ax, kErfA4), ax, kErfA3), ax, kErfA2), ax, kErfA1),
-                   ax, 1.0f);
-    s = s * s;
-    s = s * s;
-    s = s * s;
-    s = s * s;
+// The forward pass's tanh: the hardware's approximate tanh (one
+// special-function op; maximum relative error about 2^-11).
+__device__ __forceinline__ float tanh_approx(float x) {
     float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+    asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 
-__device__ __forceinline__ float erf_as(float x) { return copysignf(1.0f - erfc_power(fabsf(x)), x); }
+// erf(x) as the forward pass evaluates it: tanh(a u + b u^3), u = sqrt(2) x.
+__device__ __forceinline__ float erf_forward(float x) {
+    const float u = x * 1.4142135623730951f;
+    return tanh_approx(u * fmaf(kGeluB, u * u, kGeluA));
+}
 
-// GELU of the forward pass, erf form (Hendrycks & Gimpel 2016): with r =
-// erfc_power(|z| / sqrt(2)), 1 + erf(z / sqrt(2)) is 2 - r for z >= 0 and r
-// for z < 0, so with m = (0.5 z) r, GELU(z) = z - m for z >= 0 and m below
-// (the negative side keeps its relative accuracy: no 1 - (1 - r)
-// cancellation).
-//
-// Two activations go at once on the packed FP32 pipe (sph_f32x2.cuh): each
-// lane's value is that of the scalar form while the Horner steps, squarings
-// and scalings take half the issue slots.
-
-// z = v + bias and GELU(z) for two columns; z is returned for the training
-// saves.
+// z = v + bias and GELU(z) = 0.5 z + 0.5 z tanh(z (a + b z^2)) for two
+// columns at a time on the packed FP32 pipe (sph_f32x2.cuh); z is returned for
+// the training saves. Four issue slots and one special-function op per
+// activation.
 __device__ __forceinline__ void bias_gelu2(float v0, float v1, float b0, float b1, float& z0, float& z1, float& g0,
                                            float& g1) {
-    unpack2(add2(pack2(v0, v1), pack2(b0, b1)), z0, z1);
-    const f32x2 ax = pack2(fabsf(z0) * 0.70710678118654752f, fabsf(z1) * 0.70710678118654752f);
-    f32x2 s = fma2(pack2(kErfA6, kErfA6), ax, pack2(kErfA5, kErfA5));
-    s = fma2(s, ax, pack2(kErfA4, kErfA4));
-    s = fma2(s, ax, pack2(kErfA3, kErfA3));
-    s = fma2(s, ax, pack2(kErfA2, kErfA2));
-    s = fma2(s, ax, pack2(kErfA1, kErfA1));
-    s = fma2(s, ax, pack2(1.0f, 1.0f));
-    s = mul2(s, s);
-    s = mul2(s, s);
-    s = mul2(s, s);
-    s = mul2(s, s);
-    float s0, s1, r0, r1;
-    unpack2(s, s0, s1);
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(s0));
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(s1));
-    const f32x2 zz = pack2(z0, z1);
-    float m0, m1;
-    unpack2(mul2(mul2(pack2(0.5f, 0.5f), zz), pack2(r0, r1)), m0, m1);
-    float d0, d1;
-    unpack2(add2(zz, pack2(-m0, -m1)), d0, d1);
-    g0 = z0 >= 0.0f ? d0 : m0;
-    g1 = z1 >= 0.0f ? d1 : m1;
+    const f32x2 z = add2(pack2(v0, v1), pack2(b0, b1));
+    const f32x2 inner = fma2(mul2(z, z), pack2(kGeluB, kGeluB), pack2(kGeluA, kGeluA));
+    float t0, t1;
+    unpack2(mul2(z, inner), t0, t1);
+    const f32x2 th = pack2(tanh_approx(t0), tanh_approx(t1));
+    const f32x2 hz = mul2(pack2(0.5f, 0.5f), z);
+    unpack2(fma2(hz, th, hz), g0, g1);
+    unpack2(z, z0, z1);
 }
 
 constexpr uint32_t kForwardThreads = 512;
@@ -220,7 +198,8 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
                                                                          const float* __restrict__ features,
                                                                          uint32_t n, float* __restrict__ out,
                                                                          ForwardSaves saves,
-                                                                         unsigned int* __restrict__ error_flag) {
+                                                                         unsigned int* __restrict__ error_flag,
+                                                                         uint32_t wait_polls) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmemBar);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kSmemBar + 8);
@@ -355,7 +334,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
             }
             mma_commit(mbar);
         }
-        bool ok = mbar_wait(mbar, parity);
+        bool ok = mbar_wait(mbar, parity, wait_polls);
         if (!__syncthreads_and(ok)) {
             failed = true;
             break;
@@ -408,7 +387,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
             }
             mma_commit(mbar);
         }
-        ok = mbar_wait(mbar, parity);
+        ok = mbar_wait(mbar, parity, wait_polls);
         if (!__syncthreads_and(ok)) {
             failed = true;
             break;
@@ -461,7 +440,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
             }
             mma_commit(mbar);
         }
-        ok = mbar_wait(mbar, parity);
+        ok = mbar_wait(mbar, parity, wait_polls);
         if (!__syncthreads_and(ok)) {
             failed = true;
             break;
@@ -492,7 +471,7 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
             atomicOr(error_flag, 1u);
         }
         // Let an MMA still in flight finish (bounded) before the columns go.
-        mbar_wait(mbar, parity);
+        mbar_wait(mbar, parity, wait_polls);
         tc_fence_before();
         __syncthreads();
     }
@@ -502,15 +481,38 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     }
 }
 
-// max |erf_as(x) - erff(x)| over `count` points spread on [-6, 6] (as float
-// bits in *out).
+// max |erf_forward(x) - erff(x)| over `count` points spread on [-6, 6] (as
+// float bits in *out).
 __global__ void erf_selftest_kernel(uint32_t count, unsigned int* out) {
     float worst = 0.0f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         float x = -6.0f + 12.0f * (static_cast<float>(i) / static_cast<float>(count));
-        worst = fmaxf(worst, fabsf(erf_as(x) - erff(x)));
+        worst = fmaxf(worst, fabsf(erf_forward(x) - erff(x)));
     }
     atomicMax(out, __float_as_uint(worst));
+}
+
+// The bounded wait on its own: one CTA waits on an mbarrier of one expected
+// arrival, which thread 0 makes only when `arrive` is set, with a limit of
+// `polls` tries, as the forward pass waits for its MMAs. No tensor-core work
+// and no tensor memory are involved, so a wait that gives up leaves nothing
+// in flight. A wait that gave up sets the error flag.
+__global__ void wait_selftest_kernel(uint32_t polls, int arrive, unsigned int* error_flag) {
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (arrive != 0 && threadIdx.x == 0) {
+        uint64_t state;
+        asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(smem_u32(&mbar)) : "memory");
+        (void)state;
+    }
+    const bool ok = mbar_wait(&mbar, 0, polls);
+    if (!__syncthreads_and(ok) && threadIdx.x == 0) {
+        atomicOr(error_flag, 1u);
+    }
 }
 
 // ---- backward on the CUDA cores (FP32) ---------------------------------------
@@ -714,12 +716,16 @@ cudaError_t launch_forward(const ModelView& model, const float* features, uint32
     ForwardSaves none{};
     if (saves != nullptr) {
         mlp_forward_kernel<true><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel, *saves,
-                                                                                error_flag);
+                                                                                error_flag, kWaitPolls);
     } else {
         mlp_forward_kernel<false><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel, none,
-                                                                                 error_flag);
+                                                                                 error_flag, kWaitPolls);
     }
     return cudaGetLastError();
+}
+
+void launch_wait_selftest(uint32_t polls, int arrive, unsigned int* error_flag, cudaStream_t stream) {
+    wait_selftest_kernel<<<1, 128, 0, stream>>>(polls, arrive, error_flag);
 }
 
 void launch_erf_selftest(uint32_t count, unsigned int* out, cudaStream_t stream) {
@@ -871,6 +877,7 @@ struct sph_mlp {
     float beta1 = 0.9F;
     float beta2 = 0.999F;
     float epsilon = 1e-8F;
+    uint32_t free_axes = 0;
     std::string last_error;
 };
 
@@ -907,6 +914,7 @@ sph::mlp::ModelView view(const sph_mlp* m) {
     v.in_mean = m->norm;
     v.in_inv_std = m->norm + kIn;
     v.out_scale = m->norm + 2 * kIn;
+    v.free_axes = m->free_axes;
     return v;
 }
 
@@ -1190,6 +1198,14 @@ int sph_mlp_set_adam(sph_mlp* m, float beta1, float beta2, float epsilon) {
     return SPH_OK;
 }
 
+int sph_mlp_set_net_force_free(sph_mlp* m, uint32_t axes) {
+    if (m == nullptr || axes > 7u) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    m->free_axes = axes;
+    return SPH_OK;
+}
+
 int sph_mlp_train_step(sph_mlp* m, const void* features, const void* targets, uint32_t count, float learning_rate,
                        float* loss) {
     if (m == nullptr || features == nullptr || targets == nullptr || count == 0 || !(learning_rate > 0.0F)) {
@@ -1220,6 +1236,20 @@ int sph_mlp_apply_gradients(sph_mlp* m, const float* grads, float learning_rate)
                                       m->epsilon, m->w1, m->w2, m->w3, m->stream));
     MLP_CUDA(m, cudaStreamSynchronize(m->stream));
     return check_error_flag(m);
+}
+
+int sph_mlp_selftest_wait(sph_mlp* m, uint32_t polls, int arrive) {
+    if (m == nullptr || polls == 0) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    MLP_CUDA(m, cudaSetDevice(m->device));
+    MLP_CUDA(m, cudaMemsetAsync(m->error, 0, sizeof(unsigned int), m->stream));
+    sph::mlp::launch_wait_selftest(polls, arrive, m->error, m->stream);
+    MLP_CUDA(m, cudaGetLastError());
+    const int status = check_error_flag(m);
+    MLP_CUDA(m, cudaMemsetAsync(m->error, 0, sizeof(unsigned int), m->stream));
+    MLP_CUDA(m, cudaStreamSynchronize(m->stream));
+    return status;
 }
 
 int sph_mlp_selftest_erf(sph_mlp* m, uint32_t count, float* max_abs_error) {

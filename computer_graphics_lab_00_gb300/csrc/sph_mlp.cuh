@@ -40,6 +40,7 @@ struct ModelView {
     const float* in_mean;     // [32] feature normalisation
     const float* in_inv_std;  // [32]
     const float* out_scale;   // [3]  output = network * scale
+    uint32_t free_axes;       // bit a: each tank's mean correction along axis a is removed
 };
 
 // Activations kept for backward (may be null for inference).
@@ -52,8 +53,15 @@ struct ForwardSaves {
     float* y;             // [n][4]   network output before scaling
 };
 
+// Tries of a bounded mbarrier wait before the forward pass gives up on its
+// MMAs (sets *error_flag, drains, frees its tensor memory and returns).
+constexpr uint32_t kWaitPolls = 1u << 22;
+
 cudaError_t launch_forward(const ModelView& model, const float* features, uint32_t n, float* out_accel,
                            const ForwardSaves* saves, unsigned int* error_flag, cudaStream_t stream);
+// One CTA waits on an mbarrier (arrived at only when `arrive`) with at most
+// `polls` tries; sets *error_flag when the wait gives up.
+void launch_wait_selftest(uint32_t polls, int arrive, unsigned int* error_flag, cudaStream_t stream);
 
 // Backward of the mean squared error on normalised targets, FP32.
 // d_params receives the gradient of the FP32 parameter vector; loss (device,
@@ -75,7 +83,7 @@ cudaError_t launch_quantise(const float* params, __nv_bfloat16* w1, __nv_bfloat1
 // Sets the forward kernel's shared-memory limit; call once per device before
 // any stream capture that contains a forward launch.
 cudaError_t prepare_forward();
-// max |erf_as - erff| over [-6, 6] as float bits in *out (pre-zeroed).
+// max |erf of the forward pass - erff| over [-6, 6] as float bits in *out (pre-zeroed).
 void launch_erf_selftest(uint32_t count, unsigned int* out, cudaStream_t stream);
 
 }  // namespace mlp

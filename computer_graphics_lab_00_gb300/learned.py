@@ -48,6 +48,8 @@ def _declare(lib):
         "sph_mlp_stream": (ctypes.c_int, [ctypes.c_void_p, P(ctypes.c_void_p)]),
         "sph_mlp_selftest_erf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, f32p]),
         "sph_mlp_apply_gradients": (ctypes.c_int, [ctypes.c_void_p, f32p, ctypes.c_float]),
+        "sph_mlp_set_net_force_free": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
+        "sph_mlp_selftest_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int]),
     }
     for name, (restype, argtypes) in sigs.items():
         fn = getattr(lib, name)
@@ -67,6 +69,7 @@ class MlpGpu:
         self._lib = load()
         _declare(self._lib)
         self._h = ctypes.c_void_p()
+        self.free_axes = 0
         self._check(self._lib.sph_mlp_create(device, seed, ctypes.byref(self._h)), "sph_mlp_create")
 
     def close(self):
@@ -142,6 +145,12 @@ class MlpGpu:
                                                  count, lr, _fp(loss)), "sph_mlp_train_step")
         return float(loss[0])
 
+    def set_net_force_free(self, axes: int) -> None:
+        """Learned steps take each tank's mean correction off along the axes
+        in the mask (bit 0 x, 1 y, 2 z; 0 keeps it)."""
+        self._check(self._lib.sph_mlp_set_net_force_free(self._h, axes), "sph_mlp_set_net_force_free")
+        self.free_axes = int(axes)
+
     def apply_gradients(self, grads, lr: float = 1e-3) -> None:
         """Adam with an externally reduced gradient (data-parallel training)."""
         g = np.ascontiguousarray(grads, dtype=np.float32)
@@ -153,6 +162,10 @@ class MlpGpu:
         out = np.zeros(1, np.float32)
         self._check(self._lib.sph_mlp_selftest_erf(self._h, count, _fp(out)), "sph_mlp_selftest_erf")
         return float(out[0])
+
+    def selftest_wait(self, polls: int, arrive: bool) -> int:
+        """Status of a bounded mbarrier wait (SPH_OK or SPH_ERR_TIMEOUT)."""
+        return int(self._lib.sph_mlp_selftest_wait(self._h, polls, 1 if arrive else 0))
 
     # -- checkpoints: FP32 weights + normalisation, JSON ----------------------------
     def save(self, path) -> None:

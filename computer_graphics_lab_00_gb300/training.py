@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import time
 from dataclasses import dataclass
+from pathlib import Path
 
 import numpy as np
 
@@ -36,6 +37,12 @@ from .batch import BatchSolverGpu
 FINE_DT = 1.0 / 1200.0
 COARSE_DT = 1.0 / 240.0
 RATIO = 5
+# Seed offsets of the tank sets beside the training set: validation tanks
+# choose the output gain and mean-free axes, held-out tanks only evaluate.
+VALIDATION_SEED = 500
+HELD_OUT_SEED = 1000
+# The committed network (python -m computer_graphics_lab_00_gb300.training).
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "sph_correction.npz"
 
 
 def learned_tanks(tanks: int = 64, particles: int = 32768, seed: int = 0, spacing: float = 0.02) -> W.TankSet:
@@ -73,6 +80,49 @@ def learned_tanks(tanks: int = 64, particles: int = 32768, seed: int = 0, spacin
                      "even tanks dam break, odd tanks drop; extents U[0.8, 1.4] m")
 
 
+@dataclass
+class TankMix:
+    """Several tank sets stepped as one batch (tanks in set order)."""
+
+    parts: list
+
+    @property
+    def params(self) -> list:
+        return [p for part in self.parts for p in part.params]
+
+    @property
+    def counts(self) -> list:
+        return [c for part in self.parts for c in part.counts]
+
+    @property
+    def total_particles(self) -> int:
+        return int(sum(part.total_particles for part in self.parts))
+
+    @property
+    def name(self) -> str:
+        return "+".join(part.name for part in self.parts)
+
+    def initial_state(self, tank: int):
+        for part in self.parts:
+            if tank < len(part.counts):
+                return part.initial_state(tank)
+            tank -= len(part.counts)
+        raise IndexError("tank out of range")
+
+
+def training_tanks(seed: int = 0) -> TankMix:
+    """The training set: 64 tanks of 32,768 particles (config 4's tanks) and
+    64 of 8,192 (the tank size of the batched learned form), dam breaks and
+    drops."""
+    return TankMix([learned_tanks(64, 32768, seed=seed), learned_tanks(64, 8192, seed=seed + 1)])
+
+
+def validation_tanks(seed: int = 0) -> list:
+    """Validation sets that choose the output gain and the mean-free axes."""
+    return [learned_tanks(16, 32768, seed=seed + VALIDATION_SEED),
+            learned_tanks(32, 8192, seed=seed + VALIDATION_SEED + 1)]
+
+
 def load_tanks(tankset: W.TankSet, device: int = 0) -> BatchSolverGpu:
     solver = BatchSolverGpu(tankset.params, tankset.counts, device=device)
     for t in range(len(tankset.counts)):
@@ -80,8 +130,35 @@ def load_tanks(tankset: W.TankSet, device: int = 0) -> BatchSolverGpu:
     return solver
 
 
-def generate(tankset: W.TankSet, snapshots: int = 40, duration: float = 2.0, device: int = 0):
-    """(features [S*N, 32], targets [S*N, 3]) on the GPU from fine trajectories."""
+def tank_mean_free(values, counts):
+    """values [N, 3] (id order, tanks contiguous) minus each tank's mean row."""
+    import torch
+
+    sizes = [int(c) for c in counts]
+    owner = torch.repeat_interleave(torch.arange(len(sizes), device=values.device),
+                                    torch.tensor(sizes, device=values.device))
+    sums = torch.zeros((len(sizes), values.shape[1]), dtype=torch.float64, device=values.device)
+    sums.index_add_(0, owner, values.double())
+    means = sums / torch.tensor(sizes, dtype=torch.float64, device=values.device)[:, None]
+    return (values.double() - means[owner]).float()
+
+
+def generate(tankset, snapshots: int = 40, duration: float = 2.0, device: int = 0, target_mix: float = 1.0,
+             mean_free: bool = False, policy=None):
+    """(features [S*N, 32], targets [S*N, 3]) on the GPU from fine trajectories.
+
+    At each snapshot state s(t) the target is the correction that makes one
+    plain coarse step from s(t) land on five fine steps: target_mix times the
+    velocity form (v_fine - v_coarse) / D plus (1 - target_mix) times the
+    position form (x_fine - x_coarse) / D^2 (a correction a moves the coarse
+    position by a D^2). With mean_free each tank's mean target is removed.
+
+    With a `policy` model the snapshot states come from a learned rollout
+    (coarse steps corrected by that model) instead of the fine trajectory,
+    with targets from the same fine and coarse steps: the states the learned
+    solver actually visits, so that a model trained on them learns to act on
+    its own errors.
+    """
     import torch
 
     solver = load_tanks(tankset, device)
@@ -89,21 +166,31 @@ def generate(tankset: W.TankSet, snapshots: int = 40, duration: float = 2.0, dev
     dev = torch.device("cuda", device)
     feats = torch.empty((snapshots, n, 32), dtype=torch.float32, device=dev)
     targs = torch.empty((snapshots, n, 3), dtype=torch.float32, device=dev)
+    pc = torch.empty((n, 4), dtype=torch.float32, device=dev)
     vc = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    pf = torch.empty((n, 4), dtype=torch.float32, device=dev)
     vf = torch.empty((n, 4), dtype=torch.float32, device=dev)
     fine_total = int(round(duration / FINE_DT))
     interval = max(RATIO + 1, fine_total // snapshots)
     for k in range(snapshots):
-        solver.run(FINE_DT, interval if k == 0 else interval - RATIO)
+        if policy is None:
+            solver.run(FINE_DT, interval if k == 0 else interval - RATIO)
+        else:
+            solver.run_learned(COARSE_DT, max(1, interval // RATIO), policy)
         solver.snapshot(0, save=True)
         solver.learned_features(COARSE_DT, feats[k].data_ptr())
         solver.run_learned(COARSE_DT, 1, None)
-        solver.copy_state(None, vc.data_ptr())
+        solver.copy_state(pc.data_ptr(), vc.data_ptr())
         solver.snapshot(0, save=False)
         solver.run(FINE_DT, RATIO)
-        solver.copy_state(None, vf.data_ptr())
+        solver.copy_state(pf.data_ptr(), vf.data_ptr())
+        if policy is not None:
+            solver.snapshot(0, save=False)  # the rollout goes on from s(t)
         solver.synchronize()
-        targs[k] = (vf[:, :3] - vc[:, :3]) / COARSE_DT
+        target = target_mix * (vf[:, :3] - vc[:, :3]) / COARSE_DT
+        if target_mix < 1.0:
+            target = target + (1.0 - target_mix) * (pf[:, :3] - pc[:, :3]) / (COARSE_DT * COARSE_DT)
+        targs[k] = tank_mean_free(target, tankset.counts) if mean_free else target
     solver.close()
     return feats.reshape(-1, 32), targs.reshape(-1, 3)
 
@@ -158,90 +245,219 @@ class Comparison:
                 "fine_mean_compression": float(self.fine_compression.mean())}
 
 
-def compare_with_fine(tankset: W.TankSet, mlp, duration: float = 2.0, every: float = 0.1, device: int = 0) -> dict:
-    """Learned coarse run, plain coarse run and plain fine run from the same
-    start; density error and centre-of-mass drift of the coarse runs against
-    the fine run at matching times."""
+def reference_runs(tankset, duration: float = 2.0, every: float = 0.1, device: int = 0) -> dict:
+    """Compression and centre of mass of the plain fine run (the judge) and
+    of the plain coarse run (D = 1/240 s, no network) every `every` seconds."""
     coarse_per_check = int(round(every / COARSE_DT))
     checks = int(round(duration / every))
     fine = load_tanks(tankset, device)
-    learned = load_tanks(tankset, device)
     plain = load_tanks(tankset, device)
-    rec = {"fine": [], "learned": [], "plain": []}
+    rec = {"fine": [], "plain": []}
     for _ in range(checks):
         fine.run(FINE_DT, coarse_per_check * RATIO)
-        learned.run_learned(COARSE_DT, coarse_per_check, mlp)
         plain.run_learned(COARSE_DT, coarse_per_check, None)
-        for name, solver in (("fine", fine), ("learned", learned), ("plain", plain)):
-            rec[name].append(_compression_and_com(solver.stats()))
+        rec["fine"].append(_compression_and_com(fine.stats()))
+        rec["plain"].append(_compression_and_com(plain.stats()))
+    fine.close()
+    plain.close()
+    return {"every": every, "checks": checks, **rec}
+
+
+def _summary(run, fine, every):
+    c_f = np.array([c for c, _ in fine])
+    com_f = np.array([com for _, com in fine])
+    c = np.array([c for c, _ in run])
+    com = np.array([x for _, x in run])
+    nonfinite = ~np.isfinite(c) | ~np.isfinite(com).all(-1)
+    err = np.where(nonfinite, np.inf, np.abs(c - c_f))
+    drift = np.where(nonfinite, np.inf, np.linalg.norm(com - com_f, axis=-1))
+    return Comparison([every * (k + 1) for k in range(len(run))], err, drift, c_f).summary()
+
+
+def compare_with_fine(tankset, mlp, duration: float = 2.0, every: float = 0.1, device: int = 0,
+                      reference: dict | None = None) -> dict:
+    """Learned coarse run, plain coarse run and plain fine run from the same
+    start; density error and centre-of-mass drift of the coarse runs against
+    the fine run at matching times. `reference` (from reference_runs) skips
+    the two plain runs."""
+    if reference is None:
+        reference = reference_runs(tankset, duration, every, device)
+    learned = load_tanks(tankset, device)
+    run = []
+    for _ in range(reference["checks"]):
+        learned.run_learned(COARSE_DT, int(round(reference["every"] / COARSE_DT)), mlp)
+        run.append(_compression_and_com(learned.stats()))
     learned.learned_check()
-    out = {}
-    c_f = np.array([c for c, _ in rec["fine"]])
-    com_f = np.array([com for _, com in rec["fine"]])
-    for name in ("learned", "plain"):
-        c = np.array([c for c, _ in rec[name]])
-        com = np.array([x for _, x in rec[name]])
-        nonfinite = ~np.isfinite(c) | ~np.isfinite(com).all(-1)
-        err = np.where(nonfinite, np.inf, np.abs(c - c_f))
-        drift = np.where(nonfinite, np.inf, np.linalg.norm(com - com_f, axis=-1))
-        out[name] = Comparison([every * (k + 1) for k in range(checks)], err, drift, c_f).summary()
-    for solver in (fine, learned, plain):
-        solver.close()
-    return out
+    learned.close()
+    return {"learned": _summary(run, reference["fine"], reference["every"]),
+            "plain": _summary(reference["plain"], reference["fine"], reference["every"])}
 
 
-def run_with_fallback(tankset: W.TankSet, mlp, coarse_steps: int = 600, check_every: int = 10,
-                      threshold: float = 0.01, hold: int = 20, device: int = 0) -> dict:
-    """Learned coarse steps with the plain fine solver as judge and fallback
-    (see the module docstring); returns timings and error statistics."""
+GAINS = (0.03, 0.05, 0.075, 0.1, 0.15, 0.2)
+FREE_AXES = (0, 5, 7)  # none; x and z; x, y and z (MlpGpu.set_net_force_free)
+
+
+def choose_output(mlp, validations: list, gains=GAINS, axes_options=FREE_AXES) -> tuple[dict, list]:
+    """The output gain and the mean-free axes of the correction, chosen on
+    validation tanks (`validations`: (tank set, reference_runs) pairs).
+
+    The network is the least-squares fit of one coarse interval, but part of
+    its output is particle-scale noise, and its estimate of a tank's net
+    correction is noisy too; a rollout integrates both, twice, into
+    centre-of-mass drift. Scaling the correction down trades the fitted gain
+    against that noise, and taking each tank's mean off along some axes
+    removes the net part. Picks the combination whose worst ratio over the
+    validation sets of (density error / plain coarse's, centre-of-mass
+    drift / plain coarse's) is smallest, and leaves it set on the model (its
+    output scale and net-force-free axes)."""
+    mean, std, scale = mlp.normalisation()
+    rows = []
+    for axes in axes_options:
+        mlp.set_net_force_free(axes)
+        for g in gains:
+            mlp.set_normalisation(mean, std, scale * np.float32(g))
+            ratios = []
+            for tankset, reference in validations:
+                cmp = compare_with_fine(tankset, mlp, reference=reference)
+                lrn, pln = cmp["learned"], cmp["plain"]
+                ratios.append((lrn["mean_density_error"] / pln["mean_density_error"],
+                               lrn["mean_com_drift_m"] / pln["mean_com_drift_m"]))
+            rows.append({"gain": g, "axes": axes, "ratios": ratios, "score": max(max(r) for r in ratios)})
+    best = min(rows, key=lambda r: r["score"])
+    mlp.set_net_force_free(best["axes"])
+    mlp.set_normalisation(mean, std, scale * np.float32(best["gain"]))
+    return best, rows
+
+
+def fit(tankset, validations: list, snapshots: int = 40, steps: int = 4000, batch: int = 65536,
+        lr: float = 1e-3, seed: int = 0, onpolicy_rounds: int = 1, target_mix: float = 1.0) -> tuple:
+    """The training recipe: fine-trajectory snapshots, Adam on the project's
+    kernels, output gain and mean-free axes chosen on the validation sets;
+    then, per on-policy round, snapshots of the learned rollout (with their
+    fine-solver targets) join the data, a fresh model is trained on all of
+    it and the output is chosen again. Returns (model, report)."""
+    import torch
+
+    from .learned import MlpGpu
+
+    t0 = time.perf_counter()
+    feats, targs = generate(tankset, snapshots=snapshots, target_mix=target_mix)
+    refs = [(v, reference_runs(v)) for v in validations]
+    report = {"data_seconds": [time.perf_counter() - t0], "train": [], "choices": []}
+    mlp = MlpGpu(seed=seed)
+    report["train"].append(train(mlp, feats, targs, steps=steps, batch=batch, lr=lr, seed=seed))
+    best, rows = choose_output(mlp, refs)
+    report["choices"].append(rows)
+    for r in range(onpolicy_rounds):
+        t0 = time.perf_counter()
+        f2, t2 = generate(tankset, snapshots=snapshots, target_mix=target_mix, policy=mlp)
+        report["data_seconds"].append(time.perf_counter() - t0)
+        feats = torch.cat([feats, f2])
+        targs = torch.cat([targs, t2])
+        del f2, t2
+        mlp.close()
+        mlp = MlpGpu(seed=seed + r + 1)
+        report["train"].append(train(mlp, feats, targs, steps=steps, batch=batch, lr=lr, seed=seed + r + 1))
+        best, rows = choose_output(mlp, refs)
+        report["choices"].append(rows)
+    report["gain"] = best["gain"]
+    report["free_axes"] = best["axes"]
+    report["samples"] = int(feats.shape[0])
+    del feats, targs
+    return mlp, report
+
+
+def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 5, sample: int = 8,
+                      threshold: float = 0.01, hold: int = 20, record_every: int = 60, device: int = 0) -> dict:
+    """Learned coarse steps with the plain fine solver as judge and fallback.
+
+    Every `check_every` coarse steps a rotating 1/`sample` share of the
+    tanks on learned steps is judged: the fine solver re-runs the interval
+    (five fine steps from the same start) for those tanks only, and a tank
+    whose mean compression differs from the fine result by more than
+    `threshold` keeps the fine result and stays on fine steps for `hold`
+    coarse intervals. Between its judgements a tank also falls back when its
+    compression has moved more than 2 `threshold` away from the fine
+    compression of its last judgement (drift the local check cannot see).
+    Tanks on fine steps take five fine steps per interval. Per-tank
+    compression and centre of mass are recorded every `record_every` coarse
+    steps (outside the timed region) for comparison with run_plain_fine."""
     import torch
 
     solver = load_tanks(tankset, device)
     tanks = solver.tanks
     hold_left = np.zeros(tanks, dtype=np.int64)
+    last_fine = np.full(tanks, np.nan)
     fallback_intervals = 0
     checks = 0
+    judged = 0
     rejected = 0
+    drift_rejected = 0
     errors = []
+    records = []
+    wall = 0.0
+    turn = 0
+    all_on = np.ones(tanks, np.uint8)
     torch.cuda.synchronize()
     start = time.perf_counter()
     for c in range(coarse_steps):
+        if record_every and c % record_every == 0:
+            # Records sit outside the timed region.
+            solver.synchronize()
+            wall += time.perf_counter() - start
+            solver.set_active(all_on)
+            records.append(_compression_and_com(solver.stats()))
+            solver.synchronize()
+            start = time.perf_counter()
         on_fine = hold_left > 0
-        learned_mask = (~on_fine).astype(np.uint8)
-        check = (c % check_every == 0) and learned_mask.any()
-        if check:
+        learned = ~on_fine
+        if c % check_every == 0 and learned.any():
             checks += 1
+            # The judged share: tanks t with t % sample == turn, rotating.
+            share = learned & (np.arange(tanks) % sample == turn)
+            turn = (turn + 1) % sample
             solver.snapshot(0, save=True)
-            solver.set_active(learned_mask)
+            solver.set_active(learned.astype(np.uint8))
             solver.run_learned(COARSE_DT, 1, mlp)
             c_learned, _ = _compression_and_com(solver.stats())
-            solver.snapshot(1, save=True)
-            solver.snapshot(0, save=False)
-            solver.set_active(np.ones(tanks, np.uint8))
-            solver.run(FINE_DT, RATIO)
-            c_fine, _ = _compression_and_com(solver.stats())
-            err = np.abs(c_learned - c_fine)
-            bad = (err > threshold) | ~np.isfinite(err)
-            keep_learned = learned_mask.astype(bool) & ~bad
-            errors.extend(err[learned_mask.astype(bool)].tolist())
-            solver.restore_tanks(1, keep_learned.astype(np.uint8))
-            newly = bad & learned_mask.astype(bool)
-            rejected += int(newly.sum())
-            hold_left[newly] = hold
+            # Drift since the last judgement of each unjudged learned tank.
+            drifted = learned & ~share & np.isfinite(last_fine) & (np.abs(c_learned - last_fine) > 2 * threshold)
+            drifted |= learned & ~np.isfinite(c_learned)
+            fine_set = share | on_fine | drifted
+            if fine_set.any():
+                solver.snapshot(1, save=True)
+                solver.restore_tanks(0, (share | drifted).astype(np.uint8))
+                solver.set_active(fine_set.astype(np.uint8))
+                solver.run(FINE_DT, RATIO)
+                c_fine, _ = _compression_and_com(solver.stats())
+                err = np.abs(c_learned - c_fine)
+                bad = share & ((err > threshold) | ~np.isfinite(err))
+                judged += int(share.sum())
+                errors.extend(err[share].tolist())
+                keep_learned = share & ~bad
+                if keep_learned.any():
+                    solver.restore_tanks(1, keep_learned.astype(np.uint8))
+                last_fine[fine_set] = c_fine[fine_set]
+                newly = bad | drifted
+                rejected += int(bad.sum())
+                drift_rejected += int(drifted.sum())
+                hold_left[newly] = hold
             fallback_intervals += int(on_fine.sum())
         else:
-            if learned_mask.any():
-                solver.set_active(learned_mask)
+            if learned.any():
+                solver.set_active(learned.astype(np.uint8))
                 solver.run_learned(COARSE_DT, 1, mlp)
             if on_fine.any():
                 solver.set_active(on_fine.astype(np.uint8))
                 solver.run(FINE_DT, RATIO)
                 fallback_intervals += int(on_fine.sum())
         hold_left = np.maximum(hold_left - 1, 0)
-    solver.set_active(np.ones(tanks, np.uint8))
+    solver.synchronize()
+    wall += time.perf_counter() - start
+    solver.set_active(all_on)
     solver.learned_check()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - start
+    if record_every:
+        records.append(_compression_and_com(solver.stats()))
     final = solver.stats()
     solver.close()
     n = tankset.total_particles
@@ -249,34 +465,64 @@ def run_with_fallback(tankset: W.TankSet, mlp, coarse_steps: int = 600, check_ev
         "coarse_steps": coarse_steps, "wall_s": wall,
         "sim_s_particles_per_s": n * coarse_steps * COARSE_DT / wall,
         "fallback_fraction": fallback_intervals / (coarse_steps * tanks),
-        "checks": checks, "rejected_checks": rejected,
+        "checks": checks, "judged_tank_intervals": judged, "rejected_checks": rejected,
+        "drift_fallbacks": drift_rejected,
         "check_errors_mean": float(np.mean(errors)) if errors else None,
         "final_mean_compression": float(np.mean([s.mean_compression for s in final])),
         "nonfinite_particles": int(sum(s.nonfinite for s in final)),
+        "records": records,
     }
 
 
-def run_plain_fine(tankset: W.TankSet, coarse_steps: int = 600, device: int = 0) -> dict:
-    """The plain batched form at the fine step over the same simulated time."""
+def run_plain_fine(tankset, coarse_steps: int = 600, record_every: int = 60, device: int = 0) -> dict:
+    """The plain batched form at the fine step over the same simulated time,
+    with the same per-tank records as run_with_fallback."""
     import torch
 
     solver = load_tanks(tankset, device)
-    torch.cuda.synchronize()
-    start = time.perf_counter()
-    solver.run(FINE_DT, coarse_steps * RATIO)
-    solver.synchronize()
-    wall = time.perf_counter() - start
+    records = []
+    wall = 0.0
+    step = record_every if record_every else coarse_steps
+    done = 0
+    while done < coarse_steps:
+        if record_every:
+            records.append(_compression_and_com(solver.stats()))
+        k = min(step, coarse_steps - done)
+        solver.synchronize()
+        torch.cuda.synchronize()
+        start = time.perf_counter()
+        solver.run(FINE_DT, k * RATIO)
+        solver.synchronize()
+        wall += time.perf_counter() - start
+        done += k
+    if record_every:
+        records.append(_compression_and_com(solver.stats()))
     final = solver.stats()
     solver.close()
     n = tankset.total_particles
     return {"wall_s": wall, "sim_s_particles_per_s": n * coarse_steps * COARSE_DT / wall,
-            "final_mean_compression": float(np.mean([s.mean_compression for s in final]))}
+            "final_mean_compression": float(np.mean([s.mean_compression for s in final])), "records": records}
+
+
+def fallback_errors(learned: dict, plain: dict) -> dict:
+    """Density error (|mean compression - plain fine's| per tank) and
+    centre-of-mass drift of the learned-with-fallback run at the records."""
+    c_l = np.array([c for c, _ in learned["records"]])
+    c_p = np.array([c for c, _ in plain["records"]])
+    com_l = np.array([x for _, x in learned["records"]])
+    com_p = np.array([x for _, x in plain["records"]])
+    err = np.abs(c_l - c_p)
+    drift = np.linalg.norm(com_l - com_p, axis=-1)
+    return {"mean_density_error": float(err.mean()), "final_density_error": float(err[-1].mean()),
+            "max_tank_density_error": float(err.max()), "mean_com_drift_m": float(drift.mean())}
 
 
 def save_model(mlp, path, info: dict | None = None) -> None:
-    """FP32 parameters and normalisation as a small .npz checkpoint."""
+    """FP32 parameters, normalisation (the output scale includes the chosen
+    gain) and the net-force-free axes as a small .npz checkpoint."""
     mean, std, scale = mlp.normalisation()
     np.savez_compressed(path, params=mlp.params(), feature_mean=mean, feature_std=std, output_scale=scale,
+                        free_axes=np.array([mlp.free_axes], np.uint32),
                         info=np.frombuffer(repr(info or {}).encode(), dtype=np.uint8))
 
 
@@ -284,11 +530,13 @@ def load_model(mlp, path) -> None:
     data = np.load(path)
     mlp.set_params(data["params"])
     mlp.set_normalisation(data["feature_mean"], data["feature_std"], data["output_scale"])
+    mlp.set_net_force_free(int(data["free_axes"][0]) if "free_axes" in data else 0)
 
 
 def main() -> None:
-    """Trains the correction on the 64 x 32,768 dam-break/drop tanks and
-    writes a checkpoint: python -m computer_graphics_lab_00_gb300.training OUT.npz"""
+    """Trains the correction (64 tanks of 32,768 and 64 of 8,192 particles,
+    dam breaks and drops; fit()) and writes a checkpoint:
+    python -m computer_graphics_lab_00_gb300.training OUT.npz"""
     import argparse
     import json
 
@@ -296,14 +544,15 @@ def main() -> None:
 
     ap = argparse.ArgumentParser(description=main.__doc__)
     ap.add_argument("out")
-    ap.add_argument("--tanks", type=int, default=64)
-    ap.add_argument("--particles", type=int, default=32768)
+    ap.add_argument("--particles", type=int, default=32768, help="tank size of the held-out evaluation")
     ap.add_argument("--snapshots", type=int, default=40)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--batch", type=int, default=65536)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--evaluate", action="store_true", help="compare with the fine run on held-out tanks")
+    ap.add_argument("--onpolicy-rounds", type=int, default=1)
+    ap.add_argument("--evaluate", action="store_true",
+                    help="compare with the fine run on 64 held-out tanks over 2 s")
     ap.add_argument("--fallback-run", action="store_true",
                     help="load OUT and run the batched learned form (1,024 x 8,192 tanks, 600 coarse steps, "
                          "per-tank fallback) beside the plain batched form at the fine step")
@@ -318,24 +567,24 @@ def main() -> None:
         learned = run_with_fallback(tankset, mlp, coarse_steps=args.coarse_steps)
         plain = run_plain_fine(tankset, coarse_steps=args.coarse_steps)
         learned["speedup_vs_plain_fine"] = learned["sim_s_particles_per_s"] / plain["sim_s_particles_per_s"]
-        learned["final_compression_vs_plain_fine"] = abs(learned["final_mean_compression"]
-                                                         - plain["final_mean_compression"])
+        learned["vs_plain_fine"] = fallback_errors(learned, plain)
+        learned.pop("records")
+        plain.pop("records")
         print(json.dumps({"tanks": args.fallback_tanks, "particles_per_tank": args.fallback_particles,
                           "learned_with_fallback": learned, "plain_fine": plain}))
         return
-    tankset = learned_tanks(args.tanks, args.particles, seed=args.seed)
-    t0 = time.perf_counter()
-    feats, targs = generate(tankset, snapshots=args.snapshots)
-    t1 = time.perf_counter()
-    mlp = MlpGpu(seed=args.seed)
-    report = train(mlp, feats, targs, steps=args.steps, batch=args.batch, lr=args.lr, seed=args.seed)
-    report["data_seconds"] = t1 - t0
-    del feats, targs
-    save_model(mlp, args.out, {"tanks": args.tanks, "particles": args.particles, "steps": args.steps})
+    tankset = training_tanks(args.seed)
+    mlp, report = fit(tankset, validation_tanks(args.seed), snapshots=args.snapshots, steps=args.steps,
+                      batch=args.batch, lr=args.lr, seed=args.seed, onpolicy_rounds=args.onpolicy_rounds)
+    save_model(mlp, args.out, {"tanks": tankset.name, "steps": args.steps, "onpolicy_rounds": args.onpolicy_rounds,
+                               "gain": report["gain"], "free_axes": report["free_axes"]})
     if args.evaluate:
-        held_out = learned_tanks(8, args.particles, seed=args.seed + 1000)
+        held_out = learned_tanks(64, args.particles, seed=args.seed + HELD_OUT_SEED)
         report["held_out"] = compare_with_fine(held_out, mlp)
-    print(json.dumps({k: v for k, v in report.items() if k not in ("feature_mean", "feature_std")}))
+    for t in report["train"]:
+        for k in ("feature_mean", "feature_std", "output_scale"):
+            t.pop(k, None)
+    print(json.dumps(report))
 
 
 if __name__ == "__main__":

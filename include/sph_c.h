@@ -495,8 +495,16 @@ int sph_mlp_set_net_force_free(sph_mlp* mlp, uint32_t axes);
  * fluid path); the update rule is adamStep (src/gfx/neural_math.cpp:1177-1208). */
 int sph_mlp_apply_gradients(sph_mlp* mlp, const float* grads, float learning_rate);
 /* Diagnostic: largest |erf(x) - erff(x)| of the forward pass's erf
- * (Abramowitz & Stegun 7.1.28) over `count` points on [-6, 6]. */
+ * (tanh(a u + b u^3), u = sqrt(2) x, the approximation behind the tanh form
+ * of GELU, with the hardware tanh) over `count` points on [-6, 6]. */
 int sph_mlp_selftest_erf(sph_mlp* mlp, uint32_t count, float* max_abs_error);
+/* Diagnostic of the bounded device waits: one block waits on an mbarrier
+ * with at most `polls` tries, as the forward pass waits for its tensor-core
+ * work; the barrier is arrived at only when `arrive` is nonzero. Returns
+ * SPH_OK when the wait completed and SPH_ERR_TIMEOUT when it gave up; either
+ * way the context stays usable. No counterpart in the reference (its GPU
+ * failure path is a fatal error, src/gfx/fluid.cpp:95-100). */
+int sph_mlp_selftest_wait(sph_mlp* mlp, uint32_t polls, int arrive);
 
 /* Learned coarse substeps (no counterpart in the reference): the plain SPH
  * force as in sph_step, plus the MLP's acceleration correction, then the

@@ -5,8 +5,10 @@ LINEAR forward/backward (src/gfx/neural_math.cpp:119-132 and its backward),
 the mean squared error, and Adam (neural_math.cpp:1177-1208); the central
 finite-difference gradient check follows tests/gradient_check.h:22-60
 (double precision, step 1e-5, error scaled by the typical gradient size).
-GELU (erf form, Hendrycks & Gimpel 2016) and BF16 rounding (round to nearest
-even of the FP32 value) are new here and specified by this build.
+GELU (Hendrycks & Gimpel 2016, z Phi(z) with erf(z / sqrt 2) taken as
+tanh(a z + b z^3), a = sqrt(2 / pi), b = 0.044715 a) and BF16 rounding (round
+to nearest even of the FP32 value) are new here and specified by this build;
+the GPU evaluates the tanh with the hardware's approximate tanh.
 
 `forward(..., bf16=True)` rounds where the GPU rounds: the normalised input,
 the weights and both hidden activations become BF16 before each product,
@@ -42,12 +44,22 @@ def unpack(params):
             p[W3:B3].reshape(OUT, HIDDEN), p[B3:PARAMS])
 
 
+GELU_A = math.sqrt(2.0 / math.pi)
+GELU_B = 0.044715 * GELU_A
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(z * (GELU_A + GELU_B * z * z)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(z * (GELU_A + GELU_B * z * z))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * (GELU_A + 3.0 * GELU_B * z * z)
+
+
+def gelu_erf(z):
+    """The exact erf form, for comparing the approximation against it."""
+    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
 
 
 def normalise(features, mean, std):

@@ -1,6 +1,7 @@
 """The learned coarse step through the C ABI: with no correction it is the
-plain substep bit for bit; features are finite; the training and
-fallback pipeline runs end to end on a small set."""
+plain substep bit for bit; features are finite; the committed network
+beats the plain coarse step on held-out tanks; the training and fallback
+pipeline runs end to end on a small set."""
 from __future__ import annotations
 
 import numpy as np
@@ -93,3 +94,25 @@ def test_pipeline_end_to_end(native, small, tmp_path):
         fb = T.run_with_fallback(small, mlp, coarse_steps=12, check_every=4)
         assert fb["coarse_steps"] == 12 and fb["checks"] >= 1
         assert 0.0 <= fb["fallback_fraction"] <= 1.0
+
+
+@pytest.mark.parametrize("particles", [32768, 8192])
+def test_trained_correction_beats_the_plain_coarse_step(native, particles):
+    """What the trained network gains over the method without it. On 16
+    held-out tanks (dam breaks and drops of 32,768 particles, config 4's
+    size, or of 8,192, the batched learned form's), from seeds used neither
+    in training nor in choosing the output gain, over 2 s of simulated time:
+    the learned coarse step (D = 1/240 s) has a smaller mean density error
+    AND a smaller centre-of-mass drift against the plain fine run (1/1200 s)
+    than the plain coarse step at the same D (each ratio below 1; the
+    measured ratios are in the design notes)."""
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    held = T.learned_tanks(16, particles, seed=T.HELD_OUT_SEED)
+    with MlpGpu() as mlp:
+        T.load_model(mlp, T.WEIGHTS)
+        cmp = T.compare_with_fine(held, mlp, duration=2.0, every=0.1)
+    learned, plain = cmp["learned"], cmp["plain"]
+    assert np.isfinite(learned["mean_density_error"]) and np.isfinite(learned["mean_com_drift_m"])
+    assert learned["mean_density_error"] < plain["mean_density_error"], cmp
+    assert learned["mean_com_drift_m"] < plain["mean_com_drift_m"], cmp

@@ -44,14 +44,49 @@ def test_forward_matches_oracle(native, torch_cuda, n):
         torch.cuda.synchronize()  # torch's copies and fill finish before the library's stream reads them
         mlp.forward(d_f.data_ptr(), n, d_out.data_ptr())
         got = d_out.cpu().numpy()
-    y, _ = M.forward(params, f, mean, std, scale)
+    y, cache = M.forward(params, f, mean, std, scale)
     want = y * scale
     assert np.all(got[:, 3] == 0.0)
-    # BF16 activations: a one-ulp difference before rounding can move a BF16
-    # value by 2^-8 relative, so compare against the output's own scale.
     err = np.abs(got[:, :3] - want)
-    assert err.max() <= 2e-2 * max(1.0, np.abs(want).max()), err.max()
+    bound = forward_error_bound(cache) * scale
+    assert np.all(err <= bound), (err / bound).max()
     assert np.median(err) <= 2e-3 * max(1.0, np.abs(want).max())
+
+
+def bf16_ulp(v):
+    """The BF16 spacing at |v| (8 significant bits), at least that of 2^-126."""
+    e = np.floor(np.log2(np.maximum(np.abs(v), 2.0 ** -126)))
+    return 2.0 ** (e - 7)
+
+
+def forward_error_bound(cache):
+    """Per-element bound on |GPU - oracle| of the network output (before the
+    output scale). The oracle rounds to BF16 where the GPU does; what may
+    differ is carried through each layer in double:
+      - each FP32 sum of the tensor cores: 2^-22 of the sum of |terms|
+        (32- and 128-term dot products in FP32; K 2^-24 with K <= 128 is
+        2^-17; the bound uses 2^-16);
+      - the GELU: the hardware tanh's relative error (2^-10.5 taken) times
+        0.5 |z| |t|, plus the slope times the error of z;
+      - BF16 rounding: an error of d before rounding gives at most d plus
+        one BF16 ulp of the value after it (a rounding boundary crossed)."""
+    x, z1, h1, z2, h2 = cache["x"], cache["z1"], cache["h1"], cache["z2"], cache["h2"]
+    w1, w2, w3 = np.abs(cache["w1"]), np.abs(cache["w2"]), np.abs(cache["w3"])
+    acc = 2.0 ** -16
+    tanh_rel = 2.0 ** -10.5
+
+    def gelu_error(z, dz):
+        t = np.tanh(z * (M.GELU_A + M.GELU_B * z * z))
+        slope = np.abs(M.gelu_grad(z))
+        return slope * dz + 0.5 * np.abs(z) * (tanh_rel * np.abs(t) + 1e-6) + 1e-6 * np.abs(M.gelu(z))
+
+    dz1 = acc * (np.abs(x) @ w1.T) + acc * np.abs(z1)
+    dh1 = gelu_error(z1, dz1)
+    dh1 = dh1 + bf16_ulp(np.abs(h1) + dh1)
+    dz2 = dh1 @ w2.T + acc * (np.abs(h1) @ w2.T) + acc * np.abs(z2)
+    dh2 = gelu_error(z2, dz2)
+    dh2 = dh2 + bf16_ulp(np.abs(h2) + dh2)
+    return dh2 @ w3.T + acc * (np.abs(h2) @ w3.T) + 1e-6
 
 
 def test_gradients_match_oracle(native, torch_cuda):
@@ -127,14 +162,42 @@ def test_training_fits_a_smooth_target(native, torch_cuda):
     assert last < 0.1 * first, (first, last)
 
 
-def test_forward_erf_is_within_its_published_bound(native):
-    """The forward pass evaluates GELU's erf by Abramowitz & Stegun 7.1.28
-    (absolute error 3e-7) with one approximate reciprocal; in FP32 the 16th
-    power scales the polynomial's rounding, and a float32 evaluation of the
-    same steps stays under 1.8e-6 against the exact erf. Against erff the
-    GPU must stay below 2.5e-6, three orders under the BF16 rounding the
-    activation gets next."""
+def test_forward_erf_is_within_its_stated_bound(native):
+    """The forward pass takes erf(x) as tanh(a u + b u^3), u = sqrt(2) x (the
+    approximation behind GELU's tanh form: within 3.6e-4 of the exact erf on
+    [-6, 6]), with the hardware's approximate tanh (relative error about
+    2^-11). Against erff the GPU stays below 1e-3, under the BF16 rounding
+    (relative step 2^-8) the activation gets next."""
     from computer_graphics_lab_00_gb300.learned import MlpGpu
 
+    z = np.linspace(-8.0, 8.0, 100001)
+    assert np.abs(M.gelu(z) - M.gelu_erf(z)).max() < 4.8e-4
     with MlpGpu() as mlp:
-        assert mlp.selftest_erf() < 2.5e-6
+        assert mlp.selftest_erf() < 1e-3
+
+
+def test_bounded_wait_gives_up_with_a_status_and_the_context_stays_usable(native, torch_cuda):
+    """The forward pass waits for its tensor-core work on an mbarrier with a
+    bounded number of tries. A wait on a barrier nobody arrives at (no MMA in
+    flight) gives up after a few hundred tries: SPH_ERR_TIMEOUT comes back
+    through the C ABI, and the same model then runs a forward pass that
+    matches the oracle (the context was not lost)."""
+    from computer_graphics_lab_00_gb300 import abi
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    torch = torch_cuda
+    with MlpGpu(seed=5) as mlp:
+        assert mlp.selftest_wait(256, arrive=False) == abi.SPH_ERR_TIMEOUT
+        assert mlp.selftest_wait(256, arrive=True) == abi.SPH_OK
+        assert mlp.selftest_wait(256, arrive=False) == abi.SPH_ERR_TIMEOUT
+        n = 300
+        f, _, mean, std, scale = case(n, seed=11)
+        params = mlp.params()
+        mlp.set_normalisation(mean, std, scale)
+        d_f = torch.from_numpy(f).cuda()
+        d_out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        mlp.forward(d_f.data_ptr(), n, d_out.data_ptr())
+        got = d_out.cpu().numpy()
+    y, cache = M.forward(params, f, mean, std, scale)
+    assert np.all(np.abs(got[:, :3] - y * scale) <= forward_error_bound(cache) * scale)

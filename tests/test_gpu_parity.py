@@ -315,6 +315,10 @@ def test_errors_are_status_codes(native):
     dict(neighbour_kernel=4, block_size=256, queue_depth=32, radix_bits=6, schedule=0, sort=1),
     dict(neighbour_kernel=3, block_size=128, queue_depth=16, radix_bits=6, schedule=1, sort=1),
     dict(neighbour_kernel=0, block_size=128, queue_depth=16, radix_bits=6, schedule=0, sort=1),
+    dict(neighbour_kernel=5, block_size=128, queue_depth=16, radix_bits=7, schedule=0, sort=0),
+    dict(neighbour_kernel=5, block_size=128, queue_depth=16, radix_bits=8, schedule=1, sort=0),
+    dict(neighbour_kernel=5, block_size=128, queue_depth=32, radix_bits=6, schedule=1, sort=1),
+    dict(neighbour_kernel=5, block_size=256, queue_depth=32, radix_bits=6, schedule=0, sort=1),
 ])
 def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     """Every launch shape the autotuner may pick gives the oracle's bits."""
@@ -455,7 +459,8 @@ def test_pair_list_overflow_falls_back_bit_exact(native, oracle):
     pos[:, 3] = 1000.0
     vel = np.zeros((n, 4), np.float32)
     for variant, schedule, block, queue in ((2, 0, 256, 32), (3, 1, 256, 32), (4, 0, 256, 32), (4, 1, 256, 32),
-                                            (4, 0, 256, 24), (4, 0, 256, 16), (4, 0, 128, 32), (4, 0, 64, 32)):
+                                            (4, 0, 256, 24), (4, 0, 256, 16), (4, 0, 128, 32), (4, 0, 64, 32),
+                                            (5, 0, 128, 32), (5, 1, 128, 32)):
         with FluidSolverGpu(params, n) as solver:
             solver.set_tuning(neighbour_kernel=variant, schedule=schedule, block_size=block, queue_depth=queue)
             solver.upload(pos, vel)
