@@ -100,6 +100,7 @@ def workload_config(case, world: int) -> dict:
         "spacing": float(p.emitter_half_extents[3]),
         "jitter": "uniform +-1e-4 m, splitmix64 seed 0",
         "l2": "flushed before every timed substep (256 MB write); working set ~120 MB",
+        "timed_substeps": "spread evenly over the 1,000-substep run (untimed substeps between them)",
         "parallelism": "single tank" if world == 1 else f"{world} replicas (no data exchange)",
     }
 
@@ -655,10 +656,15 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
 
     # Warm-up (builds the CUDA graph).
-    solver.run(dt, max(args.warmup, 3))
+    warm = max(args.warmup, 3)
+    solver.run(dt, warm)
     solver.synchronize()
 
-    # Timed leg: device-resident state, one substep per timed interval.
+    # Timed leg: device-resident state, one substep per timed interval. The
+    # timed substeps are spread evenly over the workload's whole run (1,000
+    # substeps: the dam collapses and compresses, and the cost per substep
+    # changes with it), untimed substeps between them.
+    gap = max(0, (case.steps - warm) // max(args.steps, 1) - 1)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     sampler = ClockSampler(local) if rank == 0 else None
@@ -666,12 +672,20 @@ def run_gb300(args) -> None:
         sampler.__enter__()
     barrier()
     wall0 = time.perf_counter()
+    pair_samples = []
     for k in range(args.steps):
+        if gap:
+            solver.run(dt, gap)
         with torch.cuda.stream(stream):
             flush.zero_()
             starts[k].record(stream)
         solver.run(dt, 1)
         ends[k].record(stream)
+        if gap:
+            # Candidate and in-range pair counts of the state just timed
+            # (a counting pass outside the timed interval).
+            st = solver.stats()
+            pair_samples.append((st.candidates, st.pairs_in_range))
     barrier()
     wall = time.perf_counter() - wall0
     if sampler:
@@ -694,8 +708,10 @@ def run_gb300(args) -> None:
     # particle), one substep, download it (32 B a particle), the velocity
     # upload overlapping the keys and sort.
     e2e_steps = args.e2e_steps or min(args.steps, 100)
-    host_pos = torch.from_numpy(pos0.copy()).pin_memory()
-    host_vel = torch.from_numpy(vel0.copy()).pin_memory()
+    # From the state the timed leg ended in.
+    end_pos, end_vel = solver.state()
+    host_pos = torch.from_numpy(end_pos.copy()).pin_memory()
+    host_vel = torch.from_numpy(end_vel.copy()).pin_memory()
     hp, hv = host_pos.data_ptr(), host_vel.data_ptr()
     solver.step_host(hp, hv, n, dt, 1, hp, hv)
     barrier()
@@ -742,8 +758,26 @@ def run_gb300(args) -> None:
             traffic = None
     step_alg = 120 * n + 12 * cells
     step_ms = device_ms / args.steps
-    flops = 20 * pairs.candidates + 55 * pairs.pairs_in_range
-    nominal_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+    if pair_samples:
+        cand = sum(c for c, _ in pair_samples) / len(pair_samples)
+        inr = sum(r for _, r in pair_samples) / len(pair_samples)
+    else:
+        cand, inr = pairs.candidates, pairs.pairs_in_range
+    flops = 20 * cand + 55 * inr
+    # Nominal FP32 rate of this device: SMs x 128 lanes x 2 flop (FMA) x the
+    # maximum SM clock (read from the device; MEASURED_PEAKS.json's if absent).
+    props = torch.cuda.get_device_properties(local)
+    sm_count = props.multi_processor_count
+    max_mhz = None
+    try:
+        max_mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("sm_max_mhz"))
+    except Exception:
+        pass
+    if clocks_max := (sampler.summary().get("sm_max_mhz") if sampler else None):
+        max_mhz = float(clocks_max)
+    if not max_mhz:
+        max_mhz = 2070.0
+    nominal_fp32 = sm_count * 128 * 2 * max_mhz * 1e6 / 1e12
 
     clocks = sampler.summary() if sampler else None
     out = {
@@ -769,8 +803,9 @@ def run_gb300(args) -> None:
         "step_roofline": {"alg_bytes": step_alg, "achieved_gbs": step_alg / (step_ms / 1e3) / 1e9,
                           "frac_of_peak": step_alg / (step_ms / 1e3) / 1e9 / peak},
         "fp32": {"alg_flops_per_step": flops, "achieved_tflops": flops / (step_ms / 1e3) / 1e12,
-                 "nominal_peak_tflops": nominal_fp32, "candidates": pairs.candidates,
-                 "pairs_in_range": pairs.pairs_in_range},
+                 "nominal_peak_tflops": nominal_fp32, "frac": flops / (step_ms / 1e3) / 1e12 / nominal_fp32,
+                 "sm_count": sm_count, "sm_max_mhz": max_mhz, "candidates": cand, "pairs_in_range": inr,
+                 "pairs_from": "mean over the timed substeps" if pair_samples else "initial state"},
         "phase_ms": phases,
         "gpu_launches": launches,
         "clocks": clocks,

@@ -39,7 +39,7 @@ void to_api(const sph::TuneChoice& c, sph_tuning* out) {
     out->neighbour_kernel = c.tuning.variant;
     out->block_size = c.tuning.block;
     out->queue_depth = c.tuning.queue;
-    out->schedule = c.schedule ? 1u : 0u;
+    out->schedule = c.schedule;
     out->sort = c.onesweep ? 1u : 0u;
 }
 
@@ -447,7 +447,7 @@ int sph_get_tuning(const sph_ctx* ctx, sph_tuning* out) {
     out->neighbour_kernel = t.variant;
     out->block_size = t.block;
     out->queue_depth = t.queue;
-    out->schedule = ctx->engine.schedule_on() ? 1u : 0u;
+    out->schedule = ctx->engine.schedule_on();
     out->sort = ctx->engine.onesweep_on() ? 1u : 0u;
     return SPH_OK;
 }
@@ -460,14 +460,14 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning) {
     t.variant = tuning->neighbour_kernel;
     t.block = tuning->block_size;
     t.queue = tuning->queue_depth;
-    if (tuning->schedule > 1 || tuning->sort > 1) {
+    if (tuning->schedule > 2 || tuning->sort > 1) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     int status = ctx->engine.set_tuning(t);
     if (status != SPH_OK) {
         return status;
     }
-    status = ctx->engine.set_schedule(tuning->schedule != 0);
+    status = ctx->engine.set_schedule(tuning->schedule);
     if (status != SPH_OK) {
         return status;
     }
@@ -671,7 +671,7 @@ int sph_batch_get_tuning(const sph_batch* batch, sph_tuning* out) {
 }
 
 int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
-    if (batch == nullptr || tuning == nullptr || tuning->schedule > 1 || tuning->sort > 1) {
+    if (batch == nullptr || tuning == nullptr || tuning->schedule > 2 || tuning->sort > 1) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     sph::NeighbourTuning t = batch->engine.tuning();
@@ -680,7 +680,7 @@ int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
     t.queue = tuning->queue_depth;
     int status = batch->engine.set_tuning(t);
     if (status == SPH_OK) {
-        status = batch->engine.set_schedule(tuning->schedule != 0);
+        status = batch->engine.set_schedule(tuning->schedule);
     }
     if (status == SPH_OK) {
         status = batch->engine.set_onesweep(tuning->sort != 0);

@@ -639,7 +639,7 @@ int Engine::emit(uint32_t tank, uint32_t count) {
     return SPH_OK;
 }
 
-// Morton processing order: rank_ is refreshed from the current positions
+// Morton (or Hilbert) processing order: rank_ is refreshed from the current positions
 // every kScheduleRefresh grid builds (particles move a fraction of a cell per
 // substep, so an order a few substeps old keeps its locality), after an emit
 // and whenever the particle count changed since the last refresh. An upload or
@@ -647,7 +647,7 @@ int Engine::emit(uint32_t tank, uint32_t count) {
 // ids; the usual refresh renews its locality). Never called while a graph
 // is being captured: the graphs only hold the per-substep order scatter.
 int Engine::prepare_schedule(uint32_t* launches) {
-    if (!use_schedule_ || total_count_ == 0) {
+    if (schedule_curve_ == 0 || total_count_ == 0) {
         return SPH_OK;
     }
     if (rank_count_ == total_count_ && since_refresh_ + 1 < kScheduleRefresh) {
@@ -667,7 +667,7 @@ int Engine::prepare_schedule(uint32_t* launches) {
     const uint32_t tank_bits = bit_width(static_cast<uint32_t>(tanks_.size()) - 1U);
     const uint32_t axis_bits = std::max(1U, std::min({bit_width(cells - 1U), 10U, (32U - tank_bits) / 3U}));
     SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, 3U * axis_bits + tank_bits, grid_,
-                                sweep_, rank_, stream_, launches));
+                                sweep_, rank_, stream_, launches, schedule_curve_ == 2));
     rank_count_ = total_count_;
     since_refresh_ = 0;
     return SPH_OK;
@@ -706,7 +706,7 @@ int Engine::enqueue_grid(uint32_t* launches) {
 int Engine::enqueue_bounds(uint32_t* launches) {
     uint32_t n = total_count_;
     Schedule schedule{};
-    if (use_schedule_) {
+    if (schedule_curve_ != 0) {
         if (rank_count_ != n) {
             return SPH_ERR_INVALID_ARGUMENT;  // prepare_schedule did not run for this particle count
         }
@@ -715,7 +715,7 @@ int Engine::enqueue_bounds(uint32_t* launches) {
     }
     SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_, svel_,
                                   stank_, schedule, stream_));
-    tuning_.order = use_schedule_ ? order_ : nullptr;
+    tuning_.order = schedule_curve_ != 0 ? order_ : nullptr;
     if (launches != nullptr) {
         *launches += 1;
     }
@@ -1053,7 +1053,7 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
     int status = snapshot(true);
     const NeighbourTuning original = tuning_;
     const uint32_t original_bits = radix_bits_;
-    const bool original_schedule = use_schedule_;
+    const uint32_t original_schedule = schedule_curve_;
     const bool original_onesweep = onesweep_;
     auto measure = [&](const TuneChoice& c, float* ms) -> int {
         int st = set_tuning(c.tuning);
@@ -1093,7 +1093,7 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
     std::vector<TuneChoice> stage1;
     for (uint32_t variant : {3u, 4u}) {
         for (uint32_t block : {128u, 256u}) {
-            for (bool schedule : {false, true}) {
+            for (uint32_t schedule : {0u, 1u, 2u}) {
                 TuneChoice c;
                 c.tuning = original;
                 c.tuning.variant = variant;
@@ -1510,8 +1510,11 @@ int Engine::set_onesweep(bool on) {
     return SPH_OK;
 }
 
-int Engine::set_schedule(bool on) {
-    use_schedule_ = on;
+int Engine::set_schedule(uint32_t curve) {
+    if (curve > 2) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    schedule_curve_ = curve;
     rank_count_ = 0xFFFFFFFFu;
     if (graph_ != nullptr) {
         cudaGraphExecDestroy(graph_);

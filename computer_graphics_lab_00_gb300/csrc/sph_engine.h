@@ -33,7 +33,7 @@ int validate_params(const sph_params& params);
 struct TuneChoice {
     NeighbourTuning tuning{};
     uint32_t radix_bits = 6;
-    bool schedule = false;
+    uint32_t schedule = 0;  // processing order: 0 sorted, 1 Morton, 2 Hilbert
     bool onesweep = true;
     float ms = 0.0F;
 };
@@ -96,8 +96,8 @@ public:
     int set_active(const std::vector<uint8_t>& active);
     int set_radix_bits(uint32_t bits);
     int set_tuning(const NeighbourTuning& tuning);
-    int set_schedule(bool on);
-    bool schedule_on() const { return use_schedule_; }
+    int set_schedule(uint32_t curve);  // 0 sorted order, 1 Morton, 2 Hilbert
+    uint32_t schedule_on() const { return schedule_curve_; }
     // Grid sort: one kernel per 8-bit digit pass, or three kernels per
     // radix_bits-wide pass.
     int set_onesweep(bool on);
@@ -163,7 +163,7 @@ private:
     uint32_t radix_bits_ = 6;
     RadixPlan plan_{};
     NeighbourTuning tuning_{};
-    bool use_schedule_ = true;
+    uint32_t schedule_curve_ = 1;  // processing order: 0 sorted, 1 Morton, 2 Hilbert
     bool capturing_ = false;               // a graph capture is open on stream_
     uint32_t* rank_ = nullptr;             // Morton slot of each particle id (a permutation)
     uint32_t* order_ = nullptr;            // sorted positions in processing order

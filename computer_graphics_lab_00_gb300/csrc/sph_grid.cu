@@ -278,18 +278,55 @@ __host__ __device__ inline SweepLayout sweep_layout(unsigned long long* base, ui
 constexpr uint32_t kKeysThreads = 1024;
 constexpr uint32_t kKeysItems = kSweepTile / kKeysThreads;
 
-// Morton code of a particle's cell for the processing order: the grid's own
+// Hilbert index of the cell (x0, x1, x2) of a 2^bits cube, after J.
+// Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707 (2004):
+// the coordinates are turned into the curve's "transpose" (undo the
+// excess work level by level, then Gray-code), whose bits, interleaved with
+// x0's bit highest at each level, are the index. Consecutive indices are
+// face-adjacent cells, so runs of the order stay compact at every scale.
+__device__ __forceinline__ uint32_t hilbert3(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t bits) {
+    uint32_t x[3] = {x0, x1, x2};
+    const uint32_t top = 1u << (bits - 1u);
+    for (uint32_t q = top; q > 1u; q >>= 1) {
+        const uint32_t low = q - 1u;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (x[i] & q) {
+                x[0] ^= low;
+            } else {
+                const uint32_t swap = (x[0] ^ x[i]) & low;
+                x[0] ^= swap;
+                x[i] ^= swap;
+            }
+        }
+    }
+    x[1] ^= x[0];
+    x[2] ^= x[1];
+    uint32_t flip = 0;
+    for (uint32_t q = top; q > 1u; q >>= 1) {
+        if (x[2] & q) {
+            flip ^= q - 1u;
+        }
+    }
+    return (spread3(x[0] ^ flip) << 2) | (spread3(x[1] ^ flip) << 1) | spread3(x[2] ^ flip);
+}
+
+// Curve key of a particle's cell for the processing order: the grid's own
 // cell (so a cell's particles stay together), offset from the cell of the
-// tank's low corner and clamped to `bits` bits per axis, the tank index
-// above them.
-__device__ __forceinline__ uint32_t morton_key(float4 p, const TankConst* t, uint32_t tank, uint32_t bits) {
+// tank's low corner and clamped to `bits` bits per axis, as a Morton code or
+// a Hilbert index, the tank index above it.
+__device__ __forceinline__ uint32_t morton_key(float4 p, const TankConst* t, uint32_t tank, uint32_t bits,
+                                               bool hilbert) {
     const float h = __ldg(&t->h);
     const int limit = static_cast<int>((1u << bits) - 1u);
     const int cx = min(max(cell_coord(p.x, h) - cell_coord(__ldg(&t->low[0]), h), 0), limit);
     const int cy = min(max(cell_coord(p.y, h) - cell_coord(__ldg(&t->low[1]), h), 0), limit);
     const int cz = min(max(cell_coord(p.z, h) - cell_coord(__ldg(&t->low[2]), h), 0), limit);
-    return (tank << (3 * bits)) | spread3(static_cast<uint32_t>(cx)) | (spread3(static_cast<uint32_t>(cy)) << 1) |
-           (spread3(static_cast<uint32_t>(cz)) << 2);
+    const uint32_t code = hilbert ? hilbert3(static_cast<uint32_t>(cx), static_cast<uint32_t>(cy),
+                                             static_cast<uint32_t>(cz), bits)
+                                  : spread3(static_cast<uint32_t>(cx)) | (spread3(static_cast<uint32_t>(cy)) << 1) |
+                                        (spread3(static_cast<uint32_t>(cz)) << 2);
+    return (tank << (3 * bits)) | code;
 }
 
 // kMorton false: the spatial-hash bucket keys of the grid (spread evenly over
@@ -303,7 +340,7 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
                                                                  uint32_t* __restrict__ keys, uint32_t passes,
                                                                  uint32_t* __restrict__ tile_counts,
                                                                  uint32_t* __restrict__ hist, uint32_t morton_bits,
-                                                                 const uint32_t* __restrict__ ids) {
+                                                                 const uint32_t* __restrict__ ids, int hilbert) {
     __shared__ uint32_t counts[kSweepMaxPasses][kSweepBins];
     for (uint32_t k = threadIdx.x; k < kSweepMaxPasses * kSweepBins; k += blockDim.x) {
         (&counts[0][0])[k] = 0;
@@ -324,7 +361,7 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
         const uint32_t i = first + r * kKeysThreads + threadIdx.x;
         const TankConst* t = tanks + tank[r];
         if (kMorton) {
-            const uint32_t key = morton_key(p[r], t, tank[r], morton_bits);
+            const uint32_t key = morton_key(p[r], t, tank[r], morton_bits, hilbert != 0);
             if (i < n) {
                 keys[i] = key;
             }
@@ -501,7 +538,7 @@ namespace {
 
 cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                             uint32_t* keys, uint32_t passes, unsigned long long* sweep, uint32_t morton_bits,
-                            const uint32_t* ids, cudaStream_t stream) {
+                            const uint32_t* ids, cudaStream_t stream, bool hilbert = false) {
     cudaError_t err = cudaMemsetAsync(sweep, 0, onesweep_scratch_words(n, passes) * sizeof(unsigned long long), stream);
     if (err != cudaSuccess) {
         return err;
@@ -510,10 +547,10 @@ cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const Ta
     SweepLayout l = sweep_layout(sweep, tiles, passes);
     if (morton_bits != 0) {
         keys_hist_kernel<true><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes, l.tile_counts,
-                                                                   l.hist, morton_bits, ids);
+                                                                   l.hist, morton_bits, ids, hilbert ? 1 : 0);
     } else {
         keys_hist_kernel<false><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes,
-                                                                    l.tile_counts, l.hist, 0, ids);
+                                                                    l.tile_counts, l.hist, 0, ids, 0);
     }
     return cudaGetLastError();
 }
@@ -531,7 +568,8 @@ cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, con
 
 cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                                uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
-                               unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches) {
+                               unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches,
+                               bool hilbert) {
     if (n == 0) {
         return cudaSuccess;
     }
@@ -543,7 +581,7 @@ cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const
         return cudaErrorInvalidValue;
     }
     cudaError_t err =
-        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, nullptr, stream);
+        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, nullptr, stream, hilbert);
     if (err == cudaSuccess) {
         err = launch_onesweep_sort(scratch, n, passes, sweep, stream, launches, true);
     }

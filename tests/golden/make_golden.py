@@ -5,7 +5,8 @@ The reference's unmodified src/physics/fluid_sph.cpp is compiled in place
 cases; its outputs are frozen here so that machines without the reference
 tree (the GPU host) can still pin the oracle and the CUDA path to it.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # the small cases (.npz)
+    python tests/golden/make_golden.py --long-run   # the 1M-particle, 1,000-substep digests (.json)
 """
 from __future__ import annotations
 
@@ -117,9 +118,46 @@ def surface_small() -> dict:
             "vertices_24": full.view(np.uint8).reshape(-1, 16), "vertices_24_cap600": short.view(np.uint8).reshape(-1, 16)}
 
 
+def state_digest(pos: np.ndarray, vel: np.ndarray) -> tuple[str, str]:
+    """SHA-256 of the float32 position and velocity arrays (id order)."""
+    import hashlib
+
+    return (hashlib.sha256(np.ascontiguousarray(pos, np.float32).tobytes()).hexdigest(),
+            hashlib.sha256(np.ascontiguousarray(vel, np.float32).tobytes()).hexdigest())
+
+
+def long_run_1m(threads: int) -> dict:
+    """The 1,048,576-particle dam break (dam_break_1m) over its 1,000 substeps
+    of 1/600 s through the reference: every 100 substeps the digests of the
+    whole state and its FP64 mean density and centre of mass."""
+    case = W.dam_break_1m()
+    pos, vel = case.initial_state()
+    ref = Reference()
+    ref.set_state(pos, vel)
+    rows = []
+    for k in range(1, case.steps + 1):
+        ref.substep(case.params, case.dt, threads=threads)
+        if k % 100 == 0:
+            pos, vel = ref.state()
+            dp, dv = state_digest(pos, vel)
+            p64 = pos.astype(np.float64)
+            rows.append({"substep": k, "pos_sha256": dp, "vel_sha256": dv, "mean_density": float(p64[:, 3].mean()),
+                         "centre_of_mass": [float(p64[:, a].mean()) for a in range(3)]})
+            print(rows[-1], flush=True)
+    return {"workload": case.name, "particles": case.count, "dt": case.dt, "checkpoints": rows}
+
+
 def main() -> None:
     if build_reference() is None:
         raise SystemExit("the reference tree is needed to regenerate the golden vectors")
+    if "--long-run" in sys.argv:
+        # About ten minutes on 8 cores; kept out of the default regeneration.
+        import json
+        import os
+
+        data = long_run_1m(os.cpu_count() or 1)
+        (OUT / "dam_break_1m_long.json").write_text(json.dumps(data, indent=1))
+        return
     for name, make in (("scene_frames", scene_frames), ("dam_break_small", dam_break_small),
                        ("collisions_overflow", collisions_overflow), ("obstacles_small", obstacles_small),
                        ("surface_small", surface_small)):

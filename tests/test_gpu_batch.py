@@ -42,7 +42,7 @@ def load(ts):
     return solver
 
 
-@pytest.mark.parametrize("schedule,substeps", [(0, 5), (1, 5), (1, 20)])
+@pytest.mark.parametrize("schedule,substeps", [(0, 5), (1, 5), (1, 20), (2, 20)])
 def test_each_tank_matches_the_oracle(native, oracle, tanks, schedule, substeps):
     """Sorted and Morton processing orders; 20 substeps cross a remake of the
     Morton order (one every 16 grid builds), which keys the tank above the

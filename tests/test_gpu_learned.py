@@ -61,11 +61,11 @@ def test_features_are_finite_and_plausible(native, small):
 
 
 def test_features_do_not_depend_on_the_processing_order(native, small):
-    """Sorted and Morton processing orders give the same feature bits."""
+    """Sorted, Morton and Hilbert processing orders give the same feature bits."""
     import torch
 
     got = []
-    for schedule in (0, 1):
+    for schedule in (0, 1, 2):
         s = T.load_tanks(small)
         s.set_tuning(schedule=schedule)
         s.run(T.FINE_DT, 20)
@@ -74,7 +74,7 @@ def test_features_do_not_depend_on_the_processing_order(native, small):
         s.synchronize()
         got.append(f.cpu().numpy())
         s.close()
-    assert same(got[0], got[1])
+    assert same(got[0], got[1]) and same(got[0], got[2])
 
 
 def test_pipeline_end_to_end(native, small, tmp_path):

@@ -319,6 +319,9 @@ def test_errors_are_status_codes(native):
     dict(neighbour_kernel=5, block_size=128, queue_depth=16, radix_bits=8, schedule=1, sort=0),
     dict(neighbour_kernel=5, block_size=128, queue_depth=32, radix_bits=6, schedule=1, sort=1),
     dict(neighbour_kernel=5, block_size=256, queue_depth=32, radix_bits=6, schedule=0, sort=1),
+    dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=2, sort=1),
+    dict(neighbour_kernel=3, block_size=256, queue_depth=16, radix_bits=6, schedule=2, sort=0),
+    dict(neighbour_kernel=5, block_size=128, queue_depth=16, radix_bits=8, schedule=2, sort=1),
 ])
 def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     """Every launch shape the autotuner may pick gives the oracle's bits."""
