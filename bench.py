@@ -67,6 +67,8 @@ def parse_args():
                    help="substeps of the 256-tank leg (0 skips it)")
     p.add_argument("--learned-steps", type=int, default=20,
                    help="coarse steps of the learned 5x-dt leg at 1M (0 skips it)")
+    p.add_argument("--neighbour-kernel", type=int, default=None,
+                   help="neighbour kernel of the 1M tank's legs (sph_tuning.neighbour_kernel; default: the library's)")
     p.add_argument("--learned-eval", action=argparse.BooleanOptionalAction, default=True,
                    help="config 4: 64 held-out tanks of 32,768 over 2 s, learned and plain coarse vs plain fine")
     p.add_argument("--fallback-steps", type=int, default=600,
@@ -643,6 +645,8 @@ def run_gb300(args) -> None:
     dt = case.dt
     pos0, vel0 = case.initial_state()
     solver = FluidSolverGpu(case.params, n, device=local)
+    if args.neighbour_kernel is not None:
+        solver.set_tuning(neighbour_kernel=args.neighbour_kernel)
     solver.upload(pos0, vel0)
     pairs = solver.stats()  # candidate and in-range pair counts of the initial state
     stream = torch.cuda.ExternalStream(solver.stream(), device=torch.device("cuda", local))
@@ -793,7 +797,7 @@ def run_gb300(args) -> None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": workload_config(case, world),
+        "config": {**workload_config(case, world), "neighbour_kernel": solver.tuning()["neighbour_kernel"]},
         "particle_steps_per_s": total_particles * args.steps / (device_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
                 "steps": e2e_steps, "ms_per_step": 1e3 * e2e_wall / e2e_steps},

@@ -153,6 +153,14 @@ class SphStats(ctypes.Structure):
     ]
 
 
+# SphStats as a numpy record: a batch's statistics read as one array.
+STATS_DTYPE = np.dtype([("particles", "<u4"), ("buckets", "<u4"), ("max_bucket_count", "<u4"),
+                        ("overflow_buckets", "<u4"), ("candidates", "<u8"), ("pairs_in_range", "<u8"),
+                        ("mean_density", "<f8"), ("mean_compression", "<f8"), ("max_density", "<f8"),
+                        ("centre_of_mass", "<f8", (3,)), ("kinetic_energy", "<f8"), ("nonfinite", "<u4"),
+                        ("pad", "<u4")])
+assert STATS_DTYPE.itemsize == ctypes.sizeof(SphStats)
+
 assert ctypes.sizeof(SphCollider) == 160
 assert ctypes.sizeof(SphForceField) == 48
 assert ctypes.sizeof(SphParams) == 1856

@@ -111,6 +111,14 @@ class BatchSolverGpu:
         self._check(self._lib.sph_batch_stats(self._handle, out), "sph_batch_stats")
         return list(out)
 
+    def stats_array(self) -> np.ndarray:
+        """The same statistics as one numpy record array (abi.STATS_DTYPE),
+        without a Python object per tank."""
+        out = np.zeros(self.tanks, abi.STATS_DTYPE)
+        self._check(self._lib.sph_batch_stats(self._handle, out.ctypes.data_as(ctypes.POINTER(SphStats))),
+                    "sph_batch_stats")
+        return out
+
     def synchronize(self) -> None:
         self._check(self._lib.sph_batch_synchronize(self._handle), "sph_batch_synchronize")
 

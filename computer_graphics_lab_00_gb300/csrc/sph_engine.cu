@@ -200,7 +200,8 @@ void Engine::release() {
                        bucket_stats_,  tuning_.pair_list, tuning_.pair_count, tuning_.masks,
                        rank_,          order_,        compact_ids_, compact_sorted_, compact_ranges_,
                        snap_pos_[0], snap_vel_[0],
-                       snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_, correction_sums_};
+                       snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_, correction_sums_,
+                       compact_rank_,  compact_order_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -654,7 +655,19 @@ int Engine::prepare_schedule(uint32_t* launches) {
         ++since_refresh_;
         return SPH_OK;
     }
-    // Bits per axis: enough for the widest tank's cells, within 32 key bits.
+    uint32_t axis_bits = 0;
+    uint32_t key_bits = 0;
+    schedule_bits(&axis_bits, &key_bits);
+    SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, key_bits, grid_, sweep_, rank_,
+                                stream_, launches, schedule_curve_ == 2));
+    rank_count_ = total_count_;
+    since_refresh_ = 0;
+    return SPH_OK;
+}
+
+// Bits per axis of the curve keys: enough for the widest tank's cells,
+// within 32 key bits with the tank index above them.
+void Engine::schedule_bits(uint32_t* axis_bits, uint32_t* key_bits) const {
     uint32_t cells = 1;
     for (const TankConst& t : tanks_) {
         for (int a = 0; a < 3; ++a) {
@@ -665,12 +678,8 @@ int Engine::prepare_schedule(uint32_t* launches) {
         }
     }
     const uint32_t tank_bits = bit_width(static_cast<uint32_t>(tanks_.size()) - 1U);
-    const uint32_t axis_bits = std::max(1U, std::min({bit_width(cells - 1U), 10U, (32U - tank_bits) / 3U}));
-    SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, 3U * axis_bits + tank_bits, grid_,
-                                sweep_, rank_, stream_, launches, schedule_curve_ == 2));
-    rank_count_ = total_count_;
-    since_refresh_ = 0;
-    return SPH_OK;
+    *axis_bits = std::max(1U, std::min({bit_width(cells - 1U), 10U, (32U - tank_bits) / 3U}));
+    *key_bits = 3U * *axis_bits + tank_bits;
 }
 
 int Engine::enqueue_grid(uint32_t* launches) {
@@ -850,15 +859,45 @@ int Engine::run_compact(uint32_t substeps, uint32_t active_particles) {
     const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
     NeighbourTuning tuning = tuning_;
     tuning.order = nullptr;
+    // Bucket runs (first bucket, count) of adjacent active tanks.
+    std::vector<uint2> clear_runs;
+    for (const TankConst& t : tanks_) {
+        if (t.active == 0 || t.particle_count == 0) {
+            continue;
+        }
+        const uint32_t count = t.cell_mask + 1U;
+        if (!clear_runs.empty() && clear_runs.back().x + clear_runs.back().y == t.bucket_base) {
+            clear_runs.back().y += count;
+        } else {
+            clear_runs.push_back(make_uint2(t.bucket_base, count));
+        }
+    }
+    // The compacted set gets its own processing order (made once per call,
+    // in buffers of its own, so the full set's order stays valid).
+    Schedule schedule{};
+    if (schedule_curve_ != 0) {
+        if (compact_rank_ == nullptr) {
+            if ((status = alloc(&compact_rank_, total_capacity_)) != SPH_OK ||
+                (status = alloc(&compact_order_, total_capacity_)) != SPH_OK) {
+                return status;
+            }
+        }
+        uint32_t axis_bits = 0;
+        uint32_t key_bits = 0;
+        schedule_bits(&axis_bits, &key_bits);
+        SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, n, axis_bits, key_bits, grid_, sweep_, compact_rank_,
+                                    stream_, nullptr, schedule_curve_ == 2, compact_ids_));
+        schedule.rank = compact_rank_;
+        schedule.order = compact_order_;
+        tuning.order = compact_order_;
+    }
     for (uint32_t s = 0; s < substeps; ++s) {
-        // Only the active tanks' buckets are read, so only they need clearing
-        // (one memset per tank while that is the smaller job).
-        if (ranges <= 32) {
-            for (const TankConst& t : tanks_) {
-                if (t.active != 0 && t.particle_count > 0) {
-                    SPH_CUDA(
-                        cudaMemsetAsync(bucket_ + t.bucket_base, 0, sizeof(uint2) * (t.cell_mask + 1U), stream_));
-                }
+        // Only the active tanks' buckets are read, so only they need clearing:
+        // one memset per run of adjacent active tanks while that is the
+        // smaller job.
+        if (clear_runs.size() <= 32) {
+            for (const uint2& r : clear_runs) {
+                SPH_CUDA(cudaMemsetAsync(bucket_ + r.x, 0, sizeof(uint2) * r.y, stream_));
             }
         } else {
             SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
@@ -866,7 +905,7 @@ int Engine::run_compact(uint32_t substeps, uint32_t active_particles) {
         SPH_CUDA(launch_keys_onesweep(pos_, tank_of_, d_tanks_, n, grid_.keys, passes, sweep_, stream_, compact_ids_));
         SPH_CUDA(launch_onesweep_sort(grid_, n, passes, sweep_, stream_, nullptr));
         SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_,
-                                      svel_, stank_, Schedule{}, stream_, compact_ids_, compact_sorted_));
+                                      svel_, stank_, schedule, stream_, compact_ids_, compact_sorted_));
         if ((status = enqueue_fields(nullptr)) != SPH_OK) {
             return status;
         }

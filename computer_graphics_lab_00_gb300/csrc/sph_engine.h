@@ -147,6 +147,7 @@ private:
     int enqueue_colliders(uint32_t* launches);
     int ensure_graph();
     int prepare_schedule(uint32_t* launches);
+    void schedule_bits(uint32_t* axis_bits, uint32_t* key_bits) const;
     int run_compact(uint32_t substeps, uint32_t active_particles);
     static constexpr uint32_t kScheduleRefresh = 8;  // grid builds between Morton order refreshes
     void release();
@@ -218,6 +219,8 @@ private:
     float4* snap_vel_[kSnapshotSlots] = {nullptr, nullptr};
     float4* sforce_ = nullptr;
     float4* scorrection_ = nullptr;
+    uint32_t* compact_rank_ = nullptr;   // processing order of compacted runs (by particle id)
+    uint32_t* compact_order_ = nullptr;
     unsigned long long* correction_sums_ = nullptr;  // kCorrectionSumWords per tank
     float* sfeatures_ = nullptr;
     cudaGraphExec_t learned_graph_ = nullptr;

@@ -242,12 +242,14 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
     }
 }
 
-// Processing slot of every particle id: the inverse of the Morton-sorted ids.
+// Processing slot of every particle id: the inverse of the Morton-sorted ids
+// (entries of a compacted set name ids[entry]).
 __global__ void __launch_bounds__(256) rank_kernel(const uint32_t* __restrict__ sorted_ids, uint32_t n,
-                                                   uint32_t* __restrict__ rank) {
+                                                   uint32_t* __restrict__ rank, const uint32_t* __restrict__ ids) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) {
-        rank[sorted_ids[t]] = t;
+        const uint32_t v = sorted_ids[t];
+        rank[ids != nullptr ? ids[v] : v] = t;
     }
 }
 
@@ -569,7 +571,7 @@ cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, con
 cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                                uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
                                unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches,
-                               bool hilbert) {
+                               bool hilbert, const uint32_t* ids) {
     if (n == 0) {
         return cudaSuccess;
     }
@@ -581,14 +583,14 @@ cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const
         return cudaErrorInvalidValue;
     }
     cudaError_t err =
-        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, nullptr, stream, hilbert);
+        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, ids, stream, hilbert);
     if (err == cudaSuccess) {
         err = launch_onesweep_sort(scratch, n, passes, sweep, stream, launches, true);
     }
     if (err != cudaSuccess) {
         return err;
     }
-    rank_kernel<<<(n + 255) / 256, 256, 0, stream>>>(scratch.sorted_ids, n, rank);
+    rank_kernel<<<(n + 255) / 256, 256, 0, stream>>>(scratch.sorted_ids, n, rank, ids);
     if (launches != nullptr) {
         *launches += 2;
     }

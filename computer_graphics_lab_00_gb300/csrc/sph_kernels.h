@@ -104,11 +104,12 @@ struct Schedule {
 // with the one-kernel passes in the sort buffers of `scratch` (a copy: the
 // caller's grid pointers stay as they were), then rank[id] = slot.
 // hilbert: the cells' Hilbert index (Skilling's transpose form) instead of
-// their Morton code.
+// their Morton code. ids (optional): order the compacted set pos[ids[v]],
+// v < n; rank is still indexed by particle id (rank[ids[v]] = slot).
 cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                                uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
                                unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches,
-                               bool hilbert = false);
+                               bool hilbert = false, const uint32_t* ids = nullptr);
 
 // Bucket table (start, end) from sorted keys (table pre-zeroed), the
 // cell-ordered copies of position, velocity and tank id, and (with a

@@ -236,10 +236,10 @@ def train(mlp, feats, targs, steps: int = 3000, batch: int = 65536, lr: float = 
             "output_scale": scale.cpu().numpy().tolist()}
 
 
-def _compression_and_com(stats):
-    c = np.array([s.mean_compression for s in stats])
-    com = np.array([[s.centre_of_mass[a] for a in range(3)] for s in stats])
-    return c, com
+def _compression_and_com(solver):
+    """Per-tank mean compression and centre of mass of a batch (one read)."""
+    st = solver.stats_array()
+    return st["mean_compression"].copy(), st["centre_of_mass"].copy()
 
 
 @dataclass
@@ -269,8 +269,8 @@ def reference_runs(tankset, duration: float = 2.0, every: float = 0.1, device: i
     for _ in range(checks):
         fine.run(FINE_DT, coarse_per_check * RATIO)
         plain.run_learned(COARSE_DT, coarse_per_check, None)
-        rec["fine"].append(_compression_and_com(fine.stats()))
-        rec["plain"].append(_compression_and_com(plain.stats()))
+        rec["fine"].append(_compression_and_com(fine))
+        rec["plain"].append(_compression_and_com(plain))
     fine.close()
     plain.close()
     return {"every": every, "checks": checks, **rec}
@@ -299,7 +299,7 @@ def compare_with_fine(tankset, mlp, duration: float = 2.0, every: float = 0.1, d
     run = []
     for _ in range(reference["checks"]):
         learned.run_learned(COARSE_DT, int(round(reference["every"] / COARSE_DT)), mlp)
-        run.append(_compression_and_com(learned.stats()))
+        run.append(_compression_and_com(learned))
     learned.learned_check()
     learned.close()
     return {"learned": _summary(run, reference["fine"], reference["every"]),
@@ -380,13 +380,13 @@ def fit(tankset, validations: list, snapshots: int = 40, steps: int = 4000, batc
     return mlp, report
 
 
-def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 5, sample: int = 8,
+def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 10, sample: int = 8,
                       threshold: float = 0.01, hold: int = 20, record_every: int = 60, drift_limit: float | None = None,
                       device: int = 0) -> dict:
     """Learned coarse steps with the plain fine solver as judge and fallback.
 
     Every `check_every` coarse steps a rotating 1/`sample` share of the
-    tanks on learned steps is judged: the fine solver re-runs the interval
+    tanks on learned steps (a contiguous block of tanks) is judged: the fine solver re-runs the interval
     (five fine steps from the same start) for those tanks only, and a tank
     whose mean compression differs from the fine result by more than
     `threshold` keeps the fine result and stays on fine steps for `hold`
@@ -423,20 +423,22 @@ def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 
             solver.synchronize()
             wall += time.perf_counter() - start
             solver.set_active(all_on)
-            records.append(_compression_and_com(solver.stats()))
+            records.append(_compression_and_com(solver))
             solver.synchronize()
             start = time.perf_counter()
         on_fine = hold_left > 0
         learned = ~on_fine
         if c % check_every == 0 and learned.any():
             checks += 1
-            # The judged share: tanks t with t % sample == turn, rotating.
-            share = learned & (np.arange(tanks) % sample == turn)
+            # The judged share: the turn-th of `sample` contiguous blocks of
+            # tanks, rotating (a contiguous block restores in one copy).
+            block = np.arange(tanks) * sample // tanks
+            share = learned & (block == turn)
             turn = (turn + 1) % sample
             solver.snapshot(0, save=True)
             solver.set_active(learned.astype(np.uint8))
             solver.run_learned(COARSE_DT, 1, mlp)
-            c_learned, _ = _compression_and_com(solver.stats())
+            c_learned, _ = _compression_and_com(solver)
             # Drift since the last judgement of each unjudged learned tank.
             drifted = learned & ~np.isfinite(c_learned)
             if drift_limit is not None:
@@ -447,7 +449,7 @@ def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 
                 solver.restore_tanks(0, (share | drifted).astype(np.uint8))
                 solver.set_active(fine_set.astype(np.uint8))
                 solver.run(FINE_DT, RATIO)
-                c_fine, _ = _compression_and_com(solver.stats())
+                c_fine, _ = _compression_and_com(solver)
                 err = np.abs(c_learned - c_fine)
                 bad = share & ((err > threshold) | ~np.isfinite(err))
                 judged += int(share.sum())
@@ -475,8 +477,8 @@ def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 
     solver.set_active(all_on)
     solver.learned_check()
     if record_every:
-        records.append(_compression_and_com(solver.stats()))
-    final = solver.stats()
+        records.append(_compression_and_com(solver))
+    final = solver.stats_array()
     solver.close()
     n = tankset.total_particles
     return {
@@ -486,8 +488,8 @@ def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 
         "checks": checks, "judged_tank_intervals": judged, "rejected_checks": rejected,
         "drift_fallbacks": drift_rejected,
         "check_errors_mean": float(np.mean(errors)) if errors else None,
-        "final_mean_compression": float(np.mean([s.mean_compression for s in final])),
-        "nonfinite_particles": int(sum(s.nonfinite for s in final)),
+        "final_mean_compression": float(final["mean_compression"].mean()),
+        "nonfinite_particles": int(final["nonfinite"].sum()),
         "records": records,
     }
 
@@ -504,7 +506,7 @@ def run_plain_fine(tankset, coarse_steps: int = 600, record_every: int = 60, dev
     done = 0
     while done < coarse_steps:
         if record_every:
-            records.append(_compression_and_com(solver.stats()))
+            records.append(_compression_and_com(solver))
         k = min(step, coarse_steps - done)
         solver.synchronize()
         torch.cuda.synchronize()
@@ -514,12 +516,12 @@ def run_plain_fine(tankset, coarse_steps: int = 600, record_every: int = 60, dev
         wall += time.perf_counter() - start
         done += k
     if record_every:
-        records.append(_compression_and_com(solver.stats()))
-    final = solver.stats()
+        records.append(_compression_and_com(solver))
+    final = solver.stats_array()
     solver.close()
     n = tankset.total_particles
     return {"wall_s": wall, "sim_s_particles_per_s": n * coarse_steps * COARSE_DT / wall,
-            "final_mean_compression": float(np.mean([s.mean_compression for s in final])), "records": records}
+            "final_mean_compression": float(final["mean_compression"].mean()), "records": records}
 
 
 def fallback_errors(learned: dict, plain: dict) -> dict:
