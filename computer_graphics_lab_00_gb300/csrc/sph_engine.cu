@@ -201,7 +201,7 @@ void Engine::release() {
                        rank_,          order_,        compact_ids_, compact_sorted_, compact_ranges_,
                        snap_pos_[0], snap_vel_[0],
                        snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_, correction_sums_,
-                       compact_rank_,  compact_order_};
+                       compact_rank_,  compact_order_, sx_tiles_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -1211,7 +1211,9 @@ int Engine::ensure_learned_buffers() {
     if ((status = alloc(&sforce_, total_capacity_)) != SPH_OK ||
         (status = alloc(&scorrection_, total_capacity_)) != SPH_OK ||
         (status = alloc(&correction_sums_, tanks_.size() * kCorrectionSumWords)) != SPH_OK ||
-        (status = alloc(&sfeatures_, static_cast<size_t>(total_capacity_) * 32)) != SPH_OK) {
+        (status = alloc(&sfeatures_, static_cast<size_t>(total_capacity_) * 32)) != SPH_OK ||
+        (status = alloc(&sx_tiles_, static_cast<size_t>((total_capacity_ + mlp::kTile - 1) / mlp::kTile) *
+                                        mlp::kXTileBytes)) != SPH_OK) {
         return status;
     }
     SPH_CUDA(mlp::prepare_forward());
@@ -1233,11 +1235,15 @@ int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launc
         return status;
     }
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
+    // The features go straight into the MLP's input tiles (normalised, BF16);
+    // with no model only the plain force is needed.
     SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.order,
-                             tuning_.masks, sforce_, sfeatures_, false, stream_));
+                             tuning_.masks, sforce_, nullptr, false, stream_,
+                             model != nullptr ? model->in_mean : nullptr, model != nullptr ? model->in_inv_std : nullptr,
+                             model != nullptr ? sx_tiles_ : nullptr));
     if (model != nullptr) {
-        SPH_CUDA(mlp::launch_forward(*model, sfeatures_, n, reinterpret_cast<float*>(scorrection_), nullptr,
-                                     &counters_->error_flags, stream_));
+        SPH_CUDA(mlp::launch_forward_tiles(*model, sx_tiles_, n, reinterpret_cast<float*>(scorrection_),
+                                           &counters_->error_flags, stream_));
         if (model->free_axes != 0) {
             // No net force along these axes: each tank's mean correction is removed.
             SPH_CUDA(launch_correction_sums(scorrection_, d_tanks_, stank_, n, static_cast<uint32_t>(tanks_.size()),

@@ -223,6 +223,7 @@ private:
     uint32_t* compact_order_ = nullptr;
     unsigned long long* correction_sums_ = nullptr;  // kCorrectionSumWords per tank
     float* sfeatures_ = nullptr;
+    uint8_t* sx_tiles_ = nullptr;  // the MLP's input tiles (learned steps)
     cudaGraphExec_t learned_graph_ = nullptr;
     uint32_t learned_graph_count_ = 0xFFFFFFFFu;
     bool learned_graph_has_model_ = false;

@@ -12,6 +12,7 @@
 // Compiled with --fmad=false; the explicit __f*_rn intrinsics state the
 // rounding of each operation.
 #include "sph_kernels.h"
+#include "sph_mlp.cuh"
 
 #include <type_traits>
 
@@ -1888,7 +1889,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const floa
                                                           const uint32_t* __restrict__ order,
                                                           const uint32_t* __restrict__ masks,
                                                           float4* __restrict__ force_out,
-                                                          float* __restrict__ features_out, int id_order) {
+                                                          float* __restrict__ features_out, int id_order,
+                                                          const float* __restrict__ norm_mean,
+                                                          const float* __restrict__ norm_inv_std,
+                                                          uint8_t* __restrict__ x_tiles) {
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
     __shared__ uint32_t list[kList][kBlock];
     const uint32_t slot = blockIdx.x * kBlock + threadIdx.x;
@@ -2020,11 +2024,31 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const floa
         f[29 + a] = fminf(fmaxf((__ldg(&t->high[a]) - pos[a]) * inv_h, 0.0f), 4.0f);
     }
     force_out[p] = make_float4(fx, fy, fz, 0.0f);
-    uint32_t row = id_order ? sorted_ids[p] : p;
-    float4* dst = reinterpret_cast<float4*>(features_out + static_cast<size_t>(row) * kFeatures);
+    if (x_tiles != nullptr) {
+        // The MLP's input row p: (f - mean) / std rounded to BF16, as the
+        // forward pass would convert it, in its tile layout.
+        uint8_t* tile = x_tiles + static_cast<size_t>(p / mlp::kTile) * mlp::kXTileBytes;
+        const uint32_t local = p % mlp::kTile;
 #pragma unroll
-    for (int q = 0; q < kFeatures / 4; ++q) {
-        dst[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+        for (uint32_t c = 0; c < kFeatures / 8; ++c) {
+            uint32_t word[4];
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k) {
+                const uint32_t a = 8 * c + 2 * k;
+                const float v0 = (f[a] - __ldg(&norm_mean[a])) * __ldg(&norm_inv_std[a]);
+                const float v1 = (f[a + 1] - __ldg(&norm_mean[a + 1])) * __ldg(&norm_inv_std[a + 1]);
+                const __nv_bfloat162 pair = __floats2bfloat162_rn(v0, v1);
+                word[k] = *reinterpret_cast<const uint32_t*>(&pair);
+            }
+            *reinterpret_cast<uint4*>(tile + mlp::x_tile_offset(local, c)) = make_uint4(word[0], word[1], word[2], word[3]);
+        }
+    } else if (features_out != nullptr) {
+        uint32_t row = id_order ? sorted_ids[p] : p;
+        float4* dst = reinterpret_cast<float4*>(features_out + static_cast<size_t>(row) * kFeatures);
+#pragma unroll
+        for (int q = 0; q < kFeatures / 4; ++q) {
+            dst[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+        }
     }
 }
 
@@ -2418,13 +2442,15 @@ cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_
 cudaError_t launch_features(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
                             const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* order,
                             const uint32_t* masks, float4* force, float* features, bool id_order,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, const float* norm_mean, const float* norm_inv_std,
+                            uint8_t* x_tiles) {
     if (n == 0) {
         return cudaSuccess;
     }
     // Seven blocks per SM (72 registers) rather than six at the 80 it takes unbounded.
     features_kernel<128, 48, 7><<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
-                                                                     order, masks, force, features, id_order ? 1 : 0);
+                                                                     order, masks, force, features, id_order ? 1 : 0,
+                                                                     norm_mean, norm_inv_std, x_tiles);
     return cudaGetLastError();
 }
 

@@ -180,10 +180,14 @@ cudaError_t launch_count_nonfinite(const float4* pos, const float4* vel, uint32_
 // Learned coarse step, first half: the plain SPH force per particle
 // (force[p], sorted order) and the 32 correction features (row p, or row
 // sorted_ids[p] when id_order). Needs the variant-4 pair masks of density.
+// With x_tiles the features go instead to the MLP's input tiles, normalised
+// by (norm_mean, norm_inv_std) and rounded to BF16 (row p); with neither
+// features nor x_tiles only the force is written.
 cudaError_t launch_features(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
                             const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* order,
                             const uint32_t* masks, float4* force, float* features, bool id_order,
-                            cudaStream_t stream);
+                            cudaStream_t stream, const float* norm_mean = nullptr,
+                            const float* norm_inv_std = nullptr, uint8_t* x_tiles = nullptr);
 // Net correction of each active tank: kCorrectionSumWords unsigned words per
 // tank (x, y, z sums in 2^-24 fixed point, two's complement, and the count),
 // zeroed first. Deterministic: integer sums do not depend on atomic order.

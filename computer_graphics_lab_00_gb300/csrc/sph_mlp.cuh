@@ -21,6 +21,15 @@ constexpr int kOut = 3;
 constexpr int kOutPad = 16;  // N of the last MMA (a multiple of 16 for M = 128)
 constexpr int kTile = 128;   // particles per MMA tile (M)
 
+// The forward pass's input tile: 128 rows of 32 normalised BF16 features in
+// the tcgen05 no-swizzle K-major layout (8-row x 16-byte core matrices);
+// x_tile_offset gives the byte offset of (row, 8-feature chunk) in a tile.
+// Tiles of consecutive rows follow one another, kXTileBytes apart.
+constexpr uint32_t kXTileBytes = kTile * kIn * 2;
+__host__ __device__ constexpr uint32_t x_tile_offset(uint32_t row, uint32_t chunk) {
+    return (row >> 3) * (kIn / 8u) * 128u + chunk * 128u + (row & 7u) * 16u;
+}
+
 // Offsets of the FP32 parameter vector (the layout the C ABI exposes):
 // W1[128][32], b1[128], W2[128][128], b2[128], W3[3][128], b3[3].
 constexpr int kW1 = 0;
@@ -59,6 +68,10 @@ constexpr uint32_t kWaitPolls = 1u << 22;
 
 cudaError_t launch_forward(const ModelView& model, const float* features, uint32_t n, float* out_accel,
                            const ForwardSaves* saves, unsigned int* error_flag, cudaStream_t stream);
+// Forward over ready input tiles (x_tiles: ceil(n / 128) tiles, as written by
+// the learned step's features kernel); output as launch_forward.
+cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles, uint32_t n, float* out_accel,
+                                 unsigned int* error_flag, cudaStream_t stream);
 // One CTA waits on an mbarrier (arrived at only when `arrive`) with at most
 // `polls` tries; sets *error_flag when the wait gives up.
 void launch_wait_selftest(uint32_t polls, int arrive, unsigned int* error_flag, cudaStream_t stream);

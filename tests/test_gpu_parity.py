@@ -392,7 +392,7 @@ def test_bad_tuning_is_rejected(native):
     case = W.dam_break_16k()
     with FluidSolverGpu(case.params, 16) as solver:
         for bad in (dict(block_size=100), dict(queue_depth=12), dict(neighbour_kernel=7), dict(radix_bits=0),
-                    dict(radix_bits=9), dict(schedule=2), dict(sort=2)):
+                    dict(radix_bits=9), dict(schedule=3), dict(sort=2)):
             with pytest.raises(abi.SphError) as e:
                 solver.set_tuning(**bad)
             assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
