@@ -584,151 +584,368 @@ __global__ void wait_selftest_kernel(uint32_t polls, int arrive, unsigned int* e
     }
 }
 
-// ---- backward on the CUDA cores (FP32) ---------------------------------------
+// ---- backward on the tensor cores ----------------------------------------------
+//
+// One persistent CTA per SM (512 threads, 512 TMEM columns) takes 128-row
+// tiles of the batch. Per tile, on the CUDA cores: dY from the loss, dZ2 =
+// (dY W3) * GELU'(z2) in FP32, rounded to BF16 into two shared-memory tiles,
+// one K-major over hidden units (for dH1) and one transposed, K-major over
+// the tile's rows (for dW2); the tile's H1, H2 and X rows are staged
+// transposed the same way, each with an appended row of ones, so that the
+// bias gradients come out of the same products. On the tensor cores
+// (tcgen05 kind::f16, FP32 accumulation):
+//   dH1[r][i]  = sum_c dZ2[r][c] W2[c][i]       (TMEM, per tile)
+//   dW2[o][i]  += sum_r dZ2[r][o] H1[r][i]      (+ db2 in column 128)
+//   dW3t[c][j] += sum_r H2[r][c] dY[r][j]
+// then dZ1 = dH1 * GELU'(z1) (FP32, rounded to BF16, transposed) and
+//   dW1[o][i]  += sum_r dZ1[r][o] X[r][i]       (+ db1 in column 32).
+// The weight gradients stay in TMEM across all of a CTA's tiles; at the end
+// each CTA writes one parameter-shaped partial, and partials are summed in CTA
+// order (deterministic). db3 and the loss are summed on the CUDA cores in a
+// fixed order. The BF16 roundings (dY for dW3, dZ2, dZ1) are those of the
+// oracle's loss_and_grad(..., bf16_grads=True).
 
-constexpr uint32_t kRowsPerChunk = 1024;
+constexpr uint32_t kBwThreads = 512;
+constexpr uint32_t kBwRows = 128;                              // K of the weight-gradient products
+constexpr uint32_t kBwH1Rows = kHidden + 16;                   // h1 rows, a row of ones, padding
+constexpr uint32_t kBwXRows = kIn + 16;                        // x rows, a row of ones, padding
+constexpr uint32_t kBwW2T = 0;                                 // W2 transposed [i][c]
+constexpr uint32_t kBwA = kBwW2T + kHidden * kHidden * 2;      // dZ2 [r][c], then dZ1 transposed [o][r]
+constexpr uint32_t kBwT2 = kBwA + kBwRows * kHidden * 2;       // dZ2 transposed [o][r]
+constexpr uint32_t kBwH1 = kBwT2 + kHidden * kBwRows * 2;      // H1 transposed + ones [i][r]
+constexpr uint32_t kBwH2 = kBwH1 + kBwH1Rows * kBwRows * 2;    // H2 transposed [c][r]
+constexpr uint32_t kBwDY = kBwH2 + kHidden * kBwRows * 2;      // dY transposed [j][r], rows 3..15 zero
+constexpr uint32_t kBwX = kBwDY + kOutPad * kBwRows * 2;       // X transposed + ones [i][r]
+constexpr uint32_t kBwW3 = kBwX + kBwXRows * kBwRows * 2;      // W3 as FP32 [3][128]
+constexpr uint32_t kBwRed = kBwW3 + kOut * kHidden * 4;        // per-quarter sums: dY (3) and loss
+constexpr uint32_t kBwBar = kBwRed + 64;
+constexpr uint32_t kBwBytes = kBwBar + 16;
+static_assert(kBwBytes <= 227u * 1024u, "one CTA's shared memory");
+// TMEM columns of the accumulators (starts at multiples of 32).
+constexpr uint32_t kBwColDH1 = 0;    // 128
+constexpr uint32_t kBwColDW2 = 128;  // 144: dW2 (128), db2 (1), padding
+constexpr uint32_t kBwColDW3 = 288;  // 16: dW3 transposed (3 used)
+constexpr uint32_t kBwColDW1 = 320;  // 48: dW1 (32), db1 (1), padding
+constexpr uint32_t kBwTmemCols = 512;
 
-// Per row: dY from the loss, dH2 = dY W3, dZ2 = dH2 * GELU'(z2), dH1 = dZ2 W2,
-// dZ1 = dH1 * GELU'(z1). Weights as the forward saw them (BF16 values).
-__global__ void __launch_bounds__(128) backward_rows_kernel(ModelView model, ForwardSaves saves,
-                                                            const float* __restrict__ targets, uint32_t n,
-                                                            float* __restrict__ dz1, float* __restrict__ dz2,
-                                                            float* __restrict__ dy_out, float* __restrict__ loss_parts) {
-    extern __shared__ float sm[];
-    float* w2 = sm;                          // [128][128]
-    float* w3 = w2 + kHidden * kHidden;      // [3][128]
-    float* rows = w3 + kOut * kHidden;       // [128 threads][128] dZ2 rows
-    __shared__ float block_loss[4];
-    for (uint32_t i = threadIdx.x; i < kHidden * kHidden; i += blockDim.x) {
-        w2[i] = __bfloat162float(model.w2[i]);
+// Byte offset of element (row, k) in a K-major no-swizzle tile of `k_elems`
+// BF16 elements a row.
+__device__ __forceinline__ uint32_t elem_offset(uint32_t row, uint32_t k, uint32_t k_elems) {
+    return tile_offset(row, k >> 3, k_elems) + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ void store_bf16(uint8_t* base, uint32_t offset, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(base + offset) = __float2bfloat16_rn(v);
+}
+
+__global__ void __launch_bounds__(kBwThreads, 1) mlp_backward_tc_kernel(ModelView model, ForwardSaves saves,
+                                                                        const float* __restrict__ targets, uint32_t n,
+                                                                        float* __restrict__ partial,
+                                                                        unsigned int* __restrict__ error_flag,
+                                                                        uint32_t wait_polls) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kBwBar);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kBwBar + 8);
+    float* w3f = reinterpret_cast<float*>(smem + kBwW3);
+    float* red = reinterpret_cast<float*>(smem + kBwRed);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5;
+    const uint32_t lane = tid & 31u;
+    const uint32_t quarter = warp & 3u;
+    const uint32_t group = warp >> 2;  // 32 columns each
+    const uint32_t local_row = quarter * 32u + lane;
+
+    // Staged once: W2 transposed, W3 as FP32, the constant rows.
+    for (uint32_t e = tid; e < kHidden * kHidden; e += blockDim.x) {
+        const uint32_t c = e / kHidden;
+        const uint32_t i = e % kHidden;
+        *reinterpret_cast<__nv_bfloat16*>(smem + kBwW2T + elem_offset(i, c, kHidden)) = model.w2[e];
     }
-    for (uint32_t i = threadIdx.x; i < kOut * kHidden; i += blockDim.x) {
-        w3[i] = __bfloat162float(model.w3[i]);
+    for (uint32_t e = tid; e < kOut * kHidden; e += blockDim.x) {
+        w3f[e] = __bfloat162float(model.w3[e]);
     }
+    for (uint32_t e = tid; e < 16u * kBwRows; e += blockDim.x) {
+        const uint32_t extra = e / kBwRows;
+        const uint32_t r = e % kBwRows;
+        store_bf16(smem + kBwH1, elem_offset(kHidden + extra, r, kBwRows), extra == 0 ? 1.0f : 0.0f);
+        store_bf16(smem + kBwX, elem_offset(kIn + extra, r, kBwRows), extra == 0 ? 1.0f : 0.0f);
+        if (extra < kOutPad - kOut) {
+            store_bf16(smem + kBwDY, elem_offset(kOut + extra, r, kBwRows), 0.0f);
+        }
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kBwTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
-    uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    float local_loss = 0.0f;
-    if (m < n) {
-        float4 y = reinterpret_cast<const float4*>(saves.y)[m];
-        float yv[3] = {y.x, y.y, y.z};
-        float dy[3];
-        const float inv = 2.0f / (static_cast<float>(n) * kOut);
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_base = (quarter * 32u) << 16;
+    constexpr uint32_t idesc_dh1 = instr_desc(kTile, kHidden);
+    constexpr uint32_t idesc_dw2 = instr_desc(kTile, kBwH1Rows);
+    constexpr uint32_t idesc_dw3 = instr_desc(kTile, kOutPad);
+    constexpr uint32_t idesc_dw1 = instr_desc(kTile, kBwXRows);
+    const uint32_t sA = smem_u32(smem + kBwA);
+    const uint32_t sT2 = smem_u32(smem + kBwT2);
+    const uint32_t sH1 = smem_u32(smem + kBwH1);
+    const uint32_t sH2 = smem_u32(smem + kBwH2);
+    const uint32_t sDY = smem_u32(smem + kBwDY);
+    const uint32_t sX = smem_u32(smem + kBwX);
+    const uint32_t sW2T = smem_u32(smem + kBwW2T);
+    constexpr uint32_t kSbo = (kBwRows / 8u) * 128u;  // K = 128 in every product
+    const float inv = 2.0f / (static_cast<float>(n) * kOut);
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    uint32_t parity = 0;
+    bool failed = false;
+    bool first = true;
+    float cta_dy[3] = {0.0f, 0.0f, 0.0f};  // thread 0: db3 of this CTA's rows
+    float cta_loss = 0.0f;
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const uint32_t row = tile * kTile + local_row;
+        const bool valid = row < n;
+        // dY and the row's squared error.
+        float dy[3] = {0.0f, 0.0f, 0.0f};
+        float err2 = 0.0f;
+        if (valid) {
+            const float4 y = reinterpret_cast<const float4*>(saves.y)[row];
+            const float yv[3] = {y.x, y.y, y.z};
 #pragma unroll
-        for (int o = 0; o < kOut; ++o) {
-            float t = targets[static_cast<size_t>(m) * kOut + o] / model.out_scale[o];
-            float e = yv[o] - t;
-            local_loss += e * e;
-            dy[o] = inv * e;
-            dy_out[static_cast<size_t>(m) * 4 + o] = dy[o];
-        }
-        float* row = rows + threadIdx.x * kHidden;
-        for (int k = 0; k < kHidden; ++k) {
-            float dh2 = dy[0] * w3[k] + dy[1] * w3[kHidden + k] + dy[2] * w3[2 * kHidden + k];
-            float d = dh2 * gelu_grad(saves.z2[static_cast<size_t>(m) * kHidden + k]);
-            row[k] = d;
-            dz2[static_cast<size_t>(m) * kHidden + k] = d;
-        }
-        for (int k = 0; k < kHidden; ++k) {
-            float acc = 0.0f;
-            for (int j = 0; j < kHidden; ++j) {
-                acc += row[j] * w2[j * kHidden + k];
+            for (uint32_t o = 0; o < kOut; ++o) {
+                const float t = targets[static_cast<size_t>(row) * kOut + o] / model.out_scale[o];
+                const float e = yv[o] - t;
+                err2 += e * e;
+                dy[o] = inv * e;
             }
-            dz1[static_cast<size_t>(m) * kHidden + k] = acc * gelu_grad(saves.z1[static_cast<size_t>(m) * kHidden + k]);
         }
-        local_loss /= static_cast<float>(n) * kOut;
+        if (group == 0) {
+#pragma unroll
+            for (uint32_t j = 0; j < kOut; ++j) {
+                store_bf16(smem + kBwDY, elem_offset(j, local_row, kBwRows), dy[j]);
+            }
+            float sums[4] = {dy[0], dy[1], dy[2], err2};
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sums[q] += __shfl_down_sync(0xFFFFFFFFu, sums[q], o);
+                }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) {
+                    red[quarter * 4u + q] = sums[q];
+                }
+            }
+        }
+        // dZ2 for this thread's 32 columns, and the transposed H1 and H2 rows.
+#pragma unroll 1
+        for (uint32_t cc = 0; cc < 2; ++cc) {
+            const uint32_t c0 = group * 32u + cc * 16u;
+            float d[16];
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                const uint32_t c = c0 + k;
+                const float dh2 = dy[0] * w3f[c] + dy[1] * w3f[kHidden + c] + dy[2] * w3f[2 * kHidden + c];
+                d[k] = valid ? dh2 * gelu_grad(saves.z2[static_cast<size_t>(row) * kHidden + c]) : 0.0f;
+            }
+            store_chunk(smem + kBwA, tile_offset(local_row, c0 / 8u, kHidden), d);
+            store_chunk(smem + kBwA, tile_offset(local_row, c0 / 8u + 1u, kHidden), d + 8);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                store_bf16(smem + kBwT2, elem_offset(c0 + k, local_row, kBwRows), d[k]);
+            }
+            uint4 h1v[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+            uint4 h2v[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+            if (valid) {
+                const uint4* h1row = reinterpret_cast<const uint4*>(saves.h1 + static_cast<size_t>(row) * kHidden + c0);
+                const uint4* h2row = reinterpret_cast<const uint4*>(saves.h2 + static_cast<size_t>(row) * kHidden + c0);
+                h1v[0] = h1row[0];
+                h1v[1] = h1row[1];
+                h2v[0] = h2row[0];
+                h2v[1] = h2row[1];
+            }
+            const __nv_bfloat16* h1e = reinterpret_cast<const __nv_bfloat16*>(h1v);
+            const __nv_bfloat16* h2e = reinterpret_cast<const __nv_bfloat16*>(h2v);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                *reinterpret_cast<__nv_bfloat16*>(smem + kBwH1 + elem_offset(c0 + k, local_row, kBwRows)) = h1e[k];
+                *reinterpret_cast<__nv_bfloat16*>(smem + kBwH2 + elem_offset(c0 + k, local_row, kBwRows)) = h2e[k];
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t acc = first ? 0u : 1u;
+#pragma unroll
+            for (uint32_t k = 0; k < kHidden / 16; ++k) {
+                mma_bf16(tmem + kBwColDH1, smem_desc(sA + k * 256u, 128u, (kHidden / 8) * 128u),
+                         smem_desc(sW2T + k * 256u, 128u, (kHidden / 8) * 128u), idesc_dh1, k > 0 ? 1u : 0u);
+            }
+#pragma unroll
+            for (uint32_t k = 0; k < kBwRows / 16; ++k) {
+                mma_bf16(tmem + kBwColDW2, smem_desc(sT2 + k * 256u, 128u, kSbo), smem_desc(sH1 + k * 256u, 128u, kSbo),
+                         idesc_dw2, k > 0 ? 1u : acc);
+                mma_bf16(tmem + kBwColDW3, smem_desc(sH2 + k * 256u, 128u, kSbo), smem_desc(sDY + k * 256u, 128u, kSbo),
+                         idesc_dw3, k > 0 ? 1u : acc);
+            }
+            mma_commit(mbar);
+            // db3 and the loss of this tile, quarters in order.
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                cta_dy[0] += red[q * 4u];
+                cta_dy[1] += red[q * 4u + 1u];
+                cta_dy[2] += red[q * 4u + 2u];
+                cta_loss += red[q * 4u + 3u];
+            }
+        }
+        bool ok = mbar_wait(mbar, parity, wait_polls);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        // dZ1 = dH1 * GELU'(z1), transposed into the A tile; the X rows.
+#pragma unroll 1
+        for (uint32_t cc = 0; cc < 2; ++cc) {
+            const uint32_t c0 = group * 32u + cc * 16u;
+            float v[16];
+            tmem_load16(tmem + lane_base + kBwColDH1 + c0, v);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                const uint32_t i = c0 + k;
+                const float d1 = valid ? v[k] * gelu_grad(saves.z1[static_cast<size_t>(row) * kHidden + i]) : 0.0f;
+                store_bf16(smem + kBwA, elem_offset(i, local_row, kBwRows), d1);
+            }
+        }
+        if (group == 0) {
+            uint4 xv[4] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0),
+                           make_uint4(0, 0, 0, 0)};
+            if (valid) {
+                const uint4* xrow = reinterpret_cast<const uint4*>(saves.x + static_cast<size_t>(row) * kIn);
+#pragma unroll
+                for (uint32_t q = 0; q < 4; ++q) {
+                    xv[q] = xrow[q];
+                }
+            }
+            const __nv_bfloat16* xe = reinterpret_cast<const __nv_bfloat16*>(xv);
+#pragma unroll
+            for (uint32_t i = 0; i < kIn; ++i) {
+                *reinterpret_cast<__nv_bfloat16*>(smem + kBwX + elem_offset(i, local_row, kBwRows)) = xe[i];
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (uint32_t k = 0; k < kBwRows / 16; ++k) {
+                mma_bf16(tmem + kBwColDW1, smem_desc(sA + k * 256u, 128u, kSbo), smem_desc(sX + k * 256u, 128u, kSbo),
+                         idesc_dw1, k > 0 ? 1u : (first ? 0u : 1u));
+            }
+            mma_commit(mbar);
+        }
+        ok = mbar_wait(mbar, parity, wait_polls);
+        if (!__syncthreads_and(ok)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u;
+        tc_fence_after();
+        first = false;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        local_loss += __shfl_down_sync(0xFFFFFFFFu, local_loss, o);
+    float* part = partial + static_cast<size_t>(blockIdx.x) * (kParams + 1);
+    if (failed) {
+        if (tid == 0) {
+            atomicOr(error_flag, 1u);
+        }
+        // Let an MMA still in flight finish (bounded) before the columns go.
+        mbar_wait(mbar, parity, wait_polls);
+        tc_fence_before();
+        __syncthreads();
+    } else if (first) {
+        // No tile for this CTA: a zero partial.
+        for (uint32_t e = tid; e < kParams + 1; e += blockDim.x) {
+            part[e] = 0.0f;
+        }
+    } else {
+        // The accumulators: lane o of each product is output row o.
+        const uint32_t o = local_row;
+        for (uint32_t ch = group; ch < kBwH1Rows / 16u; ch += 4u) {
+            float v[16];
+            tmem_load16(tmem + lane_base + kBwColDW2 + ch * 16u, v);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                const uint32_t col = ch * 16u + k;
+                if (col < kHidden) {
+                    part[kW2 + o * kHidden + col] = v[k];
+                } else if (col == kHidden) {
+                    part[kB2 + o] = v[k];
+                }
+            }
+        }
+        if (group == 0) {
+            float v[16];
+            tmem_load16(tmem + lane_base + kBwColDW3, v);
+#pragma unroll
+            for (uint32_t j = 0; j < kOut; ++j) {
+                part[kW3 + j * kHidden + o] = v[j];
+            }
+        }
+        if (group < kBwXRows / 16u) {
+            float v[16];
+            tmem_load16(tmem + lane_base + kBwColDW1 + group * 16u, v);
+#pragma unroll
+            for (uint32_t k = 0; k < 16; ++k) {
+                const uint32_t col = group * 16u + k;
+                if (col < kIn) {
+                    part[kW1 + o * kIn + col] = v[k];
+                } else if (col == kIn) {
+                    part[kB1 + o] = v[k];
+                }
+            }
+        }
+        if (tid == 0) {
+            part[kB3] = cta_dy[0];
+            part[kB3 + 1] = cta_dy[1];
+            part[kB3 + 2] = cta_dy[2];
+            part[kParams] = cta_loss / (static_cast<float>(n) * kOut);
+        }
+        tc_fence_before();
+        __syncthreads();
     }
-    if ((threadIdx.x & 31) == 0) {
-        block_loss[threadIdx.x >> 5] = local_loss;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        loss_parts[blockIdx.x] = block_loss[0] + block_loss[1] + block_loss[2] + block_loss[3];
+    tc_fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBwTmemCols) : "memory");
     }
 }
 
-// partial[chunk][o][k] = sum over the chunk's rows of dz[m][o] * in[m][k]
-// (k == in_dim stands for the bias input 1). One 32 x 32 (o, k) tile per
-// block; fixed order, so the result is deterministic.
-__global__ void __launch_bounds__(256) weight_grad_kernel(const float* __restrict__ dz, uint32_t dz_stride,
-                                                          const __nv_bfloat16* __restrict__ in, uint32_t in_dim,
-                                                          uint32_t out_dim, uint32_t n, float* __restrict__ partial) {
-    __shared__ float sdz[32][33];
-    __shared__ float sin[32][33];
-    const uint32_t chunk = blockIdx.x;
-    const uint32_t o0 = blockIdx.y * 32;
-    const uint32_t k0 = blockIdx.z * 32;
-    const uint32_t tx = threadIdx.x & 31;  // k
-    const uint32_t ty = threadIdx.x >> 5;  // 0..7 -> o = ty + 8 j
-    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    const uint32_t first = chunk * kRowsPerChunk;
-    const uint32_t last = min(first + kRowsPerChunk, n);
-    for (uint32_t base = first; base < last; base += 32) {
-        for (uint32_t e = threadIdx.x; e < 32 * 32; e += blockDim.x) {
-            uint32_t r = e >> 5;
-            uint32_t c = e & 31;
-            uint32_t m = base + r;
-            bool row_ok = m < last;
-            sdz[r][c] = (row_ok && o0 + c < out_dim) ? dz[static_cast<size_t>(m) * dz_stride + o0 + c] : 0.0f;
-            float x = 0.0f;
-            if (row_ok) {
-                uint32_t k = k0 + c;
-                x = k < in_dim ? __bfloat162float(in[static_cast<size_t>(m) * in_dim + k]) : (k == in_dim ? 1.0f : 0.0f);
-            }
-            sin[r][c] = x;
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (uint32_t r = 0; r < 32; ++r) {
-            float x = sin[r][tx];
-#pragma unroll
-            for (uint32_t j = 0; j < 4; ++j) {
-                acc[j] += sdz[r][ty + 8 * j] * x;
-            }
-        }
-        __syncthreads();
-    }
-    const uint32_t cols = in_dim + 1;
-#pragma unroll
-    for (uint32_t j = 0; j < 4; ++j) {
-        uint32_t o = o0 + ty + 8 * j;
-        uint32_t k = k0 + tx;
-        if (o < out_dim && k < cols) {
-            partial[(static_cast<size_t>(chunk) * out_dim + o) * cols + k] = acc[j];
-        }
-    }
-}
-
-// Sums the chunk partials in chunk order into the parameter gradient: W part
-// at grad[w_off + o * in_dim + k], bias at grad[b_off + o].
-__global__ void reduce_grad_kernel(const float* __restrict__ partial, uint32_t chunks, uint32_t out_dim, uint32_t in_dim,
-                                   float* __restrict__ grad, uint32_t w_off, uint32_t b_off) {
-    uint32_t cols = in_dim + 1;
-    uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= out_dim * cols) {
+// grads[p] = sum over CTAs (in order) of the partials; loss likewise.
+__global__ void reduce_partials_kernel(const float* __restrict__ partial, uint32_t ctas, float* __restrict__ grads,
+                                       float* __restrict__ loss) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p > static_cast<uint32_t>(kParams)) {
         return;
     }
     float s = 0.0f;
-    for (uint32_t c = 0; c < chunks; ++c) {
-        s += partial[static_cast<size_t>(c) * out_dim * cols + idx];
+    for (uint32_t c = 0; c < ctas; ++c) {
+        s += partial[static_cast<size_t>(c) * (kParams + 1) + p];
     }
-    uint32_t o = idx / cols;
-    uint32_t k = idx % cols;
-    if (k < in_dim) {
-        grad[w_off + o * in_dim + k] = s;
+    if (p < static_cast<uint32_t>(kParams)) {
+        grads[p] = s;
     } else {
-        grad[b_off + o] = s;
-    }
-}
-
-__global__ void loss_sum_kernel(const float* __restrict__ parts, uint32_t count, float* __restrict__ loss) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        float s = 0.0f;
-        for (uint32_t i = 0; i < count; ++i) {
-            s += parts[i];
-        }
         *loss = s;
     }
 }
@@ -866,57 +1083,33 @@ cudaError_t prepare_forward() {
 }
 
 size_t backward_scratch_floats(uint32_t n) {
-    uint32_t chunks = (n + kRowsPerChunk - 1) / kRowsPerChunk;
-    size_t partial = static_cast<size_t>(chunks) * kHidden * (kHidden + 1);
-    return 2 * static_cast<size_t>(n) * kHidden + 4 * static_cast<size_t>(n) + partial + (n + 127) / 128 + 64;
+    // One parameter-shaped partial (+ loss) per CTA; at most one CTA a tile.
+    const size_t tiles = (static_cast<size_t>(n) + kTile - 1) / kTile;
+    return (tiles == 0 ? 1 : tiles) * (kParams + 1);
 }
 
 cudaError_t launch_backward(const ModelView& model, const ForwardSaves& saves, const float* targets, uint32_t n,
-                            float* d_params, float* loss, float* scratch, cudaStream_t stream) {
+                            float* d_params, float* loss, float* scratch, unsigned int* error_flag,
+                            cudaStream_t stream) {
     if (n == 0) {
         return cudaSuccess;
     }
-    float* dz1 = scratch;
-    float* dz2 = dz1 + static_cast<size_t>(n) * kHidden;
-    float* dy = dz2 + static_cast<size_t>(n) * kHidden;
-    uint32_t chunks = (n + kRowsPerChunk - 1) / kRowsPerChunk;
-    float* partial = dy + 4 * static_cast<size_t>(n);
-    float* loss_parts = partial + static_cast<size_t>(chunks) * kHidden * (kHidden + 1);
-    uint32_t blocks = (n + 127) / 128;
-    size_t smem = (kHidden * kHidden + kOut * kHidden + 128 * kHidden) * sizeof(float);
-    cudaError_t attr = once_per_device(&g_backward_ready, [smem] {
-        return cudaFuncSetAttribute(backward_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(smem));
+    cudaError_t attr = once_per_device(&g_backward_ready, [] {
+        return cudaFuncSetAttribute(mlp_backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(kBwBytes));
     });
     if (attr != cudaSuccess) {
         return attr;
     }
-    backward_rows_kernel<<<blocks, 128, smem, stream>>>(model, saves, targets, n, dz1, dz2, dy, loss_parts);
-    loss_sum_kernel<<<1, 32, 0, stream>>>(loss_parts, blocks, loss);
-    struct Layer {
-        const float* dz;
-        uint32_t stride;
-        const __nv_bfloat16* in;
-        uint32_t in_dim;
-        uint32_t out_dim;
-        uint32_t w_off;
-        uint32_t b_off;
-    };
-    const Layer layers[3] = {
-        {dy, 4, saves.h2, static_cast<uint32_t>(kHidden), static_cast<uint32_t>(kOut), static_cast<uint32_t>(kW3),
-         static_cast<uint32_t>(kB3)},
-        {dz2, static_cast<uint32_t>(kHidden), saves.h1, static_cast<uint32_t>(kHidden),
-         static_cast<uint32_t>(kHidden), static_cast<uint32_t>(kW2), static_cast<uint32_t>(kB2)},
-        {dz1, static_cast<uint32_t>(kHidden), saves.x, static_cast<uint32_t>(kIn), static_cast<uint32_t>(kHidden),
-         static_cast<uint32_t>(kW1), static_cast<uint32_t>(kB1)},
-    };
-    for (const Layer& l : layers) {
-        dim3 grid(chunks, (l.out_dim + 31) / 32, (l.in_dim + 1 + 31) / 32);
-        weight_grad_kernel<<<grid, 256, 0, stream>>>(l.dz, l.stride, l.in, l.in_dim, l.out_dim, n, partial);
-        uint32_t entries = l.out_dim * (l.in_dim + 1);
-        reduce_grad_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(partial, chunks, l.out_dim, l.in_dim, d_params,
-                                                                      l.w_off, l.b_off);
-    }
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    int device = 0;
+    cudaGetDevice(&device);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const uint32_t ctas = std::min<uint32_t>(tiles, static_cast<uint32_t>(sms));
+    mlp_backward_tc_kernel<<<ctas, kBwThreads, kBwBytes, stream>>>(model, saves, targets, n, scratch, error_flag,
+                                                                   kWaitPolls);
+    reduce_partials_kernel<<<(kParams + 1 + 255) / 256, 256, 0, stream>>>(scratch, ctas, d_params, loss);
     return cudaGetLastError();
 }
 
@@ -1059,7 +1252,7 @@ int gradients(sph_mlp* m, const void* features, const void* targets, uint32_t n)
     MLP_CUDA(m, sph::mlp::launch_forward(v, static_cast<const float*>(features), n, nullptr, &saves, m->error,
                                          m->stream));
     MLP_CUDA(m, sph::mlp::launch_backward(v, saves, static_cast<const float*>(targets), n, m->grads, m->loss,
-                                          m->scratch, m->stream));
+                                          m->scratch, m->error, m->stream));
     return SPH_OK;
 }
 

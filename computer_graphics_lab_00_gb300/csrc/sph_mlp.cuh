@@ -1,11 +1,10 @@
 // sph_mlp.cuh — the learned acceleration correction: a 32 -> 128 -> 128 -> 3
 // MLP with GELU, BF16 weights and FP32 accumulation.
 //
-// Forward runs on the 5th-generation tensor cores: tcgen05.mma (kind::f16,
-// BF16 operands from shared memory, FP32 accumulators in tensor memory),
-// 128 particles per MMA tile. Backward and Adam run on the CUDA cores in FP32
-// (the weight gradients are reductions over the batch; training is a one-off
-// cost next to inference in every learned step).
+// Forward and backward run on the 5th-generation tensor cores: tcgen05.mma
+// (kind::f16, BF16 operands from shared memory, FP32 accumulators in tensor
+// memory), 128 particles per MMA tile; the elementwise parts and Adam run on
+// the CUDA cores in FP32.
 #pragma once
 
 #include <cstdint>
@@ -76,13 +75,17 @@ cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles,
 // `polls` tries; sets *error_flag when the wait gives up.
 void launch_wait_selftest(uint32_t polls, int arrive, unsigned int* error_flag, cudaStream_t stream);
 
-// Backward of the mean squared error on normalised targets, FP32.
-// d_params receives the gradient of the FP32 parameter vector; loss (device,
-// one float) the mean squared error. scratch holds 2 * n * 128 floats plus
-// kParams * kChunks floats for the deterministic batch reduction.
+// Backward of the mean squared error on normalised targets on the tensor
+// cores: dH1 = dZ2 W2 and the weight and bias gradients as tcgen05 products
+// with FP32 accumulation (dY for W3, dZ2 and dZ1 rounded to BF16 on the way
+// in), the elementwise parts in FP32. d_params receives the gradient of the
+// FP32 parameter vector and loss (device, one float) the mean squared error;
+// scratch holds backward_scratch_floats(n) floats. A tensor-core wait that
+// gives up sets *error_flag.
 size_t backward_scratch_floats(uint32_t n);
 cudaError_t launch_backward(const ModelView& model, const ForwardSaves& saves, const float* targets, uint32_t n,
-                            float* d_params, float* loss, float* scratch, cudaStream_t stream);
+                            float* d_params, float* loss, float* scratch, unsigned int* error_flag,
+                            cudaStream_t stream);
 
 // Adam (src/gfx/neural_math.cpp:1177-1208) on the FP32 vector, then the
 // BF16 weight copies are refreshed from it.

@@ -88,21 +88,28 @@ def forward(params, features, mean, std, scale, bf16_rounding=True):
     return y, cache
 
 
-def loss_and_grad(params, features, targets, mean, std, scale, bf16_rounding=True):
-    """Mean squared error on normalised targets and its gradient (double)."""
+def loss_and_grad(params, features, targets, mean, std, scale, bf16_rounding=True, bf16_grads=False):
+    """Mean squared error on normalised targets and its gradient (double).
+
+    bf16_grads rounds the backward's operands to BF16 where the GPU's
+    tensor-core backward does: dY on its way into the W3 gradient (its bias
+    gradient sums the unrounded dY), dZ2 (computed from the unrounded dY)
+    into the W2 and b2 gradients and into dH1 = dZ2 W2, and dZ1 into the W1
+    and b1 gradients."""
     y, c = forward(params, features, mean, std, scale, bf16_rounding)
     t = np.asarray(targets, np.float64) / np.asarray(scale, np.float64)
     n = y.shape[0]
     e = y - t
     loss = float((e * e).sum() / (n * OUT))
     dy = 2.0 * e / (n * OUT)
+    r = (lambda a: bf16(np.asarray(a, np.float32)).astype(np.float64)) if bf16_grads else (lambda a: a)
     g = np.zeros(PARAMS)
-    g[W3:B3] = (dy.T @ c["h2"]).reshape(-1)
+    g[W3:B3] = (r(dy).T @ c["h2"]).reshape(-1)
     g[B3:PARAMS] = dy.sum(0)
-    dz2 = (dy @ c["w3"]) * gelu_grad(c["z2"])
+    dz2 = r((dy @ c["w3"]) * gelu_grad(c["z2"]))
     g[W2:B2] = (dz2.T @ c["h1"]).reshape(-1)
     g[B2:W3] = dz2.sum(0)
-    dz1 = (dz2 @ c["w2"]) * gelu_grad(c["z1"])
+    dz1 = r((dz2 @ c["w2"]) * gelu_grad(c["z1"]))
     g[W1:B1] = (dz1.T @ c["x"]).reshape(-1)
     g[B1:W2] = dz1.sum(0)
     return loss, g

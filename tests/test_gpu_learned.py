@@ -116,3 +116,28 @@ def test_trained_correction_beats_the_plain_coarse_step(native, particles):
     assert np.isfinite(learned["mean_density_error"]) and np.isfinite(learned["mean_com_drift_m"])
     assert learned["mean_density_error"] < plain["mean_density_error"], cmp
     assert learned["mean_com_drift_m"] < plain["mean_com_drift_m"], cmp
+
+
+@pytest.mark.parametrize("axes", [7, 5, 0])
+def test_net_force_free_axes_take_each_tank_mean_off_exactly(native, small, axes):
+    """A model whose output is the constant (0.5, -0.25, 0.125) in every row
+    (all weights zero; the last bias is the output, exactly representable in
+    the 2^-24 fixed point of the tank sums). With all three axes net-force
+    free each correction minus its tank's mean is +0, so the learned step is
+    the plain substep bit for bit; with an axis kept, it is not."""
+    from computer_graphics_lab_00_gb300.learned import PARAMS, MlpGpu
+
+    with MlpGpu(seed=1) as mlp:
+        params = np.zeros(PARAMS, np.float32)
+        params[-3:] = [0.5, -0.25, 0.125]
+        mlp.set_params(params)
+        mlp.set_normalisation(np.zeros(32, np.float32), np.ones(32, np.float32), np.ones(3, np.float32))
+        mlp.set_net_force_free(axes)
+        a = T.load_tanks(small)
+        b = T.load_tanks(small)
+        a.run_learned(T.COARSE_DT, 2, mlp)
+        b.run_learned(T.COARSE_DT, 2, None)
+        equal = all(same(x, y) for t in range(len(small.counts)) for x, y in zip(a.download(t), b.download(t)))
+        a.close()
+        b.close()
+    assert equal == (axes == 7)
