@@ -761,6 +761,7 @@ int Engine::ensure_graph() {
     if (status != SPH_OK) {
         return status;
     }
+    SPH_CUDA(prepare_staged_integrate());
     cudaGraph_t graph = nullptr;
     SPH_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     uint32_t launches = 0;
@@ -1518,11 +1519,14 @@ int Engine::selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t*
 
 int Engine::set_tuning(const NeighbourTuning& tuning) {
     bool queue_ok = tuning.queue == 8 || tuning.queue == 16 || tuning.queue == 24 || tuning.queue == 32;
-    if (tuning.variant > 5 || tuning.block < 32 || tuning.block > 512 || tuning.block % 32 != 0 || !queue_ok ||
+    if (tuning.variant > 6 || tuning.block < 32 || tuning.block > 512 || tuning.block % 32 != 0 || !queue_ok ||
         static_cast<size_t>(tuning.queue) * tuning.block * sizeof(uint32_t) > 48 * 1024) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     if (tuning.variant >= 2 && tuning.block != 64 && tuning.block != 128 && tuning.block != 256) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (tuning.variant == 6 && tuning.block != 128 && tuning.block != 256) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     NeighbourTuning kept = tuning_;

@@ -14,6 +14,7 @@
 #include "sph_kernels.h"
 #include "sph_mlp.cuh"
 
+#include <mutex>
 #include <type_traits>
 
 namespace sph {
@@ -1437,6 +1438,364 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(cons
                     sorted_ids[p], pos_out, vel_out);
 }
 
+// ---- shared-memory-staged integrate ----------------------------------------
+//
+// A block owns kThreads consecutive processing slots; in the Morton or
+// Hilbert order they fill a compact run of cells, whose 27-bucket
+// neighbourhoods overlap. Before any pair force the block copies the sorted
+// position/density and velocity/pressure of every non-empty bucket its
+// particles visit, each bucket once, into shared memory (cp.async, 16 bytes
+// a lane, L1 bypassed), so the pairs read shared memory instead of gathering
+// each neighbour through L1 and L2. Buckets are deduplicated by a shared
+// hash table that one lane per run of same-cell lanes fills. A block whose
+// buckets overflow the table or the data area reads global memory instead,
+// with the same lists.
+//
+// Each lane lists its pairs from density's masks in (bucket, slot) order
+// while the copies are in flight, up to kList of them; after the copies land
+// it runs the list, then lists and runs the rest of its walk in list-sized
+// rounds. The pairs go through add_pair_force_rcp in the reference's order,
+// so every bit equals integrate_mask_kernel's (fluid_sph.cpp:234-258).
+
+namespace staged {
+
+constexpr uint32_t kEmptyKey = 0xFFFFFFFFu;  // bucket keys are below the bucket total (< 2^32 - 1)
+constexpr uint32_t kSlack = 32;              // data entries past kCap: a bad list entry stays in bounds
+
+__device__ __forceinline__ uint32_t table_slot(uint32_t key, uint32_t bits) {
+    return (key * 0x9E3779B1u) >> (32u - bits);
+}
+
+__device__ __forceinline__ void copy16_async(void* dst_shared, const void* src_global) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(dst_shared))),
+                 "l"(src_global)
+                 : "memory");
+}
+
+__device__ __forceinline__ void copies_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Global bucket index of neighbour b (the walk order of neighbour_range).
+__device__ __forceinline__ uint32_t neighbour_key(uint32_t cx, uint32_t cy, uint32_t cz, uint32_t b, uint32_t mask,
+                                                  uint32_t base) {
+    const uint32_t dz = b / 9u;
+    const uint32_t dy = (b / 3u) % 3u;
+    const uint32_t dx = b % 3u;
+    return base + spatial_hash(cx + dx - 1u, cy + dy - 1u, cz + dz - 1u, mask);
+}
+
+// Shared-memory layout (bytes). The region after the table holds the pair
+// lists (u16 data indices, [kList][kThreads]); before them, while the table
+// is built, it holds each slot's bucket start, count, the occupied slots in
+// order and the scan's warp totals. The global-memory path keeps u32 lists
+// in the (then unused) data area.
+template <uint32_t kThreads, uint32_t kList, uint32_t kCap, uint32_t kTable>
+struct Layout {
+    static constexpr uint32_t kWarps = kThreads / 32u;
+    static constexpr size_t kEntries = static_cast<size_t>(kCap) + kSlack;
+    static constexpr size_t kPos = 0;
+    static constexpr size_t kVel = kPos + kEntries * 16u;
+    static constexpr size_t kKey = kVel + kEntries * 16u;
+    static constexpr size_t kOff = kKey + static_cast<size_t>(kTable) * 4u;
+    static constexpr size_t kRegion = kOff + static_cast<size_t>(kTable) * 2u;
+    static constexpr size_t kStart = kRegion;
+    static constexpr size_t kCnt = kStart + static_cast<size_t>(kTable) * 4u;
+    static constexpr size_t kOcc = kCnt + static_cast<size_t>(kTable);
+    static constexpr size_t kMisc = kOcc + static_cast<size_t>(kTable) * 2u;
+    static constexpr size_t kBuildEnd = kMisc + (2u + kWarps) * 4u;
+    static constexpr size_t kListEnd = kRegion + static_cast<size_t>(kList) * kThreads * 2u;
+    static constexpr size_t kBytes = kBuildEnd > kListEnd ? kBuildEnd : kListEnd;
+    static_assert(kThreads % 32u == 0 && kTable % kThreads == 0 && kTable % 4u == 0, "table split by thread");
+    static_assert(kTable * kCellCapacity < 65536u, "scan packs entries and slots in one word");
+    static_assert(kCap + kSlack <= 65536u, "data indices are 16-bit");
+    static_assert(static_cast<size_t>(kList) * kThreads * 4u <= kEntries * 32u, "global lists fit the data area");
+    static_assert(kList >= kCellCapacity, "a list takes a whole bucket");
+};
+
+}  // namespace staged
+
+template <uint32_t kThreads, uint32_t kList, uint32_t kCap, uint32_t kTableBits, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) integrate_staged_kernel(
+    const float4* __restrict__ spos2, const float4* __restrict__ svel, const uint32_t* __restrict__ sorted_ids,
+    const uint2* __restrict__ bucket, const TankConst* __restrict__ tanks, const uint16_t* __restrict__ stank,
+    uint32_t n, const uint32_t* __restrict__ order, const uint32_t* __restrict__ masks, float4* __restrict__ pos_out,
+    float4* __restrict__ vel_out) {
+    constexpr uint32_t kTable = 1u << kTableBits;
+    using L = staged::Layout<kThreads, kList, kCap, kTable>;
+    constexpr uint32_t kPer = kTable / kThreads;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float4* s_pos = reinterpret_cast<float4*>(smem + L::kPos);
+    float4* s_vel = reinterpret_cast<float4*>(smem + L::kVel);
+    uint32_t* s_key = reinterpret_cast<uint32_t*>(smem + L::kKey);
+    uint16_t* s_off = reinterpret_cast<uint16_t*>(smem + L::kOff);
+    uint16_t* s_list = reinterpret_cast<uint16_t*>(smem + L::kRegion);
+    uint32_t* g_list = reinterpret_cast<uint32_t*>(smem + L::kPos);
+    uint32_t* s_start = reinterpret_cast<uint32_t*>(smem + L::kStart);
+    uint8_t* s_cnt = smem + L::kCnt;
+    uint16_t* s_occ = reinterpret_cast<uint16_t*>(smem + L::kOcc);
+    uint32_t* s_misc = reinterpret_cast<uint32_t*>(smem + L::kMisc);  // [0] table full, [2 + w] warp totals
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31u;
+    const uint32_t warp = tid >> 5;
+    const uint32_t slot = blockIdx.x * kThreads + tid;
+    uint32_t p = slot;
+    if (order != nullptr && p < n) {
+        p = order[p];
+    }
+    bool valid = p < n;
+    const uint32_t tank = valid && stank != nullptr ? stank[p] : 0u;
+    const TankConst* t = tanks + tank;
+    valid = valid && __ldg(&t->active) != 0;
+    for (uint32_t i = tid; i < kTable; i += kThreads) {
+        s_key[i] = staged::kEmptyKey;
+        s_off[i] = 0;
+    }
+    if (tid == 0) {
+        s_misc[0] = 0;
+    }
+    PairConst k{};
+    uint32_t cell_mask = 0;
+    uint32_t base = 0;
+    uint32_t cx = 0;
+    uint32_t cy = 0;
+    uint32_t cz = 0;
+    float4 self = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 self_vel = self;
+    if (valid) {
+        k.h = __ldg(&t->h);
+        k.c_spiky = __ldg(&t->c_spiky);
+        k.c_visc = __ldg(&t->c_visc);
+        k.neg_mass = __ldg(&t->neg_mass);
+        k.visc_mass = __ldg(&t->visc_mass);
+        cell_mask = __ldg(&t->cell_mask);
+        base = __ldg(&t->bucket_base);
+        self = spos2[p];
+        self_vel = svel[p];
+        cx = static_cast<uint32_t>(cell_coord(self.x, k.h));
+        cy = static_cast<uint32_t>(cell_coord(self.y, k.h));
+        cz = static_cast<uint32_t>(cell_coord(self.z, k.h));
+    }
+    __syncthreads();
+
+    // 1. The first lane of each run of lanes in one cell (of one tank) enters
+    //    the cell's non-empty buckets into the table.
+    {
+        const uint32_t pcx = __shfl_up_sync(0xFFFFFFFFu, cx, 1);
+        const uint32_t pcy = __shfl_up_sync(0xFFFFFFFFu, cy, 1);
+        const uint32_t pcz = __shfl_up_sync(0xFFFFFFFFu, cz, 1);
+        const uint32_t ptank = __shfl_up_sync(0xFFFFFFFFu, tank, 1);
+        const uint32_t vmask = __ballot_sync(0xFFFFFFFFu, valid);
+        const bool prev_valid = lane > 0 && ((vmask >> (lane - 1u)) & 1u) != 0;
+        const bool leader = valid && (!prev_valid || pcx != cx || pcy != cy || pcz != cz || ptank != tank);
+        if (leader) {
+            // Nine bucket ranges at a time, loaded back to back.
+#pragma unroll
+            for (uint32_t dz = 0; dz < 3u; ++dz) {
+                uint32_t keys[9];
+                uint2 ranges[9];
+#pragma unroll
+                for (uint32_t j = 0; j < 9u; ++j) {
+                    keys[j] = staged::neighbour_key(cx, cy, cz, 9u * dz + j, cell_mask, base);
+                    ranges[j] = __ldg(&bucket[keys[j]]);
+                }
+#pragma unroll
+                for (uint32_t j = 0; j < 9u; ++j) {
+                    const uint32_t key = keys[j];
+                    const uint32_t cnt = min(ranges[j].y - ranges[j].x, kCellCapacity);
+                    if (cnt == 0) {
+                        continue;
+                    }
+                    uint32_t h = staged::table_slot(key, kTableBits);
+                    uint32_t probe = 0;
+                    for (; probe < kTable; ++probe) {
+                        const uint32_t old = atomicCAS(&s_key[h], staged::kEmptyKey, key);
+                        if (old == staged::kEmptyKey) {
+                            s_start[h] = ranges[j].x;
+                            s_cnt[h] = static_cast<uint8_t>(cnt);
+                            break;
+                        }
+                        if (old == key) {
+                            break;
+                        }
+                        h = (h + 1u) & (kTable - 1u);
+                    }
+                    if (probe == kTable) {
+                        atomicOr(&s_misc[0], 1u);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // 2. Data offsets: a block-wide scan of (entries << 16 | slots) over the
+    //    table, kPer consecutive slots a thread.
+    uint32_t mine = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; ++j) {
+        const uint32_t s = tid * kPer + j;
+        if (s_key[s] != staged::kEmptyKey) {
+            mine += (static_cast<uint32_t>(s_cnt[s]) << 16) | 1u;
+        }
+    }
+    uint32_t inclusive = mine;
+#pragma unroll
+    for (uint32_t o = 1; o < 32u; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inclusive, o);
+        if (lane >= o) {
+            inclusive += v;
+        }
+    }
+    if (lane == 31u) {
+        s_misc[2u + warp] = inclusive;
+    }
+    __syncthreads();
+    uint32_t before = inclusive - mine;
+    uint32_t total = 0;
+    for (uint32_t w = 0; w < L::kWarps; ++w) {
+        const uint32_t v = s_misc[2u + w];
+        before += w < warp ? v : 0u;
+        total += v;
+    }
+    const uint32_t occupied = total & 0xFFFFu;
+    // Block-uniform: every thread read the same words after the barrier.
+    const bool staged_data = s_misc[0] == 0 && (total >> 16) <= kCap;
+    if (staged_data) {
+        uint32_t e = before >> 16;
+        uint32_t o = before & 0xFFFFu;
+#pragma unroll
+        for (uint32_t j = 0; j < kPer; ++j) {
+            const uint32_t s = tid * kPer + j;
+            if (s_key[s] != staged::kEmptyKey) {
+                s_off[s] = static_cast<uint16_t>(e);
+                s_occ[o] = static_cast<uint16_t>(s);
+                e += s_cnt[s];
+                ++o;
+            }
+        }
+    }
+    __syncthreads();
+
+    // 3. Copies: a warp per bucket, a lane per entry.
+    if (staged_data) {
+        for (uint32_t q = warp; q < occupied; q += L::kWarps) {
+            const uint32_t s = s_occ[q];
+            if (lane < s_cnt[s]) {
+                const uint32_t src = s_start[s] + lane;
+                const uint32_t dst = static_cast<uint32_t>(s_off[s]) + lane;
+                staged::copy16_async(s_pos + dst, spos2 + src);
+                staged::copy16_async(s_vel + dst, svel + src);
+            }
+        }
+    }
+    __syncthreads();  // the build arrays are dead: the region holds the lists now
+
+    // 4. Lists and pairs. The first list comes from the 27 mask words loaded
+    //    back to back; a walk longer than one list reloads the rest.
+    uint32_t words[27];
+#pragma unroll
+    for (uint32_t b = 0; b < 27u; ++b) {
+        words[b] = valid ? __ldg(&masks[static_cast<size_t>(b) * n + slot]) : 0u;
+    }
+    auto walk = [&](auto data_form) {
+        constexpr bool kShared = decltype(data_form)::value;
+        auto append = [&](uint32_t b, uint32_t word, uint32_t& listed) {
+            const uint32_t key = staged::neighbour_key(cx, cy, cz, b, cell_mask, base);
+            uint32_t first;
+            if constexpr (kShared) {
+                uint32_t h = staged::table_slot(key, kTableBits);
+                for (uint32_t probe = 0; probe < kTable && s_key[h] != key; ++probe) {
+                    h = (h + 1u) & (kTable - 1u);
+                }
+                first = s_off[h];
+            } else {
+                first = __ldg(&bucket[key]).x;
+            }
+            while (word != 0) {
+                const uint32_t s = static_cast<uint32_t>(__ffs(word) - 1);
+                word &= word - 1u;
+                if constexpr (kShared) {
+                    s_list[listed * kThreads + tid] = static_cast<uint16_t>(first + s);
+                } else {
+                    g_list[listed * kThreads + tid] = first + s;
+                }
+                ++listed;
+            }
+        };
+        // The first list: buckets 0.. until one would not fit (b_next).
+        auto fill_first = [&](uint32_t& b_next) -> uint32_t {
+            uint32_t listed = 0;
+            uint32_t stop = 27u;
+#pragma unroll
+            for (uint32_t b = 0; b < 27u; ++b) {
+                const uint32_t word = words[b];
+                if (stop != 27u || word == 0) {
+                    continue;
+                }
+                if (listed + static_cast<uint32_t>(__popc(word)) > kList) {
+                    stop = b;
+                    continue;
+                }
+                append(b, word, listed);
+            }
+            b_next = stop;
+            return listed;
+        };
+        // A later list: buckets b_next.. (masks reloaded).
+        auto fill_rest = [&](uint32_t& b_next) -> uint32_t {
+            uint32_t listed = 0;
+            for (; b_next < 27u; ++b_next) {
+                const uint32_t word = __ldg(&masks[static_cast<size_t>(b_next) * n + slot]);
+                if (word == 0) {
+                    continue;
+                }
+                if (listed + static_cast<uint32_t>(__popc(word)) > kList) {
+                    break;
+                }
+                append(b_next, word, listed);
+            }
+            return listed;
+        };
+        float fx = 0.0f;
+        float fy = 0.0f;
+        float fz = 0.0f;
+        auto run = [&](uint32_t listed) {
+            for (uint32_t e = 0; e < listed; ++e) {
+                if constexpr (kShared) {
+                    const uint32_t q = s_list[e * kThreads + tid];
+                    add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, s_pos[q], s_vel[q],
+                                       fx, fy, fz);
+                } else {
+                    const uint32_t q = g_list[e * kThreads + tid];
+                    add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                                       __ldg(&svel[q]), fx, fy, fz);
+                }
+            }
+        };
+        uint32_t b = 27u;
+        const uint32_t listed = valid ? fill_first(b) : 0u;
+        if constexpr (kShared) {
+            staged::copies_wait_all();
+        }
+        __syncthreads();  // every lane's copies have landed
+        if (!valid) {
+            return;
+        }
+        run(listed);
+        while (b < 27u) {
+            run(fill_rest(b));
+        }
+        finish_particle(t, self, max_like_std(self.w, 1e-6f), self_vel.x, self_vel.y, self_vel.z, self_vel.w, fx, fy,
+                        fz, sorted_ids[p], pos_out, vel_out);
+    };
+    if (staged_data) {
+        walk(std::true_type{});
+    } else {
+        walk(std::false_type{});
+    }
+}
+
 // ---- cell-cooperative variant ------------------------------------------------
 //
 // A warp owns 32 consecutive processing slots. Consecutive slots whose
@@ -2239,6 +2598,58 @@ __global__ void division_selftest_kernel(uint64_t seed, uint64_t count, int mode
 
 }  // namespace
 
+namespace {
+
+// The staged integrate shapes: 128 threads with 1,248 data entries (55 KB of
+// shared memory, four blocks an SM) or 256 threads with 2,016 (94 KB, two).
+// The data areas hold a 99th-percentile block of the 1M dam break (973 and
+// 1,419 entries on average, 1,245 and 1,842 at the 99th percentile).
+#define SPH_STAGED_128 128u, 48u, 1248u, 9u, 4
+#define SPH_STAGED_256 256u, 48u, 2016u, 10u, 2
+
+template <uint32_t kThreads, uint32_t kList, uint32_t kCap, uint32_t kTableBits, int kMinBlocks>
+constexpr size_t staged_bytes() {
+    return staged::Layout<kThreads, kList, kCap, (1u << kTableBits)>::kBytes;
+}
+
+std::mutex g_staged_guard;
+uint64_t g_staged_ready = 0;  // bit d: the attributes are set on device d
+
+template <uint32_t kThreads, uint32_t kList, uint32_t kCap, uint32_t kTableBits, int kMinBlocks>
+cudaError_t launch_staged(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
+                          const TankConst* tanks, const uint16_t* stank, uint32_t n, const uint32_t* order,
+                          const uint32_t* masks, float4* pos, float4* vel, cudaStream_t stream) {
+    constexpr size_t bytes = staged_bytes<kThreads, kList, kCap, kTableBits, kMinBlocks>();
+    integrate_staged_kernel<kThreads, kList, kCap, kTableBits, kMinBlocks>
+        <<<(n + kThreads - 1) / kThreads, kThreads, bytes, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
+                                                                     order, masks, pos, vel);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t prepare_staged_integrate() {
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    std::lock_guard<std::mutex> lock(g_staged_guard);
+    if (device < 64 && (g_staged_ready >> device & 1u) != 0) {
+        return cudaSuccess;
+    }
+    e = cudaFuncSetAttribute(integrate_staged_kernel<SPH_STAGED_128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(staged_bytes<SPH_STAGED_128>()));
+    if (e == cudaSuccess) {
+        e = cudaFuncSetAttribute(integrate_staged_kernel<SPH_STAGED_256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(staged_bytes<SPH_STAGED_256>()));
+    }
+    if (e == cudaSuccess && device < 64) {
+        g_staged_ready |= 1ull << device;
+    }
+    return e;
+}
+
 cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, const uint2* bucket, const TankConst* tanks,
                            const uint16_t* stank, uint32_t n, StepCounters* counters, cudaStream_t stream,
                            const NeighbourTuning& tuning) {
@@ -2265,7 +2676,7 @@ cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, cons
         }
         return cudaGetLastError();
     }
-    if (tuning.variant == 4) {
+    if (tuning.variant == 4 || tuning.variant == 6) {
         uint32_t blocks = (n + 127) / 128;
         if (counters != nullptr) {
             density_mask_kernel<true><<<blocks, 128, 0, stream>>>(spos, svel, spos2, bucket, tanks, stank, n,
@@ -2316,6 +2727,18 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
         integrate_coop_kernel<1><<<blocks, kCoopWarps * 32u, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n,
                                                                         tuning.order, tuning.masks, pos, vel);
         return cudaGetLastError();
+    }
+    if (tuning.variant == 6) {
+        const cudaError_t prepared = prepare_staged_integrate();
+        if (prepared != cudaSuccess) {
+            return prepared;
+        }
+        if (tuning.block == 256) {
+            return launch_staged<SPH_STAGED_256>(spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order,
+                                                 tuning.masks, pos, vel, stream);
+        }
+        return launch_staged<SPH_STAGED_128>(spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order,
+                                             tuning.masks, pos, vel, stream);
     }
     if (tuning.variant == 4) {
         switch (tuning.block) {

@@ -130,7 +130,9 @@ cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* so
 // them (reciprocal divisions); 5: cell-cooperative (a warp's particles of one
 // cell share a candidate list in shared memory; density stores chunk-major
 // masks over that list, 27 words per particle at most, and integrate
-// computes the listed pairs one per lane). block: threads per block of integrate
+// computes the listed pairs one per lane); 6: the masks of 4, and an
+// integrate that stages every bucket its block visits in shared memory once
+// (block 128 or 256). block: threads per block of integrate
 // (64/128/256 for variants 2-3); queue: in-range pairs buffered per thread
 // (variant 1: 8, 16, 24 or 32). pair_list / pair_count / list_cap: the
 // per-particle pair lists of variants 2-3 (device buffers the engine owns).
@@ -154,6 +156,10 @@ cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, cons
 
 // Forces, semi-implicit Euler, speed clamp and walls (fluid_sph.cpp:225-305).
 // Writes the id-order state.
+// Sets the shared-memory attributes of the staged integrate (variant 6) on the
+// current device, once; call before capturing a launch of it.
+cudaError_t prepare_staged_integrate();
+
 cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint32_t* sorted_ids, const uint2* bucket,
                              const TankConst* tanks, const uint16_t* stank, uint32_t n, float4* pos, float4* vel,
                              cudaStream_t stream, const NeighbourTuning& tuning);

@@ -130,9 +130,11 @@ typedef struct sph_tuning {
                                   3: as 2, divisions through a shared correctly rounded reciprocal;
                                   4: density stores per-bucket pair masks, integrate expands them;
                                   5: cell-cooperative: the particles of a cell share one candidate list in
-                                     shared memory, lanes take candidates (density) and pairs (integrate) */
+                                     shared memory, lanes take candidates (density) and pairs (integrate);
+                                  6: the masks of 4; integrate copies every bucket its block visits into
+                                     shared memory once and reads the pairs there (Morton or Hilbert order) */
     uint32_t block_size;       /* threads per block of integrate (32..512, multiple of 32; 64/128/256 for 2-4;
-                                  default 128) */
+                                  128/256 for 6; default 128) */
     uint32_t queue_depth;      /* in-range pairs buffered per thread: 8, 16, 24 or 32 */
     uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 (default) Morton order of
                                   the cells; 2 Hilbert order of the cells; orders 1 and 2 are remade every

@@ -28,7 +28,7 @@ def state_digest(pos: np.ndarray, vel: np.ndarray) -> tuple[str, str]:
             hashlib.sha256(np.ascontiguousarray(vel, np.float32).tobytes()).hexdigest())
 
 
-@pytest.mark.parametrize("neighbour_kernel", [4, 5])
+@pytest.mark.parametrize("neighbour_kernel", [4, 5, 6])
 def test_1m_dam_break_1000_substeps_is_the_reference_run(native, neighbour_kernel):
     golden = json.loads(GOLDEN.read_text())
     case = W.dam_break_1m()

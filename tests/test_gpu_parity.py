@@ -136,7 +136,8 @@ def test_ragged_counts_bit_exact(native, oracle, n):
     assert_bit_exact(gv, ov, f"velocities n={n}")
 
 
-def test_overflowing_bucket_keeps_first_32_ids(native, oracle):
+@pytest.mark.parametrize("variant", [4, 6])
+def test_overflowing_bucket_keeps_first_32_ids(native, oracle, variant):
     """More than 32 particles in one cell: only the first 32 by id are
     neighbours (fluid_sph.cpp:179-187); counts stay un-truncated."""
     params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
@@ -149,6 +150,7 @@ def test_overflowing_bucket_keeps_first_32_ids(native, oracle):
     pos[:, 3] = 1000.0
     vel = np.zeros((n, 4), np.float32)
     with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(neighbour_kernel=variant)
         solver.upload(pos, vel)
         solver.build_grid()
         grid = solver.grid()
@@ -162,13 +164,16 @@ def test_overflowing_bucket_keeps_first_32_ids(native, oracle):
     assert_bit_exact(gv, ov, "velocities with an overflowing bucket")
 
 
-def test_hash_collisions_and_duplicate_buckets(native, oracle):
+@pytest.mark.parametrize("variant,schedule", [(4, 1), (6, 1), (6, 0)])
+def test_hash_collisions_and_duplicate_buckets(native, oracle, variant, schedule):
     """With few buckets, neighbour cells collide and the same bucket is
     visited twice for one particle; the reference counts it twice and so
-    must the kernels."""
+    must the kernels (the staged integrate copies such a bucket once and
+    reads it for both neighbours)."""
     n = 8192
     params, pos, vel = small_block(n, (16, 16, 32), box=(0.5, 0.8, 0.8), cells=1024)
     with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(neighbour_kernel=variant, schedule=schedule)
         solver.upload(pos, vel)
         solver.run(1.0 / 600.0, 5)
         gp, gv = solver.state()
@@ -322,6 +327,10 @@ def test_errors_are_status_codes(native):
     dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=2, sort=1),
     dict(neighbour_kernel=3, block_size=256, queue_depth=16, radix_bits=6, schedule=2, sort=0),
     dict(neighbour_kernel=5, block_size=128, queue_depth=16, radix_bits=8, schedule=2, sort=1),
+    dict(neighbour_kernel=6, block_size=128, queue_depth=16, radix_bits=8, schedule=1, sort=1),
+    dict(neighbour_kernel=6, block_size=256, queue_depth=16, radix_bits=7, schedule=2, sort=1),
+    dict(neighbour_kernel=6, block_size=128, queue_depth=16, radix_bits=6, schedule=0, sort=0),
+    dict(neighbour_kernel=6, block_size=256, queue_depth=32, radix_bits=8, schedule=1, sort=0),
 ])
 def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     """Every launch shape the autotuner may pick gives the oracle's bits."""
@@ -391,7 +400,8 @@ def test_grid_sorts_agree_at_one_million(native, oracle, sort, bits):
 def test_bad_tuning_is_rejected(native):
     case = W.dam_break_16k()
     with FluidSolverGpu(case.params, 16) as solver:
-        for bad in (dict(block_size=100), dict(queue_depth=12), dict(neighbour_kernel=7), dict(radix_bits=0),
+        for bad in (dict(block_size=100), dict(queue_depth=12), dict(neighbour_kernel=7), dict(neighbour_kernel=6, block_size=64),
+                    dict(radix_bits=0),
                     dict(radix_bits=9), dict(schedule=3), dict(sort=2)):
             with pytest.raises(abi.SphError) as e:
                 solver.set_tuning(**bad)
@@ -463,7 +473,8 @@ def test_pair_list_overflow_falls_back_bit_exact(native, oracle):
     vel = np.zeros((n, 4), np.float32)
     for variant, schedule, block, queue in ((2, 0, 256, 32), (3, 1, 256, 32), (4, 0, 256, 32), (4, 1, 256, 32),
                                             (4, 0, 256, 24), (4, 0, 256, 16), (4, 0, 128, 32), (4, 0, 64, 32),
-                                            (5, 0, 128, 32), (5, 1, 128, 32)):
+                                            (5, 0, 128, 32), (5, 1, 128, 32), (6, 0, 128, 32), (6, 1, 128, 32),
+                                            (6, 2, 256, 32)):
         with FluidSolverGpu(params, n) as solver:
             solver.set_tuning(neighbour_kernel=variant, schedule=schedule, block_size=block, queue_depth=queue)
             solver.upload(pos, vel)

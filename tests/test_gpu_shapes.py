@@ -85,7 +85,7 @@ def test_obstacle_course_1m_two_substeps(native, oracle):
     assert_same(gv, ov, "velocities")
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 def test_every_neighbour_kernel_with_shapes(native, oracle, variant):
     case = W.obstacle_course()
     pos, vel = case.initial_state()
