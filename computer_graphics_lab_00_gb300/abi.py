@@ -305,6 +305,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_run_learned": (c_int, [c_void_p, c_f32, c_u32, c_void_p]),
         "sph_batch_run_learned": (c_int, [c_void_p, c_f32, c_u32, c_void_p]),
         "sph_batch_learned_features": (c_int, [c_void_p, c_f32, c_void_p]),
+        "sph_batch_learned_correction": (c_int, [c_void_p, c_f32, c_void_p, c_void_p]),
         "sph_batch_learned_check": (c_int, [c_void_p]),
         "sph_batch_snapshot": (c_int, [c_void_p, c_u32, c_int]),
         "sph_batch_restore_tanks": (c_int, [c_void_p, c_u32, u8p]),

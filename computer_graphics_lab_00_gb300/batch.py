@@ -181,6 +181,13 @@ class BatchSolverGpu:
         self._check(self._lib.sph_batch_learned_features(self._handle, ctypes.c_float(dt),
                                                          ctypes.c_void_p(features_ptr)), "sph_batch_learned_features")
 
+    def learned_correction(self, dt: float, mlp, correction_ptr: int) -> None:
+        """The correction (float4 per particle, id order, device) a learned
+        substep of length dt would add to the current state."""
+        self._check(self._lib.sph_batch_learned_correction(self._handle, ctypes.c_float(dt), mlp.handle,
+                                                           ctypes.c_void_p(correction_ptr)),
+                    "sph_batch_learned_correction")
+
     def learned_check(self) -> None:
         self._check(self._lib.sph_batch_learned_check(self._handle), "sph_batch_learned_check")
 

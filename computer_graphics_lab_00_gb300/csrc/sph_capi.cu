@@ -764,6 +764,14 @@ int sph_batch_learned_features(sph_batch* batch, float dt, void* features) {
     return batch->engine.learned_features(dt, static_cast<float*>(features));
 }
 
+int sph_batch_learned_correction(sph_batch* batch, float dt, const sph_mlp* mlp, void* correction) {
+    sph::mlp::ModelView view{};
+    if (batch == nullptr || mlp == nullptr || !sph_mlp_model_view(mlp, &view)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    return batch->engine.learned_correction(dt, view, static_cast<float4*>(correction));
+}
+
 int sph_batch_learned_check(sph_batch* batch) {
     if (batch == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;

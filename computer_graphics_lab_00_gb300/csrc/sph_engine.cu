@@ -1370,6 +1370,42 @@ int Engine::learned_features(float dt, float* features) {
     return SPH_OK;
 }
 
+// The correction of a learned substep from the current state, through the
+// learned step's own kernels (BF16 input tiles, the tiled forward pass), in
+// id order; the state does not change.
+int Engine::learned_correction(float dt, const mlp::ModelView& model, float4* correction) {
+    if (correction == nullptr || !(dt > 0.0F)) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    if (total_count_ == 0) {
+        return SPH_OK;
+    }
+    SPH_CUDA(cudaSetDevice(device_));
+    int status = ensure_learned_buffers();
+    if (status == SPH_OK) {
+        status = refresh_constants(dt);
+    }
+    if (status == SPH_OK) {
+        status = enqueue_grid(nullptr);
+    }
+    if (status != SPH_OK) {
+        return status;
+    }
+    uint32_t n = total_count_;
+    NeighbourTuning masked = tuning_;
+    masked.variant = 4;
+    SPH_CUDA(mlp::prepare_forward());
+    SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
+    SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.order,
+                             tuning_.masks, sforce_, nullptr, false, stream_, model.in_mean, model.in_inv_std,
+                             sx_tiles_));
+    SPH_CUDA(mlp::launch_forward_tiles(model, sx_tiles_, n, reinterpret_cast<float*>(scorrection_),
+                                       &counters_->error_flags, stream_));
+    SPH_CUDA(launch_scatter_rows(scorrection_, grid_.sorted_ids, n, correction, stream_));
+    grid_valid_ = true;
+    return learned_error();
+}
+
 int Engine::build_grid() {
     SPH_CUDA(cudaSetDevice(device_));
     int status = refresh_constants(const_dt_ < 0.0F ? 0.0F : const_dt_);

@@ -77,6 +77,7 @@ public:
     int run_learned(float dt, uint32_t substeps, const mlp::ModelView* model);
     // Correction features of the current state, id order, n x 32 (device).
     int learned_features(float dt, float* features);
+    int learned_correction(float dt, const mlp::ModelView& model, float4* correction);
     // SPH_ERR_TIMEOUT if a tensor-core wait gave up since the last check.
     int learned_error();
     uint32_t learned_launches_per_substep() const { return learned_launches_; }

@@ -2628,6 +2628,27 @@ cudaError_t launch_staged(const float4* spos2, const float4* svel, const uint32_
 
 }  // namespace
 
+namespace {
+
+__global__ void __launch_bounds__(256) scatter_rows_kernel(const float4* __restrict__ src,
+                                                           const uint32_t* __restrict__ ids, uint32_t n,
+                                                           float4* __restrict__ dst) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) {
+        dst[ids[p]] = src[p];
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_scatter_rows(const float4* src, const uint32_t* ids, uint32_t n, float4* dst, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    scatter_rows_kernel<<<(n + 255) / 256, 256, 0, stream>>>(src, ids, n, dst);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_staged_integrate() {
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);

@@ -156,6 +156,9 @@ cudaError_t launch_density(const float4* spos, float4* svel, float4* spos2, cons
 
 // Forces, semi-implicit Euler, speed clamp and walls (fluid_sph.cpp:225-305).
 // Writes the id-order state.
+// dst[ids[p]] = src[p] for p < n (sorted order to id order).
+cudaError_t launch_scatter_rows(const float4* src, const uint32_t* ids, uint32_t n, float4* dst, cudaStream_t stream);
+
 // Sets the shared-memory attributes of the staged integrate (variant 6) on the
 // current device, once; call before capturing a launch of it.
 cudaError_t prepare_staged_integrate();

@@ -199,6 +199,31 @@ __device__ __forceinline__ void bias_gelu2(float v0, float v1, float b0, float b
     unpack2(z, z0, z1);
 }
 
+// Twice GELU for two columns: z + z tanh(z (a + b z^2)), one multiply fewer
+// than bias_gelu2; the layer that reads it takes its weights halved, which
+// leaves every BF16 product, and so every sum, as it was (power-of-two
+// scalings are exact).
+__device__ __forceinline__ void bias_gelu2_twice(float v0, float v1, float b0, float b1, float& g0, float& g1) {
+    const f32x2 z = add2(pack2(v0, v1), pack2(b0, b1));
+    const f32x2 inner = fma2(mul2(z, z), pack2(kGeluB, kGeluB), pack2(kGeluA, kGeluA));
+    float t0, t1;
+    unpack2(mul2(z, inner), t0, t1);
+    unpack2(fma2(z, pack2(tanh_approx(t0), tanh_approx(t1)), z), g0, g1);
+}
+
+// Halves eight BF16 values (exact for normal numbers).
+__device__ __forceinline__ uint4 halve_bf16x8(uint4 q) {
+    uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162*>(&w[i]);
+        const float2 f = __bfloat1622float2(v);
+        v = __floats2bfloat162_rn(0.5f * f.x, 0.5f * f.y);
+        w[i] = *reinterpret_cast<uint32_t*>(&v);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 constexpr uint32_t kForwardThreads = 512;
 constexpr uint32_t kGroups = kForwardThreads / 128;  // threads sharing one row's epilogue
 
@@ -547,6 +572,311 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     tc_fence_after();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// ---- warp-specialised forward, two tiles in flight ----------------------------
+//
+// The inference form over ready BF16 input tiles (the learned step's). One
+// persistent CTA per SM: 16 epilogue warps and one issuing warp, two tile
+// slots, each with its own 128 TMEM columns, X and H buffers and barriers.
+// The issuing warp's first lane copies input tiles in and issues each
+// layer's MMAs as soon as the slot's operands are ready; the epilogue warps
+// take each finished layer (+bias, GELU, BF16 into H; the output at the end)
+// and report back. While the tensor cores run one slot's layer the CUDA
+// cores run the other slot's epilogue, and no step waits on a block-wide
+// barrier:
+//   issuer, per pair k and slot s: [done(s, k-1)] load -> L1 ; h1 -> next load, L2 ; h2 -> L3
+//   epilogue warps:                mma -> E1 -> h1 ; mma -> E2 -> h2 ; mma -> E3 -> done
+// Per tile the operations are mlp_forward_kernel's, so the output bits are
+// the same.
+constexpr uint32_t kPairW1 = 0;
+constexpr uint32_t kPairW2 = kPairW1 + kHidden * kIn * 2;
+constexpr uint32_t kPairW3 = kPairW2 + kHidden * kHidden * 2;
+constexpr uint32_t kPairX = kPairW3 + kOutPad * kHidden * 2;        // two input tiles
+constexpr uint32_t kPairHBytes = kTile * kHidden * 2;
+constexpr uint32_t kPairH = kPairX + 2 * kXTileBytes;                // two hidden tiles
+constexpr uint32_t kPairBar = kPairH + 2 * kPairHBytes;              // 10 barriers, TMEM address
+constexpr uint32_t kPairVec = kPairBar + 128;
+constexpr uint32_t kPairBytes = kPairVec + kVecFloats * 4;
+constexpr uint32_t kPairTmemCols = 256;
+constexpr uint32_t kEpilogueWarps = kForwardThreads / 32;            // 16
+constexpr uint32_t kWsThreads = kForwardThreads + 32;                // + the issuing warp
+
+// Weights into the canonical K-major layout (16-byte chunks) and the small
+// FP32 vectors (b1, b2, input mean and 1/std, b3, output scale).
+// half_w23: W2 and W3 halved (the epilogues then store twice GELU).
+__device__ __forceinline__ void stage_model(const ModelView& model, uint8_t* smem, uint32_t w1, uint32_t w2, uint32_t w3,
+                                            float* vec, uint32_t tid, uint32_t threads, bool half_w23) {
+    for (uint32_t c = tid; c < kHidden * (kIn / 8); c += threads) {
+        const uint32_t row = c / (kIn / 8);
+        const uint32_t chunk = c % (kIn / 8);
+        *reinterpret_cast<uint4*>(smem + w1 + tile_offset(row, chunk, kIn)) =
+            *reinterpret_cast<const uint4*>(model.w1 + row * kIn + chunk * 8);
+    }
+    for (uint32_t c = tid; c < kHidden * (kHidden / 8); c += threads) {
+        const uint32_t row = c / (kHidden / 8);
+        const uint32_t chunk = c % (kHidden / 8);
+        const uint4 q = *reinterpret_cast<const uint4*>(model.w2 + row * kHidden + chunk * 8);
+        *reinterpret_cast<uint4*>(smem + w2 + tile_offset(row, chunk, kHidden)) = half_w23 ? halve_bf16x8(q) : q;
+    }
+    for (uint32_t c = tid; c < kOutPad * (kHidden / 8); c += threads) {
+        const uint32_t row = c / (kHidden / 8);
+        const uint32_t chunk = c % (kHidden / 8);
+        const uint4 q = *reinterpret_cast<const uint4*>(model.w3 + row * kHidden + chunk * 8);
+        *reinterpret_cast<uint4*>(smem + w3 + tile_offset(row, chunk, kHidden)) = half_w23 ? halve_bf16x8(q) : q;
+    }
+    for (uint32_t i = tid; i < kVecFloats; i += threads) {
+        float v = 0.0f;
+        if (i < kVecB2) {
+            v = model.params[kB1 + i];
+        } else if (i < kVecMean) {
+            v = model.params[kB2 + (i - kVecB2)];
+        } else if (i < kVecInvStd) {
+            v = model.in_mean[i - kVecMean];
+        } else if (i < kVecB3) {
+            v = model.in_inv_std[i - kVecInvStd];
+        } else if (i < kVecScale) {
+            v = i - kVecB3 < static_cast<uint32_t>(kOut) ? model.params[kB3 + (i - kVecB3)] : 0.0f;
+        } else {
+            v = i - kVecScale < static_cast<uint32_t>(kOut) ? model.out_scale[i - kVecScale] : 0.0f;
+        }
+        vec[i] = v;
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+__global__ void __launch_bounds__(kWsThreads, 1) mlp_forward_ws_kernel(ModelView model,
+                                                                       const uint8_t* __restrict__ x_tiles, uint32_t n,
+                                                                       float* __restrict__ out,
+                                                                       unsigned int* __restrict__ error_flag,
+                                                                       uint32_t wait_polls) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kPairBar);
+    uint64_t* load_bar = bars;      // [2] input tile landed (transaction bytes)
+    uint64_t* mma_bar = bars + 2;   // [2] a layer's MMAs completed (three phases a pair)
+    uint64_t* h1_bar = bars + 4;    // [2] epilogue 1 written (16 warp arrivals)
+    uint64_t* h2_bar = bars + 6;    // [2] epilogue 2 written
+    uint64_t* done_bar = bars + 8;  // [2] output read, the slot's columns free
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kPairBar + 80);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5;
+    const uint32_t lane = tid & 31u;
+    float* vec = reinterpret_cast<float*>(smem + kPairVec);
+    stage_model(model, smem, kPairW1, kPairW2, kPairW3, vec, tid, blockDim.x, true);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kPairTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (uint32_t s = 0; s < 2; ++s) {
+            mbar_init(&load_bar[s], 1);
+            mbar_init(&mma_bar[s], 1);
+            mbar_init(&h1_bar[s], kEpilogueWarps);
+            mbar_init(&h2_bar[s], kEpilogueWarps);
+            mbar_init(&done_bar[s], kEpilogueWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tiles = (n + kTile - 1) / kTile;
+    const uint32_t pairs = (tiles + 1) / 2;
+    bool failed = false;
+
+    if (warp == kEpilogueWarps) {
+        // ---- issuing warp (its first lane) ----
+        if (lane == 0) {
+            const uint32_t sW1 = smem_u32(smem + kPairW1);
+            const uint32_t sW2 = smem_u32(smem + kPairW2);
+            const uint32_t sW3 = smem_u32(smem + kPairW3);
+            constexpr uint32_t idesc_hidden = instr_desc(kTile, kHidden);
+            constexpr uint32_t idesc_out = instr_desc(kTile, kOutPad);
+            uint32_t loads_issued[2] = {0, 0};
+            uint32_t commits[2] = {0, 0};
+            auto load_tile = [&](uint32_t s, uint32_t t) {
+                bulk_load(smem + kPairX + s * kXTileBytes, x_tiles + static_cast<size_t>(t) * kXTileBytes,
+                          kXTileBytes, &load_bar[s]);
+                ++loads_issued[s];
+            };
+            auto layer = [&](uint32_t s, uint32_t a, uint32_t b, uint32_t k_row_bytes, uint32_t k_steps,
+                             uint32_t idesc) {
+                tc_fence_after();
+                for (uint32_t k = 0; k < k_steps; ++k) {
+                    mma_bf16(tmem + s * 128u, smem_desc(a + k * 256u, 128u, k_row_bytes),
+                             smem_desc(b + k * 256u, 128u, k_row_bytes), idesc, k > 0 ? 1u : 0u);
+                }
+                mma_commit(&mma_bar[s]);
+                ++commits[s];
+            };
+            if (blockIdx.x < pairs) {
+                for (uint32_t s = 0; s < 2 && 2u * blockIdx.x + s < tiles; ++s) {
+                    load_tile(s, 2u * blockIdx.x + s);
+                }
+            }
+            uint32_t k = 0;
+            for (uint32_t pair = blockIdx.x; pair < pairs && !failed; pair += gridDim.x, ++k) {
+                const uint32_t slots = 2u * pair + 1u < tiles ? 2u : 1u;
+                const uint32_t next = pair + gridDim.x;
+                for (uint32_t s = 0; s < slots && !failed; ++s) {
+                    // The slot's columns are free once the previous pair's output is read.
+                    failed = (k > 0 && !mbar_wait(&done_bar[s], (k - 1u) & 1u, wait_polls)) ||
+                             !mbar_wait(&load_bar[s], k & 1u, wait_polls);
+                    if (!failed) {
+                        layer(s, smem_u32(smem + kPairX + s * kXTileBytes), sW1, (kIn / 8) * 128u, kIn / 16,
+                              idesc_hidden);
+                    }
+                }
+                for (uint32_t s = 0; s < slots && !failed; ++s) {
+                    failed = !mbar_wait(&h1_bar[s], k & 1u, wait_polls);
+                    if (!failed) {
+                        // Layer 1 of the slot is done (its epilogue waited for
+                        // it), so its X buffer takes the next pair's tile.
+                        if (next < pairs && 2u * next + s < tiles) {
+                            load_tile(s, 2u * next + s);
+                        }
+                        layer(s, smem_u32(smem + kPairH + s * kPairHBytes), sW2, (kHidden / 8) * 128u, kHidden / 16,
+                              idesc_hidden);
+                    }
+                }
+                for (uint32_t s = 0; s < slots && !failed; ++s) {
+                    failed = !mbar_wait(&h2_bar[s], k & 1u, wait_polls);
+                    if (!failed) {
+                        layer(s, smem_u32(smem + kPairH + s * kPairHBytes), sW3, (kHidden / 8) * 128u, kHidden / 16,
+                              idesc_out);
+                    }
+                }
+            }
+            // Everything issued has completed before the columns and the
+            // shared memory go (bounded waits; the last phase of each
+            // barrier tells).
+            for (uint32_t s = 0; s < 2; ++s) {
+                if (commits[s] > 0) {
+                    failed = !mbar_wait(&mma_bar[s], (commits[s] - 1u) & 1u, wait_polls) || failed;
+                }
+                if (loads_issued[s] > 0) {
+                    failed = !mbar_wait(&load_bar[s], (loads_issued[s] - 1u) & 1u, wait_polls) || failed;
+                }
+            }
+        }
+    } else {
+        // ---- epilogue warps ----
+        const uint32_t quarter = warp & 3u;
+        const uint32_t group = warp >> 2;
+        const uint32_t local_row = quarter * 32u + lane;
+        const uint32_t lane_base = (quarter * 32u) << 16;
+        const float* b1 = vec + kVecB1;
+        const float* b2 = vec + kVecB2;
+        const float* b3 = vec + kVecB3;
+        const float* out_scale = vec + kVecScale;
+        // A warp decides together whether a wait completed, so that it
+        // leaves the loop as a whole.
+        auto wait_warp = [&](uint64_t* bar, uint32_t parity) -> bool {
+            return __all_sync(0xFFFFFFFFu, mbar_wait(bar, parity, wait_polls));
+        };
+        auto report = [&](uint64_t* bar) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(bar);
+            }
+        };
+        auto hidden = [&](uint32_t s, const float* bias_vec) {
+            uint8_t* h = smem + kPairH + s * kPairHBytes;
+            // The group's 32 columns: two 16-column TMEM loads, one wait.
+            static_assert((kHidden / 16) / kGroups == 2, "two 16-column chunks per thread");
+            const uint32_t c0 = group * 2u;
+            uint32_t r[32];
+            const uint32_t taddr = tmem + s * 128u + lane_base + c0 * 16u;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                : "r"(taddr));
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+                  "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                  "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr + 16u));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (uint32_t j = 0; j < 2; ++j) {
+                const uint32_t c = c0 + j;
+                float v[16];
+#pragma unroll
+                for (uint32_t q = 0; q < 16; ++q) {
+                    v[q] = __uint_as_float(r[16 * j + q]);
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < 16; q += 4) {
+                    const float4 b4 = reinterpret_cast<const float4*>(bias_vec + c * 16)[q / 4];
+                    bias_gelu2_twice(v[q], v[q + 1], b4.x, b4.y, v[q], v[q + 1]);
+                    bias_gelu2_twice(v[q + 2], v[q + 3], b4.z, b4.w, v[q + 2], v[q + 3]);
+                }
+                store_chunk(h, tile_offset(local_row, 2 * c, kHidden), v);
+                store_chunk(h, tile_offset(local_row, 2 * c + 1, kHidden), v + 8);
+            }
+            // The next layer's MMAs read H through the async proxy.
+            fence_async_smem();
+        };
+        uint32_t k = 0;
+        for (uint32_t pair = blockIdx.x; pair < pairs && !failed; pair += gridDim.x, ++k) {
+            const uint32_t slots = 2u * pair + 1u < tiles ? 2u : 1u;
+            // mma_bar[s] completes three times a pair: phases 3k, 3k + 1, 3k + 2.
+            for (uint32_t s = 0; s < slots && !failed; ++s) {
+                failed = !wait_warp(&mma_bar[s], (3u * k) & 1u);
+                if (!failed) {
+                    tc_fence_after();
+                    hidden(s, b1);
+                    report(&h1_bar[s]);
+                }
+            }
+            for (uint32_t s = 0; s < slots && !failed; ++s) {
+                failed = !wait_warp(&mma_bar[s], (3u * k + 1u) & 1u);
+                if (!failed) {
+                    tc_fence_after();
+                    hidden(s, b2);
+                    report(&h2_bar[s]);
+                }
+            }
+            for (uint32_t s = 0; s < slots && !failed; ++s) {
+                failed = !wait_warp(&mma_bar[s], (3u * k + 2u) & 1u);
+                if (!failed) {
+                    tc_fence_after();
+                    if (group == s) {
+                        float v[16];
+                        tmem_load16(tmem + s * 128u + lane_base, v);
+                        const uint32_t row = (2u * pair + s) * kTile + local_row;
+                        if (row < n && out != nullptr) {
+                            const float y0 = v[0] + b3[0];
+                            const float y1 = v[1] + b3[1];
+                            const float y2 = v[2] + b3[2];
+                            reinterpret_cast<float4*>(out)[row] =
+                                make_float4(y0 * out_scale[0], y1 * out_scale[1], y2 * out_scale[2], 0.0f);
+                        }
+                    }
+                    report(&done_bar[s]);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    if (__syncthreads_or(failed) && tid == 0) {
+        atomicOr(error_flag, 1u);
+    }
+    tc_fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPairTmemCols)
+                     : "memory");
     }
 }
 
@@ -1024,10 +1354,10 @@ cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles,
     cudaGetDevice(&device);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(sms) * 2u);
-    ForwardSaves none{};
-    mlp_forward_kernel<false, true><<<grid, kForwardThreads, kSmemBytesTiles, stream>>>(
-        model, nullptr, x_tiles, n, out_accel, none, error_flag, kWaitPolls);
+    const uint32_t pairs = (tiles + 1) / 2;
+    const uint32_t grid = std::min<uint32_t>(pairs, static_cast<uint32_t>(sms));
+    mlp_forward_ws_kernel<<<grid, kWsThreads, kPairBytes, stream>>>(model, x_tiles, n, out_accel, error_flag,
+                                                                     kWaitPolls);
     return cudaGetLastError();
 }
 
@@ -1077,6 +1407,10 @@ cudaError_t prepare_forward() {
         if (e == cudaSuccess) {
             e = cudaFuncSetAttribute(mlp_forward_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(kSmemBytesTiles));
+        }
+        if (e == cudaSuccess) {
+            e = cudaFuncSetAttribute(mlp_forward_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(kPairBytes));
         }
         return e;
     });

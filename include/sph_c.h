@@ -519,6 +519,12 @@ int sph_batch_run_learned(sph_batch* batch, float dt, uint32_t substeps, const s
  * array, all tanks, id order, n x 32 floats) for a substep of length dt; the
  * state does not change. Feature definitions: csrc/sph_forces.cu. */
 int sph_batch_learned_features(sph_batch* batch, float dt, void* features);
+/* The acceleration correction a learned substep of length dt would add, from
+ * the current state (device array, float4 per particle, id order; the MLP's
+ * scaled output before any net-force removal): the learned step's own path
+ * (features written as BF16 input tiles, the forward pass over them). Every
+ * tank must be active. The state does not change. */
+int sph_batch_learned_correction(sph_batch* batch, float dt, const sph_mlp* mlp, void* correction);
 /* SPH_ERR_TIMEOUT if a tensor-core completion wait gave up since the last
  * check (the step's results are then not valid). Synchronises. */
 int sph_batch_learned_check(sph_batch* batch);

@@ -39,6 +39,39 @@ def test_zero_correction_is_the_plain_step(native, oracle, small, schedule):
     b.close()
 
 
+@pytest.mark.parametrize("tanks,particles,schedule", [(4, 4096, 1), (3, 5000, 0), (1, 65536 + 300, 2)])
+def test_learned_step_correction_is_the_forward_pass(native, tanks, particles, schedule):
+    """The learned step's own path (features written as BF16 input tiles,
+    the warp-specialised forward pass with two tiles in flight per CTA) gives the correction
+    the forward pass over the FP32 features gives, bit for bit, on counts
+    with a partial last tile and an odd number of tiles."""
+    import torch
+
+    from computer_graphics_lab_00_gb300.learned import MlpGpu
+
+    ts = T.learned_tanks(tanks=tanks, particles=particles, seed=5)
+    s = T.load_tanks(ts)
+    s.set_tuning(schedule=schedule)
+    s.run(T.FINE_DT, 20)
+    n = s.total_particles
+    with MlpGpu() as mlp:
+        T.load_model(mlp, T.WEIGHTS)
+        f = torch.empty((n, 32), dtype=torch.float32, device="cuda")
+        want = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        got = torch.full((n, 4), float("nan"), dtype=torch.float32, device="cuda")
+        s.learned_features(T.COARSE_DT, f.data_ptr())
+        s.synchronize()
+        mlp.forward(f.data_ptr(), n, want.data_ptr())
+        torch.cuda.synchronize()
+        s.learned_correction(T.COARSE_DT, mlp, got.data_ptr())
+        s.synchronize()
+    w = want.cpu().numpy()[:, :3]
+    g = got.cpu().numpy()[:, :3]
+    assert np.isfinite(g).all() and np.abs(g).max() > 0
+    assert same(g, w), int((g.view(np.uint32) != w.view(np.uint32)).sum())
+    s.close()
+
+
 def test_features_are_finite_and_plausible(native, small):
     import torch
 
