@@ -14,6 +14,7 @@
 #include "sph_kernels.h"
 #include "sph_mlp.cuh"
 
+#include <algorithm>
 #include <mutex>
 #include <type_traits>
 
@@ -848,68 +849,126 @@ __device__ __forceinline__ double warp_max(double v) {
     return v;
 }
 
-// Per-tank FP64 sums. Lanes of a warp that belong to one tank reduce with
-// shuffles; a warp that straddles tanks falls back to per-lane atomics.
-__global__ void stats_kernel(const float4* __restrict__ pos, const float4* __restrict__ vel,
-                             const uint16_t* __restrict__ tank_of, const TankConst* __restrict__ tanks, uint32_t n,
-                             double* __restrict__ acc) {
-    uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t lane = threadIdx.x & 31;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        uint32_t i = base + threadIdx.x;
-        bool valid = i < n;
-        uint32_t tank = valid && tank_of != nullptr ? tank_of[i] : 0;
-        double v[kStatsPerTank] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        if (valid) {
-            float4 p = pos[i];
-            float4 u = vel[i];
-            const TankConst* t = tanks + tank;
-            double rho0 = t->rest_density;
-            double rho = p.w;
-            bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(u.x) && isfinite(u.y) &&
-                          isfinite(u.z);
-            v[0] = rho;
-            v[1] = fmax(0.0, rho - rho0) / rho0;
-            v[2] = rho;
-            v[3] = p.x;
-            v[4] = p.y;
-            v[5] = p.z;
-            v[6] = 0.5 * static_cast<double>(t->mass) *
-                   (static_cast<double>(u.x) * u.x + static_cast<double>(u.y) * u.y + static_cast<double>(u.z) * u.z);
-            v[7] = finite ? 0.0 : 1.0;
-            v[8] = 1.0;
+// Per-tank FP64 sums. Block b takes a contiguous range of particles (a
+// multiple of 32), so a warp's consecutive 32-particle iterations mostly stay
+// in one tank: each lane adds its particles into FP64 registers, and the warp
+// reduces them with shuffles and adds them to the tank's accumulators only
+// when its tank changes, and at the end. An iteration whose lanes straddle
+// two tanks (or run past the range) is added on its own, per tank.
+__device__ __forceinline__ void stats_terms(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                            const TankConst* __restrict__ t, uint32_t i, double* v) {
+    const float4 p = pos[i];
+    const float4 u = vel[i];
+    const double rho0 = t->rest_density;
+    const double rho = p.w;
+    const bool finite =
+        isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(u.x) && isfinite(u.y) && isfinite(u.z);
+    v[0] = rho;
+    v[1] = fmax(0.0, rho - rho0) * (1.0 / rho0);
+    v[2] = rho;
+    v[3] = p.x;
+    v[4] = p.y;
+    v[5] = p.z;
+    v[6] = 0.5 * static_cast<double>(t->mass) *
+           (static_cast<double>(u.x) * u.x + static_cast<double>(u.y) * u.y + static_cast<double>(u.z) * u.z);
+    v[7] = finite ? 0.0 : 1.0;
+    v[8] = 1.0;
+}
+
+__device__ __forceinline__ void stats_add(double* dst, const double* s) {
+#pragma unroll
+    for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
+        if (k == 2) {
+            atomicMax(reinterpret_cast<unsigned long long*>(dst + 2),
+                      static_cast<unsigned long long>(__double_as_longlong(fmax(s[2], 0.0))));
+        } else if (k != 9) {
+            atomicAdd(dst + k, s[k]);
         }
-        uint32_t key = valid ? tank : 0xFFFFFFFFu;
-        uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
-        double* dst = acc + static_cast<size_t>(tank) * kStatsPerTank;
-        if (peers == 0xFFFFFFFFu && valid) {
-            double s[kStatsPerTank];
+    }
+}
+
+__global__ void __launch_bounds__(256) stats_kernel(const float4* __restrict__ pos, const float4* __restrict__ vel,
+                                                    const uint16_t* __restrict__ tank_of,
+                                                    const TankConst* __restrict__ tanks, uint32_t n,
+                                                    double* __restrict__ acc) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
+    const size_t per_block = ((static_cast<size_t>(n) + gridDim.x - 1) / gridDim.x + 31) & ~static_cast<size_t>(31);
+    const size_t begin = blockIdx.x * per_block;
+    const size_t end = begin + per_block < n ? begin + per_block : n;
+    double s[kStatsPerTank];
+#pragma unroll
+    for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
+        s[k] = 0.0;
+    }
+    uint32_t current = 0xFFFFFFFFu;  // the tank the lanes' partial sums belong to (warp-uniform)
+    auto flush = [&]() {
+        if (current == 0xFFFFFFFFu) {
+            return;
+        }
+        double r[kStatsPerTank];
+#pragma unroll
+        for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
+            r[k] = k == 2 ? warp_max(s[k]) : warp_sum(s[k]);
+            s[k] = 0.0;
+        }
+        if (lane == 0) {
+            stats_add(acc + static_cast<size_t>(current) * kStatsPerTank, r);
+        }
+    };
+    for (size_t first = begin + 32u * warp; first < end; first += blockDim.x) {
+        const size_t idx = first + lane;
+        const bool valid = idx < end;
+        const uint32_t i = static_cast<uint32_t>(valid ? idx : 0);
+        const uint32_t key = valid ? (tank_of != nullptr ? tank_of[i] : 0u) : 0xFFFFFFFFu;
+        const uint32_t lead = __shfl_sync(0xFFFFFFFFu, key, 0);
+        if (__all_sync(0xFFFFFFFFu, key == lead)) {
+            // All 32 lanes hold particles of one tank: accumulate.
+            if (lead != current) {
+                flush();
+                current = lead;
+            }
+            double v[kStatsPerTank];
+            stats_terms(pos, vel, tanks + lead, i, v);
 #pragma unroll
             for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
-                s[k] = k == 2 ? warp_max(v[k]) : warp_sum(v[k]);
+                s[k] = k == 2 ? fmax(s[k], v[k]) : s[k] + v[k];
             }
-            if (lane == 0) {
+        } else {
+            // Lanes of several tanks, or past the range: per tank, now.
+            double v[kStatsPerTank];
+#pragma unroll
+            for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
+                v[k] = 0.0;
+            }
+            if (valid) {
+                stats_terms(pos, vel, tanks + key, i, v);
+            }
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+            if (valid) {
+                // Reduce within the lanes of this tank, in lane order.
+                double r[kStatsPerTank];
 #pragma unroll
                 for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
-                    if (k == 2) {
-                        atomicMax(reinterpret_cast<unsigned long long*>(dst + 2),
-                                  static_cast<unsigned long long>(__double_as_longlong(fmax(s[2], 0.0))));
-                    } else if (k != 9) {
-                        atomicAdd(dst + k, s[k]);
+                    r[k] = 0.0;
+                }
+                uint32_t m = peers;
+                while (m != 0) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+#pragma unroll
+                    for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
+                        const double x = __shfl_sync(peers, v[k], src);
+                        r[k] = k == 2 ? fmax(r[k], x) : r[k] + x;
                     }
                 }
-            }
-        } else if (valid) {
-            for (int k = 0; k < static_cast<int>(kStatsPerTank); ++k) {
-                if (k == 2) {
-                    atomicMax(reinterpret_cast<unsigned long long*>(dst + 2),
-                              static_cast<unsigned long long>(__double_as_longlong(fmax(v[2], 0.0))));
-                } else if (k != 9) {
-                    atomicAdd(dst + k, v[k]);
+                if (lane == static_cast<uint32_t>(__ffs(peers) - 1)) {
+                    stats_add(acc + static_cast<size_t>(key) * kStatsPerTank, r);
                 }
             }
         }
     }
+    flush();
 }
 
 __global__ void nonfinite_kernel(const float4* __restrict__ pos, const float4* __restrict__ vel, uint32_t n,
@@ -2867,10 +2926,13 @@ cudaError_t launch_stats(const float4* pos, const float4* vel, const uint16_t* t
     if (n == 0) {
         return cudaSuccess;
     }
-    uint32_t blocks = (n + 255) / 256;
-    if (blocks > 4 * 152) {
-        blocks = 4 * 152;
+    int device = 0;
+    int sms = 152;
+    if (cudaGetDevice(&device) == cudaSuccess) {
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     }
+    uint32_t blocks = (n + 255) / 256;
+    blocks = std::min<uint32_t>(blocks, 4u * static_cast<uint32_t>(sms));
     stats_kernel<<<blocks, 256, 0, stream>>>(pos, vel, tank_of, tanks, n, acc);
     return cudaGetLastError();
 }
