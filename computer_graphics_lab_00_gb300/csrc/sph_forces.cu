@@ -2480,51 +2480,80 @@ __device__ __forceinline__ long long correction_fixed(float v) {
     return fabsf(v) <= kCorrectionFixedMax ? __float2ll_rn(v * kCorrectionFixed) : 0ll;
 }
 
+// Block b takes a contiguous range of sorted positions (tanks are contiguous
+// in the sorted order): each lane adds its particles' fixed-point corrections
+// into 64-bit registers, and the warp reduces them and adds them to the
+// tank's sums when its tank changes and at the end. Integer sums: the result
+// does not depend on how the work is split.
 __global__ void __launch_bounds__(256) correction_sums_kernel(const float4* __restrict__ correction,
                                                               const TankConst* __restrict__ tanks,
                                                               const uint16_t* __restrict__ stank, uint32_t n,
                                                               unsigned long long* __restrict__ sums) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = p < n;
-    const uint32_t t = valid && stank != nullptr ? stank[p] : 0u;
-    const bool counted = valid && __ldg(&tanks[t].active) != 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
+    const size_t per_block = ((static_cast<size_t>(n) + gridDim.x - 1) / gridDim.x + 31) & ~static_cast<size_t>(31);
+    const size_t begin = blockIdx.x * per_block;
+    const size_t end = begin + per_block < n ? begin + per_block : n;
     long long x = 0;
     long long y = 0;
     long long z = 0;
-    if (counted) {
-        const float4 c = correction[p];
-        x = correction_fixed(c.x);
-        y = correction_fixed(c.y);
-        z = correction_fixed(c.z);
-    }
-    // Lanes of one tank add up with shuffles first (tanks are contiguous in
-    // the sorted order, so a warp rarely straddles two).
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t same = __match_any_sync(0xFFFFFFFFu, counted ? t : 0xFFFFFFFFu);
-    const uint32_t leader = static_cast<uint32_t>(__ffs(same) - 1);
-    if (same == 0xFFFFFFFFu) {
+    unsigned long long count = 0;
+    uint32_t current = 0xFFFFFFFFu;  // the tank the lanes' sums belong to (warp-uniform)
+    auto flush = [&]() {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             x += __shfl_down_sync(0xFFFFFFFFu, x, o);
             y += __shfl_down_sync(0xFFFFFFFFu, y, o);
             z += __shfl_down_sync(0xFFFFFFFFu, z, o);
+            count += __shfl_down_sync(0xFFFFFFFFu, count, o);
         }
-        if (lane == 0 && counted) {
-            unsigned long long* s = sums + static_cast<size_t>(t) * kCorrectionSumWords;
+        if (lane == 0 && current != 0xFFFFFFFFu && count != 0) {
+            unsigned long long* s = sums + static_cast<size_t>(current) * kCorrectionSumWords;
             atomicAdd(&s[0], static_cast<unsigned long long>(x));
             atomicAdd(&s[1], static_cast<unsigned long long>(y));
             atomicAdd(&s[2], static_cast<unsigned long long>(z));
-            atomicAdd(&s[3], 32ull);
+            atomicAdd(&s[3], count);
         }
-    } else if (counted) {
-        unsigned long long* s = sums + static_cast<size_t>(t) * kCorrectionSumWords;
-        atomicAdd(&s[0], static_cast<unsigned long long>(x));
-        atomicAdd(&s[1], static_cast<unsigned long long>(y));
-        atomicAdd(&s[2], static_cast<unsigned long long>(z));
-        if (lane == leader) {
-            atomicAdd(&s[3], static_cast<unsigned long long>(__popc(same)));
+        x = 0;
+        y = 0;
+        z = 0;
+        count = 0;
+    };
+    for (size_t first = begin + 32u * warp; first < end; first += blockDim.x) {
+        const size_t p = first + lane;
+        const bool valid = p < end;
+        const uint32_t t = valid && stank != nullptr ? stank[p] : 0u;
+        const bool counted = valid && __ldg(&tanks[t].active) != 0;
+        const uint32_t key = counted ? t : 0xFFFFFFFFu;
+        const uint32_t lead = __shfl_sync(0xFFFFFFFFu, key, 0);
+        long long cx = 0;
+        long long cy = 0;
+        long long cz = 0;
+        if (counted) {
+            const float4 c = correction[p];
+            cx = correction_fixed(c.x);
+            cy = correction_fixed(c.y);
+            cz = correction_fixed(c.z);
+        }
+        if (__all_sync(0xFFFFFFFFu, key == lead) && lead != 0xFFFFFFFFu) {
+            if (lead != current) {
+                flush();
+                current = lead;
+            }
+            x += cx;
+            y += cy;
+            z += cz;
+            count += 1;
+        } else if (counted) {
+            // Lanes of several tanks (or uncounted lanes): add now.
+            unsigned long long* s = sums + static_cast<size_t>(t) * kCorrectionSumWords;
+            atomicAdd(&s[0], static_cast<unsigned long long>(cx));
+            atomicAdd(&s[1], static_cast<unsigned long long>(cy));
+            atomicAdd(&s[2], static_cast<unsigned long long>(cz));
+            atomicAdd(&s[3], 1ull);
         }
     }
+    flush();
 }
 
 __global__ void __launch_bounds__(256) finish_learned_kernel(const float4* __restrict__ spos2,
@@ -2966,7 +2995,13 @@ cudaError_t launch_correction_sums(const float4* correction, const TankConst* ta
     if (e != cudaSuccess || n == 0) {
         return e;
     }
-    correction_sums_kernel<<<(n + 255) / 256, 256, 0, stream>>>(correction, tanks, stank, n, sums);
+    int device = 0;
+    int sms = 152;
+    if (cudaGetDevice(&device) == cudaSuccess) {
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    }
+    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 4u * static_cast<uint32_t>(sms));
+    correction_sums_kernel<<<blocks, 256, 0, stream>>>(correction, tanks, stank, n, sums);
     return cudaGetLastError();
 }
 
