@@ -150,9 +150,6 @@ constexpr uint32_t kVecScale = kVecB3 + 4;
 constexpr uint32_t kVecFloats = kVecScale + 4;
 constexpr uint32_t kSmemVec = kSmemBar + 64;
 constexpr uint32_t kSmemBytes = kSmemVec + kVecFloats * 4;
-// The tiled-input form double-buffers X: a second 8 KB tile after the rest.
-constexpr uint32_t kSmemX2 = (kSmemBytes + 127u) & ~127u;
-constexpr uint32_t kSmemBytesTiles = kSmemX2 + kXTileBytes;
 static_assert(kXTileBytes == kTile * kIn * 2, "one input tile");
 constexpr uint32_t kTmemCols = 128;
 
@@ -232,15 +229,13 @@ constexpr uint32_t kGroups = kForwardThreads / 128;  // threads sharing one row'
 // [MMA W2] -> +b2, GELU -> H2 -> [MMA W3] -> +b3 -> scaled output. Row r of a
 // tile is TMEM lane r; warp w reads the lane quarter w % 4 and, for the hidden
 // layers, the column group w / 4, so kGroups threads share each row's epilogue.
-// One thread issues the MMAs; an mbarrier reports their completion.
-// kTiles: the input arrives as ready tiles (x_tiles: normalised BF16 rows in
-// the K-major layout, kXTileBytes a tile, written by the learned step's
-// features kernel), one bulk copy per tile into two alternating X buffers,
-// the next tile's copy in flight while this one runs.
-template <bool kSave, bool kTiles = false>
+// One thread issues the MMAs; an mbarrier reports their completion. The
+// input is FP32 features, normalised and rounded to BF16 here (the
+// training forward and sph_mlp_forward; the learned step's own forward is
+// mlp_forward_ws_kernel, over ready BF16 tiles).
+template <bool kSave>
 __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelView model,
                                                                          const float* __restrict__ features,
-                                                                         const uint8_t* __restrict__ x_tiles,
                                                                          uint32_t n, float* __restrict__ out,
                                                                          ForwardSaves saves,
                                                                          unsigned int* __restrict__ error_flag,
@@ -248,7 +243,6 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + kSmemBar);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kSmemBar + 8);
-    uint64_t* load_bar = reinterpret_cast<uint64_t*>(smem + kSmemBar + 16);  // [2], kTiles
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5;
     const uint32_t quarter = warp & 3u;
@@ -300,10 +294,6 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     }
     if (tid == 0) {
         mbar_init(mbar, 1);
-        if (kTiles) {
-            mbar_init(&load_bar[0], 1);
-            mbar_init(&load_bar[1], 1);
-        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_async_smem();
@@ -346,45 +336,12 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
     };
     float4 next_a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float4 next_b = next_a;
-    // kTiles: copies issued into each X buffer and the waits on them done.
-    uint32_t issued[2] = {0, 0};
-    uint32_t landed[2] = {0, 0};
-    if (kTiles) {
-        if (tid == 0 && blockIdx.x < tiles) {
-            bulk_load(smem + kSmemX, x_tiles + static_cast<size_t>(blockIdx.x) * kXTileBytes, kXTileBytes, &load_bar[0]);
-        }
-        if (blockIdx.x < tiles) {
-            issued[0] = 1;
-        }
-    } else {
-        fetch(blockIdx.x, next_a, next_b);
-    }
+    fetch(blockIdx.x, next_a, next_b);
 
-    uint32_t iter = 0;
-    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x, ++iter) {
+    for (uint32_t tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const uint32_t row = tile * kTile + local_row;
         const bool valid = row < n;
-        uint32_t sXt = sX;
-        if (kTiles) {
-            const uint32_t buf = iter & 1u;
-            // The other buffer was last read by the previous tile's layer-1
-            // MMAs, which have completed: refill it with the next tile.
-            const uint32_t next = tile + gridDim.x;
-            if (next < tiles) {
-                if (tid == 0) {
-                    bulk_load(smem + (buf ? kSmemX : kSmemX2), x_tiles + static_cast<size_t>(next) * kXTileBytes,
-                              kXTileBytes, &load_bar[buf ^ 1u]);
-                }
-                ++issued[buf ^ 1u];
-            }
-            const bool ok_load = mbar_wait(&load_bar[buf], landed[buf] & 1u, wait_polls);
-            if (!__syncthreads_and(ok_load)) {
-                failed = true;
-                break;
-            }
-            ++landed[buf];
-            sXt = smem_u32(smem + (buf ? kSmemX2 : kSmemX));
-        } else {
+        const uint32_t sXt = sX;
         const float4 a = next_a;
         const float4 b = next_b;
         fetch(tile + gridDim.x, next_a, next_b);
@@ -407,7 +364,6 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
-        }
 
         // ---- layer 1: [128 x 32] x [32 x 128] ----
         if (tid == 0) {
@@ -555,17 +511,8 @@ __global__ void __launch_bounds__(kForwardThreads, 2) mlp_forward_kernel(ModelVi
         if (tid == 0) {
             atomicOr(error_flag, 1u);
         }
-        // Let an MMA still in flight finish (bounded) before the columns go,
-        // and any input copy still landing in shared memory.
+        // Let an MMA still in flight finish (bounded) before the columns go.
         mbar_wait(mbar, parity, wait_polls);
-        if (kTiles) {
-            for (uint32_t b = 0; b < 2; ++b) {
-                while (landed[b] < issued[b]) {
-                    mbar_wait(&load_bar[b], landed[b] & 1u, wait_polls);
-                    ++landed[b];
-                }
-            }
-        }
         tc_fence_before();
         __syncthreads();
     }
@@ -904,9 +851,7 @@ __global__ void wait_selftest_kernel(uint32_t polls, int arrive, unsigned int* e
     }
     __syncthreads();
     if (arrive != 0 && threadIdx.x == 0) {
-        uint64_t state;
-        asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(smem_u32(&mbar)) : "memory");
-        (void)state;
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&mbar)) : "memory");
     }
     const bool ok = mbar_wait(&mbar, 0, polls);
     if (!__syncthreads_and(ok) && threadIdx.x == 0) {
@@ -1331,10 +1276,10 @@ cudaError_t launch_forward(const ModelView& model, const float* features, uint32
     uint32_t grid = std::min<uint32_t>(tiles, static_cast<uint32_t>(sms) * 2u);
     ForwardSaves none{};
     if (saves != nullptr) {
-        mlp_forward_kernel<true><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, nullptr, n, out_accel,
+        mlp_forward_kernel<true><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel,
                                                                                 *saves, error_flag, kWaitPolls);
     } else {
-        mlp_forward_kernel<false><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, nullptr, n, out_accel,
+        mlp_forward_kernel<false><<<grid, kForwardThreads, kSmemBytes, stream>>>(model, features, n, out_accel,
                                                                                  none, error_flag, kWaitPolls);
     }
     return cudaGetLastError();
@@ -1403,10 +1348,6 @@ cudaError_t prepare_forward() {
         if (e == cudaSuccess) {
             e = cudaFuncSetAttribute(mlp_forward_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(kSmemBytes));
-        }
-        if (e == cudaSuccess) {
-            e = cudaFuncSetAttribute(mlp_forward_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(kSmemBytesTiles));
         }
         if (e == cudaSuccess) {
             e = cudaFuncSetAttribute(mlp_forward_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
