@@ -262,16 +262,43 @@ __global__ void __launch_bounds__(256) rank_kernel(const uint32_t* __restrict__ 
 // pass histogram) plus the sum of d's counts over the earlier tiles, which
 // each block adds up on its own: no block waits on another.
 
+// Above kChunkedTiles tiles a pass block would sum too many earlier tiles'
+// digit counts (the work grows with the square of the tile count), so a small
+// kernel first sums each chunk of kChunkTiles tiles, and a block then adds
+// the whole chunks before its own and the tiles of its own chunk.
+constexpr uint32_t kChunkTiles = 32;
+constexpr uint32_t kChunkedTiles = 256;
+
+inline uint32_t sweep_chunks(uint32_t tiles) { return (tiles + kChunkTiles - 1) / kChunkTiles; }
+
 struct SweepLayout {
     uint32_t* tile_counts;  // passes x tiles x bins
     uint32_t* hist;         // passes x bins
+    uint32_t* chunk_sums;   // chunks x bins (one pass at a time)
 };
 
 __host__ __device__ inline SweepLayout sweep_layout(unsigned long long* base, uint32_t tiles, uint32_t passes) {
     SweepLayout l;
     l.tile_counts = reinterpret_cast<uint32_t*>(base);
     l.hist = l.tile_counts + static_cast<size_t>(passes) * tiles * kSweepBins;
+    l.chunk_sums = l.hist + static_cast<size_t>(passes) * kSweepBins;
     return l;
+}
+
+// chunk_sums[c][d] = the digit-d counts of tiles 32c .. 32c + 31 (one block a
+// chunk, one thread a digit).
+__global__ void __launch_bounds__(kSweepBins) chunk_sums_kernel(const uint32_t* __restrict__ tile_counts,
+                                                                uint32_t tiles, uint32_t* __restrict__ chunk_sums) {
+    const uint32_t c = blockIdx.x;
+    const uint32_t d = threadIdx.x;
+    const uint32_t first = c * kChunkTiles;
+    const uint32_t last = min(first + kChunkTiles, tiles);
+    uint32_t sum = 0;
+#pragma unroll 8
+    for (uint32_t t = first; t < last; ++t) {
+        sum += __ldg(&tile_counts[static_cast<size_t>(t) * kSweepBins + d]);
+    }
+    chunk_sums[static_cast<size_t>(c) * kSweepBins + d] = sum;
 }
 
 // keys_kernel for one tile of kSweepTile particles (1024 threads, four
@@ -405,7 +432,8 @@ template <bool kAggregate>
 __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ keys_out,
     uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift, const uint32_t* __restrict__ hist,
-    const uint32_t* __restrict__ tile_counts, uint32_t* __restrict__ next_counts, uint32_t next_shift) {
+    const uint32_t* __restrict__ tile_counts, uint32_t* __restrict__ next_counts, uint32_t next_shift,
+    const uint32_t* __restrict__ chunk_sums) {
     static_assert(kSweepThreads % kSweepBins == 0 && kSweepThreads >= kSweepBins,
                   "the first kSweepBins threads each own one digit");
     constexpr uint32_t kWarps = kSweepThreads / 32;
@@ -424,15 +452,30 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
     // Every digit's keys in all earlier tiles: the block reads the earlier
     // tiles' count rows kRowLanes at a time (a row is 64 uint4, thread k reads
     // column k % 64 of row j + k / 64), eight rows' loads in flight per thread,
-    // then the partial sums of each digit meet in shared memory.
+    // then the partial sums of each digit meet in shared memory. With chunk
+    // sums, the whole chunks before this tile's chunk are one row each.
     __shared__ uint4 partial[kRowLanes][kSweepBins / 4];
     {
         const uint32_t column = threadIdx.x & 63u;
         const uint32_t lane_row = threadIdx.x >> 6;
         const uint4* rows = reinterpret_cast<const uint4*>(tile_counts);
         uint4 acc = make_uint4(0, 0, 0, 0);
+        uint32_t first_row = 0;
+        if (chunk_sums != nullptr) {
+            const uint4* chunk_rows = reinterpret_cast<const uint4*>(chunk_sums);
+            const uint32_t chunks = tile / kChunkTiles;
 #pragma unroll 8
-        for (uint32_t j = lane_row; j < tile; j += kRowLanes) {
+            for (uint32_t j = lane_row; j < chunks; j += kRowLanes) {
+                uint4 c = __ldg(&chunk_rows[static_cast<size_t>(j) * (kSweepBins / 4) + column]);
+                acc.x += c.x;
+                acc.y += c.y;
+                acc.z += c.z;
+                acc.w += c.w;
+            }
+            first_row = chunks * kChunkTiles;
+        }
+#pragma unroll 8
+        for (uint32_t j = first_row + lane_row; j < tile; j += kRowLanes) {
             uint4 c = __ldg(&rows[static_cast<size_t>(j) * (kSweepBins / 4) + column]);
             acc.x += c.x;
             acc.y += c.y;
@@ -532,7 +575,8 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_scatter_kernel(
 
 size_t onesweep_scratch_words(uint32_t n, uint32_t passes) {
     const size_t tiles = sweep_tiles(n == 0 ? 1 : n);
-    const size_t words32 = static_cast<size_t>(passes) * tiles * kSweepBins + static_cast<size_t>(passes) * kSweepBins;
+    const size_t words32 = static_cast<size_t>(passes) * tiles * kSweepBins + static_cast<size_t>(passes) * kSweepBins +
+                           static_cast<size_t>(sweep_chunks(static_cast<uint32_t>(tiles))) * kSweepBins;
     return (words32 + 1) / 2;
 }
 
@@ -666,16 +710,26 @@ cudaError_t launch_onesweep_sort(GridScratch& s, uint32_t n, uint32_t passes, un
     const uint32_t* vin = nullptr;
     uint32_t* kout = s.keys_a;
     uint32_t* vout = s.vals_a;
+    const bool chunked = tiles > kChunkedTiles;
     for (uint32_t p = 0; p < passes; ++p) {
         uint32_t* next = p + 1 < passes ? l.tile_counts + static_cast<size_t>(p + 1) * tiles * kSweepBins : nullptr;
         const uint32_t* counts = l.tile_counts + static_cast<size_t>(p) * tiles * kSweepBins;
         const uint32_t* hist = l.hist + static_cast<size_t>(p) * kSweepBins;
+        if (chunked) {
+            chunk_sums_kernel<<<sweep_chunks(tiles), kSweepBins, 0, stream>>>(counts, tiles, l.chunk_sums);
+            if (launches != nullptr) {
+                *launches += 1;
+            }
+        }
+        const uint32_t* chunk_sums = chunked ? l.chunk_sums : nullptr;
         if (aggregate) {
             sweep_scatter_kernel<true><<<tiles, kSweepThreads, 0, stream>>>(kin, vin, kout, vout, n, p * kSweepBits,
-                                                                            hist, counts, next, (p + 1) * kSweepBits);
+                                                                            hist, counts, next, (p + 1) * kSweepBits,
+                                                                            chunk_sums);
         } else {
             sweep_scatter_kernel<false><<<tiles, kSweepThreads, 0, stream>>>(kin, vin, kout, vout, n, p * kSweepBits,
-                                                                             hist, counts, next, (p + 1) * kSweepBits);
+                                                                             hist, counts, next, (p + 1) * kSweepBits,
+                                                                             chunk_sums);
         }
         if (launches != nullptr) {
             *launches += 1;

@@ -397,6 +397,28 @@ def test_grid_sorts_agree_at_one_million(native, oracle, sort, bits):
     assert_grid_equal(got, oracle.grid_build(case.params, pos, threads=oracle.hardware_threads))
 
 
+def test_grid_and_substeps_past_256_sort_tiles(native, oracle):
+    """2,064,384 particles (504 sort tiles): the one-sweep passes add whole
+    32-tile chunk sums before their own chunk's tiles. The grid and two
+    substeps (Morton order, whose keys take the same sort) are the oracle's."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(4.0, 3.0, 2.0), lattice=(192, 128, 84),
+                           cell_count=W.cell_count_uncapped(192 * 128 * 84))
+    n = 192 * 128 * 84
+    pos, vel = W.jittered_block(params, n, seed=4)
+    threads = oracle.hardware_threads
+    with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(sort=1)
+        solver.upload(pos, vel)
+        solver.build_grid()
+        got = solver.grid()
+        solver.run(1.0 / 600.0, 2)
+        gp, gv = solver.state()
+    assert_grid_equal(got, oracle.grid_build(params, pos, threads=threads))
+    op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 2, threads=threads)
+    assert_bit_exact(gp, op, "positions past 256 sort tiles")
+    assert_bit_exact(gv, ov, "velocities past 256 sort tiles")
+
+
 def test_bad_tuning_is_rejected(native):
     case = W.dam_break_16k()
     with FluidSolverGpu(case.params, 16) as solver:
