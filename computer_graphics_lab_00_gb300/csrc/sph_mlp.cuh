@@ -68,7 +68,9 @@ constexpr uint32_t kWaitPolls = 1u << 22;
 cudaError_t launch_forward(const ModelView& model, const float* features, uint32_t n, float* out_accel,
                            const ForwardSaves* saves, unsigned int* error_flag, cudaStream_t stream);
 // Forward over ready input tiles (x_tiles: ceil(n / 128) tiles, as written by
-// the learned step's features kernel); output as launch_forward.
+// the learned step's features kernel); output as launch_forward, bit for bit.
+// Warp-specialised: one persistent CTA per SM, two tiles in flight (TMEM
+// columns, buffers and mbarriers per tile slot).
 cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles, uint32_t n, float* out_accel,
                                  unsigned int* error_flag, cudaStream_t stream);
 // One CTA waits on an mbarrier (arrived at only when `arrive`) with at most
