@@ -1422,7 +1422,8 @@ __global__ void __launch_bounds__(128) density_mask_kernel(const float4* __restr
 // a block, 180 KB an SM): a compressed tank (about 40 pairs a particle) then
 // rarely drains mid-walk, and L1 keeps 76 KB; 44 or 48 entries leave too
 // little L1 and ran 8-20 % slower.
-template <int kBlock, int kList, int kMinBlocks = 1>
+// kGroup: mask words and bucket starts loaded kGroup buckets at a time (27 % kGroup == 0).
+template <int kBlock, int kList, int kMinBlocks = 1, uint32_t kGroup = 3>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(const float4* __restrict__ spos2,
                                                                 const float4* __restrict__ svel,
                                                                 const uint32_t* __restrict__ sorted_ids,
@@ -1434,6 +1435,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(cons
                                                                 float4* __restrict__ vel_out) {
     // One bucket may hand over 32 pairs at once, after the warp has drained.
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
+    static_assert(27u % kGroup == 0, "groups of buckets tile the 27");
     __shared__ uint32_t list[kList][kBlock];
     const uint32_t slot = blockIdx.x * kBlock + threadIdx.x;
     uint32_t p = slot;
@@ -1465,25 +1467,38 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(cons
     float fy = 0.0f;
     float fz = 0.0f;
     uint32_t listed = 0;
-    for (uint32_t b = 0; b < 27u; ++b) {
-        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + slot]);
-        // When any lane's list cannot take this bucket's pairs, every lane
-        // drains its list (in order) at once, so the force code runs with
-        // all lanes busy rather than once per lane that filled up.
-        if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
-            for (uint32_t e = 0; e < listed; ++e) {
-                uint32_t q = list[e][threadIdx.x];
-                add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
-                                   __ldg(&svel[q]), fx, fy, fz);
-            }
-            listed = 0;
+    // kGroup buckets at a time: their mask words, then the first slots of the
+    // buckets with pairs, are loaded back to back, so a particle waits for
+    // two loads per group instead of two per bucket.
+    for (uint32_t b0 = 0; b0 < 27u; b0 += kGroup) {
+        uint32_t words[kGroup];
+        uint32_t firsts[kGroup];
+#pragma unroll
+        for (uint32_t j = 0; j < kGroup; ++j) {
+            words[j] = __ldg(&masks[static_cast<size_t>(b0 + j) * n + slot]);
         }
-        if (word != 0) {
-            uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
+#pragma unroll
+        for (uint32_t j = 0; j < kGroup; ++j) {
+            firsts[j] = words[j] != 0 ? neighbour_range(bucket, cx, cy, cz, b0 + j, cell_mask, base).x : 0u;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kGroup; ++j) {
+            uint32_t word = words[j];
+            // When any lane's list cannot take this bucket's pairs, every lane
+            // drains its list (in order) at once, so the force code runs with
+            // all lanes busy rather than once per lane that filled up.
+            if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
+                for (uint32_t e = 0; e < listed; ++e) {
+                    uint32_t q = list[e][threadIdx.x];
+                    add_pair_force_rcp(k, self, self_vel.x, self_vel.y, self_vel.z, self_vel.w, __ldg(&spos2[q]),
+                                       __ldg(&svel[q]), fx, fy, fz);
+                }
+                listed = 0;
+            }
             while (word != 0) {
-                uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
+                uint32_t s = static_cast<uint32_t>(__ffs(word) - 1);
                 word &= word - 1;
-                list[listed][threadIdx.x] = start + slot;
+                list[listed][threadIdx.x] = firsts[j] + s;
                 ++listed;
             }
         }
@@ -2394,21 +2409,34 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const floa
         ++pairs;
     };
     uint32_t listed = 0;
-    for (uint32_t b = 0; b < 27u; ++b) {
-        uint32_t word = __ldg(&masks[static_cast<size_t>(b) * n + slot]);
-        // Every lane drains together when any lane's list is about to overflow.
-        if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
-            for (uint32_t e = 0; e < listed; ++e) {
-                visit(list[e][threadIdx.x]);
-            }
-            listed = 0;
+    // Three buckets at a time: their mask words, then the first slots of the
+    // buckets with pairs, loaded back to back (as integrate_mask_kernel).
+    constexpr uint32_t kGroup = 3;
+    for (uint32_t b0 = 0; b0 < 27u; b0 += kGroup) {
+        uint32_t words[kGroup];
+        uint32_t firsts[kGroup];
+#pragma unroll
+        for (uint32_t j = 0; j < kGroup; ++j) {
+            words[j] = __ldg(&masks[static_cast<size_t>(b0 + j) * n + slot]);
         }
-        if (word != 0) {
-            uint32_t start = neighbour_range(bucket, cx, cy, cz, b, cell_mask, base).x;
+#pragma unroll
+        for (uint32_t j = 0; j < kGroup; ++j) {
+            firsts[j] = words[j] != 0 ? neighbour_range(bucket, cx, cy, cz, b0 + j, cell_mask, base).x : 0u;
+        }
+#pragma unroll
+        for (uint32_t j = 0; j < kGroup; ++j) {
+            uint32_t word = words[j];
+            // Every lane drains together when any lane's list is about to overflow.
+            if (__any_sync(live, listed + static_cast<uint32_t>(__popc(word)) > static_cast<uint32_t>(kList))) {
+                for (uint32_t e = 0; e < listed; ++e) {
+                    visit(list[e][threadIdx.x]);
+                }
+                listed = 0;
+            }
             while (word != 0) {
-                uint32_t slot = static_cast<uint32_t>(__ffs(word) - 1);
+                uint32_t s = static_cast<uint32_t>(__ffs(word) - 1);
                 word &= word - 1;
-                list[listed][threadIdx.x] = start + slot;
+                list[listed][threadIdx.x] = firsts[j] + s;
                 ++listed;
             }
         }
