@@ -7,7 +7,7 @@ finite-difference gradient check follows tests/gradient_check.h:22-60
 (double precision, step 1e-5, error scaled by the typical gradient size).
 GELU (Hendrycks & Gimpel 2016, z Phi(z) with erf(z / sqrt 2) taken as
 tanh(a z + b z^3), a = sqrt(2 / pi), b = 0.044715 a) and BF16 rounding (round
-to nearest even of the FP32 value) are new here and specified by this build;
+to nearest even of the FP32 value) are new here (the reference has neither);
 the GPU evaluates the tanh with the hardware's approximate tanh.
 
 `forward(..., bf16=True)` rounds where the GPU rounds: the normalised input,
