@@ -797,7 +797,8 @@ def run_gb300(args) -> None:
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {**workload_config(case, world), "neighbour_kernel": solver.tuning()["neighbour_kernel"]},
+        "config": {**workload_config(case, world), "neighbour_kernel": solver.tuning()["neighbour_kernel"],
+                   "grid_sort": solver.tuning()["sort"]},
         "particle_steps_per_s": total_particles * args.steps / (device_ms / 1e3),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
                 "steps": e2e_steps, "ms_per_step": 1e3 * e2e_wall / e2e_steps},

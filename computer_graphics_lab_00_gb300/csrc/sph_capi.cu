@@ -40,7 +40,7 @@ void to_api(const sph::TuneChoice& c, sph_tuning* out) {
     out->block_size = c.tuning.block;
     out->queue_depth = c.tuning.queue;
     out->schedule = c.schedule;
-    out->sort = c.onesweep ? 1u : 0u;
+    out->sort = c.counting ? 2u : (c.onesweep ? 1u : 0u);
 }
 
 int autotune(sph::Engine& engine, float dt, uint32_t substeps, sph_tuning* best, float* best_ms) {
@@ -448,7 +448,7 @@ int sph_get_tuning(const sph_ctx* ctx, sph_tuning* out) {
     out->block_size = t.block;
     out->queue_depth = t.queue;
     out->schedule = ctx->engine.schedule_on();
-    out->sort = ctx->engine.onesweep_on() ? 1u : 0u;
+    out->sort = ctx->engine.counting_on() ? 2u : (ctx->engine.onesweep_on() ? 1u : 0u);
     return SPH_OK;
 }
 
@@ -460,7 +460,7 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning) {
     t.variant = tuning->neighbour_kernel;
     t.block = tuning->block_size;
     t.queue = tuning->queue_depth;
-    if (tuning->schedule > 2 || tuning->sort > 1) {
+    if (tuning->schedule > 2 || tuning->sort > 2) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     int status = ctx->engine.set_tuning(t);
@@ -472,6 +472,9 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning) {
         return status;
     }
     status = ctx->engine.set_onesweep(tuning->sort != 0);
+    if (status == SPH_OK) {
+        status = ctx->engine.set_counting(tuning->sort == 2);
+    }
     if (status != SPH_OK) {
         return status;
     }
@@ -666,12 +669,13 @@ int sph_batch_get_tuning(const sph_batch* batch, sph_tuning* out) {
     c.radix_bits = batch->engine.radix_bits();
     c.schedule = batch->engine.schedule_on();
     c.onesweep = batch->engine.onesweep_on();
+    c.counting = batch->engine.counting_on();
     to_api(c, out);
     return SPH_OK;
 }
 
 int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
-    if (batch == nullptr || tuning == nullptr || tuning->schedule > 2 || tuning->sort > 1) {
+    if (batch == nullptr || tuning == nullptr || tuning->schedule > 2 || tuning->sort > 2) {
         return SPH_ERR_INVALID_ARGUMENT;
     }
     sph::NeighbourTuning t = batch->engine.tuning();
@@ -684,6 +688,9 @@ int sph_batch_set_tuning(sph_batch* batch, const sph_tuning* tuning) {
     }
     if (status == SPH_OK) {
         status = batch->engine.set_onesweep(tuning->sort != 0);
+    }
+    if (status == SPH_OK) {
+        status = batch->engine.set_counting(tuning->sort == 2);
     }
     if (status == SPH_OK) {
         status = batch->engine.set_radix_bits(tuning->radix_bits);

@@ -201,7 +201,7 @@ void Engine::release() {
                        rank_,          order_,        compact_ids_, compact_sorted_, compact_ranges_,
                        snap_pos_[0], snap_vel_[0],
                        snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_, correction_sums_,
-                       compact_rank_,  compact_order_, sx_tiles_};
+                       compact_rank_,  compact_order_, sx_tiles_, counts_, block_sums_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -277,7 +277,9 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         (status = alloc(&bucket_stats_, 2)) != SPH_OK ||
         (status = alloc(&tuning_.pair_list, static_cast<size_t>(n) * tuning_.list_cap)) != SPH_OK ||
         (status = alloc(&tuning_.pair_count, n)) != SPH_OK ||
-        (status = alloc(&tuning_.masks, static_cast<size_t>(n) * 27)) != SPH_OK) {
+        (status = alloc(&tuning_.masks, static_cast<size_t>(n) * 27)) != SPH_OK ||
+        (status = alloc(&counts_, total_buckets_)) != SPH_OK ||
+        (status = alloc(&block_sums_, counting_block_sums(total_buckets_))) != SPH_OK) {
         return status;
     }
     if ((status = alloc(&rank_, n)) != SPH_OK || (status = alloc(&order_, n)) != SPH_OK) {
@@ -690,12 +692,17 @@ int Engine::enqueue_grid(uint32_t* launches) {
             return status;
         }
     }
-    SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
-    if (onesweep_) {
+    if (counting_) {
+        // Every bucket's range comes out of the count scan: no table clear.
+        SPH_CUDA(launch_counting_grid(pos_, tank_of_, d_tanks_, n, total_buckets_, grid_, counts_, block_sums_, bucket_,
+                                      stream_, launches));
+    } else if (onesweep_) {
+        SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
         const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
         SPH_CUDA(launch_keys_onesweep(pos_, tank_of_, d_tanks_, n, grid_.keys, passes, sweep_, stream_));
         SPH_CUDA(launch_onesweep_sort(grid_, n, passes, sweep_, stream_, launches));
     } else {
+        SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
         SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
         SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, launches));
     }
@@ -722,8 +729,13 @@ int Engine::enqueue_bounds(uint32_t* launches) {
         schedule.rank = rank_;
         schedule.order = order_;
     }
-    SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_, svel_,
-                                  stank_, schedule, stream_));
+    if (counting_) {
+        SPH_CUDA(launch_order_gather(grid_, n, bucket_, counts_, pos_, vel_, tank_of_, spos_, svel_, stank_, schedule,
+                                     stream_));
+    } else {
+        SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_,
+                                      svel_, stank_, schedule, stream_));
+    }
     tuning_.order = schedule_curve_ != 0 ? order_ : nullptr;
     if (launches != nullptr) {
         *launches += 1;
@@ -1095,6 +1107,7 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
     const uint32_t original_bits = radix_bits_;
     const uint32_t original_schedule = schedule_curve_;
     const bool original_onesweep = onesweep_;
+    const bool original_counting = counting_;
     auto measure = [&](const TuneChoice& c, float* ms) -> int {
         int st = set_tuning(c.tuning);
         if (st == SPH_OK) {
@@ -1105,6 +1118,9 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
         }
         if (st == SPH_OK) {
             st = set_onesweep(c.onesweep);
+        }
+        if (st == SPH_OK) {
+            st = set_counting(c.counting);
         }
         if (st == SPH_OK) {
             st = snapshot(false);
@@ -1142,6 +1158,7 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
                 c.schedule = schedule;
                 c.radix_bits = original_bits;
                 c.onesweep = original_onesweep;
+                c.counting = original_counting;
                 stage1.push_back(c);
             }
         }
@@ -1159,14 +1176,17 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
             tried->push_back(c);
         }
     }
-    // Stage 2: the grid sort (one-sweep, or three kernels per pass at 5-8 bits).
+    // Stage 2: the grid sort (counting placement, one-sweep, or three kernels
+    // per pass at 5-8 bits).
     const TuneChoice stage1_winner = winner;
-    for (uint32_t bits : {0u, 5u, 6u, 7u, 8u}) {
+    for (uint32_t bits : {1u, 0u, 5u, 6u, 7u, 8u}) {
         TuneChoice c = stage1_winner;
-        c.onesweep = bits == 0;
-        c.radix_bits = bits == 0 ? stage1_winner.radix_bits : bits;
-        if (status != SPH_OK || (c.onesweep == stage1_winner.onesweep &&
-                                 (c.onesweep || c.radix_bits == stage1_winner.radix_bits))) {
+        c.counting = bits == 1;
+        c.onesweep = bits <= 1;
+        c.radix_bits = bits <= 1 ? stage1_winner.radix_bits : bits;
+        if (status != SPH_OK ||
+            (c.counting == stage1_winner.counting && c.onesweep == stage1_winner.onesweep &&
+             (c.counting || c.onesweep || c.radix_bits == stage1_winner.radix_bits))) {
             continue;
         }
         status = measure(c, &c.ms);
@@ -1192,12 +1212,16 @@ int Engine::autotune(float dt, uint32_t substeps, TuneChoice* best, std::vector<
         if (status == SPH_OK) {
             status = set_onesweep(winner.onesweep);
         }
+        if (status == SPH_OK) {
+            status = set_counting(winner.counting);
+        }
         *best = winner;
     } else {
         set_tuning(original);
         set_schedule(original_schedule);
         set_radix_bits(original_bits);
         set_onesweep(original_onesweep);
+        set_counting(original_counting);
     }
     cudaEventDestroy(start);
     cudaEventDestroy(stop);
@@ -1432,7 +1456,7 @@ int Engine::grid_download(uint32_t tank, uint32_t* cell_of, uint32_t* cell_count
     SPH_CUDA(cudaSetDevice(device_));
     SPH_CUDA(cudaStreamSynchronize(stream_));
     // The sort buffers an earlier substep left hold its result.
-    if (grid_.sorted_keys == nullptr) {
+    if (grid_.sorted_ids == nullptr) {
         RadixPlan p = plan_;
         grid_.sorted_keys = p.passes % 2 == 1 ? grid_.keys_a : grid_.keys_b;
         grid_.sorted_ids = p.passes % 2 == 1 ? grid_.vals_a : grid_.vals_b;
@@ -1579,6 +1603,11 @@ int Engine::set_tuning(const NeighbourTuning& tuning) {
     return SPH_OK;
 }
 
+int Engine::set_counting(bool on) {
+    counting_ = on;
+    return set_onesweep(onesweep_);  // drops the graphs and the grid as a sort change does
+}
+
 int Engine::set_onesweep(bool on) {
     onesweep_ = on;
     if (graph_ != nullptr) {
@@ -1651,17 +1680,22 @@ int Engine::profile(float dt, uint32_t substeps, double* phase_ms) {
         if ((status = prepare_schedule(nullptr)) != SPH_OK) {  // counted with the keys
             return status;
         }
-        SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
         const uint32_t passes = onesweep_passes(bit_width(total_buckets_ - 1U));
-        if (onesweep_) {
+        if (counting_) {
+            // keys: the whole counting placement; sort: nothing left.
+            SPH_CUDA(launch_counting_grid(pos_, tank_of_, d_tanks_, n, total_buckets_, grid_, counts_, block_sums_,
+                                          bucket_, stream_, nullptr));
+        } else if (onesweep_) {
+            SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
             SPH_CUDA(launch_keys_onesweep(pos_, tank_of_, d_tanks_, n, grid_.keys, passes, sweep_, stream_));
         } else {
+            SPH_CUDA(cudaMemsetAsync(bucket_, 0, sizeof(uint2) * total_buckets_, stream_));
             SPH_CUDA(launch_keys(pos_, tank_of_, d_tanks_, n, grid_.keys, stream_));
         }
         SPH_CUDA(cudaEventRecord(events_[1], stream_));
-        if (onesweep_) {
+        if (!counting_ && onesweep_) {
             SPH_CUDA(launch_onesweep_sort(grid_, n, passes, sweep_, stream_, nullptr));
-        } else {
+        } else if (!counting_) {
             SPH_CUDA(launch_radix_sort(grid_, n, plan_, stream_, nullptr));
         }
         SPH_CUDA(cudaEventRecord(events_[2], stream_));

@@ -35,6 +35,7 @@ struct TuneChoice {
     uint32_t radix_bits = 6;
     uint32_t schedule = 0;  // processing order: 0 sorted, 1 Morton, 2 Hilbert
     bool onesweep = true;
+    bool counting = false;  // grid sort mode 2 (counting placement), over onesweep
     float ms = 0.0F;
 };
 
@@ -103,6 +104,9 @@ public:
     // radix_bits-wide pass.
     int set_onesweep(bool on);
     bool onesweep_on() const { return onesweep_; }
+    // Grid sort mode 2: counting placement instead of the radix passes.
+    int set_counting(bool on);
+    bool counting_on() const { return counting_; }
     int selftest_division(uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
     const NeighbourTuning& tuning() const { return tuning_; }
     uint32_t radix_bits() const { return radix_bits_; }
@@ -176,6 +180,9 @@ private:
     uint32_t* compact_ranges_ = nullptr;   // (global base, compact base, count) per active tank
     std::vector<uint32_t> compact_ranges_host_;
     bool onesweep_ = true;
+    bool counting_ = true;
+    uint32_t* counts_ = nullptr;      // per bucket: counting placement
+    uint32_t* block_sums_ = nullptr;  // its scan's block sums
     unsigned long long* sweep_ = nullptr;  // per-pass tile digit counts and histograms of the one-kernel passes
     float const_dt_ = -1.0f;
     bool consts_dirty_ = true;   // tank table to upload (constants, counts, active flags)

@@ -45,6 +45,256 @@ __global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ po
     keys[i] = __ldg(&t->bucket_base) + spatial_hash(cx, cy, cz, __ldg(&t->cell_mask));
 }
 
+// ---- counting placement (grid sort mode 2) -----------------------------------
+//
+// The grid without a radix sort. Every particle takes a place in its bucket
+// with one atomic add (count_keys_kernel), an exclusive scan of the bucket
+// counts gives every bucket its range in the sorted arrays (and so the bucket
+// table), and the particles are placed in those ranges in the atomics'
+// arbitrary order (place_kernel). order_gather_kernel then puts each bucket's
+// first min(count, 32) particles by id at the front of its range in ascending
+// id order, which is the reference's insertion order (fluid_sph.cpp:160-188),
+// and gathers their state there; the rest of an overflowing bucket follows in
+// any order, and no neighbour walk reads past its 32nd entry.
+
+constexpr uint32_t kScanItems = 16;                       // counts per thread of a scan block
+constexpr uint32_t kScanTile = 256 * kScanItems;          // 4,096 buckets per scan block
+
+__global__ void __launch_bounds__(256) count_keys_kernel(const float4* __restrict__ pos,
+                                                         const uint16_t* __restrict__ tank_of,
+                                                         const TankConst* __restrict__ tanks, uint32_t n,
+                                                         uint32_t* __restrict__ keys, uint32_t* __restrict__ ranks,
+                                                         uint32_t* __restrict__ counts) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const TankConst* t = tanks + (tank_of != nullptr ? tank_of[i] : 0);
+    const float h = __ldg(&t->h);
+    const float4 p = pos[i];
+    const uint32_t cx = static_cast<uint32_t>(cell_coord(p.x, h));
+    const uint32_t cy = static_cast<uint32_t>(cell_coord(p.y, h));
+    const uint32_t cz = static_cast<uint32_t>(cell_coord(p.z, h));
+    const uint32_t key = __ldg(&t->bucket_base) + spatial_hash(cx, cy, cz, __ldg(&t->cell_mask));
+    keys[i] = key;
+    ranks[i] = atomicAdd(&counts[key], 1u);
+}
+
+// Block sums of the bucket counts, kScanTile buckets a block.
+__global__ void __launch_bounds__(256) scan_reduce_kernel(const uint32_t* __restrict__ counts, uint32_t buckets,
+                                                          uint32_t* __restrict__ block_sums) {
+    const uint32_t first = blockIdx.x * kScanTile;
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t r = 0; r < kScanItems; ++r) {
+        const uint32_t b = first + r * 256u + threadIdx.x;
+        sum += b < buckets ? __ldg(&counts[b]) : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+    }
+    __shared__ uint32_t warp_sums[8];
+    if ((threadIdx.x & 31u) == 0) {
+        warp_sums[threadIdx.x >> 5] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) {
+            total += warp_sums[w];
+        }
+        block_sums[blockIdx.x] = total;
+    }
+}
+
+// Exclusive scan of the block sums in place: one block of 1,024 threads, in
+// rounds of 1,024 sums carried over.
+__global__ void __launch_bounds__(1024) scan_top_kernel(uint32_t* __restrict__ block_sums, uint32_t blocks) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) {
+        carry = 0;
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < blocks; base += 1024u) {
+        const uint32_t b = base + threadIdx.x;
+        const uint32_t v = b < blocks ? block_sums[b] : 0u;
+        uint32_t inc = v;
+#pragma unroll
+        for (uint32_t o = 1; o < 32u; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) {
+                inc += u;
+            }
+        }
+        if (lane == 31u) {
+            warp_sums[warp] = inc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane];
+            uint32_t winc = w;
+#pragma unroll
+            for (uint32_t o = 1; o < 32u; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, winc, o);
+                if (lane >= o) {
+                    winc += u;
+                }
+            }
+            warp_sums[lane] = winc - w;  // exclusive warp offsets
+        }
+        __syncthreads();
+        const uint32_t before = carry + warp_sums[warp] + inc - v;
+        if (b < blocks) {
+            block_sums[b] = before;
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023u) {
+            carry = before + v;
+        }
+        __syncthreads();
+    }
+}
+
+// The bucket table from the counts and the scanned block sums: bucket b's
+// range is [start, start + count) in the sorted arrays. The counts are reset
+// on the way (the final ordering counts an overflowing bucket's tail in them).
+__global__ void __launch_bounds__(256) scan_down_kernel(uint32_t* __restrict__ counts, uint32_t buckets,
+                                                        const uint32_t* __restrict__ block_sums,
+                                                        uint2* __restrict__ bucket) {
+    static_assert(kScanItems % 4 == 0, "counts move as uint4");
+    const uint32_t first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t c[kScanItems];
+    // Whole uint4 groups when the thread's buckets are all present (buckets
+    // is then a multiple of 4 past them); element by element at the end.
+    const bool whole = first + kScanItems <= buckets;
+    if (whole) {
+        const uint4* src = reinterpret_cast<const uint4*>(counts + first);
+#pragma unroll
+        for (uint32_t r = 0; r < kScanItems / 4; ++r) {
+            const uint4 v = src[r];
+            c[4 * r] = v.x;
+            c[4 * r + 1] = v.y;
+            c[4 * r + 2] = v.z;
+            c[4 * r + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (uint32_t r = 0; r < kScanItems; ++r) {
+            c[r] = first + r < buckets ? counts[first + r] : 0u;
+        }
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t r = 0; r < kScanItems; ++r) {
+        sum += c[r];
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = threadIdx.x >> 5;
+    uint32_t inc = sum;
+#pragma unroll
+    for (uint32_t o = 1; o < 32u; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) {
+            inc += u;
+        }
+    }
+    __shared__ uint32_t warp_sums[8];
+    if (lane == 31u) {
+        warp_sums[warp] = inc;
+    }
+    __syncthreads();
+    uint32_t start = block_sums[blockIdx.x] + inc - sum;
+    for (uint32_t w = 0; w < warp; ++w) {
+        start += warp_sums[w];
+    }
+    if (whole) {
+        uint4* dst = reinterpret_cast<uint4*>(bucket + first);
+#pragma unroll
+        for (uint32_t r = 0; r < kScanItems / 2; ++r) {
+            const uint32_t a = start;
+            const uint32_t b = a + c[2 * r];
+            const uint32_t e = b + c[2 * r + 1];
+            dst[r] = make_uint4(a, b, b, e);
+            start = e;
+        }
+        uint4* zero = reinterpret_cast<uint4*>(counts + first);
+#pragma unroll
+        for (uint32_t r = 0; r < kScanItems / 4; ++r) {
+            zero[r] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    } else {
+#pragma unroll
+        for (uint32_t r = 0; r < kScanItems; ++r) {
+            const uint32_t b = first + r;
+            if (b < buckets) {
+                bucket[b] = make_uint2(start, start + c[r]);
+                counts[b] = 0;
+            }
+            start += c[r];
+        }
+    }
+}
+
+// Each particle at its bucket's start plus its atomic rank (any order).
+__global__ void __launch_bounds__(256) place_kernel(const uint32_t* __restrict__ keys,
+                                                    const uint32_t* __restrict__ ranks, uint32_t n,
+                                                    const uint2* __restrict__ bucket, uint32_t* __restrict__ placed) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        placed[__ldg(&bucket[keys[i]]).x + ranks[i]] = i;
+    }
+}
+
+// The final order and the gather in one pass, a thread per placed slot:
+// particle i (placed in its bucket in the atomics' order) counts the members
+// of its bucket with a smaller id (all of them in a bucket of at most
+// kCountAll, else until it has found 32), which is its place when below 32
+// (the reference's insertion order, ascending ids); the rest of an
+// overflowing bucket follows the 32 in any order (an atomic count), and no
+// neighbour walk reads past a bucket's 32nd entry. The particle's state, tank
+// and processing slot go to that place as bounds_gather_kernel writes them.
+constexpr uint32_t kCountAll = 64;  // buckets up to this size are ranked in full
+
+__global__ void __launch_bounds__(256) order_gather_kernel(const uint32_t* __restrict__ keys,
+                                                           const uint32_t* __restrict__ placed, uint32_t n,
+                                                           const uint2* __restrict__ bucket,
+                                                           uint32_t* __restrict__ tail_counts,
+                                                           uint32_t* __restrict__ sorted_ids,
+                                                           const float4* __restrict__ pos,
+                                                           const float4* __restrict__ vel,
+                                                           const uint16_t* __restrict__ tank_of,
+                                                           float4* __restrict__ spos, float4* __restrict__ svel,
+                                                           uint16_t* __restrict__ stank, Schedule schedule) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) {
+        return;
+    }
+    const uint32_t i = placed[q];
+    const uint32_t key = keys[i];
+    const uint2 r = __ldg(&bucket[key]);
+    const bool full = r.y - r.x <= kCountAll;
+    uint32_t smaller = 0;
+    for (uint32_t k = r.x; k < r.y && (full || smaller < kCellCapacity); ++k) {
+        smaller += __ldg(&placed[k]) < i ? 1u : 0u;
+    }
+    const uint32_t p = full || smaller < kCellCapacity ? r.x + smaller
+                                                        : r.x + kCellCapacity + atomicAdd(&tail_counts[key], 1u);
+    sorted_ids[p] = i;
+    spos[p] = pos[i];
+    svel[p] = vel[i];
+    if (tank_of != nullptr) {
+        stank[p] = tank_of[i];
+    }
+    if (schedule.rank != nullptr) {
+        schedule.order[schedule.rank[i]] = p;
+    }
+}
+
 // Per-tile digit histogram, written digit-major: hist[d * tiles + tile].
 __global__ void __launch_bounds__(kRadixThreads) radix_upsweep(const uint32_t* __restrict__ keys, uint32_t n,
                                                                uint32_t shift, uint32_t mask, uint32_t tiles,
@@ -219,12 +469,14 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
     if (p >= n) {
         return;
     }
-    uint32_t key = sorted_keys[p];
-    if (p == 0 || sorted_keys[p - 1] != key) {
-        bucket_words[2 * static_cast<size_t>(key)] = p;
-    }
-    if (p + 1 == n || sorted_keys[p + 1] != key) {
-        bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
+    if (sorted_keys != nullptr) {  // else the counting placement wrote the bucket table
+        uint32_t key = sorted_keys[p];
+        if (p == 0 || sorted_keys[p - 1] != key) {
+            bucket_words[2 * static_cast<size_t>(key)] = p;
+        }
+        if (p + 1 == n || sorted_keys[p + 1] != key) {
+            bucket_words[2 * static_cast<size_t>(key) + 1] = p + 1;
+        }
     }
     uint32_t i = sorted_ids[p];
     if (ids != nullptr) {
@@ -770,6 +1022,45 @@ RadixPlan plan_radix(uint32_t key_bits, uint32_t digit_bits) {
     }
     plan.passes = passes;
     return plan;
+}
+
+size_t counting_block_sums(uint32_t buckets) { return (static_cast<size_t>(buckets) + kScanTile - 1) / kScanTile; }
+
+cudaError_t launch_counting_grid(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                 uint32_t buckets, GridScratch& s, uint32_t* counts, uint32_t* block_sums,
+                                 uint2* bucket, cudaStream_t stream, uint32_t* launches) {
+    s.sorted_keys = nullptr;
+    s.sorted_ids = s.vals_b;
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * buckets, stream);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    const uint32_t particle_blocks = (n + 255) / 256;
+    const uint32_t scan_blocks = static_cast<uint32_t>(counting_block_sums(buckets));
+    if (n > 0) {
+        count_keys_kernel<<<particle_blocks, 256, 0, stream>>>(pos, tank_of, tanks, n, s.keys, s.keys_a, counts);
+    }
+    scan_reduce_kernel<<<scan_blocks, 256, 0, stream>>>(counts, buckets, block_sums);
+    scan_top_kernel<<<1, 1024, 0, stream>>>(block_sums, scan_blocks);
+    scan_down_kernel<<<scan_blocks, 256, 0, stream>>>(counts, buckets, block_sums, bucket);
+    if (n > 0) {
+        place_kernel<<<particle_blocks, 256, 0, stream>>>(s.keys, s.keys_a, n, bucket, s.vals_a);
+    }
+    if (launches != nullptr) {
+        *launches += n > 0 ? 5 : 3;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_order_gather(const GridScratch& s, uint32_t n, const uint2* bucket, uint32_t* counts,
+                                const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
+                                float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    order_gather_kernel<<<(n + 255) / 256, 256, 0, stream>>>(s.keys, s.vals_a, n, bucket, counts, s.vals_b, pos, vel,
+                                                             tank_of, spos, svel, stank, schedule);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_keys(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n, uint32_t* keys,

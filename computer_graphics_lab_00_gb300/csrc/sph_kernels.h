@@ -47,6 +47,18 @@ struct GridScratch {
     const uint32_t* sorted_ids = nullptr;
 };
 
+// The grid without a radix sort (sort mode 2): one atomic place per particle
+// in its bucket and an exclusive scan of the bucket counts (the bucket
+// table); launch_order_gather then puts each bucket's 32 smallest ids at its
+// front in ascending order and gathers the state there. keys -> s.keys (id
+// order), sorted ids -> s.vals_b (s.keys_a, s.vals_a: atomic ranks and the
+// unordered placement); s.sorted_keys becomes null. counts: `buckets` words;
+// block_sums: counting_block_sums(buckets) words.
+size_t counting_block_sums(uint32_t buckets);
+cudaError_t launch_counting_grid(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                 uint32_t buckets, GridScratch& s, uint32_t* counts, uint32_t* block_sums,
+                                 uint2* bucket, cudaStream_t stream, uint32_t* launches);
+
 cudaError_t launch_keys(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n, uint32_t* keys,
                         cudaStream_t stream);
 
@@ -98,6 +110,12 @@ struct Schedule {
     const uint32_t* rank = nullptr;  // n: processing slot of each particle id
     uint32_t* order = nullptr;       // n: sorted positions in processing order
 };
+
+// The counting placement's final step (after launch_counting_grid): each
+// bucket's 32 smallest ids in ascending order at its front, and the gather.
+cudaError_t launch_order_gather(const GridScratch& s, uint32_t n, const uint2* bucket, uint32_t* counts,
+                                const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
+                                float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream);
 
 // Morton keys of the particles' cells (morton_bits bits per axis, counted
 // from each tank's low corner and clamped, the tank index above them), sorted

@@ -285,7 +285,8 @@ class FluidSolverGpu:
         return out.as_dict()
 
     def set_tuning(self, **knobs) -> None:
-        """Changes the launch shape (radix_bits, neighbour_kernel, block_size, queue_depth)."""
+        """Changes the launch shape (radix_bits, neighbour_kernel, block_size, queue_depth,
+        schedule, sort)."""
         current = self.tuning()
         current.update(knobs)
         t = abi.SphTuning(**current)

@@ -141,7 +141,11 @@ typedef struct sph_tuning {
                                   8 grid builds */
     uint32_t sort;             /* grid sort: 0 three kernels per digit pass (radix_bits wide);
                                   1 one kernel per 8-bit pass, tile offsets from tile digit counts
-                                    made by the previous pass (radix_bits unused) */
+                                    made by the previous pass (radix_bits unused);
+                                  2 (default) counting placement: one atomic place per particle in its
+                                    bucket, a scan of the bucket counts, each bucket's 32 smallest ids
+                                    put at its front in order with the gather (no radix passes).
+                                  The particle sets of the learned form's fallback use sort 1. */
 } sph_tuning;
 
 typedef struct sph_ctx sph_ctx;
@@ -381,7 +385,10 @@ int sph_run(sph_ctx* ctx, float dt, uint32_t substeps);
  * each phase, measured with CUDA events on the context stream, to
  * phase_ms[0..5]: keys, radix sort, bounds + gather, density, integrate, and
  * shapes (the force-field and collider passes; 0 without fields and
- * colliders). Synchronises. Results are identical to sph_run. */
+ * colliders). Under sort 2 the keys phase holds the counting placement up to
+ * the scan and placement, the sort phase nothing, and bounds + gather the
+ * final ordering with the gather. Synchronises. Results are identical to
+ * sph_run. */
 #define SPH_PROFILE_PHASES 6
 int sph_profile_substeps(sph_ctx* ctx, float dt, uint32_t substeps, double* phase_ms);
 /* Reads / replaces the launch shape (an autotuner's knobs). */

@@ -136,8 +136,8 @@ def test_ragged_counts_bit_exact(native, oracle, n):
     assert_bit_exact(gv, ov, f"velocities n={n}")
 
 
-@pytest.mark.parametrize("variant", [4, 6])
-def test_overflowing_bucket_keeps_first_32_ids(native, oracle, variant):
+@pytest.mark.parametrize("variant,sort", [(4, 1), (6, 1), (4, 2), (4, 0)])
+def test_overflowing_bucket_keeps_first_32_ids(native, oracle, variant, sort):
     """More than 32 particles in one cell: only the first 32 by id are
     neighbours (fluid_sph.cpp:179-187); counts stay un-truncated."""
     params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
@@ -150,7 +150,7 @@ def test_overflowing_bucket_keeps_first_32_ids(native, oracle, variant):
     pos[:, 3] = 1000.0
     vel = np.zeros((n, 4), np.float32)
     with FluidSolverGpu(params, n) as solver:
-        solver.set_tuning(neighbour_kernel=variant)
+        solver.set_tuning(neighbour_kernel=variant, sort=sort)
         solver.upload(pos, vel)
         solver.build_grid()
         grid = solver.grid()
@@ -162,6 +162,35 @@ def test_overflowing_bucket_keeps_first_32_ids(native, oracle, variant):
     op, ov = oracle.substep(params, pos, vel, 1.0 / 600.0)
     assert_bit_exact(gp, op, "positions with an overflowing bucket")
     assert_bit_exact(gv, ov, "velocities with an overflowing bucket")
+
+
+@pytest.mark.parametrize("sort", [1, 2])
+def test_one_crowded_cell(native, oracle, sort):
+    """3,000 of 3,100 particles in one cell: the counting placement ranks a
+    bucket past 64 members only until it has found 32 smaller ids, and must
+    still put the 32 smallest first in order; the grid and a substep equal
+    the oracle's."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
+                           lattice=(4, 4, 8), cell_count=1024)
+    rng = np.random.default_rng(11)
+    n = 3100
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = (0.481 + rng.uniform(0.0, 0.038, size=(n, 3))).astype(np.float32)
+    pos[rng.permutation(n)[:100], :3] = rng.uniform(0.1, 0.9, size=(100, 3)).astype(np.float32)
+    pos[:, 3] = 1000.0
+    vel = np.zeros((n, 4), np.float32)
+    with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(sort=sort)
+        solver.upload(pos, vel)
+        solver.build_grid()
+        grid = solver.grid()
+        assert grid[1].max() >= 2900
+        solver.substep(1.0 / 600.0)
+        gp, gv = solver.state()
+    assert_grid_equal(grid, oracle.grid_build(params, pos))
+    op, ov = oracle.substep(params, pos, vel, 1.0 / 600.0)
+    assert_bit_exact(gp, op, "positions with a crowded cell")
+    assert_bit_exact(gv, ov, "velocities with a crowded cell")
 
 
 @pytest.mark.parametrize("variant,schedule", [(4, 1), (6, 1), (6, 0)])
@@ -331,6 +360,10 @@ def test_errors_are_status_codes(native):
     dict(neighbour_kernel=6, block_size=256, queue_depth=16, radix_bits=7, schedule=2, sort=1),
     dict(neighbour_kernel=6, block_size=128, queue_depth=16, radix_bits=6, schedule=0, sort=0),
     dict(neighbour_kernel=6, block_size=256, queue_depth=32, radix_bits=8, schedule=1, sort=0),
+    dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=1, sort=2),
+    dict(neighbour_kernel=4, block_size=128, queue_depth=16, radix_bits=7, schedule=0, sort=2),
+    dict(neighbour_kernel=6, block_size=128, queue_depth=16, radix_bits=7, schedule=2, sort=2),
+    dict(neighbour_kernel=1, block_size=128, queue_depth=16, radix_bits=7, schedule=1, sort=2),
 ])
 def test_launch_shapes_do_not_change_bits(native, oracle, tuning):
     """Every launch shape the autotuner may pick gives the oracle's bits."""
@@ -383,7 +416,7 @@ def test_morton_order_across_remakes_and_count_changes(native, oracle):
         assert_bit_exact(gv, ov, "velocities after the count change")
 
 
-@pytest.mark.parametrize("sort,bits", [(1, 6), (0, 5), (0, 8)])
+@pytest.mark.parametrize("sort,bits", [(1, 6), (0, 5), (0, 8), (2, 6)])
 def test_grid_sorts_agree_at_one_million(native, oracle, sort, bits):
     """The one-sweep sort (3 look-back passes over 21-bit keys at 1M) and the
     three-kernel passes give the oracle's grid bit for bit."""
@@ -424,7 +457,7 @@ def test_bad_tuning_is_rejected(native):
     with FluidSolverGpu(case.params, 16) as solver:
         for bad in (dict(block_size=100), dict(queue_depth=12), dict(neighbour_kernel=7), dict(neighbour_kernel=6, block_size=64),
                     dict(radix_bits=0),
-                    dict(radix_bits=9), dict(schedule=3), dict(sort=2)):
+                    dict(radix_bits=9), dict(schedule=3), dict(sort=3)):
             with pytest.raises(abi.SphError) as e:
                 solver.set_tuning(**bad)
             assert e.value.status == abi.SPH_ERR_INVALID_ARGUMENT
