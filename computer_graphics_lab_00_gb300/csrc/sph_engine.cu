@@ -13,6 +13,39 @@ namespace {
 // std::numbers::pi_v<float> (fluid_sph.cpp:20).
 constexpr float kPi = 3.14159265358979323846F;
 
+// step_host's id ranges for n particles: the first Engine::kHostFirstNum /
+// kHostFirstDen of the ids, then the rest, the cut on a multiple of 128
+// slots so that both ranges' mask rows stay aligned. No split when n is too
+// small for two ranges.
+IdSplit host_split(uint32_t n, uint32_t ranges) {
+    IdSplit split;
+    if (ranges != 2) {
+        return split;
+    }
+    const uint32_t cut = static_cast<uint32_t>(static_cast<uint64_t>(n) * Engine::kHostFirstNum /
+                                               Engine::kHostFirstDen) & ~127U;
+    if (cut == 0 || cut >= n) {
+        return split;
+    }
+    split.count = 2;
+    split.start[0] = 0;
+    split.start[1] = cut;
+    split.start[2] = n;
+    return split;
+}
+
+bool same_split(const IdSplit& a, const IdSplit& b) {
+    if (a.count != b.count) {
+        return false;
+    }
+    for (uint32_t c = 0; c <= a.count && a.count > 1; ++c) {
+        if (a.start[c] != b.start[c]) {
+            return false;
+        }
+    }
+    return true;
+}
+
 uint32_t bit_width(uint32_t v) {
     uint32_t bits = 0;
     while (v != 0) {
@@ -169,6 +202,7 @@ void Engine::release() {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    drop_host_graph();
     if (learned_graph_ != nullptr) {
         cudaGraphExecDestroy(learned_graph_);
         learned_graph_ = nullptr;
@@ -370,6 +404,7 @@ int Engine::update_shape_flags() {
             cudaGraphExecDestroy(graph_);
             graph_ = nullptr;
         }
+        drop_host_graph();
         if (learned_graph_ != nullptr) {
             cudaGraphExecDestroy(learned_graph_);
             learned_graph_ = nullptr;
@@ -523,9 +558,17 @@ int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, 
     if (status != SPH_OK) {
         return status;
     }
-    // Positions first: the keys and the sort read nothing else. The
-    // velocities follow on the copy stream, with upload's keepRendered copy
-    // and the non-finite check of both arrays, while those passes run.
+    // The overlapped form: one tank in a curve order, the mask kernels, no
+    // colliders (they move particles of every id range after integrate).
+    const bool overlap = tanks_.size() == 1 && schedule_curve_ != 0 && tuning_.variant == 4 && !has_colliders_ &&
+                         count >= kHostOverlapMin;
+    want_ranges_ = overlap ? kHostRanges : 0;
+    // Positions first: the grid reads nothing else. The velocities follow on
+    // the copy stream, with upload's keepRendered copy and the non-finite
+    // check of both arrays, while the grid is built. In the overlapped form
+    // the first gather leaves the velocities out and the copy stream gathers
+    // them beside the density pass (which writes only the pressure word of
+    // each sorted velocity).
     const size_t bytes = sizeof(float4) * count;
     SPH_CUDA(cudaMemcpyAsync(pos_, pos_in, bytes, cudaMemcpyHostToDevice, stream_));
     SPH_CUDA(cudaEventRecord(copy_events_[0], stream_));
@@ -540,11 +583,41 @@ int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, 
     SPH_CUDA(launch_count_nonfinite(pos_, vel_, count, bucket_stats_, copy_stream_));
     SPH_CUDA(cudaMemcpyAsync(flag_host_, bucket_stats_, sizeof(uint32_t), cudaMemcpyDeviceToHost, copy_stream_));
     SPH_CUDA(cudaEventRecord(copy_events_[1], copy_stream_));
-    // The first substep launched directly, its gather waiting for the copy
-    // stream; the rest through the graph, as run() does.
-    gather_wait_ = copy_events_[1];
-    status = enqueue_substep(nullptr);
-    gather_wait_ = nullptr;
+    if (overlap && substeps == 1) {
+        // The one-substep form from a graph (the order remade beforehand
+        // when due; the capture holds only its scatter).
+        if ((status = prepare_schedule(nullptr)) != SPH_OK || (status = ensure_host_graph()) != SPH_OK) {
+            return status;
+        }
+        SPH_CUDA(cudaGraphLaunch(host_graph_, stream_));
+    } else if (overlap) {
+        defer_vel_ = true;
+        status = enqueue_grid(nullptr);
+        defer_vel_ = false;
+        if (status != SPH_OK) {
+            return status;
+        }
+        // The copy stream: sorted ids ready -> velocities gathered. Integrate
+        // waits for it, and so for the check before it (integrate rewrites
+        // the arrays the check and the keepRendered copy read).
+        SPH_CUDA(cudaEventRecord(copy_events_[2], stream_));
+        SPH_CUDA(cudaStreamWaitEvent(copy_stream_, copy_events_[2], 0));
+        SPH_CUDA(launch_gather_vel(grid_.sorted_ids, count, vel_, svel_, copy_stream_));
+        SPH_CUDA(cudaEventRecord(copy_events_[3], copy_stream_));
+        if ((status = enqueue_fields(nullptr)) != SPH_OK) {
+            return status;
+        }
+        SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, count, nullptr, stream_, tuning_));
+        SPH_CUDA(cudaStreamWaitEvent(stream_, copy_events_[3], 0));
+        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, count, pos_, vel_,
+                                  stream_, tuning_));
+    } else {
+        // The first substep launched directly, its gather waiting for the
+        // copy stream; the rest through the graph, as run() does.
+        gather_wait_ = copy_events_[1];
+        status = enqueue_substep(nullptr);
+        gather_wait_ = nullptr;
+    }
     if (status != SPH_OK) {
         return status;
     }
@@ -552,28 +625,155 @@ int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, 
         if ((status = ensure_graph()) != SPH_OK) {
             return status;
         }
-        for (uint32_t s = 1; s < substeps; ++s) {
+        const uint32_t graphed = overlap ? substeps - 1 : substeps;
+        for (uint32_t s = 1; s < graphed; ++s) {
             if ((status = prepare_schedule(nullptr)) != SPH_OK) {
                 return status;
             }
             SPH_CUDA(cudaGraphLaunch(graph_, stream_));
         }
+        if (overlap) {  // the last substep direct, its integrate in id ranges
+            if ((status = enqueue_grid(nullptr)) != SPH_OK || (status = enqueue_fields(nullptr)) != SPH_OK) {
+                return status;
+            }
+            SPH_CUDA(
+                launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, count, nullptr, stream_, tuning_));
+            if ((status = enqueue_integrate_ranges()) != SPH_OK) {
+                return status;
+            }
+        }
     }
     grid_valid_ = true;
     // The check lands long before the substeps end: read it then, and queue
-    // the download behind them so that it starts as the last pass ends.
+    // the download behind them so that it starts as the last pass ends (in
+    // the overlapped form, each id range's rows as soon as they are
+    // integrated).
     SPH_CUDA(cudaEventSynchronize(copy_events_[1]));
     if (*flag_host_ != 0) {
         SPH_CUDA(cudaStreamSynchronize(stream_));
         return SPH_ERR_NONFINITE;  // the caller's arrays are left as they were
     }
-    if (pos_out != nullptr) {
-        SPH_CUDA(cudaMemcpyAsync(pos_out, pos_, bytes, cudaMemcpyDeviceToHost, stream_));
-    }
-    if (vel_out != nullptr) {
-        SPH_CUDA(cudaMemcpyAsync(vel_out, vel_, bytes, cudaMemcpyDeviceToHost, stream_));
+    if (overlap) {
+        const uint32_t ranges = rank_split_.count > 1 ? rank_split_.count : 1U;
+        for (uint32_t c = 0; c < ranges; ++c) {
+            const size_t first = ranges > 1 ? rank_split_.start[c] : 0;
+            const size_t rows = (ranges > 1 ? rank_split_.start[c + 1] : count) - first;
+            SPH_CUDA(cudaStreamWaitEvent(copy_stream_, copy_events_[4 + c], 0));
+            if (pos_out != nullptr) {
+                SPH_CUDA(cudaMemcpyAsync(pos_out + 4 * first, pos_ + first, sizeof(float4) * rows,
+                                         cudaMemcpyDeviceToHost, copy_stream_));
+            }
+            if (vel_out != nullptr) {
+                SPH_CUDA(cudaMemcpyAsync(vel_out + 4 * first, vel_ + first, sizeof(float4) * rows,
+                                         cudaMemcpyDeviceToHost, copy_stream_));
+            }
+        }
+        SPH_CUDA(cudaStreamSynchronize(copy_stream_));
+    } else {
+        if (pos_out != nullptr) {
+            SPH_CUDA(cudaMemcpyAsync(pos_out, pos_, bytes, cudaMemcpyDeviceToHost, stream_));
+        }
+        if (vel_out != nullptr) {
+            SPH_CUDA(cudaMemcpyAsync(vel_out, vel_, bytes, cudaMemcpyDeviceToHost, stream_));
+        }
     }
     SPH_CUDA(cudaStreamSynchronize(stream_));
+    return SPH_OK;
+}
+
+// The integrate pass over the id ranges of the processing order, range by
+// range, an event after each (step_host downloads range c's rows once its
+// event fires). Without ranges in the order: one whole pass, one event.
+// While capturing, the events become the graph's external event records.
+int Engine::enqueue_integrate_ranges() {
+    const uint32_t n = total_count_;
+    const uint32_t ranges = rank_split_.count > 1 && schedule_curve_ != 0 ? rank_split_.count : 1U;
+    NeighbourTuning t = tuning_;
+    for (uint32_t c = 0; c < ranges; ++c) {
+        if (ranges > 1) {
+            t.slot_begin = rank_split_.start[c];
+            t.slot_end = rank_split_.start[c + 1];
+        }
+        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_, t));
+        SPH_CUDA(cudaEventRecordWithFlags(copy_events_[4 + c], stream_,
+                                          capturing_ ? cudaEventRecordExternal : cudaEventRecordDefault));
+    }
+    return SPH_OK;
+}
+
+void Engine::drop_host_graph() {
+    if (host_graph_ != nullptr) {
+        cudaGraphExecDestroy(host_graph_);
+        host_graph_ = nullptr;
+    }
+}
+
+// step_host's one-substep overlapped form as a graph on stream_: the grid
+// (its gather without velocities), the velocity gather on the copy stream once
+// the ids are sorted and the upload is checked (events[1], recorded outside),
+// density beside it, then integrate by id ranges with an external event after
+// each. Captured again when the count, the order's id ranges or the launch
+// shape change.
+int Engine::ensure_host_graph() {
+    if (host_graph_ != nullptr && host_graph_count_ == total_count_ && same_split(host_graph_split_, rank_split_)) {
+        return SPH_OK;
+    }
+    drop_host_graph();
+    const uint32_t n = total_count_;
+    cudaGraph_t graph = nullptr;
+    SPH_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    capturing_ = true;
+    defer_vel_ = true;
+    int status = enqueue_grid(nullptr);
+    defer_vel_ = false;
+    cudaError_t err = cudaSuccess;
+    if (status == SPH_OK) {
+        err = cudaEventRecord(copy_events_[2], stream_);
+        if (err == cudaSuccess) {
+            err = cudaStreamWaitEvent(copy_stream_, copy_events_[2], 0);  // the copy stream joins the capture
+        }
+        if (err == cudaSuccess) {
+            err = cudaStreamWaitEvent(copy_stream_, copy_events_[1], cudaEventWaitExternal);
+        }
+        if (err == cudaSuccess) {
+            err = launch_gather_vel(grid_.sorted_ids, n, vel_, svel_, copy_stream_);
+        }
+        if (err == cudaSuccess) {
+            err = cudaEventRecord(copy_events_[3], copy_stream_);
+        }
+    }
+    if (status == SPH_OK && err == cudaSuccess) {
+        status = enqueue_fields(nullptr);
+    }
+    if (status == SPH_OK && err == cudaSuccess) {
+        err = launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, tuning_);
+        if (err == cudaSuccess) {
+            err = cudaStreamWaitEvent(stream_, copy_events_[3], 0);  // and rejoins it
+        }
+    }
+    if (status == SPH_OK && err == cudaSuccess) {
+        status = enqueue_integrate_ranges();
+    }
+    capturing_ = false;
+    const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
+    if (status == SPH_OK && err == cudaSuccess) {
+        err = end;
+    }
+    if (err == cudaSuccess && status == SPH_OK) {
+        err = cudaGraphInstantiate(&host_graph_, graph, 0);
+    }
+    if (graph != nullptr) {
+        cudaGraphDestroy(graph);
+    }
+    if (status != SPH_OK) {
+        return status;
+    }
+    if (err != cudaSuccess) {
+        host_graph_ = nullptr;
+        return fail(err, "step_host graph");
+    }
+    host_graph_count_ = n;
+    host_graph_split_ = rank_split_;
     return SPH_OK;
 }
 
@@ -653,16 +853,24 @@ int Engine::prepare_schedule(uint32_t* launches) {
     if (schedule_curve_ == 0 || total_count_ == 0) {
         return SPH_OK;
     }
-    if (rank_count_ == total_count_ && since_refresh_ + 1 < kScheduleRefresh) {
-        ++since_refresh_;
-        return SPH_OK;
-    }
     uint32_t axis_bits = 0;
     uint32_t key_bits = 0;
     schedule_bits(&axis_bits, &key_bits);
+    IdSplit split = host_split(total_count_, want_ranges_);
+    if (key_bits + bit_width(split.count > 1 ? split.count - 1U : 0U) > 32) {
+        split = IdSplit{};
+    }
+    // Wanted id ranges that the order lacks force a remake; ranges no longer
+    // wanted leave with the next regular refresh.
+    if (rank_count_ == total_count_ && since_refresh_ + 1 < kScheduleRefresh &&
+        (want_ranges_ == 0 || same_split(rank_split_, split))) {
+        ++since_refresh_;
+        return SPH_OK;
+    }
     SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, key_bits, grid_, sweep_, rank_,
-                                stream_, launches, schedule_curve_ == 2));
+                                stream_, launches, schedule_curve_ == 2, nullptr, split));
     rank_count_ = total_count_;
+    rank_split_ = split;
     since_refresh_ = 0;
     return SPH_OK;
 }
@@ -729,11 +937,12 @@ int Engine::enqueue_bounds(uint32_t* launches) {
         schedule.rank = rank_;
         schedule.order = order_;
     }
+    const float4* vel = defer_vel_ ? nullptr : vel_;  // else step_host gathers them beside the density pass
     if (counting_) {
-        SPH_CUDA(launch_order_gather(grid_, n, bucket_, counts_, pos_, vel_, tank_of_, spos_, svel_, stank_, schedule,
+        SPH_CUDA(launch_order_gather(grid_, n, bucket_, counts_, pos_, vel, tank_of_, spos_, svel_, stank_, schedule,
                                      stream_));
     } else {
-        SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel_, tank_of_, spos_,
+        SPH_CUDA(launch_bounds_gather(grid_.sorted_keys, grid_.sorted_ids, n, bucket_, pos_, vel, tank_of_, spos_,
                                       svel_, stank_, schedule, stream_));
     }
     tuning_.order = schedule_curve_ != 0 ? order_ : nullptr;
@@ -769,6 +978,7 @@ int Engine::ensure_graph() {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    drop_host_graph();
     int status = prepare_schedule(nullptr);
     if (status != SPH_OK) {
         return status;
@@ -809,6 +1019,7 @@ int Engine::run(float dt, uint32_t substeps) {
         return SPH_OK;
     }
     SPH_CUDA(cudaSetDevice(device_));
+    want_ranges_ = 0;  // the next regular refresh drops step_host's id ranges
     int status = refresh_constants(dt);
     if (status != SPH_OK) {
         return status;
@@ -1600,6 +1811,7 @@ int Engine::set_tuning(const NeighbourTuning& tuning) {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    drop_host_graph();
     return SPH_OK;
 }
 
@@ -1614,6 +1826,7 @@ int Engine::set_onesweep(bool on) {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    drop_host_graph();
     if (learned_graph_ != nullptr) {
         cudaGraphExecDestroy(learned_graph_);
         learned_graph_ = nullptr;
@@ -1634,6 +1847,7 @@ int Engine::set_schedule(uint32_t curve) {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    drop_host_graph();
     grid_valid_ = false;
     return SPH_OK;
 }
@@ -1648,6 +1862,7 @@ int Engine::set_radix_bits(uint32_t bits) {
         cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
     }
+    drop_host_graph();
     grid_.sorted_keys = nullptr;
     grid_.sorted_ids = nullptr;
     grid_valid_ = false;

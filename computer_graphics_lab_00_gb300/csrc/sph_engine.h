@@ -41,6 +41,13 @@ struct TuneChoice {
 
 class Engine {
 public:
+    // step_host integrates the first kHostFirstNum / kHostFirstDen of the ids,
+    // downloads them while it integrates the rest (kHostRanges id ranges),
+    // from kHostOverlapMin particles up.
+    static constexpr uint32_t kHostRanges = 2;
+    static constexpr uint32_t kHostFirstNum = 2;
+    static constexpr uint32_t kHostFirstDen = 3;
+    static constexpr uint32_t kHostOverlapMin = 1u << 18;
     ~Engine();
 
     // Allocates for `tanks` tanks with the given capacities (particles) and
@@ -145,6 +152,11 @@ private:
     int enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launches);
     int ensure_learned_buffers();
     int enqueue_substep(uint32_t* launches);
+    // Integrate the id ranges of the processing order one by one, an event
+    // after each (step_host).
+    int enqueue_integrate_ranges();
+    int ensure_host_graph();  // captures step_host's overlapped substep
+    void drop_host_graph();
     int refresh_constants(float dt);
     void attach_shapes(uint32_t tank);  // copies tank's colliders and fields to staging, sets pointers
     int update_shape_flags();           // has_fields_ / has_colliders_; graphs recaptured on change
@@ -175,6 +187,8 @@ private:
     uint32_t* order_ = nullptr;            // sorted positions in processing order
     uint32_t rank_count_ = 0xFFFFFFFFu;    // particle count rank_ was made for
     uint32_t since_refresh_ = 0;           // grid builds since rank_ was made
+    uint32_t want_ranges_ = 0;             // id ranges the next order should carry (step_host), 0: none
+    IdSplit rank_split_{};                 // the id ranges rank_ was made with
     uint32_t* compact_ids_ = nullptr;      // ids of the active tanks' particles (a batch run with most tanks idle)
     uint32_t* compact_sorted_ = nullptr;   // their ids in sorted order, for the write-back
     uint32_t* compact_ranges_ = nullptr;   // (global base, compact base, count) per active tank
@@ -219,8 +233,14 @@ private:
     bool grid_valid_ = false;
     uint32_t nonfinite_host_ = 0;
     cudaStream_t copy_stream_ = nullptr;  // step_host: velocity upload and checks beside the keys and sort
-    cudaEvent_t copy_events_[2] = {};     // positions landed; velocities landed and checked
+    // step_host: positions landed; velocities landed and checked; sorted ids
+    // ready; velocities gathered; then one per integrated id range.
+    cudaEvent_t copy_events_[4 + IdSplit::kMax] = {};
+    cudaGraphExec_t host_graph_ = nullptr;  // step_host's one-substep overlapped form
+    uint32_t host_graph_count_ = 0;
+    IdSplit host_graph_split_{};
     cudaEvent_t gather_wait_ = nullptr;   // when set, a direct-launched gather first waits for it
+    bool defer_vel_ = false;              // a direct-launched gather leaves the velocities out
     uint32_t* flag_host_ = nullptr;       // page-locked non-finite count read back by step_host
     std::vector<uint8_t> user_active_;
     float4* snap_pos_[kSnapshotSlots] = {nullptr, nullptr};

@@ -1432,17 +1432,16 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(cons
                                                                 const uint16_t* __restrict__ stank, uint32_t n, const uint32_t* __restrict__ order,
                                                                 const uint32_t* __restrict__ masks,
                                                                 float4* __restrict__ pos_out,
-                                                                float4* __restrict__ vel_out) {
+                                                                float4* __restrict__ vel_out, uint32_t slots) {
     // One bucket may hand over 32 pairs at once, after the warp has drained.
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
     static_assert(27u % kGroup == 0, "groups of buckets tile the 27");
     __shared__ uint32_t list[kList][kBlock];
+    // The launch's first `slots` processing slots (order and masks start at
+    // the range's first slot; n stays the masks' row stride).
     const uint32_t slot = blockIdx.x * kBlock + threadIdx.x;
-    uint32_t p = slot;
-    if (order != nullptr && p < n) {
-        p = order[p];
-    }
-    bool valid = p < n;
+    bool valid = slot < slots;
+    const uint32_t p = valid && order != nullptr ? order[slot] : slot;
     const TankConst* t = tanks + (valid && stank != nullptr ? stank[p] : 0);
     valid = valid && __ldg(&t->active) != 0;
     // The lanes with a particle; they walk the 27 buckets in step.
@@ -2854,6 +2853,13 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
     if (n == 0) {
         return cudaSuccess;
     }
+    const uint32_t slot_end = std::min(tuning.slot_end, n);
+    if ((tuning.variant != 4 || tuning.order == nullptr) && (tuning.slot_begin != 0 || slot_end != n)) {
+        return cudaErrorInvalidValue;  // a slot range needs the mask kernel and a processing order
+    }
+    if (tuning.slot_begin >= slot_end) {
+        return cudaSuccess;
+    }
     if (tuning.variant == 0) {
         integrate_kernel<<<(n + 127) / 128, 128, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, pos,
                                                               vel);
@@ -2878,18 +2884,22 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
                                              tuning.masks, pos, vel, stream);
     }
     if (tuning.variant == 4) {
+        const uint32_t b = tuning.slot_begin;
+        const uint32_t slots = slot_end - b;
+        const uint32_t* order = tuning.order != nullptr ? tuning.order + b : nullptr;
+        const uint32_t* masks = tuning.masks + b;
         switch (tuning.block) {
         case 64:
-            integrate_mask_kernel<64, 48><<<(n + 63) / 64, 64, 0, stream>>>(spos2, svel, sorted_ids, bucket, tanks,
-                                                                            stank, n, tuning.order, tuning.masks, pos, vel);
+            integrate_mask_kernel<64, 48><<<(slots + 63) / 64, 64, 0, stream>>>(
+                spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks, pos, vel, slots);
             break;
         case 256:
-            integrate_mask_kernel<256, 32><<<(n + 255) / 256, 256, 0, stream>>>(
-                spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
+            integrate_mask_kernel<256, 32><<<(slots + 255) / 256, 256, 0, stream>>>(
+                spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks, pos, vel, slots);
             break;
         default:
-            integrate_mask_kernel<128, 40, 9><<<(n + 127) / 128, 128, 0, stream>>>(
-                spos2, svel, sorted_ids, bucket, tanks, stank, n, tuning.order, tuning.masks, pos, vel);
+            integrate_mask_kernel<128, 40, 9><<<(slots + 127) / 128, 128, 0, stream>>>(
+                spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks, pos, vel, slots);
             break;
         }
         return cudaGetLastError();

@@ -286,7 +286,9 @@ __global__ void __launch_bounds__(256) order_gather_kernel(const uint32_t* __res
                                                         : r.x + kCellCapacity + atomicAdd(&tail_counts[key], 1u);
     sorted_ids[p] = i;
     spos[p] = pos[i];
-    svel[p] = vel[i];
+    if (vel != nullptr) {  // else gather_vel_kernel writes them later
+        svel[p] = vel[i];
+    }
     if (tank_of != nullptr) {
         stank[p] = tank_of[i];
     }
@@ -485,13 +487,30 @@ __global__ void __launch_bounds__(256) bounds_gather_kernel(const uint32_t* __re
         global_sorted[p] = i;
     }
     spos[p] = pos[i];
-    svel[p] = vel[i];
+    if (vel != nullptr) {  // else gather_vel_kernel writes them later
+        svel[p] = vel[i];
+    }
     if (tank_of != nullptr) {
         stank[p] = tank_of[i];
     }
     if (schedule.rank != nullptr) {
         schedule.order[schedule.rank[i]] = p;
     }
+}
+
+// The velocities of a gather that skipped them: svel[p].xyz = vel[i].xyz,
+// with no write to .w (the density pass writes the pressure there, and may
+// run at the same time).
+__global__ void __launch_bounds__(256) gather_vel_kernel(const uint32_t* __restrict__ sorted_ids, uint32_t n,
+                                                         const float4* __restrict__ vel, float4* __restrict__ svel) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) {
+        return;
+    }
+    const float4 v = vel[sorted_ids[p]];
+    float* row = reinterpret_cast<float*>(svel + p);
+    *reinterpret_cast<float2*>(row) = make_float2(v.x, v.y);
+    row[2] = v.z;
 }
 
 // Processing slot of every particle id: the inverse of the Morton-sorted ids
@@ -621,7 +640,8 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
                                                                  uint32_t* __restrict__ keys, uint32_t passes,
                                                                  uint32_t* __restrict__ tile_counts,
                                                                  uint32_t* __restrict__ hist, uint32_t morton_bits,
-                                                                 const uint32_t* __restrict__ ids, int hilbert) {
+                                                                 const uint32_t* __restrict__ ids, int hilbert,
+                                                                 IdSplit split, uint32_t split_at) {
     __shared__ uint32_t counts[kSweepMaxPasses][kSweepBins];
     for (uint32_t k = threadIdx.x; k < kSweepMaxPasses * kSweepBins; k += blockDim.x) {
         (&counts[0][0])[k] = 0;
@@ -642,7 +662,15 @@ __global__ void __launch_bounds__(kKeysThreads) keys_hist_kernel(const float4* _
         const uint32_t i = first + r * kKeysThreads + threadIdx.x;
         const TankConst* t = tanks + tank[r];
         if (kMorton) {
-            const uint32_t key = morton_key(p[r], t, tank[r], morton_bits, hilbert != 0);
+            uint32_t key = morton_key(p[r], t, tank[r], morton_bits, hilbert != 0);
+            if (split.count > 1 && i < n) {  // the particle's id range above the curve key
+                const uint32_t id = ids != nullptr ? ids[i] : i;
+                uint32_t range = 0;
+                for (uint32_t c = 1; c < split.count; ++c) {
+                    range += id >= split.start[c] ? 1u : 0u;
+                }
+                key |= range << split_at;
+            }
             if (i < n) {
                 keys[i] = key;
             }
@@ -836,7 +864,8 @@ namespace {
 
 cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                             uint32_t* keys, uint32_t passes, unsigned long long* sweep, uint32_t morton_bits,
-                            const uint32_t* ids, cudaStream_t stream, bool hilbert = false) {
+                            const uint32_t* ids, cudaStream_t stream, bool hilbert = false,
+                            IdSplit split = IdSplit{}, uint32_t split_at = 0) {
     cudaError_t err = cudaMemsetAsync(sweep, 0, onesweep_scratch_words(n, passes) * sizeof(unsigned long long), stream);
     if (err != cudaSuccess) {
         return err;
@@ -845,10 +874,11 @@ cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const Ta
     SweepLayout l = sweep_layout(sweep, tiles, passes);
     if (morton_bits != 0) {
         keys_hist_kernel<true><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes, l.tile_counts,
-                                                                   l.hist, morton_bits, ids, hilbert ? 1 : 0);
+                                                                   l.hist, morton_bits, ids, hilbert ? 1 : 0,
+                                                                   split, split_at);
     } else {
         keys_hist_kernel<false><<<tiles, kKeysThreads, 0, stream>>>(pos, tank_of, tanks, n, keys, passes,
-                                                                    l.tile_counts, l.hist, 0, ids, 0);
+                                                                    l.tile_counts, l.hist, 0, ids, 0, IdSplit{}, 0);
     }
     return cudaGetLastError();
 }
@@ -867,19 +897,27 @@ cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, con
 cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                                uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
                                unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches,
-                               bool hilbert, const uint32_t* ids) {
+                               bool hilbert, const uint32_t* ids, const IdSplit& split) {
     if (n == 0) {
         return cudaSuccess;
     }
-    if (morton_bits == 0 || morton_bits > 10 || key_bits > 32) {
+    const uint32_t split_bits = split.count > 1 ? bit_width32(split.count - 1u) : 0u;
+    bool ranges_ok = split.count <= IdSplit::kMax && (split.count <= 1 || (split.start[0] == 0 && split.start[split.count] == n));
+    for (uint32_t c = 0; ranges_ok && split.count > 1 && c < split.count; ++c) {
+        ranges_ok = split.start[c] < split.start[c + 1];
+    }
+    if (morton_bits == 0 || morton_bits > 10 || key_bits + split_bits > 32 || !ranges_ok) {
         return cudaErrorInvalidValue;
     }
+    const uint32_t split_at = key_bits;
+    key_bits += split_bits;
     const uint32_t passes = onesweep_passes(key_bits);
     if (passes > kSweepMaxPasses) {
         return cudaErrorInvalidValue;
     }
     cudaError_t err =
-        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, ids, stream, hilbert);
+        keys_and_counts(pos, tank_of, tanks, n, scratch.keys, passes, sweep, morton_bits, ids, stream, hilbert,
+                        split, split_at);
     if (err == cudaSuccess) {
         err = launch_onesweep_sort(scratch, n, passes, sweep, stream, launches, true);
     }
@@ -1049,6 +1087,15 @@ cudaError_t launch_counting_grid(const float4* pos, const uint16_t* tank_of, con
     if (launches != nullptr) {
         *launches += n > 0 ? 5 : 3;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_vel(const uint32_t* sorted_ids, uint32_t n, const float4* vel, float4* svel,
+                              cudaStream_t stream) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    gather_vel_kernel<<<(n + 255) / 256, 256, 0, stream>>>(sorted_ids, n, vel, svel);
     return cudaGetLastError();
 }
 

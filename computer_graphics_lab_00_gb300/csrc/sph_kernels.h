@@ -80,6 +80,27 @@ constexpr uint32_t kSweepThreads = 512;                      // threads of a pas
 constexpr uint32_t kSweepItems = 8;                          // keys per thread in a tile
 constexpr uint32_t kSweepTile = kSweepThreads * kSweepItems;  // 4096 keys per tile
 inline uint32_t sweep_tiles(uint32_t n) { return (n + kSweepTile - 1) / kSweepTile; }
+// Bits to write values up to v (0 for v = 0).
+inline uint32_t bit_width32(uint32_t v) {
+    uint32_t b = 0;
+    while (v != 0) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+// The particle ids cut into consecutive ranges: range c holds the ids
+// [start[c], start[c + 1]), start[0] = 0 and start[count] = n. A processing
+// order made with it puts range c's ids in the slots [start[c], start[c + 1])
+// (each range in curve order), so a pass over those slots touches only those
+// ids' outputs. count 0 or 1: no split.
+struct IdSplit {
+    static constexpr uint32_t kMax = 8;
+    uint32_t count = 0;
+    uint32_t start[kMax + 1] = {};
+};
+
 inline uint32_t onesweep_passes(uint32_t key_bits) { return key_bits == 0 ? 1 : (key_bits + kSweepBits - 1) / kSweepBits; }
 size_t onesweep_scratch_words(uint32_t n, uint32_t passes);
 // Keys (as launch_keys) plus the first pass's tile counts and every pass's
@@ -112,7 +133,8 @@ struct Schedule {
 };
 
 // The counting placement's final step (after launch_counting_grid): each
-// bucket's 32 smallest ids in ascending order at its front, and the gather.
+// bucket's 32 smallest ids in ascending order at its front, and the gather
+// (vel = null: the velocities are left to launch_gather_vel).
 cudaError_t launch_order_gather(const GridScratch& s, uint32_t n, const uint2* bucket, uint32_t* counts,
                                 const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
                                 float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream);
@@ -124,16 +146,24 @@ cudaError_t launch_order_gather(const GridScratch& s, uint32_t n, const uint2* b
 // hilbert: the cells' Hilbert index (Skilling's transpose form) instead of
 // their Morton code. ids (optional): order the compacted set pos[ids[v]],
 // v < n; rank is still indexed by particle id (rank[ids[v]] = slot).
+// split (count > 1): the particle's id range goes above the curve key, so the
+// ids of range c take the slots [split.start[c], split.start[c + 1]).
 cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
                                uint32_t morton_bits, uint32_t key_bits, GridScratch scratch,
                                unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches,
-                               bool hilbert = false, const uint32_t* ids = nullptr);
+                               bool hilbert = false, const uint32_t* ids = nullptr, const IdSplit& split = IdSplit{});
+
+// svel[p].xyz = vel[sorted_ids[p]].xyz, .w untouched: the velocities of a
+// gather launched with vel = null (the density pass may run meanwhile).
+cudaError_t launch_gather_vel(const uint32_t* sorted_ids, uint32_t n, const float4* vel, float4* svel,
+                              cudaStream_t stream);
 
 // Bucket table (start, end) from sorted keys (table pre-zeroed), the
 // cell-ordered copies of position, velocity and tank id, and (with a
 // schedule) the processing order.
 // With `ids` the sorted entries index a compacted set: the particle is
 // ids[entry], and global_sorted[p] receives its id for the write-back.
+// vel = null leaves the sorted velocities to launch_gather_vel.
 cudaError_t launch_bounds_gather(const uint32_t* sorted_keys, const uint32_t* sorted_ids, uint32_t n, uint2* bucket,
                                  const float4* pos, const float4* vel, const uint16_t* tank_of, float4* spos,
                                  float4* svel, uint16_t* stank, const Schedule& schedule, cudaStream_t stream,
@@ -164,6 +194,10 @@ struct NeighbourTuning {
     uint32_t* masks = nullptr;  // 27 words per particle, bucket-major (variant 4)
     const uint32_t* order = nullptr;  // processing order (null: sorted order)
     bool all_tanks = false;           // density of inactive tanks too (variant 4 skips them otherwise)
+    // Integrate only the processing slots [slot_begin, min(slot_end, n))
+    // (variant 4; the other variants take the whole range only).
+    uint32_t slot_begin = 0;
+    uint32_t slot_end = 0xFFFFFFFFu;
 };
 
 // Density and pressure (fluid_sph.cpp:200-222). Writes spos2 = (xyz, rho)

@@ -194,8 +194,13 @@ int sph_upload(sph_ctx* ctx, const float* positions, const float* velocities, ui
 int sph_download(sph_ctx* ctx, float* positions, float* velocities);
 /* sph_upload + `substeps` substeps of `dt` + sph_download in one call, for
  * a caller that keeps the state on the host: the same results and checks,
- * with the velocity upload overlapping the first substep's grid keys and
- * sort (page-locked host arrays let the copies run asynchronously).
+ * with the velocity upload overlapping the first substep's grid build. From
+ * 2^18 particles (one tank, a curve processing order, neighbour kernel 4, no
+ * colliders) the velocities are gathered beside the density pass and the
+ * last substep integrates two id ranges in turn (the first two thirds of the
+ * ids, then the rest), downloading the first range's rows while the second
+ * integrates; one substep then runs as one CUDA graph launch. Page-locked
+ * host arrays let the copies run asynchronously.
  * `velocities` may be NULL (zeros); either output may be NULL or alias its
  * input. On SPH_ERR_NONFINITE the outputs are left as they were and the
  * context holds the rejected state, as after a rejected sph_upload.

@@ -1,7 +1,8 @@
 """sph_step_host: upload, substeps and download in one call, with the
-velocity upload overlapping the first substep's keys and sort. Same bits as
-sph_upload + sph_run + sph_download, the same checks, and the reference's
-substep (oracle) underneath."""
+velocity upload overlapping the first substep's grid build (and, from 2^18
+particles, the density pass, with the download overlapping integrate). Same
+bits as sph_upload + sph_run + sph_download, the same checks, and the
+reference's substep (oracle) underneath."""
 from __future__ import annotations
 
 import numpy as np
@@ -133,3 +134,90 @@ def test_edge_cases(native):
         assert np.array_equal(bits(p), bits(want_p)) and np.array_equal(bits(v), bits(want_v))
         p, v = s.step_host_arrays(pos, vel, case.dt, 1)
         assert p.shape == pos.shape
+
+
+def first_particles(count, substeps_in=3):
+    """The first `count` particles of the 1M dam break a few substeps in."""
+    case = W.dam_break_1m()
+    with FluidSolverGpu(case.params, case.count) as s:
+        s.upload(*case.initial_state())
+        s.run(case.dt, substeps_in)
+        pos, vel = s.state()
+    return case, pos[:count].copy(), vel[:count].copy()
+
+
+@pytest.mark.parametrize("count,substeps,schedule,sort", [
+    (300_001, 1, 1, 2),    # an odd count: the cut on a 128-slot boundary, a ragged second range
+    (300_001, 3, 2, 2),    # Hilbert order, the last of three substeps in id ranges
+    (1_048_576, 2, 1, 1),  # one-kernel radix passes
+    (1_048_576, 1, 1, 0),  # three kernels per radix pass
+    (262_144, 1, 0, 2),    # bucket order: no id ranges, the plain form
+])
+def test_overlapped_form_equals_upload_run_download(native, count, substeps, schedule, sort):
+    """From 2^18 particles (one tank, a curve order, the mask kernels, no
+    colliders) the velocities are gathered beside the density pass and the
+    last integrate runs in two id ranges, the first range's rows downloading
+    while the second integrates; results, the context's state and previous
+    positions equal the unsplit run's, call after call."""
+    case, pos, vel = first_particles(count)
+    with FluidSolverGpu(case.params, case.count) as a, FluidSolverGpu(case.params, case.count) as b:
+        for s in (a, b):
+            s.set_tuning(schedule=schedule, sort=sort)
+        a.upload(pos, vel)
+        b_p, b_v = pos, vel
+        for call in range(3):
+            a.run(case.dt, substeps)
+            want_p, want_v = a.state()
+            uploaded = b_p
+            b_p, b_v = b.step_host_arrays(b_p, b_v, case.dt, substeps)
+            assert np.array_equal(bits(b_p), bits(want_p)), call
+            assert np.array_equal(bits(b_v), bits(want_v)), call
+            p, v = b.state()
+            assert np.array_equal(bits(p), bits(want_p)) and np.array_equal(bits(v), bits(want_v))
+            # previous = the positions this call uploaded.
+            assert np.array_equal(bits(b.previous_particles()), bits(uploaded)), call
+
+
+def test_overlapped_form_after_run_and_back(native):
+    """Alternating step_host (an order split by id range) and run (the plain
+    order) keeps the bits of a run-only context."""
+    case, pos, vel = first_particles(400_000)
+    with FluidSolverGpu(case.params, case.count) as a, FluidSolverGpu(case.params, case.count) as b:
+        a.upload(pos, vel)
+        a.run(case.dt, 9)
+        want_p, want_v = a.state()
+        p, v = b.step_host_arrays(pos, vel, case.dt, 2)
+        b.run(case.dt, 3)
+        p, v = b.state()
+        p, v = b.step_host_arrays(p, v, case.dt, 1)
+        b.run(case.dt, 1)
+        p, v = b.state()
+        p, v = b.step_host_arrays(p, v, case.dt, 2)
+        assert np.array_equal(bits(p), bits(want_p)) and np.array_equal(bits(v), bits(want_v))
+
+
+def test_overlapped_form_optional_arrays_and_nonfinite(native):
+    case, pos, vel = first_particles(300_001)
+    with FluidSolverGpu(case.params, case.count) as a, FluidSolverGpu(case.params, case.count) as b:
+        a.upload(pos, None)
+        a.run(case.dt, 1)
+        want_p, want_v = a.state()
+        out_p = np.full_like(pos, 7.0)
+        b.step_host(pos.ctypes.data, None, len(pos), case.dt, 1, out_p.ctypes.data, None)
+        assert np.array_equal(bits(out_p), bits(want_p))
+        got_v = b.state()[1]
+        assert np.array_equal(bits(got_v), bits(want_v))
+        bad = vel.copy()
+        bad[299_999, 2] = np.nan
+        out_p[:] = 3.0
+        out_v = np.full_like(pos, 5.0)
+        with pytest.raises(abi.SphError) as e:
+            b.step_host(pos.ctypes.data, bad.ctypes.data, len(pos), case.dt, 1, out_p.ctypes.data,
+                        out_v.ctypes.data)
+        assert e.value.status == abi.SPH_ERR_NONFINITE
+        assert (out_p == 3.0).all() and (out_v == 5.0).all()
+        a.upload(pos, vel)
+        a.run(case.dt, 1)
+        want_p, want_v = a.state()
+        got_p, got_v = b.step_host_arrays(pos, vel, case.dt, 1)
+        assert np.array_equal(bits(got_p), bits(want_p)) and np.array_equal(bits(got_v), bits(want_v))
