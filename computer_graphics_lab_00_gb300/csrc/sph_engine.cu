@@ -14,23 +14,27 @@ namespace {
 constexpr float kPi = 3.14159265358979323846F;
 
 // step_host's id ranges for n particles: the first Engine::kHostFirstNum /
-// kHostFirstDen of the ids, then the rest, the cut on a multiple of 128
-// slots so that both ranges' mask rows stay aligned. No split when n is too
-// small for two ranges.
+// kHostFirstDen of the ids, then the rest in `ranges` - 1 equal parts, every
+// cut on a multiple of 128 slots so that each range's mask rows stay
+// aligned. No split when n is too small for distinct cuts.
 IdSplit host_split(uint32_t n, uint32_t ranges) {
     IdSplit split;
-    if (ranges != 2) {
+    if (ranges < 2 || ranges > IdSplit::kMax) {
         return split;
     }
-    const uint32_t cut = static_cast<uint32_t>(static_cast<uint64_t>(n) * Engine::kHostFirstNum /
-                                               Engine::kHostFirstDen) & ~127U;
-    if (cut == 0 || cut >= n) {
-        return split;
-    }
-    split.count = 2;
+    const uint64_t first = static_cast<uint64_t>(n) * Engine::kHostFirstNum / Engine::kHostFirstDen;
+    split.count = ranges;
     split.start[0] = 0;
-    split.start[1] = cut;
-    split.start[2] = n;
+    for (uint32_t c = 1; c < ranges; ++c) {
+        const uint64_t cut = first + (static_cast<uint64_t>(n) - first) * (c - 1) / (ranges - 1);
+        split.start[c] = static_cast<uint32_t>(cut) & ~127U;
+    }
+    split.start[ranges] = n;
+    for (uint32_t c = 0; c < ranges; ++c) {
+        if (split.start[c] >= split.start[c + 1]) {
+            return IdSplit{};
+        }
+    }
     return split;
 }
 
@@ -222,6 +226,16 @@ void Engine::release() {
     if (copy_stream_ != nullptr) {
         cudaStreamDestroy(copy_stream_);
         copy_stream_ = nullptr;
+    }
+    for (cudaEvent_t& e : range_events_) {
+        if (e != nullptr) {
+            cudaEventDestroy(e);
+            e = nullptr;
+        }
+    }
+    if (range_stream_ != nullptr) {
+        cudaStreamDestroy(range_stream_);
+        range_stream_ = nullptr;
     }
     if (flag_host_ != nullptr) {
         cudaFreeHost(flag_host_);
@@ -544,7 +558,11 @@ int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, 
     SPH_CUDA(cudaSetDevice(device_));
     if (copy_stream_ == nullptr) {
         SPH_CUDA(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+        SPH_CUDA(cudaStreamCreateWithFlags(&range_stream_, cudaStreamNonBlocking));
         for (cudaEvent_t& e : copy_events_) {
+            SPH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        for (cudaEvent_t& e : range_events_) {
             SPH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
         SPH_CUDA(cudaMallocHost(&flag_host_, sizeof(uint32_t)));
@@ -681,22 +699,39 @@ int Engine::step_host(const float* pos_in, const float* vel_in, uint32_t count, 
     return SPH_OK;
 }
 
-// The integrate pass over the id ranges of the processing order, range by
-// range, an event after each (step_host downloads range c's rows once its
-// event fires). Without ranges in the order: one whole pass, one event.
-// While capturing, the events become the graph's external event records.
+// The integrate pass over the id ranges of the processing order, an event
+// after each (step_host downloads range c's rows once its event fires).
+// Range c + 1 is a programmatic dependent of range c (ranges write disjoint
+// rows and read only what density wrote), so its blocks start as range c's
+// last blocks leave the SMs, where a plain second launch would wait for
+// range c's slowest block. Range c's event is recorded on range_stream_
+// after a plain wait for range c, which also joins stream_ again after the
+// last range. Without ranges in the order: one whole pass, one event.
+// While capturing, the range events become the graph's external records.
 int Engine::enqueue_integrate_ranges() {
     const uint32_t n = total_count_;
     const uint32_t ranges = rank_split_.count > 1 && schedule_curve_ != 0 ? rank_split_.count : 1U;
+    const unsigned int record = capturing_ ? cudaEventRecordExternal : cudaEventRecordDefault;
     NeighbourTuning t = tuning_;
     for (uint32_t c = 0; c < ranges; ++c) {
         if (ranges > 1) {
             t.slot_begin = rank_split_.start[c];
             t.slot_end = rank_split_.start[c + 1];
+            t.programmatic = c > 0;
         }
-        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_, t));
-        SPH_CUDA(cudaEventRecordWithFlags(copy_events_[4 + c], stream_,
-                                          capturing_ ? cudaEventRecordExternal : cudaEventRecordDefault));
+        SPH_CUDA(launch_integrate(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, pos_, vel_, stream_,
+                                  t));
+        if (ranges == 1) {
+            SPH_CUDA(cudaEventRecordWithFlags(copy_events_[4], stream_, record));
+        } else {
+            SPH_CUDA(cudaEventRecord(range_events_[0], stream_));
+            SPH_CUDA(cudaStreamWaitEvent(range_stream_, range_events_[0], 0));
+            SPH_CUDA(cudaEventRecordWithFlags(copy_events_[4 + c], range_stream_, record));
+        }
+    }
+    if (ranges > 1) {
+        SPH_CUDA(cudaEventRecord(range_events_[1], range_stream_));
+        SPH_CUDA(cudaStreamWaitEvent(stream_, range_events_[1], 0));
     }
     return SPH_OK;
 }

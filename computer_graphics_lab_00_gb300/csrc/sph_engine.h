@@ -41,12 +41,13 @@ struct TuneChoice {
 
 class Engine {
 public:
-    // step_host integrates the first kHostFirstNum / kHostFirstDen of the ids,
-    // downloads them while it integrates the rest (kHostRanges id ranges),
-    // from kHostOverlapMin particles up.
-    static constexpr uint32_t kHostRanges = 2;
-    static constexpr uint32_t kHostFirstNum = 2;
-    static constexpr uint32_t kHostFirstDen = 3;
+    // step_host integrates kHostRanges id ranges in turn (the first
+    // kHostFirstNum / kHostFirstDen of the ids, then equal parts of the rest)
+    // and downloads each range's rows while the next integrates, from
+    // kHostOverlapMin particles up.
+    static constexpr uint32_t kHostRanges = 3;
+    static constexpr uint32_t kHostFirstNum = 1;
+    static constexpr uint32_t kHostFirstDen = 2;
     static constexpr uint32_t kHostOverlapMin = 1u << 18;
     ~Engine();
 
@@ -236,6 +237,10 @@ private:
     // step_host: positions landed; velocities landed and checked; sorted ids
     // ready; velocities gathered; then one per integrated id range.
     cudaEvent_t copy_events_[4 + IdSplit::kMax] = {};
+    // step_host: id ranges after the first integrate on range_stream_, so
+    // their blocks fill the first range's tail; its fork and join events.
+    cudaStream_t range_stream_ = nullptr;
+    cudaEvent_t range_events_[2] = {};
     cudaGraphExec_t host_graph_ = nullptr;  // step_host's one-substep overlapped form
     uint32_t host_graph_count_ = 0;
     IdSplit host_graph_split_{};

@@ -1436,6 +1436,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) integrate_mask_kernel(cons
     // One bucket may hand over 32 pairs at once, after the warp has drained.
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
     static_assert(27u % kGroup == 0, "groups of buckets tile the 27");
+    // A launch that follows this one programmatically (the next slot range,
+    // which reads nothing this one writes) may start once every block of
+    // this one has started: its blocks then fill this launch's tail.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ uint32_t list[kList][kBlock];
     // The launch's first `slots` processing slots (order and masks start at
     // the range's first slot; n stays the masks' row stride).
@@ -2888,21 +2892,29 @@ cudaError_t launch_integrate(const float4* spos2, const float4* svel, const uint
         const uint32_t slots = slot_end - b;
         const uint32_t* order = tuning.order != nullptr ? tuning.order + b : nullptr;
         const uint32_t* masks = tuning.masks + b;
+        // programmatic: the launch may begin while the one before it in the
+        // stream finishes (that launch must not write what this one reads).
+        cudaLaunchAttribute attr{};
+        attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr.val.programmaticStreamSerializationAllowed = 1;
+        auto launch = [&](auto kernel, uint32_t block) {
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3((slots + block - 1) / block);
+            cfg.blockDim = dim3(block);
+            cfg.stream = stream;
+            cfg.attrs = tuning.programmatic ? &attr : nullptr;
+            cfg.numAttrs = tuning.programmatic ? 1 : 0;
+            return cudaLaunchKernelEx(&cfg, kernel, spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks,
+                                      pos, vel, slots);
+        };
         switch (tuning.block) {
         case 64:
-            integrate_mask_kernel<64, 48><<<(slots + 63) / 64, 64, 0, stream>>>(
-                spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks, pos, vel, slots);
-            break;
+            return launch(integrate_mask_kernel<64, 48>, 64);
         case 256:
-            integrate_mask_kernel<256, 32><<<(slots + 255) / 256, 256, 0, stream>>>(
-                spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks, pos, vel, slots);
-            break;
+            return launch(integrate_mask_kernel<256, 32>, 256);
         default:
-            integrate_mask_kernel<128, 40, 9><<<(slots + 127) / 128, 128, 0, stream>>>(
-                spos2, svel, sorted_ids, bucket, tanks, stank, n, order, masks, pos, vel, slots);
-            break;
+            return launch(integrate_mask_kernel<128, 40, 9>, 128);
         }
-        return cudaGetLastError();
     }
     if (tuning.variant >= 2) {
         bool rcp = tuning.variant == 3;

@@ -198,6 +198,9 @@ struct NeighbourTuning {
     // (variant 4; the other variants take the whole range only).
     uint32_t slot_begin = 0;
     uint32_t slot_end = 0xFFFFFFFFu;
+    // Variant 4's integrate launched as a programmatic dependent of the
+    // launch before it in the stream (which must write nothing it reads).
+    bool programmatic = false;
 };
 
 // Density and pressure (fluid_sph.cpp:200-222). Writes spos2 = (xyz, rho)

@@ -197,8 +197,8 @@ int sph_download(sph_ctx* ctx, float* positions, float* velocities);
  * with the velocity upload overlapping the first substep's grid build. From
  * 2^18 particles (one tank, a curve processing order, neighbour kernel 4, no
  * colliders) the velocities are gathered beside the density pass and the
- * last substep integrates two id ranges in turn (the first two thirds of the
- * ids, then the rest), downloading the first range's rows while the second
+ * last substep integrates three id ranges in turn (the first half of the
+ * ids, then two quarters), downloading each range's rows while the next
  * integrates; one substep then runs as one CUDA graph launch. Page-locked
  * host arrays let the copies run asynchronously.
  * `velocities` may be NULL (zeros); either output may be NULL or alias its

@@ -147,7 +147,7 @@ def first_particles(count, substeps_in=3):
 
 
 @pytest.mark.parametrize("count,substeps,schedule,sort", [
-    (300_001, 1, 1, 2),    # an odd count: the cut on a 128-slot boundary, a ragged second range
+    (300_001, 1, 1, 2),    # an odd count: cuts on 128-slot boundaries, a ragged last range
     (300_001, 3, 2, 2),    # Hilbert order, the last of three substeps in id ranges
     (1_048_576, 2, 1, 1),  # one-kernel radix passes
     (1_048_576, 1, 1, 0),  # three kernels per radix pass
@@ -156,8 +156,8 @@ def first_particles(count, substeps_in=3):
 def test_overlapped_form_equals_upload_run_download(native, count, substeps, schedule, sort):
     """From 2^18 particles (one tank, a curve order, the mask kernels, no
     colliders) the velocities are gathered beside the density pass and the
-    last integrate runs in two id ranges, the first range's rows downloading
-    while the second integrates; results, the context's state and previous
+    last integrate runs in three id ranges, each range's rows downloading
+    while the next integrates; results, the context's state and previous
     positions equal the unsplit run's, call after call."""
     case, pos, vel = first_particles(count)
     with FluidSolverGpu(case.params, case.count) as a, FluidSolverGpu(case.params, case.count) as b:
