@@ -1505,26 +1505,31 @@ int Engine::enqueue_learned_substep(const mlp::ModelView* model, uint32_t* launc
     if ((status = enqueue_fields(launches)) != SPH_OK) {
         return status;
     }
+    const bool free = model != nullptr && model->free_axes != 0;
     SPH_CUDA(launch_density(spos_, svel_, spos2_, bucket_, d_tanks_, stank_, n, nullptr, stream_, masked));
+    if (free) {  // zeroed here, so that nothing but kernels sits between features and finish
+        SPH_CUDA(zero_correction_sums(static_cast<uint32_t>(tanks_.size()), correction_sums_, stream_));
+    }
     // The features go straight into the MLP's input tiles (normalised, BF16);
-    // with no model only the plain force is needed.
+    // with no model only the plain force is needed. The MLP, the sums and
+    // the finishing pass are programmatic dependents, each waiting for the
+    // grid before it: their set-up overlaps that grid's last blocks.
     SPH_CUDA(launch_features(spos2_, svel_, grid_.sorted_ids, bucket_, d_tanks_, stank_, n, tuning_.order,
                              tuning_.masks, sforce_, nullptr, false, stream_,
                              model != nullptr ? model->in_mean : nullptr, model != nullptr ? model->in_inv_std : nullptr,
                              model != nullptr ? sx_tiles_ : nullptr));
     if (model != nullptr) {
         SPH_CUDA(mlp::launch_forward_tiles(*model, sx_tiles_, n, reinterpret_cast<float*>(scorrection_),
-                                           &counters_->error_flags, stream_));
-        if (model->free_axes != 0) {
+                                           &counters_->error_flags, stream_, true));
+        if (free) {
             // No net force along these axes: each tank's mean correction is removed.
             SPH_CUDA(launch_correction_sums(scorrection_, d_tanks_, stank_, n, static_cast<uint32_t>(tanks_.size()),
-                                            correction_sums_, stream_));
+                                            correction_sums_, stream_, true));
         }
     }
-    const bool free = model != nullptr && model->free_axes != 0;
     SPH_CUDA(launch_finish_learned(spos2_, svel_, grid_.sorted_ids, d_tanks_, stank_, n, sforce_,
                                    model != nullptr ? scorrection_ : nullptr, free ? correction_sums_ : nullptr,
-                                   free ? model->free_axes : 0u, pos_, vel_, stream_));
+                                   free ? model->free_axes : 0u, pos_, vel_, stream_, true));
     if (launches != nullptr) {
         *launches += model != nullptr ? (free ? 5 : 4) : 3;
     }

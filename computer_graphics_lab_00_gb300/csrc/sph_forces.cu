@@ -2330,6 +2330,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) features_kernel(const floa
                                                           const float* __restrict__ norm_inv_std,
                                                           uint8_t* __restrict__ x_tiles) {
     static_assert(kList >= 32, "a pair list must hold a whole bucket");
+    // The MLP launched after this pass may set up (weights, tensor memory)
+    // once every block of this one has started; it waits for this grid's
+    // end before it reads a tile.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     __shared__ uint32_t list[kList][kBlock];
     const uint32_t slot = blockIdx.x * kBlock + threadIdx.x;
     uint32_t p = slot;
@@ -2520,6 +2524,9 @@ __global__ void __launch_bounds__(256) correction_sums_kernel(const float4* __re
                                                               const TankConst* __restrict__ tanks,
                                                               const uint16_t* __restrict__ stank, uint32_t n,
                                                               unsigned long long* __restrict__ sums) {
+    // Launched programmatically after the MLP: wait for its corrections.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = threadIdx.x >> 5;
     const size_t per_block = ((static_cast<size_t>(n) + gridDim.x - 1) / gridDim.x + 31) & ~static_cast<size_t>(31);
@@ -2597,6 +2604,8 @@ __global__ void __launch_bounds__(256) finish_learned_kernel(const float4* __res
                                                              const unsigned long long* __restrict__ sums,
                                                              uint32_t free_axes, float4* __restrict__ pos_out,
                                                              float4* __restrict__ vel_out) {
+    // Launched programmatically after the MLP or the sums: wait for them.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) {
         return;
@@ -3039,11 +3048,44 @@ cudaError_t launch_features(const float4* spos2, const float4* svel, const uint3
     return cudaGetLastError();
 }
 
+namespace {
+
+// A launch that may begin while the kernel before it in the stream finishes
+// (programmatic stream serialisation); the kernel waits for that grid's end
+// (griddepcontrol.wait) before it reads what the grid wrote.
+template <typename Kernel, typename... Args>
+cudaError_t launch_after(bool programmatic, dim3 grid, dim3 block, size_t smem, cudaStream_t stream, Kernel kernel,
+                         Args... args) {
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = programmatic ? &attr : nullptr;
+    cfg.numAttrs = programmatic ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+}  // namespace
+
+cudaError_t zero_correction_sums(uint32_t tank_count, unsigned long long* sums, cudaStream_t stream) {
+    return cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * kCorrectionSumWords * tank_count, stream);
+}
+
 cudaError_t launch_correction_sums(const float4* correction, const TankConst* tanks, const uint16_t* stank, uint32_t n,
-                                   uint32_t tank_count, unsigned long long* sums, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * kCorrectionSumWords * tank_count, stream);
-    if (e != cudaSuccess || n == 0) {
-        return e;
+                                   uint32_t tank_count, unsigned long long* sums, cudaStream_t stream,
+                                   bool programmatic) {
+    if (!programmatic) {
+        const cudaError_t e = zero_correction_sums(tank_count, sums, stream);
+        if (e != cudaSuccess) {
+            return e;
+        }
+    }
+    if (n == 0) {
+        return cudaSuccess;
     }
     int device = 0;
     int sms = 152;
@@ -3051,20 +3093,19 @@ cudaError_t launch_correction_sums(const float4* correction, const TankConst* ta
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     }
     const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 4u * static_cast<uint32_t>(sms));
-    correction_sums_kernel<<<blocks, 256, 0, stream>>>(correction, tanks, stank, n, sums);
-    return cudaGetLastError();
+    return launch_after(programmatic, dim3(blocks), dim3(256), 0, stream, correction_sums_kernel, correction, tanks,
+                        stank, n, sums);
 }
 
 cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,
                                   const TankConst* tanks, const uint16_t* stank, uint32_t n, const float4* force,
                                   const float4* correction, const unsigned long long* sums, uint32_t free_axes,
-                                  float4* pos, float4* vel, cudaStream_t stream) {
+                                  float4* pos, float4* vel, cudaStream_t stream, bool programmatic) {
     if (n == 0) {
         return cudaSuccess;
     }
-    finish_learned_kernel<<<(n + 255) / 256, 256, 0, stream>>>(spos2, svel, sorted_ids, tanks, stank, n, force,
-                                                                correction, sums, free_axes, pos, vel);
-    return cudaGetLastError();
+    return launch_after(programmatic, dim3((n + 255) / 256), dim3(256), 0, stream, finish_learned_kernel, spos2, svel,
+                        sorted_ids, tanks, stank, n, force, correction, sums, free_axes, pos, vel);
 }
 
 cudaError_t launch_division_selftest(uint64_t seed, uint64_t count, int mode, unsigned long long* mismatches,

@@ -255,17 +255,23 @@ cudaError_t launch_features(const float4* spos2, const float4* svel, const uint3
 // Net correction of each active tank: kCorrectionSumWords unsigned words per
 // tank (x, y, z sums in 2^-24 fixed point, two's complement, and the count),
 // zeroed first. Deterministic: integer sums do not depend on atomic order.
+// programmatic: launched as a programmatic dependent of the MLP, the sums
+// already zeroed (zero_correction_sums, earlier in the stream).
 constexpr uint32_t kCorrectionSumWords = 4;
+cudaError_t zero_correction_sums(uint32_t tank_count, unsigned long long* sums, cudaStream_t stream);
 cudaError_t launch_correction_sums(const float4* correction, const TankConst* tanks, const uint16_t* stank, uint32_t n,
-                                   uint32_t tank_count, unsigned long long* sums, cudaStream_t stream);
+                                   uint32_t tank_count, unsigned long long* sums, cudaStream_t stream,
+                                   bool programmatic = false);
 // Second half: acceleration = plain + correction[p] (null: none), minus the
 // tank's mean correction along the axes in `free_axes` (bit a: axis a) when
 // `sums` (launch_correction_sums) is given, then the plain step's velocity
-// update, clamp, walls and id-order write.
+// update, clamp, walls and id-order write. programmatic: launched as a
+// programmatic dependent of the kernel before it (features, MLP or sums).
 cudaError_t launch_finish_learned(const float4* spos2, const float4* svel, const uint32_t* sorted_ids,
                                   const TankConst* tanks, const uint16_t* stank, uint32_t n, const float4* force,
                                   const float4* correction, const unsigned long long* sums, uint32_t free_axes,
-                                  float4* pos, float4* vel, cudaStream_t stream);
+                                  float4* pos, float4* vel, cudaStream_t stream,
+                                  bool programmatic = false);
 // Counts x / y (over `count` generated pairs) where division through a
 // correctly rounded reciprocal differs from IEEE division. mode 0: every
 // divisor mantissa; mode 1: random signs, mantissas, exponents.

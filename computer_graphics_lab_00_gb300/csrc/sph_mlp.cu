@@ -613,6 +613,9 @@ __global__ void __launch_bounds__(kWsThreads, 1) mlp_forward_ws_kernel(ModelView
     const uint32_t warp = tid >> 5;
     const uint32_t lane = tid & 31u;
     float* vec = reinterpret_cast<float*>(smem + kPairVec);
+    // A kernel launched programmatically after this one (the correction sums
+    // or the finishing pass) may start once every CTA has started.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     stage_model(model, smem, kPairW1, kPairW2, kPairW3, vec, tid, blockDim.x, true);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -634,6 +637,10 @@ __global__ void __launch_bounds__(kWsThreads, 1) mlp_forward_ws_kernel(ModelView
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
+    // Launched programmatically after the features pass, the CTA staged the
+    // weights and took its tensor memory while that pass finished; the
+    // input tiles are read only after its grid has ended.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
     const uint32_t tiles = (n + kTile - 1) / kTile;
     const uint32_t pairs = (tiles + 1) / 2;
@@ -1286,7 +1293,7 @@ cudaError_t launch_forward(const ModelView& model, const float* features, uint32
 }
 
 cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles, uint32_t n, float* out_accel,
-                                 unsigned int* error_flag, cudaStream_t stream) {
+                                 unsigned int* error_flag, cudaStream_t stream, bool programmatic) {
     if (n == 0) {
         return cudaSuccess;
     }
@@ -1301,9 +1308,17 @@ cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const uint32_t pairs = (tiles + 1) / 2;
     const uint32_t grid = std::min<uint32_t>(pairs, static_cast<uint32_t>(sms));
-    mlp_forward_ws_kernel<<<grid, kWsThreads, kPairBytes, stream>>>(model, x_tiles, n, out_accel, error_flag,
-                                                                     kWaitPolls);
-    return cudaGetLastError();
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kWsThreads);
+    cfg.dynamicSmemBytes = kPairBytes;
+    cfg.stream = stream;
+    cfg.attrs = programmatic ? &attr : nullptr;
+    cfg.numAttrs = programmatic ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, mlp_forward_ws_kernel, model, x_tiles, n, out_accel, error_flag, kWaitPolls);
 }
 
 void launch_wait_selftest(uint32_t polls, int arrive, unsigned int* error_flag, cudaStream_t stream) {

@@ -70,9 +70,12 @@ cudaError_t launch_forward(const ModelView& model, const float* features, uint32
 // Forward over ready input tiles (x_tiles: ceil(n / 128) tiles, as written by
 // the learned step's features kernel); output as launch_forward, bit for bit.
 // Warp-specialised: one persistent CTA per SM, two tiles in flight (TMEM
-// columns, buffers and mbarriers per tile slot).
+// columns, buffers and mbarriers per tile slot). programmatic: launched as a
+// programmatic dependent of the kernel that writes the tiles, each CTA
+// staging the weights and taking its tensor memory while that kernel ends.
 cudaError_t launch_forward_tiles(const ModelView& model, const uint8_t* x_tiles, uint32_t n, float* out_accel,
-                                 unsigned int* error_flag, cudaStream_t stream);
+                                 unsigned int* error_flag, cudaStream_t stream,
+                                 bool programmatic = false);
 // One CTA waits on an mbarrier (arrived at only when `arrive`) with at most
 // `polls` tries; sets *error_flag when the wait gives up.
 void launch_wait_selftest(uint32_t polls, int arrive, unsigned int* error_flag, cudaStream_t stream);
