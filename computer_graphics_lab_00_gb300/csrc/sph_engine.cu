@@ -249,7 +249,7 @@ void Engine::release() {
                        rank_,          order_,        compact_ids_, compact_sorted_, compact_ranges_,
                        snap_pos_[0], snap_vel_[0],
                        snap_pos_[1],   snap_vel_[1],  sforce_,      scorrection_, sfeatures_, correction_sums_,
-                       compact_rank_,  compact_order_, sx_tiles_, counts_, block_sums_};
+                       compact_rank_,  compact_order_, sx_tiles_, counts_, block_sums_, curve_ranges_};
     for (void* b : buffers) {
         if (b != nullptr) {
             cudaFree(b);
@@ -330,7 +330,8 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         (status = alloc(&block_sums_, counting_block_sums(total_buckets_))) != SPH_OK) {
         return status;
     }
-    if ((status = alloc(&rank_, n)) != SPH_OK || (status = alloc(&order_, n)) != SPH_OK) {
+    if ((status = alloc(&rank_, n)) != SPH_OK || (status = alloc(&order_, n)) != SPH_OK ||
+        (status = alloc(&curve_ranges_, size_t{1} << (3 * kCurveCountBits))) != SPH_OK) {
         return status;
     }
     if (tanks_.size() > 1) {
@@ -878,8 +879,10 @@ int Engine::emit(uint32_t tank, uint32_t count) {
 }
 
 // Morton (or Hilbert) processing order: rank_ is refreshed from the current positions
-// every kScheduleRefresh grid builds (particles move a fraction of a cell per
-// substep, so an order a few substeps old keeps its locality), after an emit
+// every kScheduleRefresh grid builds, kCountingRefresh when one tank's order
+// is made by counting (particles move a fraction of a cell per substep, so an
+// order a few substeps old keeps its locality; a fresher one runs the
+// neighbour passes faster, the counting form is cheap enough to pay for that), after an emit
 // and whenever the particle count changed since the last refresh. An upload or
 // a restore of the same count keeps the order (still a permutation of the
 // ids; the usual refresh renews its locality). Never called while a graph
@@ -895,15 +898,29 @@ int Engine::prepare_schedule(uint32_t* launches) {
     if (key_bits + bit_width(split.count > 1 ? split.count - 1U : 0U) > 32) {
         split = IdSplit{};
     }
+    // One tank without id ranges: group by curve cells (coarsened past
+    // kCurveCountBits an axis, and so that the bins fit the grid's count
+    // scratch) with one atomic each; else sort the curve keys.
+    uint32_t count_bits = std::min(axis_bits, kCurveCountBits);
+    while (count_bits > 0 && (size_t{1} << (3 * count_bits)) > total_buckets_) {
+        --count_bits;
+    }
+    const bool by_counting = counting_curve_ && tanks_.size() == 1 && split.count <= 1 && count_bits > 0;
     // Wanted id ranges that the order lacks force a remake; ranges no longer
     // wanted leave with the next regular refresh.
-    if (rank_count_ == total_count_ && since_refresh_ + 1 < kScheduleRefresh &&
+    if (rank_count_ == total_count_ && since_refresh_ + 1 < (by_counting ? kCountingRefresh : kScheduleRefresh) &&
         (want_ranges_ == 0 || same_split(rank_split_, split))) {
         ++since_refresh_;
         return SPH_OK;
     }
-    SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, key_bits, grid_, sweep_, rank_,
-                                stream_, launches, schedule_curve_ == 2, nullptr, split));
+    if (by_counting) {
+        SPH_CUDA(launch_curve_rank_counting(pos_, d_tanks_, total_count_, axis_bits, axis_bits - count_bits,
+                                            schedule_curve_ == 2, grid_.keys_a, grid_.vals_a, counts_, block_sums_,
+                                            curve_ranges_, rank_, stream_, launches));
+    } else {
+        SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, key_bits, grid_, sweep_,
+                                    rank_, stream_, launches, schedule_curve_ == 2, nullptr, split));
+    }
     rank_count_ = total_count_;
     rank_split_ = split;
     since_refresh_ = 0;

@@ -168,6 +168,7 @@ private:
     void schedule_bits(uint32_t* axis_bits, uint32_t* key_bits) const;
     int run_compact(uint32_t substeps, uint32_t active_particles);
     static constexpr uint32_t kScheduleRefresh = 8;  // grid builds between Morton order refreshes
+    static constexpr uint32_t kCountingRefresh = 3;  // the same, one tank's order made by counting
     void release();
     template <typename T> int alloc(T** ptr, size_t count);
 
@@ -188,6 +189,11 @@ private:
     uint32_t* order_ = nullptr;            // sorted positions in processing order
     uint32_t rank_count_ = 0xFFFFFFFFu;    // particle count rank_ was made for
     uint32_t since_refresh_ = 0;           // grid builds since rank_ was made
+    // One tank's curve order by counting (cells grouped, no radix sort);
+    // bins up to 2^(3 kCurveCountBits): whole cells up to 128 a side.
+    static constexpr uint32_t kCurveCountBits = 7;
+    bool counting_curve_ = true;
+    uint2* curve_ranges_ = nullptr;
     uint32_t want_ranges_ = 0;             // id ranges the next order should carry (step_host), 0: none
     IdSplit rank_split_{};                 // the id ranges rank_ was made with
     uint32_t* compact_ids_ = nullptr;      // ids of the active tanks' particles (a batch run with most tanks idle)

@@ -883,6 +883,47 @@ cudaError_t keys_and_counts(const float4* pos, const uint16_t* tank_of, const Ta
     return cudaGetLastError();
 }
 
+// ---- a curve order by counting (one tank) ----------------------------------
+//
+// The processing order needs locality, not a sorted sequence: particles are
+// grouped by the curve code of a coarsened cell (2^shift cells a side) with
+// one atomic place each, the groups laid out in curve order by a scan of
+// their counts, and a group's particles take its slots in the atomics' order.
+
+__device__ __forceinline__ uint32_t coarse_curve_key(float4 p, const TankConst* t, uint32_t axis_bits, uint32_t shift,
+                                                     bool hilbert) {
+    const float h = __ldg(&t->h);
+    const int limit = static_cast<int>((1u << axis_bits) - 1u);
+    const uint32_t cx = static_cast<uint32_t>(min(max(cell_coord(p.x, h) - cell_coord(__ldg(&t->low[0]), h), 0), limit)) >> shift;
+    const uint32_t cy = static_cast<uint32_t>(min(max(cell_coord(p.y, h) - cell_coord(__ldg(&t->low[1]), h), 0), limit)) >> shift;
+    const uint32_t cz = static_cast<uint32_t>(min(max(cell_coord(p.z, h) - cell_coord(__ldg(&t->low[2]), h), 0), limit)) >> shift;
+    const uint32_t bits = axis_bits - shift;
+    return hilbert ? hilbert3(cx, cy, cz, bits) : spread3(cx) | (spread3(cy) << 1) | (spread3(cz) << 2);
+}
+
+__global__ void __launch_bounds__(256) curve_count_kernel(const float4* __restrict__ pos,
+                                                          const TankConst* __restrict__ tanks, uint32_t n,
+                                                          uint32_t axis_bits, uint32_t shift, int hilbert,
+                                                          uint32_t* __restrict__ keys, uint32_t* __restrict__ within,
+                                                          uint32_t* __restrict__ counts) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const uint32_t key = coarse_curve_key(pos[i], tanks, axis_bits, shift, hilbert != 0);
+    keys[i] = key;
+    within[i] = atomicAdd(&counts[key], 1u);
+}
+
+__global__ void __launch_bounds__(256) curve_rank_kernel(const uint32_t* __restrict__ keys,
+                                                         const uint32_t* __restrict__ within, uint32_t n,
+                                                         const uint2* __restrict__ ranges, uint32_t* __restrict__ rank) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        rank[i] = __ldg(&ranges[keys[i]]).x + within[i];
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_keys_onesweep(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
@@ -1086,6 +1127,35 @@ cudaError_t launch_counting_grid(const float4* pos, const uint16_t* tank_of, con
     }
     if (launches != nullptr) {
         *launches += n > 0 ? 5 : 3;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_curve_rank_counting(const float4* pos, const TankConst* tanks, uint32_t n, uint32_t axis_bits,
+                                      uint32_t shift, bool hilbert, uint32_t* keys, uint32_t* within,
+                                      uint32_t* counts, uint32_t* block_sums, uint2* ranges, uint32_t* rank,
+                                      cudaStream_t stream, uint32_t* launches) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    if (axis_bits == 0 || axis_bits > 10 || shift >= axis_bits) {
+        return cudaErrorInvalidValue;
+    }
+    const uint32_t bins = 1u << (3u * (axis_bits - shift));
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * bins, stream);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    const uint32_t blocks = (n + 255) / 256;
+    const uint32_t scan_blocks = static_cast<uint32_t>(counting_block_sums(bins));
+    curve_count_kernel<<<blocks, 256, 0, stream>>>(pos, tanks, n, axis_bits, shift, hilbert ? 1 : 0, keys, within,
+                                                   counts);
+    scan_reduce_kernel<<<scan_blocks, 256, 0, stream>>>(counts, bins, block_sums);
+    scan_top_kernel<<<1, 1024, 0, stream>>>(block_sums, scan_blocks);
+    scan_down_kernel<<<scan_blocks, 256, 0, stream>>>(counts, bins, block_sums, ranges);
+    curve_rank_kernel<<<blocks, 256, 0, stream>>>(keys, within, n, ranges, rank);
+    if (launches != nullptr) {
+        *launches += 5;
     }
     return cudaGetLastError();
 }

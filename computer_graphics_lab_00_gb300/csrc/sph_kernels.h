@@ -153,6 +153,18 @@ cudaError_t launch_morton_rank(const float4* pos, const uint16_t* tank_of, const
                                unsigned long long* sweep, uint32_t* rank, cudaStream_t stream, uint32_t* launches,
                                bool hilbert = false, const uint32_t* ids = nullptr, const IdSplit& split = IdSplit{});
 
+// Processing order of one tank by counting: particles grouped by the curve
+// code (Morton, or Hilbert when `hilbert`) of their cell coarsened by 2^shift
+// a side (axis_bits - shift bits an axis), the groups in curve order, a
+// group's particles in the order of their atomic places; rank[id] = slot.
+// Scratch: keys and within (n words each), counts (zero or not; the bins are
+// zeroed first and left zero), block_sums (counting_block_sums(bins)),
+// ranges (bins = 2^(3 (axis_bits - shift)) entries).
+cudaError_t launch_curve_rank_counting(const float4* pos, const TankConst* tanks, uint32_t n, uint32_t axis_bits,
+                                      uint32_t shift, bool hilbert, uint32_t* keys, uint32_t* within,
+                                      uint32_t* counts, uint32_t* block_sums, uint2* ranges, uint32_t* rank,
+                                      cudaStream_t stream, uint32_t* launches);
+
 // svel[p].xyz = vel[sorted_ids[p]].xyz, .w untouched: the velocities of a
 // gather launched with vel = null (the density pass may run meanwhile).
 cudaError_t launch_gather_vel(const uint32_t* sorted_ids, uint32_t n, const float4* vel, float4* svel,
