@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(256) keys_kernel(const float4* __restrict__ po
 // and gathers their state there; the rest of an overflowing bucket follows in
 // any order, and no neighbour walk reads past its 32nd entry.
 
-constexpr uint32_t kScanItems = 16;                       // counts per thread of a scan block
-constexpr uint32_t kScanTile = 256 * kScanItems;          // 4,096 buckets per scan block
+constexpr uint32_t kScanItems = 4;                        // counts per thread of a scan block
+constexpr uint32_t kScanTile = 256 * kScanItems;          // 1,024 buckets per scan block (more blocks in flight)
 
 __global__ void __launch_bounds__(256) count_keys_kernel(const float4* __restrict__ pos,
                                                          const uint16_t* __restrict__ tank_of,
