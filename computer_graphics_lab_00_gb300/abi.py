@@ -274,6 +274,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "sph_set_tuning": (c_int, [c_void_p, P(SphTuning)]),
         "sph_selftest_division": (c_int, [c_void_p, ctypes.c_uint64, ctypes.c_uint64, c_int, P(ctypes.c_uint64)]),
         "sph_launches_per_substep": (c_int, [c_void_p, u32p]),
+        "sph_kernels_launched": (c_int, [c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
         "sph_device_bytes": (c_int, [c_void_p, P(ctypes.c_uint64)]),
     }
     u8p = P(ctypes.c_uint8)

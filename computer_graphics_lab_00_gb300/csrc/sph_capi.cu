@@ -496,6 +496,14 @@ int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches) {
     return SPH_OK;
 }
 
+int sph_kernels_launched(const sph_ctx* ctx, uint64_t* kernels) {
+    if (ctx == nullptr || kernels == nullptr) {
+        return SPH_ERR_INVALID_ARGUMENT;
+    }
+    *kernels = ctx->engine.kernels_launched();
+    return SPH_OK;
+}
+
 int sph_device_bytes(const sph_ctx* ctx, uint64_t* bytes) {
     if (ctx == nullptr || bytes == nullptr) {
         return SPH_ERR_INVALID_ARGUMENT;

@@ -913,13 +913,18 @@ int Engine::prepare_schedule(uint32_t* launches) {
         ++since_refresh_;
         return SPH_OK;
     }
+    uint32_t made = 0;
     if (by_counting) {
         SPH_CUDA(launch_curve_rank_counting(pos_, d_tanks_, total_count_, axis_bits, axis_bits - count_bits,
                                             schedule_curve_ == 2, grid_.keys_a, grid_.vals_a, counts_, block_sums_,
-                                            curve_ranges_, rank_, stream_, launches));
+                                            curve_ranges_, rank_, stream_, &made));
     } else {
         SPH_CUDA(launch_morton_rank(pos_, tank_of_, d_tanks_, total_count_, axis_bits, key_bits, grid_, sweep_,
-                                    rank_, stream_, launches, schedule_curve_ == 2, nullptr, split));
+                                    rank_, stream_, &made, schedule_curve_ == 2, nullptr, split));
+    }
+    kernels_launched_ += made;
+    if (launches != nullptr) {
+        *launches += made;
     }
     rank_count_ = total_count_;
     rank_split_ = split;
@@ -1096,6 +1101,7 @@ int Engine::run(float dt, uint32_t substeps) {
             return status;
         }
         SPH_CUDA(cudaGraphLaunch(graph_, stream_));
+        kernels_launched_ += launches_per_substep_;
     }
     grid_valid_ = true;
     return SPH_OK;

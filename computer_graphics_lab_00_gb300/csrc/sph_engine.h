@@ -139,6 +139,9 @@ public:
     uint32_t total_count() const { return total_count_; }
     const sph_params& params(uint32_t tank) const { return params_[tank]; }
     uint32_t launches_per_substep() const { return launches_per_substep_; }
+    // Kernels launched by run() (its graphs) and by the processing-order
+    // remakes, counted as they are enqueued.
+    uint64_t kernels_launched() const { return kernels_launched_; }
     uint64_t device_bytes() const { return device_bytes_; }
     cudaStream_t stream() const { return stream_; }
     float4* positions() const { return pos_; }
@@ -237,6 +240,7 @@ private:
     cudaGraphExec_t graph_ = nullptr;
     uint32_t graph_count_ = 0xFFFFFFFFu;
     uint32_t launches_per_substep_ = 0;
+    uint64_t kernels_launched_ = 0;
     bool grid_valid_ = false;
     uint32_t nonfinite_host_ = 0;
     cudaStream_t copy_stream_ = nullptr;  // step_host: velocity upload and checks beside the keys and sort

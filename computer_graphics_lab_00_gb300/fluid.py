@@ -306,6 +306,13 @@ class FluidSolverGpu:
         self._check(self._lib.sph_launches_per_substep(self._ctx, ctypes.byref(out)), "sph_launches_per_substep")
         return int(out.value)
 
+    def kernels_launched(self) -> int:
+        """sph_kernels_launched: kernels enqueued so far by run (the substep
+        graph) and by the processing-order remakes."""
+        out = ctypes.c_uint64()
+        self._check(self._lib.sph_kernels_launched(self._ctx, ctypes.byref(out)), "sph_kernels_launched")
+        return out.value
+
     def device_bytes(self) -> int:
         out = ctypes.c_uint64()
         self._check(self._lib.sph_device_bytes(self._ctx, ctypes.byref(out)), "sph_device_bytes")

@@ -408,6 +408,11 @@ int sph_set_tuning(sph_ctx* ctx, const sph_tuning* tuning);
 int sph_selftest_division(sph_ctx* ctx, uint64_t seed, uint64_t count, int mode, uint64_t* mismatches);
 /* Number of kernel launches one substep enqueues. */
 int sph_launches_per_substep(const sph_ctx* ctx, uint32_t* launches);
+/* Kernels the context has launched through sph_run / sph_step (the substep
+ * graph's kernels) and through the processing-order remakes of every path,
+ * counted as they are enqueued: the difference across a region of sph_run
+ * calls is the number of kernels that region ran. */
+int sph_kernels_launched(const sph_ctx* ctx, uint64_t* kernels);
 /* Bytes of device memory the context holds. */
 int sph_device_bytes(const sph_ctx* ctx, uint64_t* bytes);
 

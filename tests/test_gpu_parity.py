@@ -538,3 +538,24 @@ def test_pair_list_overflow_falls_back_bit_exact(native, oracle):
         op, ov = oracle.run_substeps(params, pos, vel, 1.0 / 600.0, 2)
         assert_bit_exact(gp, op, f"positions with list overflow, variant {variant}")
         assert_bit_exact(gv, ov, f"velocities with list overflow, variant {variant}")
+
+
+def test_kernel_counter_counts_the_graph_and_the_order_remakes(native):
+    """sph_kernels_launched advances by the substep graph's kernels for every
+    substep run, plus the processing-order remakes: one tank's order is made
+    by counting (five kernels) every third build; the plain bucket order
+    (schedule 0) has none."""
+    case = W.dam_break_16k()
+    with FluidSolverGpu(case.params, case.count) as s:
+        s.upload(*case.initial_state())
+        s.run(case.dt, 1)
+        per = s.launches_per_substep()
+        assert per >= 8  # counting grid (5), gather, density, integrate
+        before = s.kernels_launched()
+        s.run(case.dt, 9)
+        assert s.kernels_launched() - before == 9 * per + 3 * 5
+        s.set_tuning(schedule=0)
+        s.run(case.dt, 1)
+        before = s.kernels_launched()
+        s.run(case.dt, 6)
+        assert s.kernels_launched() - before == 6 * s.launches_per_substep()
