@@ -331,7 +331,8 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         return status;
     }
     if ((status = alloc(&rank_, n)) != SPH_OK || (status = alloc(&order_, n)) != SPH_OK ||
-        (status = alloc(&curve_ranges_, size_t{1} << (3 * kCurveCountBits))) != SPH_OK) {
+        (status = alloc(&curve_ranges_, std::min(size_t{1} << (3 * kCurveCountBits),
+                                                 static_cast<size_t>(total_buckets_)))) != SPH_OK) {
         return status;
     }
     if (tanks_.size() > 1) {
@@ -898,14 +899,13 @@ int Engine::prepare_schedule(uint32_t* launches) {
     if (key_bits + bit_width(split.count > 1 ? split.count - 1U : 0U) > 32) {
         split = IdSplit{};
     }
-    // One tank without id ranges: group by curve cells (coarsened past
-    // kCurveCountBits an axis, and so that the bins fit the grid's count
-    // scratch) with one atomic each; else sort the curve keys.
-    uint32_t count_bits = std::min(axis_bits, kCurveCountBits);
-    while (count_bits > 0 && (size_t{1} << (3 * count_bits)) > total_buckets_) {
-        --count_bits;
-    }
-    const bool by_counting = counting_curve_ && tanks_.size() == 1 && split.count <= 1 && count_bits > 0;
+    // One tank without id ranges whose whole cells fit the bins (at most
+    // kCurveCountBits an axis, and within the grid's count scratch): group
+    // the particles by cell with one atomic each. Else sort the curve keys
+    // (grouping several cells a bin loses the locality the order is for).
+    const bool by_counting = counting_curve_ && tanks_.size() == 1 && split.count <= 1 &&
+                             axis_bits <= kCurveCountBits && (size_t{1} << (3 * axis_bits)) <= total_buckets_;
+    const uint32_t count_bits = axis_bits;
     // Wanted id ranges that the order lacks force a remake; ranges no longer
     // wanted leave with the next regular refresh.
     if (rank_count_ == total_count_ && since_refresh_ + 1 < (by_counting ? kCountingRefresh : kScheduleRefresh) &&

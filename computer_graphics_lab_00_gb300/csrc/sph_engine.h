@@ -192,8 +192,8 @@ private:
     uint32_t* order_ = nullptr;            // sorted positions in processing order
     uint32_t rank_count_ = 0xFFFFFFFFu;    // particle count rank_ was made for
     uint32_t since_refresh_ = 0;           // grid builds since rank_ was made
-    // One tank's curve order by counting (cells grouped, no radix sort);
-    // bins up to 2^(3 kCurveCountBits): whole cells up to 128 a side.
+    // One tank's curve order by counting (particles grouped by cell, no
+    // radix sort) when its cells fit 2^kCurveCountBits a side.
     static constexpr uint32_t kCurveCountBits = 7;
     bool counting_curve_ = true;
     uint2* curve_ranges_ = nullptr;
