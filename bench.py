@@ -567,7 +567,7 @@ def learned_eval_leg(device: int) -> dict:
 
 def learned_batched_leg(coarse_steps: int, device: int) -> dict:
     """Config 5: 1,024 tanks of 8,192 particles (uneven blocks), learned
-    coarse steps of 1/240 s with the fine solver as judge and per-tank
+    coarse steps of 1/240 s with the fine solver as checker and per-tank
     fallback, against the plain batched form at the fine step (1/1200 s)
     over the same simulated time on the same GPU."""
     from computer_graphics_lab_00_gb300 import training as T

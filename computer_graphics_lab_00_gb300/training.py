@@ -1,6 +1,6 @@
 """The learned 5x-dt correction: training data from the plain solver's own
 fine trajectories, training with the project's GPU kernels, and evaluation
-with the plain fine solver as judge and fallback.
+with the plain fine solver as checker and fallback.
 
 Steps are fine dt = 1/1200 s and coarse D = 5 dt = 1/240 s. The correction
 is an acceleration added in the coarse step; its training target at a fine
@@ -259,7 +259,7 @@ class Comparison:
 
 
 def reference_runs(tankset, duration: float = 2.0, every: float = 0.1, device: int = 0) -> dict:
-    """Compression and centre of mass of the plain fine run (the judge) and
+    """Compression and centre of mass of the plain fine run (the check) and
     of the plain coarse run (D = 1/240 s, no network) every `every` seconds."""
     coarse_per_check = int(round(every / COARSE_DT))
     checks = int(round(duration / every))
@@ -383,7 +383,7 @@ def fit(tankset, validations: list, snapshots: int = 40, steps: int = 4000, batc
 def run_with_fallback(tankset, mlp, coarse_steps: int = 600, check_every: int = 10, sample: int = 8,
                       threshold: float = 0.01, hold: int = 20, record_every: int = 60, drift_limit: float | None = None,
                       device: int = 0) -> dict:
-    """Learned coarse steps with the plain fine solver as judge and fallback.
+    """Learned coarse steps with the plain fine solver as checker and fallback.
 
     Every `check_every` coarse steps a rotating 1/`sample` share of the
     tanks on learned steps (a contiguous block of tanks) is judged: the fine solver re-runs the interval
