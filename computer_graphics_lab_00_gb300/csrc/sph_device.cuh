@@ -51,6 +51,8 @@ struct alignas(16) TankConst {
     float radius;                      // particle radius (container_min.w)
     uint32_t collider_count;           // shape colliders of this tank (<= SPH_MAX_COLLIDERS)
     uint32_t field_count;              // force fields of this tank (<= SPH_MAX_FORCE_FIELDS)
+    uint32_t curve_base;               // first cell bin of this tank (processing order of a batch)
+    uint32_t curve_dims[3];            // the tank's cells a side from its low corner
     uint32_t pad_extra;
     const sph_collider* colliders;     // this tank's colliders in device memory
     const sph_force_field* fields;     // this tank's force fields in device memory

@@ -303,6 +303,7 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
     }
     total_capacity_ = static_cast<uint32_t>(particles);
     total_buckets_ = static_cast<uint32_t>(buckets);
+    curve_layout();
     total_count_ = params.size() == 1 ? 0 : total_capacity_;
     plan_ = plan_radix(bit_width(total_buckets_ - 1U), radix_bits_);
 
@@ -331,8 +332,10 @@ int Engine::init(int device, const std::vector<sph_params>& params, const std::v
         return status;
     }
     if ((status = alloc(&rank_, n)) != SPH_OK || (status = alloc(&order_, n)) != SPH_OK ||
-        (status = alloc(&curve_ranges_, std::min(size_t{1} << (3 * kCurveCountBits),
-                                                 static_cast<size_t>(total_buckets_)))) != SPH_OK) {
+        (status = alloc(&curve_ranges_, curve_capacity_ = std::min(
+                                            std::max(size_t{1} << (3 * kCurveCountBits),
+                                                     tanks_.size() > 1 ? static_cast<size_t>(curve_bins_) : 0),
+                                            static_cast<size_t>(total_buckets_)))) != SPH_OK) {
         return status;
     }
     if (tanks_.size() > 1) {
@@ -469,6 +472,7 @@ int Engine::refresh_constants(float dt) {
         t.dt = dt;
         t.max_speed = dt > 0.0F ? 0.4F * t.h / dt : 0.0F;
     }
+    curve_layout();
     SPH_CUDA(cudaMemcpyAsync(d_tanks_, tanks_.data(), tanks_.size() * sizeof(TankConst), cudaMemcpyHostToDevice,
                              stream_));
     if (shapes_dirty_) {
@@ -879,6 +883,30 @@ int Engine::emit(uint32_t tank, uint32_t count) {
     return SPH_OK;
 }
 
+// A batch's processing order lays each tank's cells out in row order, tank
+// after tank: curve_dims = the cells a side from the tank's low corner (as the
+// order's kernel finds a particle's cell, clamped to them), curve_base = the
+// cells of the tanks before it.
+void Engine::curve_layout() {
+    uint64_t bins = 0;
+    for (TankConst& t : tanks_) {
+        uint64_t cells = 1;
+        for (int a = 0; a < 3; ++a) {
+            uint32_t d = 1;
+            if (t.h > 0.0F && std::isfinite(t.low[a] / t.h) && std::isfinite(t.high[a] / t.h)) {
+                const double lo = std::floor(static_cast<double>(t.low[a] / t.h));
+                const double hi = std::floor(static_cast<double>(t.high[a] / t.h));
+                d = hi >= lo ? static_cast<uint32_t>(std::min(hi - lo + 1.0, 4096.0)) : 1U;
+            }
+            t.curve_dims[a] = d;
+            cells *= d;
+        }
+        t.curve_base = bins <= 0xFFFFFFFFull ? static_cast<uint32_t>(bins) : 0U;
+        bins += cells;
+    }
+    curve_bins_ = bins;
+}
+
 // Morton (or Hilbert) processing order: rank_ is refreshed from the current positions
 // every kScheduleRefresh grid builds, kCountingRefresh when one tank's order
 // is made by counting (particles move a fraction of a cell per substep, so an
@@ -906,15 +934,23 @@ int Engine::prepare_schedule(uint32_t* launches) {
     const bool by_counting = counting_curve_ && tanks_.size() == 1 && split.count <= 1 &&
                              axis_bits <= kCurveCountBits && (size_t{1} << (3 * axis_bits)) <= total_buckets_;
     const uint32_t count_bits = axis_bits;
+    // A batch: the tanks' cells in row order, when they fit the bins.
+    const bool batch_counting = counting_curve_ && tanks_.size() > 1 && split.count <= 1 && curve_bins_ > 0 &&
+                                curve_bins_ <= curve_capacity_ && curve_bins_ <= total_buckets_;
     // Wanted id ranges that the order lacks force a remake; ranges no longer
     // wanted leave with the next regular refresh.
-    if (rank_count_ == total_count_ && since_refresh_ + 1 < (by_counting ? kCountingRefresh : kScheduleRefresh) &&
+    if (rank_count_ == total_count_ &&
+        since_refresh_ + 1 < (by_counting || batch_counting ? kCountingRefresh : kScheduleRefresh) &&
         (want_ranges_ == 0 || same_split(rank_split_, split))) {
         ++since_refresh_;
         return SPH_OK;
     }
     uint32_t made = 0;
-    if (by_counting) {
+    if (batch_counting) {
+        SPH_CUDA(launch_tank_cells_rank(pos_, tank_of_, d_tanks_, total_count_, static_cast<uint32_t>(curve_bins_),
+                                        grid_.keys_a, grid_.vals_a, counts_, block_sums_, curve_ranges_, rank_, stream_,
+                                        &made));
+    } else if (by_counting) {
         SPH_CUDA(launch_curve_rank_counting(pos_, d_tanks_, total_count_, axis_bits, axis_bits - count_bits,
                                             schedule_curve_ == 2, grid_.keys_a, grid_.vals_a, counts_, block_sums_,
                                             curve_ranges_, rank_, stream_, &made));

@@ -197,6 +197,9 @@ private:
     static constexpr uint32_t kCurveCountBits = 7;
     bool counting_curve_ = true;
     uint2* curve_ranges_ = nullptr;
+    size_t curve_capacity_ = 0;  // entries of curve_ranges_
+    uint64_t curve_bins_ = 0;    // a batch's cells in all (the tanks' curve_dims products)
+    void curve_layout();         // each tank's curve_dims and curve_base, and curve_bins_
     uint32_t want_ranges_ = 0;             // id ranges the next order should carry (step_host), 0: none
     IdSplit rank_split_{};                 // the id ranges rank_ was made with
     uint32_t* compact_ids_ = nullptr;      // ids of the active tanks' particles (a batch run with most tanks idle)

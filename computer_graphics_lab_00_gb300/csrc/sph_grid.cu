@@ -915,6 +915,32 @@ __global__ void __launch_bounds__(256) curve_count_kernel(const float4* __restri
     within[i] = atomicAdd(&counts[key], 1u);
 }
 
+// A batch's processing order: each tank's cells in row order (x fastest)
+// from curve_base; a particle takes a place in its cell's bin with one atomic.
+__global__ void __launch_bounds__(256) tank_cells_count_kernel(const float4* __restrict__ pos,
+                                                               const uint16_t* __restrict__ tank_of,
+                                                               const TankConst* __restrict__ tanks, uint32_t n,
+                                                               uint32_t* __restrict__ keys,
+                                                               uint32_t* __restrict__ within,
+                                                               uint32_t* __restrict__ counts) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) {
+        return;
+    }
+    const TankConst* t = tanks + tank_of[i];
+    const float4 p = pos[i];
+    const float h = __ldg(&t->h);
+    const int nx = static_cast<int>(__ldg(&t->curve_dims[0]));
+    const int ny = static_cast<int>(__ldg(&t->curve_dims[1]));
+    const int nz = static_cast<int>(__ldg(&t->curve_dims[2]));
+    const int cx = min(max(cell_coord(p.x, h) - cell_coord(__ldg(&t->low[0]), h), 0), nx - 1);
+    const int cy = min(max(cell_coord(p.y, h) - cell_coord(__ldg(&t->low[1]), h), 0), ny - 1);
+    const int cz = min(max(cell_coord(p.z, h) - cell_coord(__ldg(&t->low[2]), h), 0), nz - 1);
+    const uint32_t key = __ldg(&t->curve_base) + static_cast<uint32_t>((cz * ny + cy) * nx + cx);
+    keys[i] = key;
+    within[i] = atomicAdd(&counts[key], 1u);
+}
+
 __global__ void __launch_bounds__(256) curve_rank_kernel(const uint32_t* __restrict__ keys,
                                                          const uint32_t* __restrict__ within, uint32_t n,
                                                          const uint2* __restrict__ ranges, uint32_t* __restrict__ rank) {
@@ -1150,6 +1176,33 @@ cudaError_t launch_curve_rank_counting(const float4* pos, const TankConst* tanks
     const uint32_t scan_blocks = static_cast<uint32_t>(counting_block_sums(bins));
     curve_count_kernel<<<blocks, 256, 0, stream>>>(pos, tanks, n, axis_bits, shift, hilbert ? 1 : 0, keys, within,
                                                    counts);
+    scan_reduce_kernel<<<scan_blocks, 256, 0, stream>>>(counts, bins, block_sums);
+    scan_top_kernel<<<1, 1024, 0, stream>>>(block_sums, scan_blocks);
+    scan_down_kernel<<<scan_blocks, 256, 0, stream>>>(counts, bins, block_sums, ranges);
+    curve_rank_kernel<<<blocks, 256, 0, stream>>>(keys, within, n, ranges, rank);
+    if (launches != nullptr) {
+        *launches += 5;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tank_cells_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                   uint32_t bins, uint32_t* keys, uint32_t* within, uint32_t* counts,
+                                   uint32_t* block_sums, uint2* ranges, uint32_t* rank, cudaStream_t stream,
+                                   uint32_t* launches) {
+    if (n == 0) {
+        return cudaSuccess;
+    }
+    if (bins == 0 || tank_of == nullptr) {
+        return cudaErrorInvalidValue;
+    }
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(uint32_t) * bins, stream);
+    if (e != cudaSuccess) {
+        return e;
+    }
+    const uint32_t blocks = (n + 255) / 256;
+    const uint32_t scan_blocks = static_cast<uint32_t>(counting_block_sums(bins));
+    tank_cells_count_kernel<<<blocks, 256, 0, stream>>>(pos, tank_of, tanks, n, keys, within, counts);
     scan_reduce_kernel<<<scan_blocks, 256, 0, stream>>>(counts, bins, block_sums);
     scan_top_kernel<<<1, 1024, 0, stream>>>(block_sums, scan_blocks);
     scan_down_kernel<<<scan_blocks, 256, 0, stream>>>(counts, bins, block_sums, ranges);

@@ -165,6 +165,15 @@ cudaError_t launch_curve_rank_counting(const float4* pos, const TankConst* tanks
                                       uint32_t* counts, uint32_t* block_sums, uint2* ranges, uint32_t* rank,
                                       cudaStream_t stream, uint32_t* launches);
 
+// Processing order of a batch by counting: each tank's cells in row order (x
+// fastest, TankConst::curve_dims cells a side) from TankConst::curve_base, a
+// cell's particles in the order of their atomic places; rank[id] = slot.
+// bins: the tanks' cells in all. Scratch as launch_curve_rank_counting.
+cudaError_t launch_tank_cells_rank(const float4* pos, const uint16_t* tank_of, const TankConst* tanks, uint32_t n,
+                                   uint32_t bins, uint32_t* keys, uint32_t* within, uint32_t* counts,
+                                   uint32_t* block_sums, uint2* ranges, uint32_t* rank, cudaStream_t stream,
+                                   uint32_t* launches);
+
 // svel[p].xyz = vel[sorted_ids[p]].xyz, .w untouched: the velocities of a
 // gather launched with vel = null (the density pass may run meanwhile).
 cudaError_t launch_gather_vel(const uint32_t* sorted_ids, uint32_t n, const float4* vel, float4* svel,

@@ -138,7 +138,9 @@ typedef struct sph_tuning {
     uint32_t queue_depth;      /* in-range pairs buffered per thread: 8, 16, 24 or 32 */
     uint32_t schedule;         /* processing order: 0 sorted (bucket) order; 1 (default) Morton order of
                                   the cells; 2 Hilbert order of the cells; orders 1 and 2 are remade every
-                                  8 grid builds (every 3 for one tank, whose order is made by counting) */
+                                  8 grid builds (every 3 when made by counting: one tank whose cells fit
+                                  128 a side; a batch, where 1 and 2 both give each tank's cells in row
+                                  order, tank after tank) */
     uint32_t sort;             /* grid sort: 0 three kernels per digit pass (radix_bits wide);
                                   1 one kernel per 8-bit pass, tile offsets from tile digit counts
                                     made by the previous pass (radix_bits unused);
