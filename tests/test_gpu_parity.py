@@ -193,6 +193,38 @@ def test_one_crowded_cell(native, oracle, sort):
     assert_bit_exact(gv, ov, "velocities with a crowded cell")
 
 
+@pytest.mark.parametrize("crowd", [1, 2, 31, 32, 33, 64, 65, 100])
+def test_counting_placement_at_its_size_boundaries(native, oracle, crowd):
+    """One cell holding `crowd` particles among scattered others: buckets of
+    up to 64 members are ranked in full, larger ones until 32 smaller ids are
+    found, and past 32 the rest of the bucket follows in any order; each size
+    at those edges gives the oracle's grid (counts and first 32 ids in order)
+    and substep."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
+                           lattice=(4, 4, 8), cell_count=1024)
+    rng = np.random.default_rng(100 + crowd)
+    n = 400 + crowd
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(0.05, 0.95, size=(n, 3)).astype(np.float32)
+    crowded = rng.permutation(n)[:crowd]
+    pos[crowded, :3] = (0.481 + rng.uniform(0.0, 0.038, size=(crowd, 3))).astype(np.float32)
+    pos[:, 3] = 1000.0
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = rng.normal(0.0, 0.1, size=(n, 3)).astype(np.float32)
+    with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(sort=2)
+        solver.upload(pos, vel)
+        solver.build_grid()
+        grid = solver.grid()
+        assert grid[1].max() >= crowd
+        solver.substep(1.0 / 600.0)
+        gp, gv = solver.state()
+    assert_grid_equal(grid, oracle.grid_build(params, pos))
+    op, ov = oracle.substep(params, pos, vel, 1.0 / 600.0)
+    assert_bit_exact(gp, op, f"positions, {crowd} in one cell")
+    assert_bit_exact(gv, ov, f"velocities, {crowd} in one cell")
+
+
 @pytest.mark.parametrize("variant,schedule", [(4, 1), (6, 1), (6, 0)])
 def test_hash_collisions_and_duplicate_buckets(native, oracle, variant, schedule):
     """With few buckets, neighbour cells collide and the same bucket is
