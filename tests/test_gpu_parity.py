@@ -225,6 +225,36 @@ def test_counting_placement_at_its_size_boundaries(native, oracle, crowd):
     assert_bit_exact(gv, ov, f"velocities, {crowd} in one cell")
 
 
+@pytest.mark.parametrize("schedule", [1, 2])
+def test_curve_grid_with_particles_outside_the_box(native, oracle, schedule):
+    """Particles uploaded outside the container: the counting placement
+    buckets them by their (wrapped) cells' hash and the processing order
+    clamps their cells onto the curve's edge; the grid and the substep still
+    equal the oracle's."""
+    params = W.make_params(container_min=(0.0, 0.0, 0.0), container_max=(1.0, 1.0, 1.0),
+                           lattice=(8, 8, 16), cell_count=4096)
+    rng = np.random.default_rng(7 + schedule)
+    n = 2000
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(0.05, 0.95, size=(n, 3)).astype(np.float32)
+    out = rng.permutation(n)[:300]
+    pos[out, :3] = rng.uniform(-0.6, 1.6, size=(300, 3)).astype(np.float32)
+    pos[:, 3] = 1000.0
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = rng.normal(0.0, 0.2, size=(n, 3)).astype(np.float32)
+    with FluidSolverGpu(params, n) as solver:
+        solver.set_tuning(sort=2, schedule=schedule)
+        solver.upload(pos, vel)
+        solver.build_grid()
+        grid = solver.grid()
+        solver.substep(1.0 / 600.0)
+        gp, gv = solver.state()
+    assert_grid_equal(grid, oracle.grid_build(params, pos))
+    op, ov = oracle.substep(params, pos, vel, 1.0 / 600.0)
+    assert_bit_exact(gp, op, "positions with particles outside the box")
+    assert_bit_exact(gv, ov, "velocities with particles outside the box")
+
+
 @pytest.mark.parametrize("variant,schedule", [(4, 1), (6, 1), (6, 0)])
 def test_hash_collisions_and_duplicate_buckets(native, oracle, variant, schedule):
     """With few buckets, neighbour cells collide and the same bucket is
