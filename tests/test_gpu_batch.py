@@ -189,3 +189,46 @@ def test_256_tank_workload_spot_checks(native, oracle):
             op, ov = oracle.run_substeps(ts.params[t], *ts.initial_state(t), ts.dt, 2,
                                          threads=oracle.hardware_threads)
             assert same(gp, op) and same(gv, ov), f"tank {t}"
+
+
+def cell_bins(ts) -> tuple[int, int]:
+    """The batch processing order's cell bins (each tank's cells a side from
+    its low corner) against the batch's buckets."""
+    bins = 0
+    for p in ts.params:
+        h = np.float32(p.smoothing_radius)
+        r = np.float32(p.particle_radius)
+        cells = 1
+        for a in range(3):
+            lo = np.floor(np.float32(p.container_min[a] + r) / h)
+            hi = np.floor(np.float32(p.container_max[a] - r) / h)
+            cells *= int(max(hi - lo + 1, 1))
+        bins += cells
+    return bins, sum(int(p.cell_count) for p in ts.params)
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_batch_processing_order_by_cells_or_by_sorted_keys(native, oracle, wide):
+    """A batch's curve order: each tank's cells in row order by counting when
+    the cells fit the buckets, else sorted curve keys (wide tanks: boxes far
+    larger than their fluid). Either way, across order remakes, every tank
+    equals the oracle's run of it alone."""
+    counts = [900, 1700, 2600, 4100]
+    params = []
+    for n in counts:
+        side = 1.3 * 0.02 * n ** (1.0 / 3.0)  # a box a little larger than the fluid
+        box = (3.0, 2.0, 3.0) if wide else (side, side, side)
+        lattice = W.tank_lattice(n, (side, side, side), 0.8, 0.02)
+        params.append(W.make_params(container_min=(0, 0, 0), container_max=box, lattice=lattice,
+                                    cell_count=W.cell_count_for(n)))
+    ts = W.TankSet("wide" if wide else "snug", params, counts, 1.0 / 600.0, 10, 9)
+    bins, buckets = cell_bins(ts)
+    assert (bins > buckets) == wide
+    substeps = 10
+    with load(ts) as solver:
+        solver.set_tuning(schedule=1, sort=2)
+        solver.run(ts.dt, substeps)
+        for t in range(len(ts.counts)):
+            gp, gv = solver.download(t)
+            op, ov = oracle.run_substeps(ts.params[t], *ts.initial_state(t), ts.dt, substeps)
+            assert same(gp, op) and same(gv, ov), f"tank {t}"
