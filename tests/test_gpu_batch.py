@@ -44,9 +44,10 @@ def load(ts):
 
 @pytest.mark.parametrize("schedule,substeps,sort", [(0, 5, 1), (1, 5, 1), (1, 20, 1), (2, 20, 1), (1, 5, 2), (0, 20, 2)])
 def test_each_tank_matches_the_oracle(native, oracle, tanks, schedule, substeps, sort):
-    """Sorted and Morton processing orders; 20 substeps cross a remake of the
-    Morton order (one every 16 grid builds), which keys the tank above the
-    cell code."""
+    """Sorted and Morton processing orders; 20 substeps cross remakes of the
+    Morton order (every 8 grid builds: these tanks' boxes have more cells
+    than buckets, so the order sorts curve keys with the tank above the cell
+    code)."""
     with load(tanks) as solver:
         solver.set_tuning(schedule=schedule, sort=sort)
         solver.run(tanks.dt, substeps)
